@@ -1,0 +1,112 @@
+"""ctypes access to the C restatement (oracle/rockstar_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the CPU
+baseline of bench.py.  build() compiles the restatement with the host C
+compiler into oracle/_build/liboracle.so (no FMA contraction, so float
+arithmetic matches the C source exactly).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from . import layouts as L
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "rockstar_oracle.c")
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+
+def build(force=False):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-std=c99", "-D_DEFAULT_SOURCE", "-ffp-contract=off",
+                           "-fno-math-errno", "-fPIC", "-shared", "-o", tmp, SRC, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class OCfg(C.Structure):
+    _fields_ = [(k, C.c_double) for k in (
+        "particle_mass", "box_size", "om", "ol", "h0", "w0", "wa",
+        "fof_linking_length", "fof_fraction", "force_res", "force_res_phys_max",
+        "scale_now", "initial_metric_scaling", "include_host_potential_ratio",
+        "unbound_threshold")] + [(k, C.c_int64) for k in (
+            "min_halo_particles", "min_halo_output_size", "bound_props",
+            "shape_iterations", "weighted_shapes", "exact_ll_calc",
+            "total_particles")]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        h = C.CDLL(build())
+        vp, i64 = C.c_void_p, C.c_int64
+        h.oracle_setup.argtypes = [C.POINTER(OCfg)]
+        h.oracle_avg_spacing.restype = C.c_double
+        h.oracle_thresholds.argtypes = [vp]
+        h.oracle_fof.restype = i64
+        h.oracle_fof.argtypes = [vp, vp, vp, vp]
+        h.oracle_free.argtypes = [vp]
+        h.oracle_find_subs.restype = i64
+        h.oracle_find_subs.argtypes = [vp, vp, vp, i64, vp, vp]
+        h.oracle_compute_potential.argtypes = [vp, i64]
+        h.oracle_kinetic_energy.argtypes = [vp, i64, vp, vp, C.c_float]
+        _lib = h
+    return _lib
+
+
+def setup(cfg):
+    q = OCfg(**{k: getattr(cfg, k) for k, _ in OCfg._fields_})
+    lib().oracle_setup(C.byref(q))
+    return lib().oracle_avg_spacing()
+
+
+def thresholds():
+    out = np.zeros(8, np.float64)
+    lib().oracle_thresholds(out.ctypes.data)
+    return out
+
+
+def _take(ptr, n, dtype):
+    if n == 0:
+        lib().oracle_free(ptr)
+        return np.zeros(0, dtype)
+    buf = (C.c_char * (n * dtype.itemsize)).from_address(ptr)
+    out = np.frombuffer(bytes(buf), dtype=dtype).copy()
+    lib().oracle_free(ptr)
+    return out
+
+
+def fof(parts):
+    """rockstar(NULL, 1): returns (permuted particles, offsets, sizes)."""
+    pa = np.array(parts, dtype=L.PARTICLE, copy=True)
+    n = np.array([len(pa)], np.int64)
+    po, ps = C.c_void_p(), C.c_void_p()
+    nf = lib().oracle_fof(pa.ctypes.data, n.ctypes.data, C.byref(po), C.byref(ps))
+    off = _take(po.value, nf, np.dtype(np.int64))
+    sz = _take(ps.value, nf, np.dtype(np.int64))
+    return pa[:n[0]].copy(), off, sz
+
+
+def find_subs(parts, off, sz):
+    """find_subs over every group in order.  Returns (particles, halos, extra)."""
+    pa = np.array(parts, dtype=L.PARTICLE, copy=True)
+    off = np.ascontiguousarray(off, np.int64)
+    sz = np.ascontiguousarray(sz, np.int64)
+    hp, ep = C.c_void_p(), C.c_void_p()
+    nh = lib().oracle_find_subs(pa.ctypes.data, off.ctypes.data, sz.ctypes.data, len(sz),
+                                C.byref(hp), C.byref(ep))
+    return pa, _take(hp.value, nh, L.HALO), _take(ep.value, nh, L.EXTRA)
+
+
+def compute_potential(po):
+    po = np.array(po, dtype=L.POTENTIAL, copy=True)
+    lib().oracle_compute_potential(po.ctypes.data, len(po))
+    return po
