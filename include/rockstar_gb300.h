@@ -1,0 +1,117 @@
+/* C ABI of the GB300 halo-finding hot path.
+ *
+ * Every entry point is extern "C" and takes plain pointers and sizes.  The
+ * record layouts below are byte-for-byte those of the reference build
+ * (gcc, -DOUTPUT_RVMAX -DOUTPUT_NFW_CHI2 -DOUTPUT_INERTIA_TENSOR), so arrays
+ * can be passed between this library and code compiled against the
+ * reference headers without conversion:
+ *   rsg_particle        == struct particle        (src/particle.h:5-8)
+ *   rsg_fof             == struct fof             (src/fof.h:7-10)
+ *   rsg_halo            == struct halo            (src/halo.h:8-35)
+ *   rsg_extra_halo_info == struct extra_halo_info (src/halo.h:37-41)
+ *   rsg_potential       == struct potential       (src/potential.h:7-21)
+ * The names carry a prefix so this header can be included next to the
+ * reference's own headers.
+ *
+ * Errors: functions return 0 on success and a negative RSG_ERR_* code on
+ * failure; rsg_last_error() describes the last failure of the calling
+ * thread.  Nothing here calls exit(); a drop-in shim maps a non-zero return
+ * to the reference's rockstar_abort() (src/error.h:17-20).
+ */
+#ifndef ROCKSTAR_GB300_H
+#define ROCKSTAR_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RSG_OK 0
+#define RSG_ERR_ARGS (-1)       /* bad arguments or capacity too small */
+#define RSG_ERR_CUDA (-2)       /* a CUDA call failed */
+#define RSG_ERR_NO_DEVICE (-3)  /* no usable GPU */
+#define RSG_ERR_LIMIT (-4)      /* a bounded device loop hit its limit */
+#define RSG_ERR_INPUT (-5)      /* non-finite particle data */
+
+struct rsg_particle { int64_t id; float pos[6]; };
+struct rsg_fof { int64_t num_p; struct rsg_particle *particles; };
+struct rsg_halo {
+    int64_t id;
+    float pos[6], corevel[3], bulkvel[3];
+    float m, r, child_r, vmax_r, mgrav, vmax, rvmax, rs, klypin_rs, vrms, J[3],
+        energy, spin, alt_m[4], Xoff, Voff, b_to_a, c_to_a, A[3], b_to_a2,
+        c_to_a2, A2[3], bullock_spin, kin_to_pot, m_pe_b, m_pe_d,
+        halfmass_radius;
+    int64_t num_p, num_child_particles, p_start, desc, flags, n_core;
+    float min_pos_err, min_vel_err, min_bulkvel_err;
+    float inertia_tensor[6];
+    float inertia_tensor2[6];
+    float chi2;
+};
+struct rsg_extra_halo_info {
+    int64_t child, next_cochild, prev_cochild;
+    int64_t sub_of, ph;
+    float max_metric;
+};
+struct rsg_potential {
+    float pos[6], r2;
+    double pe;
+    float ke;
+    int32_t flags;
+};
+
+/* Hot-path parameters, named after src/config.template.h.  Fields marked
+ * (derived) are filled by rsg_config_setup(). */
+struct rsg_config {
+    double particle_mass;                /* PARTICLE_MASS (0: from box, Om, N) */
+    double box_size;                     /* BOX_SIZE */
+    double om, ol, h0, w0, wa;           /* Om, Ol, h0, W0, WA */
+    double fof_linking_length;           /* FOF_LINKING_LENGTH */
+    double fof_fraction;                 /* FOF_FRACTION */
+    double force_res, force_res_phys_max;/* FORCE_RES, FORCE_RES_PHYS_MAX */
+    double scale_now;                    /* SCALE_NOW */
+    double initial_metric_scaling;       /* INITIAL_METRIC_SCALING */
+    double include_host_potential_ratio; /* INCLUDE_HOST_POTENTIAL_RATIO */
+    double unbound_threshold;            /* UNBOUND_THRESHOLD */
+    int64_t min_halo_particles;          /* MIN_HALO_PARTICLES */
+    int64_t min_halo_output_size;        /* MIN_HALO_OUTPUT_SIZE */
+    int64_t bound_props;                 /* BOUND_PROPS */
+    int64_t shape_iterations;            /* SHAPE_ITERATIONS */
+    int64_t weighted_shapes;             /* WEIGHTED_SHAPES */
+    int64_t exact_ll_calc;               /* EXACT_LL_CALC */
+    int64_t total_particles;             /* TOTAL_PARTICLES */
+    /* (derived) */
+    double avg_particle_spacing;         /* AVG_PARTICLE_SPACING, src/config.c:24-25 */
+    double particle_thresh_dens[5];      /* src/groupies.c:127-142 */
+    double particle_rvir_dens, particle_rvir_dens_z0, dynamical_time;
+    int64_t min_dens_index;
+};
+
+/* Library version and per-thread error text. */
+int rsg_version(void);
+const char *rsg_last_error(void);
+
+/* Derives AVG_PARTICLE_SPACING, the effective FORCE_RES and the density
+ * thresholds exactly as src/config.c:17-64, src/rockstar.c:58-61 and
+ * src/groupies.c:97-142 do.  Host only. */
+int rsg_config_setup(struct rsg_config *cfg);
+
+/* 3D friends-of-friends: replaces rockstar(bounds = NULL, manual_subs = 1)
+ * (src/rockstar.c:53-128).  p[0..*num_p) is permuted in place on return so
+ * that every group is contiguous; duplicates (same position or id as the
+ * previous particle in kd-tree order, src/rockstar.c:368-397) are removed
+ * and *num_p shrinks accordingly.  Group i occupies
+ * p[fof_offsets[i] .. fof_offsets[i] + fof_sizes[i]); groups of fewer than
+ * MIN_HALO_PARTICLES are dropped as in src/fof.c:226-255.  Membership is
+ * identical to the reference; the order of groups and of particles inside
+ * a group is this library's (groups by first kd-tree position, particles in
+ * kd-tree order), as the reference's is an artefact of its union-find.
+ * Particles in no group follow the last group. */
+int rsg_rockstar_fof(struct rsg_particle *p, int64_t *num_p, const struct rsg_config *cfg,
+                     int64_t *fof_offsets, int64_t *fof_sizes, int64_t max_fofs,
+                     int64_t *num_fofs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ROCKSTAR_GB300_H */

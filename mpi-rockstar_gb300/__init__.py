@@ -1,0 +1,124 @@
+"""GB300 halo-finding hot path: host-side mirror of the reference interface.
+
+The compute runs in the CUDA library _build/librockstar_gb300.so (kernels for
+sm_103a behind the C ABI of include/rockstar_gb300.h); this module only
+moves numpy arrays across that ABI with ctypes.  There is no CPU fallback:
+if the library cannot be loaded or no GPU is present, every call raises.
+
+Function names follow the reference calls they replace:
+  rockstar_fof      <- rockstar(NULL, 1)            src/rockstar.c:53-128
+  find_subs         <- find_subs() over all groups  src/groupies.c:669-708
+                       as the loop of src/mpi_main.cpp:1363-1389 runs it
+  compute_potential <- compute_potential()          src/potential.c:183-192
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .layouts import PARTICLE, HALO, EXTRA, POTENTIAL, Config, config_struct  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "librockstar_gb300.so")
+SYNTH = os.path.join(HERE, "_build", "libsynth.so")
+
+
+class RockstarError(RuntimeError):
+    """A library call failed; carries the RSG_ERR_* code."""
+
+    def __init__(self, code, msg):
+        super().__init__("rockstar_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+def build():
+    from . import builder
+    return builder.build()
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RockstarError(-3, "CUDA extension not built: %s (call build())" % LIB)
+        h = C.CDLL(LIB)
+        vp, i64 = C.c_void_p, C.c_int64
+        h.rsg_version.restype = C.c_int
+        h.rsg_last_error.restype = C.c_char_p
+        h.rsg_config_setup.argtypes = [vp]
+        h.rsg_rockstar_fof.argtypes = [vp, vp, vp, vp, vp, i64, vp]
+        h.rsg_debug_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
+        for name, args in _EXTRA_SIGS.items():
+            if hasattr(h, name):
+                getattr(h, name).argtypes = args
+        _lib = h
+    return _lib
+
+
+_EXTRA_SIGS = {}
+
+
+def _check(rc):
+    if rc != 0:
+        raise RockstarError(rc, lib().rsg_last_error().decode(errors="replace"))
+
+
+def setup_config(cfg):
+    """Returns a filled rsg_config struct (ctypes) for a layouts.Config."""
+    st = config_struct(cfg)
+    _check(lib().rsg_config_setup(C.byref(st)))
+    return st
+
+
+def rockstar_fof(parts, cfg):
+    """3D FOF of an id-sorted particle array.  Returns (particles, offsets,
+    sizes): the permuted/deduplicated particles and each group's range."""
+    st = setup_config(cfg)
+    pa = np.array(parts, dtype=PARTICLE, copy=True)
+    n = np.array([len(pa)], np.int64)
+    cap = len(pa) // 2 + 1
+    off = np.zeros(cap, np.int64)
+    sz = np.zeros(cap, np.int64)
+    nf = np.zeros(1, np.int64)
+    _check(lib().rsg_rockstar_fof(pa.ctypes.data, n.ctypes.data, C.byref(st), off.ctypes.data,
+                                  sz.ctypes.data, cap, nf.ctypes.data))
+    k = int(nf[0])
+    return pa[:n[0]].copy(), off[:k].copy(), sz[:k].copy()
+
+
+def tree_order(parts, dim, leaf):
+    """kd-tree build permutation computed on the GPU (test hook)."""
+    pa = np.array(parts, dtype=PARTICLE, copy=True)
+    _check(lib().rsg_debug_tree_order(pa.ctypes.data, len(pa), dim, leaf))
+    return pa
+
+
+_synth = None
+
+
+def synth(cfg_id, scale=1.0, seed=20261203):
+    """Seeded synthetic snapshot (see csrc/synth.c).  Returns
+    (particles, box_size, particle_mass, n_structures)."""
+    global _synth
+    if _synth is None:
+        h = C.CDLL(SYNTH)
+        h.synth_count.restype = C.c_int64
+        h.synth_count.argtypes = [C.c_int, C.c_double, C.c_uint64]
+        h.synth_generate.argtypes = [C.c_int, C.c_double, C.c_uint64, C.c_void_p, C.c_int64,
+                                     C.c_void_p, C.c_void_p, C.c_void_p]
+        _synth = h
+    n = _synth.synth_count(cfg_id, scale, seed)
+    if n < 0:
+        raise ValueError("bad synthetic workload %r scale %r" % (cfg_id, scale))
+    p = np.zeros(n, PARTICLE)
+    box = np.zeros(1)
+    mp = np.zeros(1)
+    nh = np.zeros(1, np.int64)
+    rc = _synth.synth_generate(cfg_id, scale, seed, p.ctypes.data, n, box.ctypes.data,
+                               mp.ctypes.data, nh.ctypes.data)
+    if rc:
+        raise ValueError("synthetic generator failed (%d)" % rc)
+    return p, float(box[0]), float(mp[0]), int(nh[0])

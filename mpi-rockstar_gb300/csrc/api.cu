@@ -1,0 +1,182 @@
+// C-ABI entry points (declared in include/rockstar_gb300.h).
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "kdtree_impl.cuh"
+
+namespace rsg {
+
+struct FofOut {
+    int64_t num_p;
+    int64_t nfofs;
+};
+FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n, const rsg_config &cfg,
+                    rsg_particle *d_out, int64_t *d_off, int64_t *d_sz, cudaStream_t st);
+
+// One device context per host thread: a stream and a scratch arena that is
+// reused across calls (the role the reference's threadprivate scratch
+// buffers play, src/groupies.c:52-57).
+struct Ctx {
+    cudaStream_t st = nullptr;
+    Arena ar;
+    int dev = -1;
+};
+static thread_local Ctx *g_ctx = nullptr;
+
+Ctx &ctx() {
+    if (!g_ctx) {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+            set_error(RSG_ERR_NO_DEVICE, "no CUDA device available");
+            throw Failure();
+        }
+        g_ctx = new Ctx();
+        RSG_CUDA(cudaGetDevice(&g_ctx->dev));
+        RSG_CUDA(cudaStreamCreateWithFlags(&g_ctx->st, cudaStreamNonBlocking));
+    }
+    return *g_ctx;
+}
+
+// ---- configuration (host) ----------------------------------------------
+static const double RHO_C = 2.77519737e11;  // src/universal_constants.h:5
+static const double GRAV = 4.30117902e-9;   // src/universal_constants.h:4
+
+struct Cosmo {
+    const rsg_config *c;
+    // src/hubble.c:8-19
+    double weff(double a) const { return (a != 1.0) ? c->w0 + c->wa - c->wa * (a - 1.0) / log(a) : c->w0; }
+    double hubble(double z) const {
+        double z1 = 1.0 + z, a = 1.0 / z1;
+        return sqrt(c->om * (z1 * z1 * z1) + c->ol * pow(a, -3.0 * (1.0 + weff(a))));
+    }
+    // src/groupies.c:97-100
+    double vir(double a) const {
+        double x = (c->om / pow(a, 3)) / pow(hubble(1.0 / a - 1.0), 2.0) - 1.0;
+        return ((18 * M_PI * M_PI + 82.0 * x - 39 * x * x) / (1.0 + x));
+    }
+    // src/groupies.c:102-125; `kind` 'b' / 'c' with multiplier, or 'v' (virial)
+    float thresh(char kind, double mult, double *z0) const {
+        float scale = (float)c->scale_now;
+        float mf = (float)((c->om / pow(scale, 3)) / pow(hubble(1.0 / scale - 1.0), 2.0));
+        float cons = (float)(c->om * RHO_C / c->particle_mass);
+        float t;
+        if (kind == 'b') t = (float)(mult * cons);
+        else if (kind == 'c') t = (float)(mult * cons / mf);
+        else t = (float)(vir(scale) * cons);
+        *z0 = vir(1.0) * cons;
+        return t;
+    }
+};
+
+}  // namespace rsg
+
+using namespace rsg;
+
+extern "C" {
+
+int rsg_config_setup(struct rsg_config *c) {
+    if (!c) return RSG_ERR_ARGS;
+    if (!c->particle_mass) {
+        if (!c->total_particles) {
+            set_error(RSG_ERR_ARGS, "particle_mass = 0 needs total_particles");
+            return RSG_ERR_ARGS;
+        }
+        c->particle_mass = RHO_C * c->box_size * c->box_size * c->box_size * c->om / c->total_particles;
+    }
+    c->avg_particle_spacing = cbrt(c->particle_mass / (c->om * RHO_C));
+    if (!c->force_res_phys_max) c->force_res_phys_max = c->force_res;
+    if (c->force_res * c->scale_now > c->force_res_phys_max)
+        c->force_res = c->force_res_phys_max / c->scale_now;
+    Cosmo k{c};
+    double z0;
+    c->particle_thresh_dens[0] = k.thresh('v', 0, &z0);
+    c->particle_thresh_dens[1] = k.thresh('b', 200, &z0);
+    c->particle_thresh_dens[2] = k.thresh('c', 200, &z0);
+    c->particle_thresh_dens[3] = k.thresh('c', 500, &z0);
+    c->particle_thresh_dens[4] = k.thresh('c', 2500, &z0);
+    c->particle_rvir_dens = k.thresh('v', 0, &z0);
+    c->particle_rvir_dens_z0 = z0;
+    c->dynamical_time =
+        1.0 / sqrt((4.0 * M_PI * GRAV / 3.0) * c->particle_rvir_dens * c->particle_mass);
+    c->min_dens_index = 0;
+    for (int i = 1; i < 5; i++)
+        if (c->particle_thresh_dens[i] < c->particle_thresh_dens[c->min_dens_index])
+            c->min_dens_index = i;
+    return RSG_OK;
+}
+
+int rsg_rockstar_fof(struct rsg_particle *p, int64_t *num_p, const struct rsg_config *cfg,
+                     int64_t *fof_offsets, int64_t *fof_sizes, int64_t max_fofs,
+                     int64_t *num_fofs) {
+    if (!p || !num_p || !cfg || !num_fofs || *num_p < 0) {
+        set_error(RSG_ERR_ARGS, "rsg_rockstar_fof: null argument");
+        return RSG_ERR_ARGS;
+    }
+    try {
+        Ctx &C = ctx();
+        int64_t n = *num_p;
+        if (n == 0) {
+            *num_fofs = 0;
+            return RSG_OK;
+        }
+        C.ar.reserve((size_t)n * 600 + (256u << 20));
+        C.ar.reset();
+        rsg_particle *d_in = C.ar.get<rsg_particle>(n), *d_out = C.ar.get<rsg_particle>(n);
+        int64_t *d_off = C.ar.get<int64_t>(n / 2 + 1), *d_sz = C.ar.get<int64_t>(n / 2 + 1);
+        RSG_CUDA(cudaMemcpyAsync(d_in, p, sizeof(rsg_particle) * n, cudaMemcpyHostToDevice, C.st));
+        FofOut o = fof3d_device(C.ar, d_in, n, *cfg, d_out, d_off, d_sz, C.st);
+        if (o.nfofs > max_fofs) {
+            set_error(RSG_ERR_ARGS, "rsg_rockstar_fof: %lld groups exceed max_fofs %lld",
+                      (long long)o.nfofs, (long long)max_fofs);
+            return RSG_ERR_ARGS;
+        }
+        RSG_CUDA(cudaMemcpyAsync(p, d_out, sizeof(rsg_particle) * o.num_p, cudaMemcpyDeviceToHost, C.st));
+        if (o.nfofs) {
+            RSG_CUDA(cudaMemcpyAsync(fof_offsets, d_off, sizeof(int64_t) * o.nfofs, cudaMemcpyDeviceToHost, C.st));
+            RSG_CUDA(cudaMemcpyAsync(fof_sizes, d_sz, sizeof(int64_t) * o.nfofs, cudaMemcpyDeviceToHost, C.st));
+        }
+        RSG_CUDA(cudaStreamSynchronize(C.st));
+        *num_p = o.num_p;
+        *num_fofs = o.nfofs;
+        return RSG_OK;
+    } catch (Failure &) {
+        return error_code();
+    }
+}
+
+// Test hook: kd-tree permutation of the particle records alone (dim 3 or 6,
+// leaf size as given), returned as the permuted array.
+int rsg_debug_tree_order(struct rsg_particle *p, int64_t n, int dim, int leaf) {
+    try {
+        Ctx &C = ctx();
+        C.ar.reserve((size_t)n * 200 + (64u << 20));
+        C.ar.reset();
+        rsg_particle *d_in = C.ar.get<rsg_particle>(n);
+        Rec *recs = C.ar.get<Rec>(n);
+        RSG_CUDA(cudaMemcpyAsync(d_in, p, sizeof(rsg_particle) * n, cudaMemcpyHostToDevice, C.st));
+        std::vector<Rec> h(n);
+        std::vector<rsg_particle> hp(p, p + n);
+        for (int64_t i = 0; i < n; i++) {
+            memcpy(h[i].pos, p[i].pos, sizeof(float) * 6);
+            h[i].ridx = (int32_t)i;
+            h[i].aux = 0;
+        }
+        RSG_CUDA(cudaMemcpyAsync(recs, h.data(), sizeof(Rec) * n, cudaMemcpyHostToDevice, C.st));
+        int32_t *seg = C.ar.get<int32_t>(2);
+        int32_t hs[2] = {0, (int32_t)n};
+        RSG_CUDA(cudaMemcpyAsync(seg, hs, sizeof(hs), cudaMemcpyHostToDevice, C.st));
+        if (dim == 3) build_forest<3, Rec>(C.ar, recs, n, seg, seg + 1, 1, n, leaf, C.st);
+        else build_forest<6, Rec>(C.ar, recs, n, seg, seg + 1, 1, n, leaf, C.st);
+        RSG_CUDA(cudaMemcpyAsync(h.data(), recs, sizeof(Rec) * n, cudaMemcpyDeviceToHost, C.st));
+        RSG_CUDA(cudaStreamSynchronize(C.st));
+        for (int64_t i = 0; i < n; i++) p[i] = hp[h[i].ridx];
+        return RSG_OK;
+    } catch (Failure &) {
+        return error_code();
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,84 @@
+// Shared definitions for the GB300 halo-finding kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "rockstar_gb300.h"
+
+namespace rsg {
+
+// Error plumbing: every CUDA call is checked on the host; failures are
+// recorded in a thread-local status that the C-ABI returns to the caller.
+struct Error {
+    int code;
+    char msg[256];
+};
+void set_error(int code, const char *fmt, ...);
+int error_code();
+#define RSG_CUDA(call)                                                                 \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            ::rsg::set_error(RSG_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,  \
+                             cudaGetErrorString(e_));                                  \
+            throw ::rsg::Failure();                                                    \
+        }                                                                              \
+    } while (0)
+#define RSG_CHECK_LAUNCH() RSG_CUDA(cudaGetLastError())
+struct Failure {};
+
+// Working record for every tree build over particles: positions first so the
+// record can be loaded as two float4; `ridx` points back at the caller's
+// particle (the role the hijacked id plays in src/groupies.c:684-686).
+struct __align__(16) Rec {
+    float pos[6];
+    int32_t ridx;
+    int32_t aux;
+};
+static_assert(sizeof(Rec) == 32, "Rec must be 32 bytes");
+
+// Node of a median-of-extent kd-tree (layout of src/fast3tree.c:184-193,
+// indices instead of pointers).
+template <int D>
+struct KNode {
+    float mn[D], mx[D];
+    int32_t start, n;
+    int32_t div;     // split dimension, -1 for a leaf
+    int32_t left;    // right child is left + 1
+    int32_t parent;
+    int32_t tree;    // index of the tree (forest builds)
+};
+
+// Device-side scratch arena: one cudaMalloc, bump allocation per call.
+struct Arena {
+    char *base = nullptr;
+    size_t cap = 0, used = 0, peak = 0;
+    void reserve(size_t bytes);
+    void *take(size_t bytes);
+    template <class T>
+    T *get(size_t n) { return (T *)take(n * sizeof(T)); }
+    void reset() { used = 0; }
+    ~Arena();
+};
+
+// Exact IEEE float arithmetic without FMA contraction: the reference
+// evaluates `dist += dx*dx` as a rounded multiply followed by a rounded add.
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+
+// Order-preserving float <-> uint mapping for atomic min/max on floats.
+__device__ __forceinline__ unsigned f2ord(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+inline int nblk(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace rsg

@@ -1,0 +1,507 @@
+// 3D friends-of-friends with the reference's skip acceleration
+// (rockstar(), src/rockstar.c:53-128; src/fof.c:112-255), reformulated so
+// that every step is data parallel and the partition is identical.
+//
+// The reference visits particles in kd-tree order.  A particle i with more
+// than FOF_SKIP_THRESH (16) neighbours inside r ("dense") marks all of them
+// as skipped and merges with every particle within 2r that is already in a
+// group.  Written as a function of the neighbour sets S_r(i):
+//   * dense(i)      <=> |S_r(i)| > 16, a property of i alone;
+//   * seeds         = the lexicographically-first maximal independent set of
+//                     the dense particles in tree order (a dense particle is
+//                     processed iff no earlier processed dense particle has
+//                     it in its r-sphere);
+//   * processed(i)  <=> no seed s < i has i in S_r(s);
+//   * g(j)          = the first processed k with |S_r(k)| >= 2 and
+//                     j in S_r(k): the moment j joins some group;
+//   * the partition is the connected components of the links
+//       {(k, j) : k processed, |S_r(k)| >= 2, j in S_r(k)}
+//     plus {(s, j) : s seed, j in S_2r(s), g(j) <= s}.
+// Sphere searches walk the same kd-tree with the same float tests as
+// src/fast3tree.c:293-414, so S_r is the reference's set, node shortcut
+// included.
+#include <cub/cub.cuh>
+
+#include "kdtree_impl.cuh"
+
+namespace rsg {
+
+#define RSG_STACK 96
+
+struct TravStatus {
+    int *flag;  // set to 1 when a traversal stack overflows
+};
+
+// Sphere search (src/fast3tree.c:377-414) on tree `root` of a 3D forest.
+// on_range(start, n) receives nodes that lie entirely inside the sphere
+// (shortcut of :386-392), on_point(j) leaf points with dist < r^2.  Either
+// returns false to stop the walk.
+template <class FR, class FP>
+__device__ bool sphere3(const KNode<3> *nodes, int root, const Rec *recs, const float *c,
+                        float r, int *errflag, FR on_range, FP on_point) {
+    int stack[RSG_STACK];
+    int sp = 0;
+    stack[sp++] = root;
+    const float r2 = fmul(r, r);
+    while (sp) {
+        const KNode<3> &nd = nodes[stack[--sp]];
+        // _fast3tree_box_not_intersect_sphere
+        float d = 0.f, e;
+        bool out = false;
+#pragma unroll
+        for (int i = 0; i < 3; i++) {
+            if ((e = fsub(c[i], nd.mn[i])) < 0) {
+                d = fadd(d, fmul(e, e));
+                if (d >= r2) { out = true; break; }
+            } else if ((e = fsub(c[i], nd.mx[i])) > 0) {
+                d = fadd(d, fmul(e, e));
+                if (d >= r2) { out = true; break; }
+            }
+        }
+        if (out) continue;
+        // _fast3tree_box_inside_sphere
+        bool inside = true;
+        if (fabsf(fsub(c[0], nd.mn[0])) > r) inside = false;
+        else {
+            float dist = 0.f;
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                float dx = fsub(nd.mn[i], c[i]);
+                dx = fmul(dx, dx);
+                float dx2 = fsub(c[i], nd.mx[i]);
+                dx2 = fmul(dx2, dx2);
+                if (dx2 > dx) dx = dx2;
+                dist = fadd(dist, dx);
+                if (dist > r2) { inside = false; break; }
+            }
+        }
+        if (inside) {
+            if (!on_range(nd.start, nd.n)) return false;
+            continue;
+        }
+        if (nd.div < 0) {
+            for (int k = 0; k < nd.n; k++) {
+                int j = nd.start + k;
+                const Rec &q = recs[j];
+                float dist = 0.f;
+#pragma unroll
+                for (int t = 0; t < 3; t++) {
+                    float dx = fsub(c[t], q.pos[t]);
+                    dist = fadd(dist, fmul(dx, dx));
+                }
+                if (dist < r2)
+                    if (!on_point(j)) return false;
+            }
+            continue;
+        }
+        if (sp + 2 > RSG_STACK) {
+            atomicExch(errflag, 1);
+            return false;
+        }
+        stack[sp++] = nd.left + 1;  // right, visited after left
+        stack[sp++] = nd.left;
+    }
+    return true;
+}
+
+// ---- union-find (lock-free, root = smallest index) ----------------------
+__device__ __forceinline__ int uf_find(int *par, int x) {
+    int p = par[x];
+    while (p != x) {
+        int gp = par[p];
+        if (gp != p) par[x] = gp;  // path halving (benign race)
+        x = p;
+        p = par[x];
+    }
+    return x;
+}
+__device__ __forceinline__ void uf_unite(int *par, int a, int b) {
+    while (true) {
+        a = uf_find(par, a);
+        b = uf_find(par, b);
+        if (a == b) return;
+        if (a < b) { int t = a; a = b; b = t; }
+        if (atomicCAS(&par[a], a, b) == a) return;
+    }
+}
+
+// ---- kernels --------------------------------------------------------------
+__global__ void k_make_recs(const rsg_particle *p, int64_t n, Rec *recs, int *bad) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Rec r;
+    bool fin = true;
+#pragma unroll
+    for (int d = 0; d < 6; d++) {
+        r.pos[d] = p[i].pos[d];
+        fin &= isfinite(r.pos[d]);
+    }
+    r.ridx = (int32_t)i;
+    r.aux = 0;
+    recs[i] = r;
+    if (!fin) atomicExch(bad, 1);
+}
+
+// Duplicate candidates: a particle equal (bitwise position, or id) to its
+// successor in tree order (src/rockstar.c:379-389 compares with the next
+// kept particle, which is the successor whenever nothing was removed).
+__global__ void k_dup_probe(const Rec *recs, const rsg_particle *p, int64_t n, int *any) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i + 1 >= n) return;
+    const Rec &a = recs[i], &b = recs[i + 1];
+    bool same = true;
+#pragma unroll
+    for (int d = 0; d < 6; d++) same &= (__float_as_uint(a.pos[d]) == __float_as_uint(b.pos[d]));
+    if (same || p[a.ridx].id == p[b.ridx].id) atomicExch(any, 1);
+}
+
+// Sequential duplicate removal, only run when k_dup_probe found one.
+__global__ void k_dedupe_serial(Rec *recs, const rsg_particle *p, int64_t n, int64_t *n_out) {
+    if (blockIdx.x || threadIdx.x) return;
+    if (n < 2) { *n_out = n; return; }
+    int64_t last = n - 1;
+    for (int64_t i = n - 2; i >= 0; i--) {
+        bool same = true;
+        for (int d = 0; d < 6; d++)
+            same &= (__float_as_uint(recs[i].pos[d]) == __float_as_uint(recs[last].pos[d]));
+        if (same || p[recs[last].ridx].id == p[recs[i].ridx].id) {
+            n--;
+            recs[i] = recs[n];
+            continue;
+        }
+        last = i;
+    }
+    *n_out = n;
+}
+
+__global__ void k_count(const KNode<3> *nodes, const Rec *recs, int n, float r, uint8_t *cnt,
+                        int *err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float c[3] = {recs[i].pos[0], recs[i].pos[1], recs[i].pos[2]};
+    int k = 0;
+    sphere3(
+        nodes, 0, recs, c, r, err,
+        [&](int s, int m) { k += m; return k <= 16; },
+        [&](int j) { k++; return k <= 16; });
+    cnt[i] = (uint8_t)(k > 17 ? 17 : k);
+}
+
+// Earlier dense neighbours of every dense particle (counted, then listed).
+__global__ void k_elist(const KNode<3> *nodes, const Rec *recs, int n, float r,
+                        const uint8_t *cnt, const int *eoff, int *ecnt, int *elist, int *err) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || cnt[i] <= 16) return;
+    float c[3] = {recs[i].pos[0], recs[i].pos[1], recs[i].pos[2]};
+    int k = 0;
+    int base = eoff ? eoff[i] : 0;
+    sphere3(
+        nodes, 0, recs, c, r, err,
+        [&](int s, int m) {
+            for (int j = s; j < s + m && j < i; j++)
+                if (cnt[j] > 16) {
+                    if (elist) elist[base + k] = j;
+                    k++;
+                }
+            return true;
+        },
+        [&](int j) {
+            if (j < i && cnt[j] > 16) {
+                if (elist) elist[base + k] = j;
+                k++;
+            }
+            return true;
+        });
+    if (!elist) ecnt[i] = k;
+}
+
+// One pass of the ordered greedy independent set: state 0 undecided,
+// 1 seed, 2 not a seed.  Decisions only use final states of earlier
+// particles, so in-place updates within a pass are safe.
+__global__ void k_mis(const int *dense, int nd, const int *eoff, const int *elist,
+                      uint8_t *state, int *changed) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nd) return;
+    int i = dense[t];
+    if (state[i] != 0) return;
+    bool all_out = true;
+    for (int e = eoff[i]; e < eoff[i + 1]; e++) {
+        uint8_t s = ((volatile uint8_t *)state)[elist[e]];
+        if (s == 1) {
+            state[i] = 2;
+            *changed = 1;
+            return;
+        }
+        if (s == 0) all_out = false;
+    }
+    if (all_out) {
+        state[i] = 1;
+        *changed = 1;
+    } else {
+        atomicAdd(changed + 1, 1);
+    }
+}
+
+__global__ void k_seed_mark(const KNode<3> *nodes, const Rec *recs, int n, float r,
+                            const uint8_t *state, uint8_t *skipped, int *err) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || state[s] != 1) return;
+    float c[3] = {recs[s].pos[0], recs[s].pos[1], recs[s].pos[2]};
+    sphere3(
+        nodes, 0, recs, c, r, err,
+        [&](int a, int m) {
+            for (int j = a; j < a + m; j++)
+                if (j > s) skipped[j] = 1;
+            return true;
+        },
+        [&](int j) {
+            if (j > s) skipped[j] = 1;
+            return true;
+        });
+}
+
+__global__ void k_link_r(const KNode<3> *nodes, const Rec *recs, int n, float r,
+                         const uint8_t *cnt, const uint8_t *skipped, int *gtime, int *par,
+                         int *err) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || skipped[k] || cnt[k] < 2) return;
+    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+    sphere3(
+        nodes, 0, recs, c, r, err,
+        [&](int a, int m) {
+            for (int j = a; j < a + m; j++) {
+                atomicMin(&gtime[j], k);
+                uf_unite(par, k, j);
+            }
+            return true;
+        },
+        [&](int j) {
+            atomicMin(&gtime[j], k);
+            uf_unite(par, k, j);
+            return true;
+        });
+}
+
+__global__ void k_link_2r(const KNode<3> *nodes, const Rec *recs, int n, float r2x,
+                          const uint8_t *state, const int *gtime, int *par, int *err) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n || state[s] != 1) return;
+    float c[3] = {recs[s].pos[0], recs[s].pos[1], recs[s].pos[2]};
+    sphere3(
+        nodes, 0, recs, c, r2x, err,
+        [&](int a, int m) {
+            for (int j = a; j < a + m; j++)
+                if (gtime[j] <= s) uf_unite(par, s, j);
+            return true;
+        },
+        [&](int j) {
+            if (gtime[j] <= s) uf_unite(par, s, j);
+            return true;
+        });
+}
+
+__global__ void k_roots(int *par, int n, int *root, int *size) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int rt = uf_find(par, i);
+    root[i] = rt;
+    atomicAdd(&size[rt], 1);
+}
+
+__global__ void k_keys(const int *root, const int *size, int n, int64_t minsz, uint32_t *key,
+                       uint32_t *val) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int rt = root[i];
+    bool kept = size[rt] >= 2 && size[rt] >= minsz;
+    key[i] = kept ? (uint32_t)rt : (uint32_t)n + (uint32_t)i;
+    val[i] = (uint32_t)i;
+}
+
+__global__ void k_gather_out(const uint32_t *val, const Rec *recs, const rsg_particle *in, int n,
+                             rsg_particle *out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    out[k] = in[recs[val[k]].ridx];
+}
+
+__global__ void k_heads(const uint32_t *key, int n, int *head) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    head[k] = (key[k] < (uint32_t)n) && (k == 0 || key[k - 1] != key[k]);
+}
+
+__global__ void k_group_sizes(const int *hpos, const int *nh, const uint32_t *key, int n,
+                              int64_t *off, int64_t *sz) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= *nh) return;
+    int s = hpos[g];
+    int e = (g + 1 < *nh) ? hpos[g + 1] : n;
+    // the last group ends where the ungrouped tail (keys >= n) starts
+    if (g + 1 == *nh) {
+        int lo = s, hi = n;
+        while (lo < hi) {
+            int mid = (lo + hi) / 2;
+            if (key[mid] == key[s]) lo = mid + 1; else hi = mid;
+        }
+        e = lo;
+    }
+    off[g] = s;
+    sz[g] = e - s;
+}
+
+__global__ void k_mark_undecided(const int *dense, int nd, uint8_t *state) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nd) state[dense[t]] = 0;
+}
+__global__ void k_iota(int *a, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = i;
+}
+
+struct DFlag {
+    const uint8_t *c;
+    __device__ uint8_t operator()(int i) const { return c[i] > 16; }
+};
+
+struct FofOut {
+    int64_t num_p;
+    int64_t nfofs;
+};
+
+// Device-resident 3D FOF.  d_in: caller particles (n); d_out: permuted
+// particles; d_off/d_sz: groups (capacity n/2+1).
+FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_config &cfg,
+                    rsg_particle *d_out, int64_t *d_off, int64_t *d_sz, cudaStream_t st) {
+    FofOut res{0, 0};
+    if (n64 <= 0) return res;
+    if (n64 >= (1ll << 31) - 2) {
+        set_error(RSG_ERR_ARGS, "3D FOF supports up to 2^31-2 particles");
+        throw Failure();
+    }
+    int n = (int)n64;
+    const int T = 256;
+    Rec *recs = ar.get<Rec>(n);
+    int *flags = ar.get<int>(8);
+    RSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * 8, st));
+    k_make_recs<<<nblk(n, T), T, 0, st>>>(d_in, n, recs, flags);
+    int32_t *seg = ar.get<int32_t>(2);
+    int32_t hseg[2] = {0, n};
+    RSG_CUDA(cudaMemcpyAsync(seg, hseg, sizeof(hseg), cudaMemcpyHostToDevice, st));
+    size_t mark = ar.used;
+    Forest<3> F = build_forest<3, Rec>(ar, recs, n, seg, seg + 1, 1, n, 20, st);
+    k_dup_probe<<<nblk(n, T), T, 0, st>>>(recs, d_in, n, flags + 1);
+    int hflags[8];
+    RSG_CUDA(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    if (hflags[0]) {
+        set_error(RSG_ERR_INPUT, "non-finite particle coordinates");
+        throw Failure();
+    }
+    if (hflags[1]) {
+        int64_t *dn = ar.get<int64_t>(1);
+        k_dedupe_serial<<<1, 1, 0, st>>>(recs, d_in, n, dn);
+        int64_t nn = 0;
+        RSG_CUDA(cudaMemcpyAsync(&nn, dn, sizeof(nn), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        n = (int)nn;
+        hseg[1] = n;
+        RSG_CUDA(cudaMemcpyAsync(seg, hseg, sizeof(hseg), cudaMemcpyHostToDevice, st));
+        ar.used = mark;
+        F = build_forest<3, Rec>(ar, recs, n, seg, seg + 1, 1, n, 20, st);
+    }
+    res.num_p = n;
+    float r = (float)(cfg.avg_particle_spacing * cfg.fof_linking_length);
+    float r2x = (float)(2.0 * (double)r);
+    int *err = flags + 2;
+
+    uint8_t *cnt = ar.get<uint8_t>(n);
+    k_count<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, cnt, err);
+    // earlier-dense-neighbour lists
+    int *ecnt = ar.get<int>(n + 1), *eoff = ar.get<int>(n + 1);
+    RSG_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int) * (n + 1), st));
+    k_elist<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, cnt, nullptr, ecnt, nullptr, err);
+    size_t cb = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, cb, ecnt, eoff, n + 1, st);
+    void *ct = ar.take(cb + 256);
+    cub::DeviceScan::ExclusiveSum(ct, cb, ecnt, eoff, n + 1, st);
+    int ne = 0;
+    RSG_CUDA(cudaMemcpyAsync(&ne, eoff + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    int *elist = ar.get<int>(ne > 0 ? ne : 1);
+    k_elist<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, cnt, eoff, ecnt, elist, err);
+    // dense particle list
+    int *dense = ar.get<int>(n), *ndense = ar.get<int>(1);
+    {
+        // dense flags
+        thrust::transform_iterator<DFlag, thrust::counting_iterator<int>, uint8_t> it(
+            thrust::counting_iterator<int>(0), DFlag{cnt});
+        size_t b2 = 0;
+        cub::DeviceSelect::Flagged(nullptr, b2, thrust::counting_iterator<int>(0), it, dense,
+                                   ndense, n, st);
+        void *t2 = ar.take(b2 + 256);
+        cub::DeviceSelect::Flagged(t2, b2, thrust::counting_iterator<int>(0), it, dense, ndense,
+                                   n, st);
+    }
+    int nd = 0;
+    RSG_CUDA(cudaMemcpyAsync(&nd, ndense, sizeof(int), cudaMemcpyDeviceToHost, st));
+    uint8_t *state = ar.get<uint8_t>(n);
+    RSG_CUDA(cudaMemsetAsync(state, 2, n, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    if (nd > 0) k_mark_undecided<<<nblk(nd, T), T, 0, st>>>(dense, nd, state);
+    int *chg = ar.get<int>(2);
+    int rounds = 0;
+    while (nd > 0) {
+        RSG_CUDA(cudaMemsetAsync(chg, 0, sizeof(int) * 2, st));
+        k_mis<<<nblk(nd, T), T, 0, st>>>(dense, nd, eoff, elist, state, chg);
+        int h[2];
+        RSG_CUDA(cudaMemcpyAsync(h, chg, sizeof(h), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        rounds++;
+        if (h[1] == 0) break;
+        if (rounds > 1000000) {
+            set_error(RSG_ERR_LIMIT, "seed selection did not converge");
+            throw Failure();
+        }
+    }
+    uint8_t *skipped = ar.get<uint8_t>(n);
+    RSG_CUDA(cudaMemsetAsync(skipped, 0, n, st));
+    k_seed_mark<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, state, skipped, err);
+    int *gtime = ar.get<int>(n), *par = ar.get<int>(n);
+    RSG_CUDA(cudaMemsetAsync(gtime, 0x7f, sizeof(int) * n, st));
+    k_iota<<<nblk(n, T), T, 0, st>>>(par, n);
+    k_link_r<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, cnt, skipped, gtime, par, err);
+    k_link_2r<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r2x, state, gtime, par, err);
+    int *root = ar.get<int>(n), *size = ar.get<int>(n);
+    RSG_CUDA(cudaMemsetAsync(size, 0, sizeof(int) * n, st));
+    k_roots<<<nblk(n, T), T, 0, st>>>(par, n, root, size);
+    uint32_t *key = ar.get<uint32_t>(n), *val = ar.get<uint32_t>(n);
+    uint32_t *key2 = ar.get<uint32_t>(n), *val2 = ar.get<uint32_t>(n);
+    k_keys<<<nblk(n, T), T, 0, st>>>(root, size, n, cfg.min_halo_particles, key, val);
+    size_t sb = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, sb, key, key2, val, val2, n, 0, 32, st);
+    void *stmp = ar.take(sb + 256);
+    cub::DeviceRadixSort::SortPairs(stmp, sb, key, key2, val, val2, n, 0, 32, st);
+    k_gather_out<<<nblk(n, T), T, 0, st>>>(val2, recs, d_in, n, d_out);
+    int *head = ar.get<int>(n), *hpos = ar.get<int>(n), *nh = ar.get<int>(1);
+    k_heads<<<nblk(n, T), T, 0, st>>>(key2, n, head);
+    size_t hb = 0;
+    cub::DeviceSelect::Flagged(nullptr, hb, thrust::counting_iterator<int>(0), head, hpos, nh, n,
+                               st);
+    void *htmp = ar.take(hb + 256);
+    cub::DeviceSelect::Flagged(htmp, hb, thrust::counting_iterator<int>(0), head, hpos, nh, n, st);
+    k_group_sizes<<<nblk(n / 2 + 1, T), T, 0, st>>>(hpos, nh, key2, n, d_off, d_sz);
+    RSG_CHECK_LAUNCH();
+    int hnh = 0;
+    RSG_CUDA(cudaMemcpyAsync(&hnh, nh, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    if (hflags[2]) {
+        set_error(RSG_ERR_LIMIT, "kd-tree traversal stack overflow");
+        throw Failure();
+    }
+    res.nfofs = hnh;
+    return res;
+}
+
+}  // namespace rsg

@@ -1,0 +1,317 @@
+// Level-synchronous kd-forest build on the GPU that reproduces, element for
+// element, the in-place permutation of the reference's fast3tree build
+// (src/fast3tree.c:736-908).
+//
+// The reference splits a node [0, n) at lim = 0.5f * (max + min) of its
+// widest dimension with a two-pointer swap: a front pointer i walks up and,
+// whenever p[i] > lim, swaps it with the back pointer j, which walks down.
+// With m = #(p <= lim) the result is, in closed form:
+//   * small elements before m stay put;
+//   * the t-th big element before m (rank t, ascending) ends at n-1 (t = 0)
+//     or one slot below the (t-1)-th small element after m counted from the
+//     back;
+//   * the t-th small element after m counted from the back fills the slot of
+//     the t-th big element before m;
+//   * big elements above the last consumed back position move down one;
+//   * if the untouched tail [m, pos_last) holds two or more elements, it is
+//     rotated down by one (the front pointer stops at m and swaps it with
+//     each tail element in turn).
+// Every element's destination is therefore a function of per-node prefix
+// counts of the "big" flag, which one global scan provides for all nodes of
+// a level at once.  Degenerate nodes (max == min on the split dimension) get
+// lim = +inf so nothing moves, as in the reference's early return.
+#pragma once
+#include <cub/cub.cuh>
+#include <thrust/iterator/counting_iterator.h>
+#include <thrust/iterator/transform_iterator.h>
+
+#include "common.cuh"
+
+namespace rsg {
+
+template <class RecT, int D>
+struct PosOf;
+template <int D>
+struct PosOf<Rec, D> {
+    __device__ static float get(const Rec &r, int d) { return r.pos[d]; }
+};
+
+struct PotRec {  // struct potential (src/potential.h:7-21), 48 bytes
+    float pos[6], r2;
+    float pad;
+    double pe;
+    float ke;
+    int32_t flags;
+};
+static_assert(sizeof(PotRec) == 48, "PotRec layout");
+template <int D>
+struct PosOf<PotRec, D> {
+    __device__ static float get(const PotRec &r, int d) { return r.pos[d]; }
+};
+
+struct MetricRec {  // struct halo_metric (src/subhalo_metric.h): pos[4] + target
+    float pos[4];
+    int32_t target;
+    int32_t pad[3];
+};
+template <int D>
+struct PosOf<MetricRec, D> {
+    __device__ static float get(const MetricRec &r, int d) { return r.pos[d]; }
+};
+
+template <int D>
+struct Forest {
+    KNode<D> *nodes = nullptr;  // nodes[t] is the root of tree t
+    int32_t nnodes = 0;
+    int32_t ntrees = 0;
+};
+
+// ---- kernels ------------------------------------------------------------
+
+template <int D, class RecT>
+__global__ void k_root_init(const int32_t *rstart, const int32_t *rn, int32_t ntrees,
+                            KNode<D> *nodes, unsigned *bmin, unsigned *bmax) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntrees) return;
+    KNode<D> &nd = nodes[t];
+    nd.start = rstart[t];
+    nd.n = rn[t];
+    nd.div = -1;
+    nd.left = -1;
+    nd.parent = -1;
+    nd.tree = t;
+    for (int d = 0; d < D; d++) {
+        bmin[t * D + d] = 0xffffffffu;
+        bmax[t * D + d] = 0u;
+    }
+}
+
+// Box of every node listed in `owner` (per element), via ordered atomics.
+template <int D, class RecT>
+__global__ void k_box_accum(const RecT *recs, int64_t nrec, const int32_t *owner,
+                            unsigned *bmin, unsigned *bmax) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nrec) return;
+    int a = owner[i];
+    if (a < 0) return;
+    const RecT r = recs[i];
+    for (int d = 0; d < D; d++) {
+        unsigned o = f2ord(PosOf<RecT, D>::get(r, d));
+        atomicMin(&bmin[(int64_t)a * D + d], o);
+        atomicMax(&bmax[(int64_t)a * D + d], o);
+    }
+}
+
+template <int D>
+__global__ void k_box_final(KNode<D> *nodes, const int32_t *list, int32_t nlist,
+                            const unsigned *bmin, const unsigned *bmax) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nlist) return;
+    int a = list[k];
+    for (int d = 0; d < D; d++) {
+        nodes[a].mn[d] = ord2f(bmin[(int64_t)a * D + d]);
+        nodes[a].mx[d] = ord2f(bmax[(int64_t)a * D + d]);
+    }
+}
+
+// Choose the split dimension and limit (src/fast3tree.c:736-757).
+template <int D>
+__global__ void k_prep(KNode<D> *nodes, const int32_t *act, int32_t nact, float *lim) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nact) return;
+    KNode<D> &nd = nodes[act[k]];
+    int dim = D - 1;
+    float dmax = fsub(nd.mx[D - 1], nd.mn[D - 1]);
+    for (int i = 0; i < D - 1; i++) {
+        float d2 = fsub(nd.mx[i], nd.mn[i]);
+        if (d2 > dmax) {
+            dmax = d2;
+            dim = i;
+        }
+    }
+    nd.div = dim;
+    float l = fmul(0.5f, fadd(nd.mx[dim], nd.mn[dim]));
+    if (nd.mx[dim] == nd.mn[dim]) l = __int_as_float(0x7f800000);  // +inf: nothing moves
+    lim[k] = l;
+}
+
+template <int D, class RecT>
+__global__ void k_flags(const RecT *recs, int64_t nrec, const int32_t *owner,
+                        const int32_t *slot, const KNode<D> *nodes, const float *lim,
+                        int32_t *flag) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i > nrec) return;
+    int f = 0;
+    if (i < nrec) {
+        int a = owner[i];
+        if (a >= 0) {
+            int k = slot[a];
+            f = PosOf<RecT, D>::get(recs[i], nodes[a].div) > lim[k];
+        }
+    }
+    flag[i] = f;
+}
+
+// m (= #small) and q (= #big before m) per active node.
+template <int D>
+__global__ void k_counts(const KNode<D> *nodes, const int32_t *act, int32_t nact,
+                         const int32_t *rank, int32_t *m_out, int32_t *q_out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nact) return;
+    const KNode<D> &nd = nodes[act[k]];
+    int s = nd.start, n = nd.n;
+    int B = rank[s + n] - rank[s];
+    int m = n - B;
+    m_out[k] = m;
+    q_out[k] = rank[s + m] - rank[s];
+}
+
+template <int D>
+__global__ void k_tables(const KNode<D> *nodes, int64_t nrec, const int32_t *owner,
+                         const int32_t *slot, const int32_t *flag, const int32_t *rank,
+                         const int32_t *m_arr, int32_t *fb, int32_t *bs) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nrec) return;
+    int a = owner[i];
+    if (a < 0) return;
+    int k = slot[a];
+    int s = nodes[a].start;
+    int l = (int)(i - s);
+    int br = rank[i] - rank[s];
+    int sr = l - br;
+    int m = m_arr[k];
+    if (flag[i] && l < m) fb[s + br] = l;
+    if (!flag[i] && l >= m) bs[s + (m - 1 - sr)] = l;
+}
+
+template <int D, class RecT>
+__global__ void k_scatter(const KNode<D> *nodes, const RecT *src, RecT *dst, int64_t nrec,
+                          const int32_t *owner, const int32_t *slot, const int32_t *flag,
+                          const int32_t *rank, const int32_t *m_arr, const int32_t *q_arr,
+                          const int32_t *fb, const int32_t *bs) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nrec) return;
+    int a = owner[i];
+    if (a < 0) return;
+    int k = slot[a];
+    int s = nodes[a].start, n = nodes[a].n;
+    int l = (int)(i - s);
+    int br = rank[i] - rank[s];
+    int sr = l - br;
+    int m = m_arr[k], q = q_arr[k];
+    int big = flag[i];
+    int d;
+    if (!big && l < m) {
+        d = l;
+    } else if (big && l < m) {
+        d = (br == 0) ? n - 1 : bs[s + br - 1] - 1;
+    } else if (!big) {
+        d = fb[s + (m - 1 - sr)];
+    } else {
+        int pos_last = (q > 0) ? bs[s + q - 1] : n;
+        if (l > pos_last)
+            d = l - 1;
+        else if (pos_last - m >= 2)
+            d = (l == m) ? pos_last - 1 : l - 1;
+        else
+            d = l;
+    }
+    dst[s + d] = src[i];
+}
+
+template <class RecT>
+__global__ void k_copy_owned(const RecT *src, RecT *dst, int64_t nrec, const int32_t *owner) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nrec) return;
+    if (owner[i] >= 0) dst[i] = src[i];
+}
+
+// Split bookkeeping (src/fast3tree.c:798-846): create children for nodes
+// with 0 < m < n, turn the rest into leaves.
+template <int D>
+__global__ void k_children(KNode<D> *nodes, const int32_t *act, int32_t nact,
+                           const int32_t *m_arr, const int32_t *split_off, int32_t base,
+                           unsigned *bmin, unsigned *bmax) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nact) return;
+    int a = act[k];
+    KNode<D> &nd = nodes[a];
+    int m = m_arr[k];
+    if (m == 0 || m == nd.n) {
+        nd.div = -1;
+        nd.left = -1;
+        return;
+    }
+    int l = base + 2 * split_off[k];
+    nd.left = l;
+    for (int c = 0; c < 2; c++) {
+        KNode<D> &ch = nodes[l + c];
+        ch.start = nd.start + (c ? m : 0);
+        ch.n = c ? nd.n - m : m;
+        ch.div = -1;
+        ch.left = -1;
+        ch.parent = a;
+        ch.tree = nd.tree;
+        for (int d = 0; d < D; d++) {
+            bmin[(int64_t)(l + c) * D + d] = 0xffffffffu;
+            bmax[(int64_t)(l + c) * D + d] = 0u;
+        }
+    }
+}
+
+// Element owner update: elements of split nodes move to their child.
+template <int D>
+__global__ void k_owner_update(const KNode<D> *nodes, int64_t nrec, int32_t *owner,
+                               int32_t *box_owner, int leaf) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= nrec) return;
+    int a = owner[i];
+    if (a < 0) {
+        box_owner[i] = -1;
+        return;
+    }
+    const KNode<D> &nd = nodes[a];
+    if (nd.left < 0) {
+        owner[i] = -1;
+        box_owner[i] = -1;
+        return;
+    }
+    int l = nd.left;
+    int c = (i - nd.start) < nodes[l].n ? l : l + 1;
+    box_owner[i] = c;
+    owner[i] = (nodes[c].n > leaf) ? c : -1;
+}
+
+template <int D>
+__global__ void k_split_flags(const int32_t *m_arr, const KNode<D> *nodes, const int32_t *act,
+                              int32_t nact, int32_t *sflag) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > nact) return;
+    if (k == nact) {
+        sflag[k] = 0;
+        return;
+    }
+    int m = m_arr[k];
+    sflag[k] = (m > 0 && m < nodes[act[k]].n) ? 1 : 0;
+}
+
+template <int D>
+__global__ void k_next_active(const KNode<D> *nodes, int32_t base, int32_t nnew, int leaf,
+                              int32_t *flag) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnew) return;
+    flag[k] = nodes[base + k].n > leaf ? 1 : 0;
+}
+
+__global__ void k_slot_set(const int32_t *act, int32_t nact, int32_t *slot);
+
+// Builds a kd-forest over recs[0..nrec) whose trees are the segments
+// (rstart[t], rn[t]) (device arrays).  Elements outside every segment are
+// left alone.  `recs` is permuted in place.  Returns the forest; node
+// storage comes from the arena.
+template <int D, class RecT>
+Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstart,
+                       const int32_t *rn, int32_t ntrees, int64_t n_in_trees, int leaf,
+                       cudaStream_t st);
+
+}  // namespace rsg

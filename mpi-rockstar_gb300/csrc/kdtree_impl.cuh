@@ -1,0 +1,173 @@
+// Host driver of the level-synchronous kd-forest build (see kdtree.cuh).
+#pragma once
+#include "kdtree.cuh"
+
+namespace rsg {
+
+// Box accumulation with per-thread runs: each thread walks ITEMS consecutive
+// elements, keeps a running min/max while the owner stays the same and
+// flushes with ordered atomics when it changes, so a node spanning millions
+// of elements receives one atomic per run rather than one per element.
+template <int D, class RecT, int ITEMS>
+__global__ void k_box_runs(const RecT *recs, int64_t nrec, const int32_t *owner,
+                           unsigned *bmin, unsigned *bmax) {
+    int64_t i0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * ITEMS;
+    if (i0 >= nrec) return;
+    int cur = -1;
+    unsigned lo[D], hi[D];
+    for (int it = 0; it < ITEMS; it++) {
+        int64_t i = i0 + it;
+        if (i >= nrec) break;
+        int a = owner[i];
+        if (a != cur) {
+            if (cur >= 0)
+                for (int d = 0; d < D; d++) {
+                    atomicMin(&bmin[(int64_t)cur * D + d], lo[d]);
+                    atomicMax(&bmax[(int64_t)cur * D + d], hi[d]);
+                }
+            cur = a;
+            for (int d = 0; d < D; d++) {
+                lo[d] = 0xffffffffu;
+                hi[d] = 0u;
+            }
+        }
+        if (a < 0) continue;
+        const RecT r = recs[i];
+        for (int d = 0; d < D; d++) {
+            unsigned o = f2ord(PosOf<RecT, D>::get(r, d));
+            lo[d] = min(lo[d], o);
+            hi[d] = max(hi[d], o);
+        }
+    }
+    if (cur >= 0)
+        for (int d = 0; d < D; d++) {
+            atomicMin(&bmin[(int64_t)cur * D + d], lo[d]);
+            atomicMax(&bmax[(int64_t)cur * D + d], hi[d]);
+        }
+}
+
+template <int D>
+__global__ void k_box_final_range(KNode<D> *nodes, int32_t first, int32_t count,
+                                  const unsigned *bmin, const unsigned *bmax) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int a = first + k;
+    for (int d = 0; d < D; d++) {
+        nodes[a].mn[d] = ord2f(bmin[(int64_t)a * D + d]);
+        nodes[a].mx[d] = ord2f(bmax[(int64_t)a * D + d]);
+    }
+}
+
+__global__ void k_root_owner(const int32_t *rstart, const int32_t *rn, int32_t ntrees,
+                             int leaf, int32_t *owner, int32_t *box_owner);
+
+template <int D>
+__global__ void k_root_active(const KNode<D> *nodes, int32_t ntrees, int leaf, int32_t *flag) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntrees) return;
+    flag[t] = nodes[t].n > leaf ? 1 : 0;
+}
+
+template <int D, class RecT>
+Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstart,
+                       const int32_t *rn, int32_t ntrees, int64_t n_in_trees, int leaf,
+                       cudaStream_t st) {
+    Forest<D> F;
+    F.ntrees = ntrees;
+    if (ntrees == 0) return F;
+    const int T = 256;
+    int64_t cap = ntrees + 4 * (n_in_trees / (leaf > 1 ? leaf : 1)) + 4096;
+    if (cap > 2 * n_in_trees + ntrees + 16) cap = 2 * n_in_trees + ntrees + 16;
+    KNode<D> *nodes = ar.get<KNode<D>>(cap);
+    const size_t mark = ar.used;  // everything below is released on return
+    unsigned *bmin = ar.get<unsigned>(cap * D), *bmax = ar.get<unsigned>(cap * D);
+    int32_t *owner = ar.get<int32_t>(nrec), *box_owner = ar.get<int32_t>(nrec);
+    RecT *tmp = ar.get<RecT>(nrec);
+    int32_t *flag = ar.get<int32_t>(nrec + 1), *rank = ar.get<int32_t>(nrec + 1);
+    int32_t *fb = ar.get<int32_t>(nrec), *bs = ar.get<int32_t>(nrec);
+    int32_t *act = ar.get<int32_t>(cap), *slot = ar.get<int32_t>(cap);
+    float *lim = ar.get<float>(cap);
+    int32_t *m_arr = ar.get<int32_t>(cap), *q_arr = ar.get<int32_t>(cap);
+    int32_t *sflag = ar.get<int32_t>(cap + 1), *soff = ar.get<int32_t>(cap + 1);
+    int32_t *nflag = ar.get<int32_t>(cap);
+    int32_t *cnt = ar.get<int32_t>(2);
+    size_t cub_bytes = 0, b2 = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, flag, rank, (int)(nrec + 1), st);
+    cub::DeviceScan::ExclusiveSum(nullptr, b2, sflag, soff, (int)(cap + 1), st);
+    cub_bytes = cub_bytes > b2 ? cub_bytes : b2;
+    cub::DeviceSelect::Flagged(nullptr, b2, thrust::counting_iterator<int32_t>(0), nflag, act,
+                               cnt, (int)cap, st);
+    cub_bytes = cub_bytes > b2 ? cub_bytes : b2;
+    void *cub_tmp = ar.take(cub_bytes + 256);
+
+    k_root_init<D, RecT><<<nblk(ntrees, T), T, 0, st>>>(rstart, rn, ntrees, nodes, bmin, bmax);
+    RSG_CUDA(cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * nrec, st));
+    RSG_CUDA(cudaMemsetAsync(box_owner, 0xff, sizeof(int32_t) * nrec, st));
+    k_root_owner<<<ntrees, 256, 0, st>>>(rstart, rn, ntrees, leaf, owner, box_owner);
+    RSG_CHECK_LAUNCH();
+    const int IT = 8;
+    k_box_runs<D, RecT, IT><<<nblk((nrec + IT - 1) / IT, T), T, 0, st>>>(recs, nrec, box_owner,
+                                                                         bmin, bmax);
+    k_box_final_range<D><<<nblk(ntrees, T), T, 0, st>>>(nodes, 0, ntrees, bmin, bmax);
+    k_root_active<D><<<nblk(ntrees, T), T, 0, st>>>(nodes, ntrees, leaf, nflag);
+    cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, thrust::counting_iterator<int32_t>(0), nflag,
+                               act, cnt, ntrees, st);
+    RSG_CHECK_LAUNCH();
+    int32_t nact = 0;
+    RSG_CUDA(cudaMemcpyAsync(&nact, cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    int32_t nnodes = ntrees;
+    int level = 0;
+    while (nact > 0) {
+        if (++level > 4096) {
+            set_error(RSG_ERR_LIMIT, "kd-forest build exceeded 4096 levels");
+            throw Failure();
+        }
+        k_slot_set<<<nblk(nact, T), T, 0, st>>>(act, nact, slot);
+        k_prep<D><<<nblk(nact, T), T, 0, st>>>(nodes, act, nact, lim);
+        k_flags<D, RecT><<<nblk(nrec + 1, T), T, 0, st>>>(recs, nrec, owner, slot, nodes, lim,
+                                                          flag);
+        cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, flag, rank, (int)(nrec + 1), st);
+        k_counts<D><<<nblk(nact, T), T, 0, st>>>(nodes, act, nact, rank, m_arr, q_arr);
+        k_tables<D><<<nblk(nrec, T), T, 0, st>>>(nodes, nrec, owner, slot, flag, rank, m_arr,
+                                                 fb, bs);
+        k_scatter<D, RecT><<<nblk(nrec, T), T, 0, st>>>(nodes, recs, tmp, nrec, owner, slot,
+                                                        flag, rank, m_arr, q_arr, fb, bs);
+        k_copy_owned<RecT><<<nblk(nrec, T), T, 0, st>>>(tmp, recs, nrec, owner);
+        k_split_flags<D><<<nblk(nact + 1, T), T, 0, st>>>(m_arr, nodes, act, nact, sflag);
+        cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, sflag, soff, nact + 1, st);
+        RSG_CHECK_LAUNCH();
+        int32_t nsplit = 0;
+        RSG_CUDA(cudaMemcpyAsync(&nsplit, soff + nact, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        if (nnodes + 2 * (int64_t)nsplit > cap) {
+            set_error(RSG_ERR_LIMIT, "kd-forest node capacity %lld exceeded", (long long)cap);
+            throw Failure();
+        }
+        int32_t base = nnodes;
+        k_children<D><<<nblk(nact, T), T, 0, st>>>(nodes, act, nact, m_arr, soff, base, bmin, bmax);
+        nnodes += 2 * nsplit;
+        k_owner_update<D><<<nblk(nrec, T), T, 0, st>>>(nodes, nrec, owner, box_owner, leaf);
+        if (nsplit > 0) {
+            k_box_runs<D, RecT, IT><<<nblk((nrec + IT - 1) / IT, T), T, 0, st>>>(
+                recs, nrec, box_owner, bmin, bmax);
+            k_box_final_range<D><<<nblk(2 * nsplit, T), T, 0, st>>>(nodes, base, 2 * nsplit, bmin,
+                                                                    bmax);
+            k_next_active<D><<<nblk(2 * nsplit, T), T, 0, st>>>(nodes, base, 2 * nsplit, leaf,
+                                                                nflag);
+            cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, thrust::counting_iterator<int32_t>(base),
+                                       nflag, act, cnt, 2 * nsplit, st);
+            RSG_CHECK_LAUNCH();
+            RSG_CUDA(cudaMemcpyAsync(&nact, cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+            RSG_CUDA(cudaStreamSynchronize(st));
+        } else {
+            nact = 0;
+        }
+    }
+    F.nodes = nodes;
+    F.nnodes = nnodes;
+    ar.used = mark;
+    return F;
+}
+
+}  // namespace rsg

@@ -58,6 +58,7 @@ def lib():
         h.oracle_find_subs.argtypes = [vp, vp, vp, i64, vp, vp]
         h.oracle_compute_potential.argtypes = [vp, i64]
         h.oracle_kinetic_energy.argtypes = [vp, i64, vp, vp, C.c_float]
+        h.oracle_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
         _lib = h
     return _lib
 
@@ -110,3 +111,10 @@ def compute_potential(po):
     po = np.array(po, dtype=L.POTENTIAL, copy=True)
     lib().oracle_compute_potential(po.ctypes.data, len(po))
     return po
+
+
+def tree_order(parts, dim, leaf):
+    """The kd-tree build permutation of `parts` (fast3tree_init)."""
+    pa = np.array(parts, dtype=L.PARTICLE, copy=True)
+    lib().oracle_tree_order(pa.ctypes.data, len(pa), dim, leaf)
+    return pa

@@ -1412,3 +1412,11 @@ int64_t oracle_find_subs(struct particle *pa, const int64_t *off, const int64_t 
     *ho = hi.h; *eo = hi.e;
     return hi.n;
 }
+
+/* Test hook: the in-place permutation of fast3tree_init (src/fast3tree.c:225-240)
+ * over particle records, for dim 3 or 6 and the given leaf size. */
+void oracle_tree_order(struct particle *pa, int64_t n, int dim, int leaf) {
+    struct ktree t = {0};
+    kbuild(&t, pa, sizeof(struct particle), 8, dim, leaf, n);
+    kfree(&t);
+}

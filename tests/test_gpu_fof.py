@@ -1,0 +1,71 @@
+"""3D FOF on the GPU against the C restatement of the reference (which is
+itself pinned bit-exact to the reference sources): kd-tree permutations
+element for element, FOF partitions identical as sets."""
+import numpy as np
+import pytest
+
+from helpers import canon_partition
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("dim,leaf", [(3, 20), (6, 40), (3, 10)])
+@pytest.mark.parametrize("cfg,scale", [(1, 0.05), (2, 1 / 64)])
+def test_tree_permutation(rk, oracle, dim, leaf, cfg, scale):
+    p, box, mp, _ = rk.synth(cfg, scale)
+    a = rk.tree_order(p, dim, leaf)
+    b = oracle.tree_order(p, dim, leaf)
+    assert np.array_equal(a["id"], b["id"])
+
+
+def test_tree_degenerate(rk, oracle):
+    """Coincident coordinates and repeated values on split dimensions."""
+    rng = np.random.default_rng(3)
+    p = np.zeros(5000, rk.PARTICLE)
+    p["id"] = np.arange(5000)
+    p["pos"] = rng.integers(0, 4, size=(5000, 6)).astype(np.float32)
+    p["pos"][:700] = 1.0
+    for dim, leaf in [(3, 20), (6, 40)]:
+        assert np.array_equal(rk.tree_order(p, dim, leaf)["id"],
+                              oracle.tree_order(p, dim, leaf)["id"])
+
+
+@pytest.mark.parametrize("cfg,scale", [(1, 0.25), (1, 1.0), (2, 1 / 16)])
+def test_fof_partition(rk, oracle, cfg, scale):
+    p, box, mp, _ = rk.synth(cfg, scale)
+    c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    oracle.setup(c)
+    ro = oracle.fof(p)
+    rg = rk.rockstar_fof(p, c)
+    assert len(rg[0]) == len(ro[0])
+    assert len(rg[1]) == len(ro[1])
+    assert np.array_equal(canon_partition(*rg), canon_partition(*ro))
+    # every particle is present exactly once
+    assert np.array_equal(np.sort(rg[0]["id"]), np.sort(ro[0]["id"]))
+
+
+def test_fof_duplicates(rk, oracle):
+    """Duplicate positions / ids are removed as src/rockstar.c:379-396 does."""
+    p, box, mp, _ = rk.synth(1, 0.05)
+    p = p.copy()
+    p["pos"][10] = p["pos"][11]
+    p["pos"][200] = p["pos"][3000]
+    p["id"][500] = p["id"][501]
+    c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    oracle.setup(c)
+    ro = oracle.fof(p)
+    rg = rk.rockstar_fof(p, c)
+    assert len(rg[0]) == len(ro[0]) < len(p)
+    assert np.array_equal(np.sort(rg[0]["id"]), np.sort(ro[0]["id"]))
+    assert np.array_equal(canon_partition(*rg), canon_partition(*ro))
+
+
+def test_fof_empty_and_tiny(rk):
+    c = rk.Config()
+    for n in (0, 1, 2, 15):
+        p = np.zeros(n, rk.PARTICLE)
+        p["id"] = np.arange(n)
+        p["pos"][:, :3] = np.linspace(0, 0.01, n)[:, None]
+        out, off, sz = rk.rockstar_fof(p, c)
+        assert len(out) == n
+        assert (len(off) == 1) == (n >= 10)
