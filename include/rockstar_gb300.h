@@ -111,6 +111,22 @@ int rsg_rockstar_fof(struct rsg_particle *p, int64_t *num_p, const struct rsg_co
                      int64_t *fof_offsets, int64_t *fof_sizes, int64_t max_fofs,
                      int64_t *num_fofs);
 
+/* Substructure, particle assignment, potentials and halo properties for every
+ * group: replaces the per-group calls find_subs(f, fofinfo, haloinfo)
+ * (src/groupies.c:669-708) as the OpenMP loop of src/mpi_main.cpp:1363-1389
+ * issues them, followed by copy_halos (src/mpi_main.cpp:1335-1361).
+ * Groups i = 0..num_fofs-1 are p[fof_offsets[i] .. + fof_sizes[i]) and must
+ * not overlap.  Each group's particles are permuted in place exactly as the
+ * reference permutes f->particles (halos contiguous, sorted by distance at
+ * the top level).  Halos of all groups are written in group order to
+ * halos/extra (capacity max_halos); p_start is relative to p and the
+ * child/sub_of links are indices into the output, as copy_halos leaves
+ * them.  One call with num_fofs == 1 is the plain per-group drop-in. */
+int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offsets,
+                  const int64_t *fof_sizes, int64_t num_fofs, const struct rsg_config *cfg,
+                  struct rsg_halo *halos, struct rsg_extra_halo_info *extra, int64_t max_halos,
+                  int64_t *num_halos);
+
 #ifdef __cplusplus
 }
 #endif

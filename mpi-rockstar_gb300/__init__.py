@@ -51,6 +51,9 @@ def lib():
         h.rsg_config_setup.argtypes = [vp]
         h.rsg_rockstar_fof.argtypes = [vp, vp, vp, vp, vp, i64, vp]
         h.rsg_debug_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
+        h.rsg_debug_hierarchy.restype = i64
+        h.rsg_debug_hierarchy.argtypes = [vp, vp, vp, i64]
+        h.rsg_find_subs.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, i64, vp]
         for name, args in _EXTRA_SIGS.items():
             if hasattr(h, name):
                 getattr(h, name).argtypes = args
@@ -87,6 +90,34 @@ def rockstar_fof(parts, cfg):
                                   sz.ctypes.data, cap, nf.ctypes.data))
     k = int(nf[0])
     return pa[:n[0]].copy(), off[:k].copy(), sz[:k].copy()
+
+
+def find_subs(parts, offsets, sizes, cfg):
+    """Substructure + halo properties for every group (batched).  Returns
+    (particles after find_subs, halos, extra)."""
+    st = setup_config(cfg)
+    pa = np.array(parts, dtype=PARTICLE, copy=True)
+    off = np.ascontiguousarray(offsets, np.int64)
+    sz = np.ascontiguousarray(sizes, np.int64)
+    cap = int(sz.sum()) // 2 + len(sz) + 16
+    h = np.zeros(cap, HALO)
+    e = np.zeros(cap, EXTRA)
+    nh = np.zeros(1, np.int64)
+    _check(lib().rsg_find_subs(pa.ctypes.data, len(pa), off.ctypes.data, sz.ctypes.data, len(sz),
+                               C.byref(st), h.ctypes.data, e.ctypes.data, cap, nh.ctypes.data))
+    k = int(nh[0])
+    return pa, h[:k].copy(), e[:k].copy()
+
+
+def debug_hierarchy():
+    """(level, size, target_r) of every subgroup node of the last find_subs."""
+    cap = 1 << 22
+    lv = np.zeros(cap, np.int32)
+    n = np.zeros(cap, np.int32)
+    tr = np.zeros(cap, np.float32)
+    k = lib().rsg_debug_hierarchy(lv.ctypes.data, n.ctypes.data, tr.ctypes.data, cap)
+    k = min(k, cap)
+    return lv[:k].copy(), n[:k].copy(), tr[:k].copy()
 
 
 def tree_order(parts, dim, leaf):

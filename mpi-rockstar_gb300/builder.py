@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 INC = os.path.join(ROOT, "include")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", ARCH, "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", ARCH, "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xptxas", "-O3", "--expt-relaxed-constexpr", "-I", INC, "-I", CSRC]
 LIB = os.path.join(OUT, "librockstar_gb300.so")
 SYNTH = os.path.join(OUT, "libsynth.so")

@@ -6,8 +6,12 @@
 #include <vector>
 
 #include "kdtree_impl.cuh"
+#include "subs.cuh"
 
 namespace rsg {
+
+extern std::vector<int32_t> g_dbg_level, g_dbg_start, g_dbg_n;
+extern std::vector<float> g_dbg_target;
 
 struct FofOut {
     int64_t num_p;
@@ -145,6 +149,60 @@ int rsg_rockstar_fof(struct rsg_particle *p, int64_t *num_p, const struct rsg_co
     } catch (Failure &) {
         return error_code();
     }
+}
+
+int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offsets,
+                  const int64_t *fof_sizes, int64_t num_fofs, const struct rsg_config *cfg,
+                  struct rsg_halo *halos, struct rsg_extra_halo_info *extra, int64_t max_halos,
+                  int64_t *num_halos) {
+    if (!p || !cfg || !num_halos || num_p < 0 || num_fofs < 0 ||
+        (num_fofs && (!fof_offsets || !fof_sizes))) {
+        set_error(RSG_ERR_ARGS, "rsg_find_subs: bad arguments");
+        return RSG_ERR_ARGS;
+    }
+    try {
+        Ctx &C = ctx();
+        int64_t M = 0;
+        for (int64_t g = 0; g < num_fofs; g++) M += fof_sizes[g] > 0 ? fof_sizes[g] : 0;
+        *num_halos = 0;
+        if (M == 0) return RSG_OK;
+        int64_t hcap = M / 2 + num_fofs + 16;
+        C.ar.reserve((size_t)M * 900 + (size_t)num_p * 64 + (size_t)hcap * 360 + (256u << 20));
+        C.ar.reset();
+        rsg_particle *d_p = C.ar.get<rsg_particle>(num_p);
+        rsg_halo *d_h = C.ar.get<rsg_halo>(hcap);
+        rsg_extra_halo_info *d_e = C.ar.get<rsg_extra_halo_info>(hcap);
+        RSG_CUDA(cudaMemcpyAsync(d_p, p, sizeof(rsg_particle) * num_p, cudaMemcpyHostToDevice, C.st));
+        SubsOut o = find_subs_device(C.ar, d_p, num_p, fof_offsets, fof_sizes, num_fofs, *cfg,
+                                     d_h, d_e, hcap, C.st);
+        if (o.nhalos > max_halos) {
+            set_error(RSG_ERR_ARGS, "rsg_find_subs: %lld halos exceed max_halos %lld",
+                      (long long)o.nhalos, (long long)max_halos);
+            return RSG_ERR_ARGS;
+        }
+        RSG_CUDA(cudaMemcpyAsync(p, d_p, sizeof(rsg_particle) * num_p, cudaMemcpyDeviceToHost, C.st));
+        if (o.nhalos) {
+            RSG_CUDA(cudaMemcpyAsync(halos, d_h, sizeof(rsg_halo) * o.nhalos, cudaMemcpyDeviceToHost, C.st));
+            RSG_CUDA(cudaMemcpyAsync(extra, d_e, sizeof(rsg_extra_halo_info) * o.nhalos, cudaMemcpyDeviceToHost, C.st));
+        }
+        RSG_CUDA(cudaStreamSynchronize(C.st));
+        *num_halos = o.nhalos;
+        return RSG_OK;
+    } catch (Failure &) {
+        return error_code();
+    }
+}
+
+// Test hook: the subgroup hierarchy of the last rsg_find_subs call on this
+// thread: per node its level, size and 6D linking length (normalised units).
+int64_t rsg_debug_hierarchy(int32_t *level, int32_t *n, float *target_r, int64_t cap) {
+    int64_t k = (int64_t)rsg::g_dbg_level.size();
+    for (int64_t i = 0; i < k && i < cap; i++) {
+        level[i] = rsg::g_dbg_level[i];
+        n[i] = rsg::g_dbg_n[i];
+        target_r[i] = rsg::g_dbg_target[i];
+    }
+    return k;
 }
 
 // Test hook: kd-tree permutation of the particle records alone (dim 3 or 6,

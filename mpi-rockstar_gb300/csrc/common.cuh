@@ -81,4 +81,7 @@ __device__ __forceinline__ float ord2f(unsigned u) {
 
 inline int nblk(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
+#define RSG_STACK 96
+#define RSG_STACK6 128
+
 }  // namespace rsg

@@ -26,7 +26,6 @@
 
 namespace rsg {
 
-#define RSG_STACK 96
 
 struct TravStatus {
     int *flag;  // set to 1 when a traversal stack overflows

@@ -69,8 +69,23 @@ __device__ __forceinline__ int poisson_or_force(const rsg_halo &h1, const rsg_ha
     return 0;
 }
 
-// Cyclic 3x3 Jacobi with the 1e-6 change rule, src/jacobi.c:9-138 (the
-// reference evaluates two rotation scalars in long double; double here).
+// round_to_double(a + sqrt(x)) with the sum taken before rounding, as the
+// reference's `fabsl(a) + sqrtl(x)` in a wide long double does: sqrt(x) is
+// carried as hi + lo (lo from the exact FMA residual), the sum with a is
+// formed by an error-free transformation and rounded once.
+__device__ __forceinline__ double abs_plus_sqrt(double a, double x) {
+    double hi = sqrt(x);
+    if (!(hi > 0) || isinf(hi)) return a + hi;
+    double lo = fma(-hi, hi, x) / (2.0 * hi);
+    double sum = a + hi;
+    double bb = sum - a;
+    double err = (a - (sum - bb)) + (hi - bb);
+    return sum + (err + lo);
+}
+
+// Cyclic 3x3 Jacobi with the 1e-6 change rule, src/jacobi.c:9-138; the
+// rotation's t is rounded once from an extended sum as the reference's
+// long double expression is, s = sqrt of a double needs no extension.
 __device__ inline void jacobi3(double a[3][3], double eig[3], double v[3][3]) {
     int maxc[3], chg[3], n = 3, state = 0;
     double mx, c, s, t, u, w;
@@ -110,7 +125,7 @@ __device__ inline void jacobi3(double a[3][3], double eig[3], double v[3][3]) {
         mx = a[k][l];
         if (mx == 0) break;
         w = (eig[l] - eig[k]) * 0.5;
-        t = fabs(w) + sqrt(mx * mx + w * w);
+        t = abs_plus_sqrt(fabs(w), mx * mx + w * w);
         s = sqrt(mx * mx + t * t);
         c = t / s;
         s = mx / s;

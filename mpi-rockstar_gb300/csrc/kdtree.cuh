@@ -25,6 +25,8 @@
 #include <thrust/iterator/counting_iterator.h>
 #include <thrust/iterator/transform_iterator.h>
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace rsg {
@@ -64,6 +66,8 @@ struct Forest {
     KNode<D> *nodes = nullptr;  // nodes[t] is the root of tree t
     int32_t nnodes = 0;
     int32_t ntrees = 0;
+    // nodes created by level l of the build are [lv_first[l], lv_first[l+1])
+    std::vector<int32_t> lv_first;
 };
 
 // ---- kernels ------------------------------------------------------------

@@ -117,6 +117,8 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
     RSG_CUDA(cudaMemcpyAsync(&nact, cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     int32_t nnodes = ntrees;
+    F.lv_first.push_back(0);
+    F.lv_first.push_back(ntrees);
     int level = 0;
     while (nact > 0) {
         if (++level > 4096) {
@@ -147,6 +149,7 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
         int32_t base = nnodes;
         k_children<D><<<nblk(nact, T), T, 0, st>>>(nodes, act, nact, m_arr, soff, base, bmin, bmax);
         nnodes += 2 * nsplit;
+        F.lv_first.push_back(nnodes);
         k_owner_update<D><<<nblk(nrec, T), T, 0, st>>>(nodes, nrec, owner, box_owner, leaf);
         if (nsplit > 0) {
             k_box_runs<D, RecT, IT><<<nblk((nrec + IT - 1) / IT, T), T, 0, st>>>(

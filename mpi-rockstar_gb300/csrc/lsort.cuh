@@ -1,0 +1,216 @@
+// Exact GPU version of partition_sort_particles (src/fof.c:184-224): each
+// segment is split at the midpoint of its label range with the same
+// two-pointer swap that the kd-tree build uses (closed form in kdtree.cuh),
+// then both halves recurse.  Runs level-synchronously over many segments.
+#pragma once
+#include "kdtree.cuh"
+
+namespace rsg {
+
+struct LSeg {
+    int32_t *start, *n;   // active segments
+    int32_t *mn, *mx;     // label range
+    int32_t *pivot, *m, *q;
+};
+
+__global__ void k_ls_owner(const int32_t *start, const int32_t *n, int32_t *owner) {
+    int k = blockIdx.x;
+    int s = start[k], c = n[k];
+    for (int i = threadIdx.x; i < c; i += blockDim.x) owner[s + i] = k;
+}
+__global__ void k_ls_init(LSeg S, int32_t ns) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns) return;
+    S.mn[k] = 0x7fffffff;
+    S.mx[k] = (int32_t)0x80000000;
+}
+template <int ITEMS>
+__global__ void k_ls_minmax(const int32_t *lab, int64_t M, const int32_t *owner, LSeg S) {
+    int64_t i0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * ITEMS;
+    if (i0 >= M) return;
+    int cur = -1, lo = 0x7fffffff, hi = (int)0x80000000;
+    for (int it = 0; it < ITEMS; it++) {
+        int64_t i = i0 + it;
+        if (i >= M) break;
+        int a = owner[i];
+        if (a != cur) {
+            if (cur >= 0) {
+                atomicMin(&S.mn[cur], lo);
+                atomicMax(&S.mx[cur], hi);
+            }
+            cur = a;
+            lo = 0x7fffffff;
+            hi = (int)0x80000000;
+        }
+        if (a < 0) continue;
+        int v = lab[i];
+        lo = min(lo, v);
+        hi = max(hi, v);
+    }
+    if (cur >= 0) {
+        atomicMin(&S.mn[cur], lo);
+        atomicMax(&S.mx[cur], hi);
+    }
+}
+// pivot = min + (max - min) / 2 (src/fof.c:201); segments whose labels are
+// all equal are finished (no element is "big").
+__global__ void k_ls_pivot(LSeg S, int32_t ns) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns) return;
+    int64_t lo = S.mn[k], hi = S.mx[k];
+    S.pivot[k] = (lo == hi) ? 0x7fffffff : (int32_t)(lo + (hi - lo) / 2);
+}
+__global__ void k_ls_flags(const int32_t *lab, int64_t M, const int32_t *owner, LSeg S,
+                           int32_t *flag) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i > M) return;
+    int f = 0;
+    if (i < M) {
+        int a = owner[i];
+        if (a >= 0) f = lab[i] > S.pivot[a];
+    }
+    flag[i] = f;
+}
+__global__ void k_ls_counts(LSeg S, int32_t ns, const int32_t *rank) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns) return;
+    int s = S.start[k], n = S.n[k];
+    int B = rank[s + n] - rank[s];
+    int m = n - B;
+    S.m[k] = m;
+    S.q[k] = rank[s + m] - rank[s];
+}
+__global__ void k_ls_tables(int64_t M, const int32_t *owner, LSeg S, const int32_t *flag,
+                            const int32_t *rank, int32_t *fb, int32_t *bs) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int a = owner[i];
+    if (a < 0) return;
+    int s = S.start[a];
+    int l = (int)(i - s);
+    int br = rank[i] - rank[s];
+    int sr = l - br;
+    int m = S.m[a];
+    if (flag[i] && l < m) fb[s + br] = l;
+    if (!flag[i] && l >= m) bs[s + (m - 1 - sr)] = l;
+}
+template <class T>
+__global__ void k_ls_scatter(int64_t M, const int32_t *owner, LSeg S, const int32_t *flag,
+                             const int32_t *rank, const int32_t *fb, const int32_t *bs,
+                             const T *src, T *dst, const int32_t *lsrc, int32_t *ldst) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int a = owner[i];
+    if (a < 0) return;
+    int s = S.start[a], n = S.n[a];
+    int l = (int)(i - s);
+    int br = rank[i] - rank[s];
+    int sr = l - br;
+    int m = S.m[a], q = S.q[a];
+    int big = flag[i];
+    int d;
+    if (!big && l < m) d = l;
+    else if (big && l < m) d = (br == 0) ? n - 1 : bs[s + br - 1] - 1;
+    else if (!big) d = fb[s + (m - 1 - sr)];
+    else {
+        int pos_last = (q > 0) ? bs[s + q - 1] : n;
+        if (l > pos_last) d = l - 1;
+        else if (pos_last - m >= 2) d = (l == m) ? pos_last - 1 : l - 1;
+        else d = l;
+    }
+    dst[s + d] = src[i];
+    ldst[s + d] = lsrc[i];
+}
+template <class T>
+__global__ void k_ls_copy(int64_t M, const int32_t *owner, const T *src, T *dst,
+                          const int32_t *lsrc, int32_t *ldst) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M || owner[i] < 0) return;
+    dst[i] = src[i];
+    ldst[i] = lsrc[i];
+}
+// next round: both halves of every split segment with >= 2 elements
+__global__ void k_ls_next(LSeg S, int32_t ns, int32_t *ns_start, int32_t *ns_n, int32_t *flag) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns) return;
+    int s = S.start[k], n = S.n[k], m = S.m[k];
+    bool split = S.mn[k] != S.mx[k];
+    ns_start[2 * k] = s;
+    ns_n[2 * k] = m;
+    ns_start[2 * k + 1] = s + m;
+    ns_n[2 * k + 1] = n - m;
+    flag[2 * k] = split && m >= 2;
+    flag[2 * k + 1] = split && (n - m) >= 2;
+}
+
+// Sorts W (and its labels) inside every segment (host arrays hs/hn) the way
+// the reference's recursive partition does.
+template <class T>
+void partition_sort_labels(Arena &ar, T *W, int32_t *lab, int64_t M,
+                           const std::vector<int32_t> &hs, const std::vector<int32_t> &hn,
+                           cudaStream_t st);
+
+}  // namespace rsg
+
+namespace rsg {
+
+template <class T>
+void partition_sort_labels(Arena &ar, T *W, int32_t *lab, int64_t M,
+                           const std::vector<int32_t> &hs, const std::vector<int32_t> &hn,
+                           cudaStream_t st) {
+    std::vector<int32_t> s0, n0;
+    for (size_t k = 0; k < hs.size(); k++)
+        if (hn[k] >= 2) {
+            s0.push_back(hs[k]);
+            n0.push_back(hn[k]);
+        }
+    int32_t ns = (int32_t)s0.size();
+    if (ns == 0) return;
+    const int T_ = 256;
+    size_t mark = ar.used;
+    int64_t cap = (int64_t)ns > M / 2 + 1 ? ns : M / 2 + 1;
+    LSeg S;
+    S.start = ar.get<int32_t>(cap); S.n = ar.get<int32_t>(cap);
+    S.mn = ar.get<int32_t>(cap); S.mx = ar.get<int32_t>(cap);
+    S.pivot = ar.get<int32_t>(cap); S.m = ar.get<int32_t>(cap); S.q = ar.get<int32_t>(cap);
+    int32_t *nst = ar.get<int32_t>(2 * cap), *nn = ar.get<int32_t>(2 * cap);
+    int32_t *nflag = ar.get<int32_t>(2 * cap);
+    int32_t *owner = ar.get<int32_t>(M), *flag = ar.get<int32_t>(M + 1), *rank = ar.get<int32_t>(M + 1);
+    int32_t *fb = ar.get<int32_t>(M), *bs = ar.get<int32_t>(M);
+    T *tw = ar.get<T>(M);
+    int32_t *tl = ar.get<int32_t>(M);
+    int *cnt = ar.get<int>(1);
+    size_t b1 = 0, b2 = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b1, flag, rank, (int)(M + 1), st);
+    cub::DeviceSelect::Flagged(nullptr, b2, nst, nflag, S.start, cnt, (int)(2 * cap), st);
+    void *tmp = ar.take((b1 > b2 ? b1 : b2) + 256);
+    size_t tb = (b1 > b2 ? b1 : b2) + 256;
+    RSG_CUDA(cudaMemcpyAsync(S.start, s0.data(), 4 * ns, cudaMemcpyHostToDevice, st));
+    RSG_CUDA(cudaMemcpyAsync(S.n, n0.data(), 4 * ns, cudaMemcpyHostToDevice, st));
+    for (int round = 0; ns > 0; round++) {
+        if (round > 200) {
+            set_error(RSG_ERR_LIMIT, "label partition sort did not terminate");
+            throw Failure();
+        }
+        RSG_CUDA(cudaMemsetAsync(owner, 0xff, 4 * M, st));
+        k_ls_owner<<<ns, T_, 0, st>>>(S.start, S.n, owner);
+        k_ls_init<<<nblk(ns, T_), T_, 0, st>>>(S, ns);
+        k_ls_minmax<8><<<nblk((M + 7) / 8, T_), T_, 0, st>>>(lab, M, owner, S);
+        k_ls_pivot<<<nblk(ns, T_), T_, 0, st>>>(S, ns);
+        k_ls_flags<<<nblk(M + 1, T_), T_, 0, st>>>(lab, M, owner, S, flag);
+        cub::DeviceScan::ExclusiveSum(tmp, tb, flag, rank, (int)(M + 1), st);
+        k_ls_counts<<<nblk(ns, T_), T_, 0, st>>>(S, ns, rank);
+        k_ls_tables<<<nblk(M, T_), T_, 0, st>>>(M, owner, S, flag, rank, fb, bs);
+        k_ls_scatter<T><<<nblk(M, T_), T_, 0, st>>>(M, owner, S, flag, rank, fb, bs, W, tw, lab, tl);
+        k_ls_copy<T><<<nblk(M, T_), T_, 0, st>>>(M, owner, tw, W, tl, lab);
+        k_ls_next<<<nblk(ns, T_), T_, 0, st>>>(S, ns, nst, nn, nflag);
+        cub::DeviceSelect::Flagged(tmp, tb, nst, nflag, S.start, cnt, 2 * ns, st);
+        cub::DeviceSelect::Flagged(tmp, tb, nn, nflag, S.n, cnt, 2 * ns, st);
+        RSG_CHECK_LAUNCH();
+        RSG_CUDA(cudaMemcpyAsync(&ns, cnt, 4, cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+    }
+    ar.used = mark;
+}
+
+}  // namespace rsg

@@ -1,0 +1,822 @@
+// Halo properties after the hierarchy is settled: calc_additional_halo_props
+// (src/properties.c:513-556) for every halo of the call at once.
+//
+//  1. particle sets: the halo, its children (recursively) and, when the host
+//     is not much larger, the host's particles as potential-only sources
+//     (calc_particle_radii, src/groupies.c:212-270);
+//  2. potentials: the reference's Barnes-Hut code reproduced on the GPU -- a
+//     forest of kd-trees (10 points per leaf, exact fast3tree permutation),
+//     mass centres and opening radii bottom-up, and one thread per leaf
+//     walking the tree in the reference's order so every FP64 sum matches
+//     (src/potential.c:22-192);
+//  3. potential-only particles dropped, the rest sorted by r^2;
+//  4. core velocity, kinetic energy, then the density/shape/NFW scans for
+//     all particles and for bound particles (src/properties.c:165-510).
+#include <cub/cub.cuh>
+
+#include "halo_math.cuh"
+#include "kdtree_impl.cuh"
+
+namespace rsg {
+
+struct Seg {
+    int32_t src, n, dst, halo;
+    int32_t pot_only, flag;
+};
+
+struct Frame {
+    int32_t x, child, stage, pot;
+};
+
+// calc_particle_radii as an explicit depth-first walk; emit(x, pot_only)
+// for every visited halo in the reference's order.  The loop guard of
+// src/groupies.c:241-247 checks the halos on the current path.
+template <class F>
+__device__ bool walk_sets(const rsg_halo *H, const rsg_extra_halo_info *E, int base,
+                          double ratio, F emit) {
+    Frame st[64];
+    int sp = 0;
+    st[sp++] = Frame{base, -1, 0, 0};
+    int guard = 0;
+    while (sp) {
+        if (++guard > 10000000) return false;
+        Frame &f = st[sp - 1];
+        if (f.stage == 0) {
+            bool loop = false;
+            for (int j = 0; j < sp - 1; j++)
+                if (st[j].x == f.x) loop = true;
+            if (loop) {
+                sp--;
+                continue;
+            }
+            emit(f.x, f.pot);
+            f.child = (int32_t)E[f.x].child;
+            f.stage = 1;
+        }
+        if (f.stage == 1) {
+            if (f.child > -1) {
+                int c = f.child;
+                f.child = (int32_t)E[c].next_cochild;
+                if (sp >= 64) return false;
+                st[sp++] = Frame{c, -1, 0, f.pot};
+                continue;
+            }
+            f.stage = 2;
+            if (sp == 1) {
+                int64_t par = E[f.x].sub_of;
+                if (par > -1 &&
+                    ((double)H[par].num_child_particles * ratio < (double)H[f.x].num_child_particles)) {
+                    st[sp++] = Frame{(int32_t)par, -1, 0, 1};
+                    continue;
+                }
+            }
+        }
+        sp--;
+    }
+    return true;
+}
+
+__global__ void k_set_count(const rsg_halo *H, const rsg_extra_halo_info *E, int32_t NH,
+                            double ratio, int32_t *tot, int32_t *nseg, int *err) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h > NH) return;
+    if (h == NH) {
+        tot[h] = 0;
+        nseg[h] = 0;
+        return;
+    }
+    int t = 0, s = 0;
+    if (H[h].num_p >= 1) {
+        bool ok = walk_sets(H, E, h, ratio, [&](int x, int pot) {
+            t += (int)H[x].num_p;
+            s++;
+        });
+        if (!ok) atomicExch(err, 1);
+    }
+    tot[h] = t;
+    nseg[h] = s;
+}
+
+__global__ void k_set_segs(const rsg_halo *H, const rsg_extra_halo_info *E, int32_t NH,
+                           double ratio, const int32_t *toff, const int32_t *soff, Seg *segs) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= NH || H[h].num_p < 1) return;
+    int dst = toff[h], k = soff[h];
+    int64_t bnp = H[h].num_p;
+    walk_sets(H, E, h, ratio, [&](int x, int pot) {
+        int flag = 0;
+        if (x == h) flag = 1;
+        if (!pot && ((double)H[x].num_p < (double)bnp * 0.03)) flag = 2;
+        segs[k++] = Seg{(int32_t)H[x].p_start, (int32_t)H[x].num_p, dst, h, pot, flag};
+        dst += (int)H[x].num_p;
+    });
+}
+
+// _reset_potentials (src/groupies.c:212-233)
+__global__ void k_set_fill(const Seg *segs, const Rec *W, const rsg_halo *H, PotRec *PO) {
+    Seg sg = segs[blockIdx.x];
+    float c0 = H[sg.halo].pos[0], c1 = H[sg.halo].pos[1], c2 = H[sg.halo].pos[2];
+    for (int i = threadIdx.x; i < sg.n; i += blockDim.x) {
+        const Rec &q = W[sg.src + i];
+        PotRec r;
+#pragma unroll
+        for (int d = 0; d < 6; d++) r.pos[d] = q.pos[d];
+        float dx, r2 = 0.f;
+        dx = fsub(q.pos[0], c0); r2 = fadd(r2, fmul(dx, dx));
+        dx = fsub(q.pos[1], c1); r2 = fadd(r2, fmul(dx, dx));
+        dx = fsub(q.pos[2], c2); r2 = fadd(r2, fmul(dx, dx));
+        r.r2 = r2;
+        r.pad = __int_as_float(sg.halo);
+        r.pe = 0;
+        r.ke = sg.pot_only ? -1.f : 0.f;
+        r.flags = sg.flag;
+        PO[sg.dst + i] = r;
+    }
+}
+
+// ---- Barnes-Hut ---------------------------------------------------------
+__device__ __forceinline__ double d2d(const float *a, const float *b) {
+    double r2 = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        double dx = (double)fsub(a[k], b[k]);
+        r2 = dadd(r2, dmul(dx, dx));
+    }
+    return r2;
+}
+
+struct BHNode {
+    float mc[3], m, dmin;
+};
+
+// src/potential.c:71-82 over the node's points
+__device__ float node_dmin(const PotRec *PO, int s, int n, const float *mc) {
+    double sx = 0, bm = 0;
+    for (int i = 0; i < n; i++) {
+        double dx = d2d(mc, PO[s + i].pos);
+        if (bm < dx) bm = dx;
+        sx += dx;
+    }
+    bm = sqrt(bm) / 2.0;
+    return (float)(bm + sqrt(bm * bm + sx / (n * 1.0)));
+}
+
+// leaves: mass and mass centre from their points (src/potential.c:101-113)
+__global__ void k_bh_leaf(const KNode<3> *nodes, int32_t nn, const PotRec *PO, double mp,
+                          BHNode *B) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nn) return;
+    const KNode<3> &x = nodes[a];
+    if (x.div >= 0) return;
+    double pos[3] = {0, 0, 0};
+    for (int i = 0; i < x.n; i++)
+        for (int j = 0; j < 3; j++) pos[j] += (double)PO[x.start + i].pos[j];
+    BHNode b;
+    b.m = (float)(mp * x.n);
+    for (int j = 0; j < 3; j++) b.mc[j] = pos[j] ? (float)(pos[j] / (double)x.n) : 0.f;
+    b.dmin = node_dmin(PO, x.start, x.n, b.mc);
+    B[a] = b;
+}
+// internal nodes of one build level (src/potential.c:115-123)
+__global__ void k_bh_internal(const KNode<3> *nodes, int32_t first, int32_t count,
+                              const PotRec *PO, BHNode *B) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int a = first + k;
+    const KNode<3> &x = nodes[a];
+    if (x.div < 0) return;
+    const BHNode &L = B[x.left], &R = B[x.left + 1];
+    BHNode b;
+    b.m = fadd(L.m, R.m);
+    for (int j = 0; j < 3; j++)
+        b.mc[j] = b.m ? __fdiv_rn(fadd(fmul(R.mc[j], R.m), fmul(L.mc[j], L.m)), b.m) : 0.f;
+    b.dmin = node_dmin(PO, x.start, x.n, b.mc);
+    B[a] = b;
+}
+
+// _compute_monopole_potentials(leaf, root) (src/potential.c:133-168)
+__global__ void k_bh_walk(const KNode<3> *nodes, const int32_t *leaves, int32_t nl,
+                          const BHNode *B, PotRec *PO, double mp, double force_res, int *err) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl) return;
+    int a = leaves[t];
+    const KNode<3> &n = nodes[a];
+    const BHNode bn = B[a];
+    int stack[RSG_STACK];
+    int sp = 0;
+    stack[sp++] = n.tree;
+    while (sp) {
+        int b = stack[--sp];
+        const KNode<3> &n2 = nodes[b];
+        if (b == a) {
+            if (n.n > 20) continue;  // degenerate leaf
+            for (int i = 0; i < n.n; i++)
+                for (int j = i + 1; j < n.n; j++) {
+                    double r = sqrt(d2d(PO[n.start + i].pos, PO[n.start + j].pos));
+                    if (r < force_res) r = force_res;
+                    double dpo = mp * (1.0 / r);
+                    PO[n.start + i].pe += dpo;
+                    PO[n.start + j].pe += dpo;
+                }
+            continue;
+        }
+        int i;
+        for (i = 0; i < 3; i++)
+            if (n.mn[i] < n2.mn[i] || n.mx[i] > n2.mx[i]) break;
+        bool open = (i == 3);
+        if (!open) {
+            float r2 = (float)d2d(bn.mc, B[b].mc);
+            open = !(r2 > fmul(B[b].dmin, B[b].dmin));
+        }
+        if (open) {
+            if (n2.div < 0) {
+                for (int p = 0; p < n.n; p++)
+                    for (int q = 0; q < n2.n; q++) {
+                        double r = sqrt(d2d(PO[n.start + p].pos, PO[n2.start + q].pos));
+                        if (r < force_res) r = force_res;
+                        PO[n.start + p].pe += mp * (1.0 / r);
+                    }
+            } else {
+                if (sp + 2 > RSG_STACK) {
+                    atomicExch(err, 1);
+                    return;
+                }
+                stack[sp++] = n2.left + 1;
+                stack[sp++] = n2.left;
+            }
+        } else {
+            for (int p = 0; p < n.n; p++) {
+                float r = (float)sqrt(d2d(PO[n.start + p].pos, B[b].mc));
+                PO[n.start + p].pe += (double)__fdiv_rn(B[b].m, r);
+            }
+        }
+    }
+}
+
+// ---- sort keys: drop potential-only records, order by r^2 ----------------
+__global__ void k_po_keys(const PotRec *PO, int64_t n, uint64_t *key, uint32_t *val) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const PotRec &r = PO[i];
+    uint64_t h = (uint64_t)__float_as_int(r.pad);
+    uint64_t drop = r.ke < 0 ? 1 : 0;
+    key[i] = (h << 33) | (drop << 32) | (uint64_t)f2ord(r.r2);
+    val[i] = (uint32_t)i;
+}
+__global__ void k_po_gather(const PotRec *src, const uint32_t *perm, int64_t n, PotRec *dst) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[perm[i]];
+}
+
+// ---- per-halo scans (src/properties.c:165-510) ---------------------------
+__device__ double hubble_scaling_d(const DevCfg &c, double z) {
+    double z1 = 1.0 + z, a = 1.0 / z1;
+    double we = (a != 1.0) ? c.w0 + c.wa - c.wa * (a - 1.0) / log(a) : c.w0;
+    return sqrt(c.om * (z1 * z1 * z1) + c.ol * pow(a, -3.0 * (1.0 + we)));
+}
+
+// calculate_corevel
+__device__ void corevel(rsg_halo &h, const PotRec *q, int64_t tot, const DevCfg &C) {
+    double vel[3] = {0, 0, 0}, var[3] = {0, 0, 0}, tv, bv = 0;
+    double rt = C.rvir_dens * (4.0 * M_PI / 3.0);
+    int64_t j, cmax, rmax;
+    for (j = tot - 1; j >= 0; j--) {
+        float r2 = q[j].r2;
+        if ((double)(j * j) > (double)fmul(fmul(r2, r2), r2) * (rt * rt)) break;
+    }
+    rmax = j;
+    if (rmax < 1) return;
+    for (j = tot - 1; j >= 0; j--)
+        if ((double)q[j].r2 * 100.0 < (double)q[rmax].r2) break;
+    cmax = j;
+    if (cmax < 100) cmax = 100;
+    for (int64_t i = 0; i < rmax; i++) {
+        for (int k = 0; k < 3; k++) {
+            double dl = (double)q[i].pos[k + 3] - vel[k];
+            vel[k] += dl / ((double)(i + 1));
+            var[k] += dl * ((double)q[i].pos[k + 3] - vel[k]);
+        }
+        tv = (var[0] + var[1] + var[2]);
+        if ((i < 10) || (tv < bv * (i - 3) * i)) {
+            if (i > 3) bv = tv / (double)((i - 3) * i);
+            else bv = 0;
+            if (i < cmax) {
+                h.n_core = i;
+                h.min_vel_err = (float)bv;
+                for (int k = 0; k < 3; k++) h.corevel[k] = (float)vel[k];
+            }
+            for (int k = 0; k < 3; k++) h.bulkvel[k] = (float)vel[k];
+            h.min_bulkvel_err = (float)bv;
+        }
+    }
+    for (int k = 0; k < 3; k++) h.pos[k + 3] = h.corevel[k];
+}
+
+// compute_kinetic_energy (src/potential.c:194-211)
+__device__ void kinetic(PotRec *q, int64_t n, const float *vc, const float *pc, float scale,
+                        const DevCfg &C) {
+    double conv = 0.5 * (double)scale / RSG_GC, z1 = 1.0 / (double)scale;
+    double hub = 100.0 * hubble_scaling_d(C, z1 - 1.0);
+    for (int64_t i = 0; i < n; i++) {
+        if (q[i].ke < 0) continue;
+        q[i].ke = 0;
+        for (int j = 0; j < 3; j++) {
+            double dv = (double)fsub(q[i].pos[j + 3], vc[j]) +
+                        hub * (double)scale * (double)fsub(q[i].pos[j], pc[j]);
+            q[i].ke = (float)((double)q[i].ke + dv * dv);
+        }
+        q[i].ke = (float)((double)q[i].ke * conv);
+    }
+}
+
+__device__ inline bool unbound(const PotRec &r) { return r.pe < (double)r.ke; }
+
+// calc_shape (src/properties.c:216-326)
+__device__ void shape(rsg_halo &h, const PotRec *po, int64_t tot, int bound, const DevCfg &C) {
+    int64_t it = C.shape_iterations, an = 0;
+    float minr = fmul((float)C.force_res, (float)C.force_res);
+    double mt[3][3], orth[3][3], eig[3] = {0, 0, 0}, r = 0, dr, dr2, w = 0;
+    h.b_to_a = h.c_to_a = 0;
+    h.A[0] = h.A[1] = h.A[2] = 0;
+    if (!(h.r > 0)) return;
+    minr = (float)((double)minr * (1e6 / (double)fmul(h.r, h.r)));
+    for (int64_t j = 0; j < tot; j++) {
+        if (bound && unbound(po[j])) continue;
+        an++;
+    }
+    if (an < 3 || !(h.r > 0)) return;
+    if (an < it) it = an;
+    for (int i = 0; i < 3; i++) {
+        for (int k = 0; k < 3; k++) orth[i][k] = 0;
+        orth[i][i] = 1;
+        eig[i] = (double)fmul(h.r, h.r) * 1e-6;
+    }
+    for (int64_t i = 0; i < it; i++) {
+        for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) mt[k][l] = 0;
+        w = 0;
+        for (int64_t j = 0; j < tot; j++) {
+            if (bound && unbound(po[j])) continue;
+            r = 0;
+            for (int k = 0; k < 3; k++) {
+                dr = 0;
+                for (int l = 0; l < 3; l++) dr += orth[k][l] * (double)fsub(po[j].pos[l], h.pos[l]);
+                r += dr * dr / eig[k];
+            }
+            if (r < (double)minr) r = minr;
+            if (!(r > 0 && r <= 1)) continue;
+            double tw = (C.weighted_shapes) ? 1.0 / r : 1.0;
+            w += tw;
+            for (int k = 0; k < 3; k++) {
+                dr = (double)fsub(po[j].pos[k], h.pos[k]);
+                mt[k][k] += dr * dr * tw;
+                for (int l = 0; l < k; l++) {
+                    dr2 = (double)fsub(po[j].pos[l], h.pos[l]);
+                    mt[k][l] += dr2 * dr * tw;
+                    mt[l][k] = mt[k][l];
+                }
+            }
+        }
+        if (!w) return;
+        for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) mt[k][l] /= (double)w;
+        double mt2[3][3];
+        for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) mt2[k][l] = mt[k][l];
+        jacobi3(mt, eig, orth);
+        int a = 0, b = 1, c = 2;
+        if (eig[1] > eig[0]) {
+            b = 0;
+            a = 1;
+        }
+        if (eig[2] > eig[b]) {
+            c = b;
+            b = 2;
+        }
+        if (eig[b] > eig[a]) {
+            int t = a;
+            a = b;
+            b = t;
+        }
+        if (!eig[a] || !eig[b] || !eig[c]) return;
+        float ba = (float)sqrt(eig[b] / eig[a]);
+        float ca = (float)sqrt(eig[c] / eig[a]);
+        if ((fabs((double)fsub(ba, h.b_to_a)) < 0.01 * (double)h.b_to_a) &&
+            (fabs((double)fsub(ca, h.c_to_a)) < 0.01 * (double)h.c_to_a))
+            return;
+        h.b_to_a = (ba > 0) ? ba : 0;
+        h.c_to_a = (ca > 0) ? ca : 0;
+        r = sqrt(eig[a]);
+        for (int k = 0; k < 3; k++) {
+            h.A[k] = (float)(1e3 * r * orth[a][k]);
+            eig[k] *= ((double)fmul(h.r, h.r) * 1e-6) / (r * r);
+        }
+        h.inertia_tensor[0] = (float)mt2[0][0];
+        h.inertia_tensor[1] = (float)mt2[1][1];
+        h.inertia_tensor[2] = (float)mt2[2][2];
+        h.inertia_tensor[3] = (float)mt2[0][1];
+        h.inertia_tensor[4] = (float)mt2[1][2];
+        h.inertia_tensor[5] = (float)mt2[2][0];
+    }
+}
+
+// estimate_total_energy (src/properties.c:328-349)
+__device__ float total_energy(const PotRec *po, int64_t tot, float *ratio, const DevCfg &C) {
+    double phi = 0, tphi = 0, ke = 0, r;
+    for (int64_t i = tot - 1; i >= 0; i--) {
+        if (po[i].pe > (double)po[i].ke) {
+            ke += po[i].ke;
+            r = sqrt((double)po[i].r2);
+            if (r < C.force_res) r = C.force_res;
+            tphi += C.particle_mass * i / r + phi;
+            phi += C.particle_mass / r;
+        }
+    }
+    tphi /= 2.0;
+    *ratio = 0;
+    if (tphi) *ratio = (float)(ke / tphi);
+    float sn = (float)C.scale_now;
+    return (float)((ke - tphi) * C.particle_mass * RSG_GC / (double)sn);
+}
+
+// _calc_pseudo_evolution_masses (src/properties.c:351-382)
+__device__ void pseudo_masses(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
+                              const DevCfg &C) {
+    int64_t np_ = 0, npd = 0;
+    double r, r32, mx = 0, rpd = (double)h.rs * 4.0;
+    if (rpd < (double)h.r / 5.0) rpd = (double)h.r / 5.0;
+    rpd *= 1e-3;
+    for (int64_t j = 0; j < tot; j++) {
+        if (bound && unbound(po[j])) continue;
+        np_++;
+        r = sqrt((double)po[j].r2);
+        r32 = sqrt(r);
+        r32 = r32 * r32 * r32;
+        if ((double)(np_ * np_) / r32 > mx) mx = (double)(np_ * np_) / r32;
+        if (r < rpd) npd = np_;
+    }
+    h.m_pe_d = (float)(npd * C.particle_mass);
+    h.m_pe_b = (float)(C.particle_mass * pow(mx, 2.0 / 3.0) /
+                       cbrt(4.0 * M_PI * C.rvir_dens_z0 / 3.0));
+}
+
+// NFW pieces (src/nfw.c:14-173)
+__device__ double c_to_f(double c) {
+    double cp1 = 1.0 + c;
+    return (c * cp1 / (log1p(c) * cp1 - c));
+}
+__device__ double f_to_c(double f) {
+    double c = f, tc = c_to_f(c), nc;
+    for (int guard = 0; fabs((f - tc) / f) > 1e-7 && guard < 100000; guard++) {
+        double tc2 = c_to_f(c + 0.1), slope = (tc2 - tc) / 0.1;
+        nc = c + (f - tc) / slope;
+        if (nc < 0) c /= 2;
+        else c = nc;
+        tc = c_to_f(c);
+    }
+    return c;
+}
+__device__ float klypin_rs(float mvir, float rvir, float vmax, float rvmax, float scale) {
+    if (!mvir || !rvir || !vmax) return (float)((double)rvmax / RSG_RMAX_TO_RS);
+    float vm2 = (float)((double)vmax / RSG_VMAX_CONST);
+    vm2 = fmul(fmul(vm2, vm2), scale);
+    float f = (float)(((double)rvir / 1.0e3) * (double)vm2 / ((double)mvir * RSG_RS_CONSTANT));
+    if (f < 4.625f) return (float)((double)rvmax / RSG_RMAX_TO_RS);
+    float c = (float)f_to_c(f);
+    if (c <= 0) return (float)((double)rvmax / RSG_RMAX_TO_RS);
+    return __fdiv_rn(rvir, c);
+}
+__device__ __forceinline__ float nfw_menc(float r, float rs) {
+    return (float)(log((double)__fdiv_rn(fadd(rs, r), rs)) - (double)__fdiv_rn(r, fadd(rs, r)));
+}
+__device__ float chi2_scale(float rs, const float *br, const float *w, int64_t nb) {
+    float bm = (float)((double)nfw_menc(br[nb], rs) / ((double)nb)), last = 0, chi2 = 0, dx;
+    for (int64_t i = 0; i < nb; i++) {
+        float menc = nfw_menc(br[i + 1], rs);
+        dx = __fdiv_rn(fmul(w[i], fsub(fsub(menc, last), bm)), bm);
+        chi2 = fadd(chi2, fmul(dx, dx));
+        last = menc;
+    }
+    return chi2;
+}
+__device__ float fit_bins(float rs, const float *br, const float *w, int64_t nb, float *chi2o) {
+    if (!(rs > br[0]) || !(rs < br[nb])) rs = br[(nb + 1) / 2];
+    float irs = rs, chi2 = chi2_scale(rs, br, w, nb), drs = (float)((double)rs / 10.0), lc = 1e30f;
+    int64_t it = 0;
+    if (!(rs > 0)) return irs;
+    int guard = 0;
+    while (fabs((double)fsub(chi2, lc)) > 0.005 * (double)chi2 && it < 15 && ++guard < 100000) {
+        lc = chi2;
+        if (fadd(rs, drs) > br[nb]) drs = (float)(0.1 * (double)fsub(br[nb], rs));
+        if (fsub(rs, drs) < br[0]) drs = (float)(0.1 * (double)fsub(rs, br[0]));
+        float cr = chi2_scale(fadd(rs, drs), br, w, nb), cl = chi2_scale(fsub(rs, drs), br, w, nb);
+        float dx = (float)(0.5 * (double)fsub(cr, cl) / (double)drs);
+        float dx2 = (float)(((double)fadd(cr, cl) - 2.0 * (double)chi2) / (double)fmul(drs, drs));
+        float mv = 0;
+        if (dx2 != 0) mv = __fdiv_rn(-dx, dx2);
+        if (!mv) return rs;
+        if (fadd(rs, mv) > 4 * rs) mv = (float)(3.0 * (double)rs);
+        if ((double)fadd(rs, mv) < 0.25 * (double)rs) mv = (float)(-0.75 * (double)rs);
+        float nrs = fadd(rs, mv);
+        if (nrs > br[nb]) nrs = (float)((double)rs + 0.8 * (double)fsub(br[nb], rs));
+        else if (nrs < br[0]) nrs = (float)((double)rs + 0.8 * (double)fsub(br[0], rs));
+        float nc = chi2_scale(nrs, br, w, nb);
+        if (cr < nc) {
+            nc = cr;
+            nrs = fadd(rs, drs);
+        }
+        if (cl < nc) {
+            nc = cl;
+            nrs = fsub(rs, drs);
+        }
+        if (lc < nc) {
+            drs = (float)((double)drs * 0.5);
+            continue;
+        }
+        drs = (float)(fabs((double)fsub(rs, nrs)) / 10.0);
+        rs = nrs;
+        chi2 = nc;
+        it++;
+    }
+    *chi2o = chi2;
+    return rs;
+}
+__device__ void scale_radius(rsg_halo &h, float mvir, float rvir, float vmax, float rvmax,
+                             float scale, const PotRec *po, int64_t tot, int bound,
+                             const DevCfg &C) {
+    float br[51], w[50];
+    for (int i = 0; i < 51; i++) br[i] = 0;
+    for (int i = 0; i < 50; i++) w[i] = 0;
+    int64_t nb = 0, an = 0, pp = 0, i, j;
+    float rs = h.klypin_rs = klypin_rs(mvir, rvir, vmax, rvmax, scale);
+    for (i = 0; i < tot - 1; i++) {
+        if (bound && unbound(po[i])) continue;
+        an++;
+    }
+    if (an < 100) {
+        h.rs = rs;
+        return;
+    }
+    pp = (int64_t)ceil(((double)an / (double)50));
+    if (pp < 15) pp = (an) / ((int64_t)(an / 15));
+    br[0] = 0;
+    for (i = 0, j = 0; i < tot - 1; i++) {
+        if (bound && unbound(po[i])) continue;
+        if (++j == pp) {
+            nb++;
+            if (nb > 50) break;
+            br[nb] = (float)(1e3 * 0.5 * (sqrt((double)po[i].r2) + sqrt((double)po[i + 1].r2)));
+            w[nb - 1] = 1;
+            j = 0;
+        }
+    }
+    if (nb > 50) nb = 50;
+    for (i = 0; i < nb; i++)
+        if ((double)br[i] * 1e-3 < 3 * C.force_res) w[i] = 0.1f;
+    float chi2 = 0.0f;
+    h.rs = fit_bins(rs, br, w, nb, &chi2);
+    h.chi2 = chi2;
+}
+
+// _calc_additional_halo_props (src/properties.c:384-510)
+__device__ void more_props(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
+                           const DevCfg &C) {
+    int64_t j, pmd = 0, np_ = 0, npa[4] = {0, 0, 0, 0}, npv = 0, dtot = 0, avg = 0, nhalf = 0;
+    float scale = (float)C.scale_now;
+    const double f43 = 4.0 * M_PI / 3.0;
+    double dth = C.thresh_dens[0] * f43, d1 = C.thresh_dens[1] * f43;
+    double d2 = C.thresh_dens[2] * f43, d3 = C.thresh_dens[3] * f43, d4 = C.thresh_dens[4] * f43;
+    double rth = C.rvir_dens * f43, vconv = C.particle_mass / (double)scale;
+    double r, cv, vmax = 0, rvmax = 0, L[3] = {0, 0, 0}, Jh, m = 0, ds;
+    double vrms[3] = {0, 0, 0}, xa[3] = {0, 0, 0}, va[3] = {0, 0, 0}, md, cd, rvir, mvir;
+    for (j = 0; j < tot; j++) {
+        if (bound && unbound(po[j])) continue;
+        np_++;
+        r = sqrt((double)po[j].r2);
+        if (r < C.force_res) r = C.force_res;
+        cd = ((double)np_ / (r * r * r));
+        if (cd > dth) {
+            pmd = np_;
+            dtot = j;
+        }
+        if (cd > d1) npa[0] = np_;
+        if (cd > d2) npa[1] = np_;
+        if (cd > d3) npa[2] = np_;
+        if (cd > d4) npa[3] = np_;
+        if (cd > rth) {
+            cv = (double)np_ / r;
+            npv = np_;
+            if (pmd && cv > vmax) {
+                vmax = cv;
+                rvmax = r;
+            }
+        }
+    }
+    for (j = 0; j < dtot; j++) {
+        if (bound && unbound(po[j])) continue;
+        const float *c = h.pos, *p = po[j].pos;
+        L[0] += (double)fmul(fsub(p[1], c[1]), fsub(p[5], c[5]));
+        L[0] -= (double)fmul(fsub(p[2], c[2]), fsub(p[4], c[4]));
+        L[1] += (double)fmul(fsub(p[2], c[2]), fsub(p[3], c[3]));
+        L[1] -= (double)fmul(fsub(p[0], c[0]), fsub(p[5], c[5]));
+        L[2] += (double)fmul(fsub(p[0], c[0]), fsub(p[4], c[4]));
+        L[2] -= (double)fmul(fsub(p[1], c[1]), fsub(p[3], c[3]));
+        avg++;
+        if (avg * 2 >= pmd && !nhalf) nhalf = j;
+        for (int k = 0; k < 3; k++) {
+            xa[k] += ((double)p[k] - xa[k]) / ((double)avg);
+            md = (double)p[k + 3] - va[k];
+            va[k] += md / (double)avg;
+            vrms[k] += md * ((double)p[k + 3] - va[k]);
+        }
+    }
+    m = pmd * C.particle_mass;
+    if (!bound) h.m = (float)m;
+    else h.mgrav = (float)m;
+    for (int k = 0; k < 3; k++) vrms[k] = (avg > 0) ? (vrms[k] / avg) : 0;
+    if ((!bound) == (!C.bound_props)) {
+        h.Xoff = h.Voff = 0;
+        for (int k = 0; k < 3; k++) {
+            ds = xa[k] - (double)h.pos[k];
+            h.Xoff = (float)((double)h.Xoff + ds * ds);
+            ds = va[k] - (double)h.pos[k + 3];
+            h.Voff = (float)((double)h.Voff + ds * ds);
+        }
+        for (int k = 0; k < 4; k++) h.alt_m[k] = (float)(npa[k] * C.particle_mass);
+        h.Xoff = (float)(sqrt((double)h.Xoff) * 1e3);
+        h.Voff = (float)sqrt((double)h.Voff);
+        h.vrms = (float)sqrt(vrms[0] + vrms[1] + vrms[2]);
+        h.vmax = (float)(RSG_VMAX_CONST * sqrt(vmax * vconv));
+        h.rvmax = (float)(rvmax * 1e3);
+        h.halfmass_radius = (float)(sqrt((double)po[nhalf].r2) * 1e3);
+        h.r = (float)(cbrt((3.0 / (4.0 * M_PI)) * npa[2] / C.thresh_dens[3]) * 1e3);
+        shape(h, po, npa[2], bound, C);
+        h.b_to_a2 = h.b_to_a;
+        h.c_to_a2 = h.c_to_a;
+        for (int k = 0; k < 3; k++) h.A2[k] = h.A[k];
+        for (int k = 0; k < 6; k++) h.inertia_tensor2[k] = h.inertia_tensor[k];
+        h.r = (float)(cbrt((3.0 / (4.0 * M_PI)) * pmd / C.thresh_dens[0]) * 1e3);
+        shape(h, po, dtot, bound, C);
+        rvir = cbrt((3.0 / (4.0 * M_PI)) * npv / C.rvir_dens) * 1e3;
+        mvir = npv * C.particle_mass;
+        scale_radius(h, (float)m, h.r, h.vmax, h.rvmax, scale, po, dtot, bound, C);
+        for (j = 0; j < 3; j++) h.J[j] = (float)(C.particle_mass * (double)scale * L[j]);
+        h.energy = total_energy(po, dtot, &h.kin_to_pot, C);
+        Jh = C.particle_mass * (double)scale * sqrt(L[0] * L[0] + L[1] * L[1] + L[2] * L[2]);
+        h.spin = (float)((m > 0) ? (Jh * sqrt(fabs((double)h.energy)) / (RSG_GC * pow(m, 2.5))) : 0);
+        h.bullock_spin = (float)((m > 0) ? (Jh / (mvir * sqrt(2.0 * RSG_GC * mvir * rvir * (double)scale / 1e3))) : 0);
+        pseudo_masses(h, po, tot, bound, C);
+    }
+}
+
+__global__ void k_halo_scans(rsg_halo *H, const rsg_extra_halo_info *E, int32_t NH,
+                             PotRec *PO, const int32_t *toff, const int32_t *kept,
+                             const DevCfg *Cp) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= NH) return;
+    rsg_halo &hh = H[h];
+    if (hh.num_p < 1) return;
+    const DevCfg &C = *Cp;
+    PotRec *q = PO + toff[h];
+    int64_t tot = kept[h];
+    corevel(hh, q, tot, C);
+    float sn = (float)C.scale_now;
+    if (E[h].sub_of > -1) kinetic(q, tot, hh.corevel, hh.pos, sn, C);
+    else kinetic(q, tot, hh.bulkvel, hh.pos, sn, C);
+    more_props(hh, q, tot, 0, C);
+    more_props(hh, q, tot, 1, C);
+}
+
+__global__ void k_kept_count(const PotRec *PO, const int32_t *toff, const int32_t *tot,
+                             int32_t NH, int32_t *kept) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= NH) return;
+    int c = 0;
+    for (int i = 0; i < tot[h]; i++) c += PO[toff[h] + i].ke >= 0;
+    kept[h] = c;
+}
+__global__ void k_bh_roots(const int32_t *toff, const int32_t *tot, int32_t NH, int32_t *rflag) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < NH) rflag[h] = tot[h] > 1;
+}
+__global__ void k_bh_root_arrays(const int32_t *hlist, int32_t nr, const int32_t *toff,
+                                 const int32_t *tot, int32_t *rs, int32_t *rn) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nr) return;
+    rs[k] = toff[hlist[k]];
+    rn[k] = tot[hlist[k]];
+}
+__global__ void k_leaf_list_flags(const KNode<3> *nodes, int32_t nn, int32_t *f) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < nn) f[a] = nodes[a].div < 0;
+}
+
+static int32_t scan_i32(Arena &ar, int32_t *in, int32_t *out, int32_t n, cudaStream_t st) {
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, in, out, n, st);
+    size_t m = ar.used;
+    void *t = ar.take(b + 256);
+    cub::DeviceScan::ExclusiveSum(t, b, in, out, n, st);
+    RSG_CHECK_LAUNCH();
+    ar.used = m;
+    int32_t last = 0;
+    RSG_CUDA(cudaMemcpyAsync(&last, out + n - 1, 4, cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    return last;
+}
+static int32_t select_idx(Arena &ar, const int32_t *flag, int32_t *out, int32_t n, cudaStream_t st) {
+    int *cnt = ar.get<int>(1);
+    size_t b = 0;
+    cub::DeviceSelect::Flagged(nullptr, b, thrust::counting_iterator<int32_t>(0), flag, out, cnt, n, st);
+    size_t m = ar.used;
+    void *t = ar.take(b + 256);
+    cub::DeviceSelect::Flagged(t, b, thrust::counting_iterator<int32_t>(0), flag, out, cnt, n, st);
+    RSG_CHECK_LAUNCH();
+    ar.used = m;
+    int h = 0;
+    RSG_CUDA(cudaMemcpyAsync(&h, cnt, 4, cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    return h;
+}
+
+// Barnes-Hut potentials for the segments (rs[k], rn[k]) of PO.
+void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const int32_t *rn,
+                  int32_t ntrees, double mp, double force_res, int *err, cudaStream_t st) {
+    const int T = 256;
+    if (ntrees == 0) return;
+    Forest<3> F = build_forest<3, PotRec>(ar, PO, npo, rs, rn, ntrees, npo, 10, st);
+    BHNode *B = ar.get<BHNode>(F.nnodes);
+    k_bh_leaf<<<nblk(F.nnodes, T), T, 0, st>>>(F.nodes, F.nnodes, PO, mp, B);
+    for (int l = (int)F.lv_first.size() - 2; l >= 0; l--) {
+        int32_t a = F.lv_first[l], b = F.lv_first[l + 1];
+        if (b > a) k_bh_internal<<<nblk(b - a, 64), 64, 0, st>>>(F.nodes, a, b - a, PO, B);
+    }
+    int32_t *lf = ar.get<int32_t>(F.nnodes), *leaves = ar.get<int32_t>(F.nnodes);
+    k_leaf_list_flags<<<nblk(F.nnodes, T), T, 0, st>>>(F.nodes, F.nnodes, lf);
+    int32_t nl = select_idx(ar, lf, leaves, F.nnodes, st);
+    k_bh_walk<<<nblk(nl, 64), 64, 0, st>>>(F.nodes, leaves, nl, B, PO, mp, force_res, err);
+    RSG_CHECK_LAUNCH();
+}
+
+void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec *W,
+                      int64_t M, rsg_halo *H, rsg_extra_halo_info *E, int32_t NH,
+                      cudaStream_t st) {
+    const int T = 256;
+    if (NH == 0) return;
+    size_t mark = ar.used;
+    int *err = ar.get<int>(2);
+    RSG_CUDA(cudaMemsetAsync(err, 0, 8, st));
+    int32_t *tot = ar.get<int32_t>(NH + 1), *nseg = ar.get<int32_t>(NH + 1);
+    int32_t *toff = ar.get<int32_t>(NH + 1), *soff = ar.get<int32_t>(NH + 1);
+    k_set_count<<<nblk(NH + 1, 64), 64, 0, st>>>(H, E, NH, dc.include_host_potential_ratio, tot,
+                                                 nseg, err);
+    int32_t npo = scan_i32(ar, tot, toff, NH + 1, st);
+    int32_t ns = scan_i32(ar, nseg, soff, NH + 1, st);
+    Seg *segs = ar.get<Seg>(ns + 1);
+    PotRec *PO = ar.get<PotRec>(npo + 1), *PO2 = ar.get<PotRec>(npo + 1);
+    k_set_segs<<<nblk(NH, 64), 64, 0, st>>>(H, E, NH, dc.include_host_potential_ratio, toff, soff,
+                                            segs);
+    if (ns) k_set_fill<<<ns, 128, 0, st>>>(segs, W, H, PO);
+    RSG_CHECK_LAUNCH();
+    // potentials
+    {
+        size_t m2 = ar.used;
+        int32_t *rflag = ar.get<int32_t>(NH), *hl = ar.get<int32_t>(NH);
+        k_bh_roots<<<nblk(NH, T), T, 0, st>>>(toff, tot, NH, rflag);
+        int32_t nr = select_idx(ar, rflag, hl, NH, st);
+        int32_t *rs = ar.get<int32_t>(nr + 1), *rn = ar.get<int32_t>(nr + 1);
+        if (nr) k_bh_root_arrays<<<nblk(nr, T), T, 0, st>>>(hl, nr, toff, tot, rs, rn);
+        bh_potential(ar, PO, npo, rs, rn, nr, dc.particle_mass, dc.force_res, err, st);
+        ar.used = m2;
+    }
+    // drop potential-only records and sort every halo's records by r^2
+    {
+        size_t m2 = ar.used;
+        uint64_t *k1 = ar.get<uint64_t>(npo + 1), *k2 = ar.get<uint64_t>(npo + 1);
+        uint32_t *v1 = ar.get<uint32_t>(npo + 1), *v2 = ar.get<uint32_t>(npo + 1);
+        k_po_keys<<<nblk(npo, T), T, 0, st>>>(PO, npo, k1, v1);
+        int bits = 33;
+        while ((1ll << (bits - 33)) <= NH) bits++;
+        size_t b = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, b, k1, k2, v1, v2, npo, 0, bits, st);
+        void *t = ar.take(b + 256);
+        cub::DeviceRadixSort::SortPairs(t, b, k1, k2, v1, v2, npo, 0, bits, st);
+        k_po_gather<<<nblk(npo, T), T, 0, st>>>(PO, v2, npo, PO2);
+        RSG_CHECK_LAUNCH();
+        ar.used = m2;
+    }
+    int32_t *kept = ar.get<int32_t>(NH + 1);
+    k_kept_count<<<nblk(NH, T), T, 0, st>>>(PO2, toff, tot, NH, kept);
+    k_halo_scans<<<nblk(NH, 32), 32, 0, st>>>(H, E, NH, PO2, toff, kept, d_dc);
+    RSG_CHECK_LAUNCH();
+    int herr[2];
+    RSG_CUDA(cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    if (herr[0]) {
+        set_error(RSG_ERR_LIMIT, "halo walk or potential tree traversal exceeded its bound");
+        throw Failure();
+    }
+    ar.used = mark;
+}
+
+}  // namespace rsg

@@ -1,0 +1,1422 @@
+// Batched find_subs (src/groupies.c:520-708) on the GPU.
+//
+// The reference recurses depth first through the 6D subgroup hierarchy of one
+// FOF group at a time.  Here all groups of a call are processed together and
+// the recursion is unrolled by level:
+//   descending, level L = 0, 1, ...: for every node of level L
+//     norm_sd (FP64 moments + 3x3 Jacobi), 6D kd-tree (exact fast3tree
+//     permutation), nearest-neighbour distances of the sample (glibc rand_r
+//     stream, exact traversal order), the FOF_FRACTION quantile by the
+//     reference's own randomised quickselect, 6D FOF at that length, and the
+//     kept subgroups (>= MIN_HALO_PARTICLES) become level L+1 nodes when
+//     MIN_HALO_PARTICLES < n < parent n (src/groupies.c:535-537);
+//   halos: every node without recursed children creates one seed halo;
+//     halo order is the depth-first order of those nodes, which is the order
+//     of their first particle;
+//   ascending, level L = max .. 0: for every node, the post-recursion part
+//     of _find_subs (src/groupies.c:539-666): seed merging, particle
+//     assignment by the phase-space metric, regrouping by halo, basic
+//     properties and parent links.
+// A node's work at a level only touches its own particle range, so running
+// all nodes of a level at once performs the same operations, in the same
+// order per range, as the reference's depth-first walk.
+#include <cub/cub.cuh>
+
+#include "kdtree_impl.cuh"
+#include "lsort.cuh"
+#include "subs.cuh"
+
+// Ranges up to this size are summed by one thread in array order, so FP64
+// sums round exactly as the reference's sequential loops do.
+#define RSG_SEQ_MAX 65536
+
+namespace rsg {
+
+// Hierarchy record of the last find_subs call (level, first position, size,
+// 6D linking length per node), kept for the test hooks.
+std::vector<int32_t> g_dbg_level, g_dbg_start, g_dbg_n;
+std::vector<float> g_dbg_target;
+
+void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec *W,
+                      int64_t M, rsg_halo *H, rsg_extra_halo_info *E, int32_t NH,
+                      cudaStream_t st);
+
+// ---- reductions -------------------------------------------------------------
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+// Deterministic block sum (fixed shuffle tree, then warp totals in order).
+// All threads must call; the result is valid in every thread.
+__device__ double block_sum_d(double v, double *sm) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = warp_sum_d(v);
+    __syncthreads();
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < nw; i++) t += sm[i];
+        sm[32] = t;
+    }
+    __syncthreads();
+    return sm[32];
+}
+
+// glibc's published rand_r (three steps of the ANSI C LCG, 31-bit result).
+__device__ __forceinline__ int rand_r_glibc(unsigned *seed) {
+    unsigned next = *seed;
+    int result;
+    next *= 1103515245u;
+    next += 12345u;
+    result = (unsigned)(next / 65536u) % 2048u;
+    next *= 1103515245u;
+    next += 12345u;
+    result <<= 10;
+    result ^= (unsigned)(next / 65536u) % 1024u;
+    next *= 1103515245u;
+    next += 12345u;
+    result <<= 10;
+    result ^= (unsigned)(next / 65536u) % 1024u;
+    *seed = next;
+    return result;
+}
+
+// ---- descending phase ---------------------------------------------------------
+
+// norm_sd (src/groupies.c:788-830) + calc_deviations (src/jacobi.c:156-172).
+// Moments go to mom[node * 27]: 6 means then the 21 upper-triangular
+// second moments of the centred coordinates; sig[node * 2] gets sig_x, sig_v.
+__device__ void norm_sigmas(const double *corr, int level0, double ims, double *sig) {
+    double full[6][6];
+    int k = 0;
+    for (int a = 0; a < 6; a++)
+        for (int b = a; b < 6; b++) full[a][b] = full[b][a] = corr[k++];
+    double in[3][3];
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) in[a][b] = full[a][b];
+    double sx = min_eig_sqrt(in);
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) in[a][b] = full[a + 3][b + 3];
+    double sv = min_eig_sqrt(in);
+    if (level0) sx *= ims;  // n == num_copies holds for the group itself only
+    sig[0] = sx;
+    sig[1] = sv;
+}
+
+// Nodes up to RSG_SEQ_MAX particles: one thread, array order, so every FP64
+// sum rounds as the reference's loop does.
+__global__ void k_norm_seq(Rec *W, HierNodes N, int32_t base, int32_t count, int level0,
+                           double ims, double *sig) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    int s = N.start[node], n = N.n[node];
+    if (n <= 0 || n > RSG_SEQ_MAX) return;
+    double mean[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < n; i++)
+        for (int d = 0; d < 6; d++) mean[d] += (double)W[s + i].pos[d];
+    for (int d = 0; d < 6; d++) mean[d] /= (double)n;
+    double c[21];
+    for (int j = 0; j < 21; j++) c[j] = 0;
+    for (int i = 0; i < n; i++) {
+        float q[6];
+        for (int d = 0; d < 6; d++) {
+            q[d] = __double2float_rn((double)W[s + i].pos[d] - mean[d]);
+            W[s + i].pos[d] = q[d];
+        }
+        int j = 0;
+        for (int x = 0; x < 6; x++)
+            for (int y = x; y < 6; y++) c[j++] += (double)fmul(q[x], q[y]);
+    }
+    for (int j = 0; j < 21; j++) c[j] /= (double)n;
+    norm_sigmas(c, level0, ims, sig + 2 * k);
+}
+
+// Larger nodes: one block, deterministic tree reductions.
+__global__ void k_norm_par(Rec *W, HierNodes N, int32_t base, int level0, double ims,
+                           double *sig) {
+    __shared__ double sm[40];
+    __shared__ double mean[6], corr[21];
+    int k = blockIdx.x;
+    int node = base + k;
+    int s = N.start[node], n = N.n[node];
+    if (n <= RSG_SEQ_MAX) return;
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        for (int d = 0; d < 6; d++) acc[d] += (double)W[s + i].pos[d];
+    for (int d = 0; d < 6; d++) {
+        double t = block_sum_d(acc[d], sm);
+        if (threadIdx.x == 0) mean[d] = t / (double)n;
+    }
+    __syncthreads();
+    double cc[21];
+    for (int j = 0; j < 21; j++) cc[j] = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        float q[6];
+        for (int d = 0; d < 6; d++) {
+            q[d] = __double2float_rn((double)W[s + i].pos[d] - mean[d]);
+            W[s + i].pos[d] = q[d];
+        }
+        int j = 0;
+        for (int x = 0; x < 6; x++)
+            for (int y = x; y < 6; y++) cc[j++] += (double)fmul(q[x], q[y]);
+    }
+    for (int j = 0; j < 21; j++) {
+        double t = block_sum_d(cc[j], sm);
+        if (threadIdx.x == 0) corr[j] = t / (double)n;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) norm_sigmas(corr, level0, ims, sig + 2 * k);
+}
+
+// Divide by the dispersions unless one of them is zero (src/groupies.c:825-829).
+__global__ void k_norm_div(Rec *W, HierNodes N, int32_t base, const double *sig) {
+    int k = blockIdx.x;
+    int node = base + k;
+    int s = N.start[node], n = N.n[node];
+    double sx = sig[2 * k], sv = sig[2 * k + 1];
+    if (!sx || !sv) return;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        for (int d = 0; d < 6; d++)
+            W[s + i].pos[d] = __double2float_rn((double)W[s + i].pos[d] / (d < 3 ? sx : sv));
+}
+
+// Sample list (src/groupies.c:295-308): all particles when n <= 10000
+// (or EXACT_LL_CALC), else 10000 indices from rand_r seeded with n.
+__global__ void k_sample(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
+                         int32_t *sidx, unsigned *seed_out, int exact) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    int n = N.n[node];
+    int nt = exact ? n : (n < 10000 ? n : 10000);
+    unsigned seed = (unsigned)n;
+    if (nt != n) {
+        int o = soff[k];
+        for (int i = 0; i < nt; i++) {
+            int64_t j = rand_r_glibc(&seed);
+            j <<= 31;
+            j += rand_r_glibc(&seed);
+            j %= n;
+            sidx[o + i] = (int32_t)j;
+        }
+    }
+    seed_out[k] = seed;
+}
+
+__device__ __forceinline__ float dist6(const float *c, const float *p) {
+    float d = 0.f;
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        float dx = fsub(c[j], p[j]);
+        d = fadd(d, fmul(dx, dx));
+    }
+    return d;
+}
+__device__ __forceinline__ bool box_out6(const KNode<6> &nd, const float *c, float r) {
+    float d = 0.f, e;
+    const float r2 = fmul(r, r);
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        if ((e = fsub(c[i], nd.mn[i])) < 0) {
+            d = fadd(d, fmul(e, e));
+            if (d >= r2) return true;
+        } else if ((e = fsub(c[i], nd.mx[i])) > 0) {
+            d = fadd(d, fmul(e, e));
+            if (d >= r2) return true;
+        }
+    }
+    return false;
+}
+
+// fast3tree_find_next_closest_distance (src/fast3tree.c:956-1030), with the
+// recursion unrolled onto an explicit stack; the running radius threads
+// through the visits in the reference's order.
+__device__ float next_closest(const KNode<6> *nodes, int root, const Rec *W, const float *c,
+                              int *err) {
+    int nd = root;
+    while (nodes[nd].div >= 0) {
+        const KNode<6> &x = nodes[nd];
+        nd = (c[x.div] <= nodes[x.left].mx[x.div]) ? x.left : x.left + 1;
+    }
+    while (nd != root) {
+        int pdv = nodes[nodes[nd].parent].div;
+        if (nodes[nd].mn[pdv] == nodes[nd].mx[pdv]) nd = nodes[nd].parent;
+        else break;
+    }
+    const KNode<6> &o = nodes[nd];
+    float md = 0.f;
+    for (int j = 0; j < 6; j++) {
+        float dx = fsub(o.mx[j], o.mn[j]);
+        md = fadd(md, fmul(dx, dx));
+    }
+    for (int i = 0; i < o.n; i++) {
+        float d = dist6(c, W[o.start + i].pos);
+        if (d && d < md) md = d;
+    }
+    float r = (float)sqrt((double)md);
+    int stack[RSG_STACK6];
+    int sp = 0;
+    stack[sp++] = root;
+    while (sp) {
+        int ni = stack[--sp];
+        const KNode<6> &x = nodes[ni];
+        if (box_out6(x, c, r) || ni == nd) continue;
+        if (x.div < 0) {
+            float r2 = fmul(r, r);
+            for (int i = 0; i < x.n; i++) {
+                float d = dist6(c, W[x.start + i].pos);
+                if (d < r2) r2 = d;
+            }
+            r = (float)sqrt((double)r2);
+            continue;
+        }
+        int a = x.left, b = x.left + 1;
+        if (c[x.div] > fmul(0.5f, fadd(x.mn[x.div], x.mx[x.div]))) {
+            a = x.left + 1;
+            b = x.left;
+        }
+        if (sp + 2 > RSG_STACK6) {
+            atomicExch(err, 1);
+            return r;
+        }
+        stack[sp++] = b;
+        stack[sp++] = a;
+    }
+    return r;
+}
+
+__global__ void k_nn(const KNode<6> *nodes, const Rec *W, HierNodes N, int32_t base,
+                     const int32_t *soff, const int32_t *sidx, float *prad, int exact, int *err) {
+    int k = blockIdx.x;
+    int node = base + k;
+    int s = N.start[node], n = N.n[node];
+    int nt = exact ? n : (n < 10000 ? n : 10000);
+    int o = soff[k];
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        int j = (nt == n) ? t : sidx[o + t];
+        float c[6];
+#pragma unroll
+        for (int d = 0; d < 6; d++) c[d] = W[s + j].pos[d];
+        prad[o + t] = next_closest(nodes, k, W, c, err);
+    }
+}
+
+// find_median_r / rad_partition (src/groupies.c:735-786), run as is on the
+// sample's distances in sample order with the continuing rand_r stream.
+__global__ void k_target(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
+                         float *prad, const unsigned *seed_in, float frac, int exact) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    int n = N.n[node];
+    int nt = exact ? n : (n < 10000 ? n : 10000);
+    float *a = prad + soff[k];
+    unsigned seed = seed_in[k];
+    float res;
+    int64_t kk = (int64_t)__float2ll_rz(fmul(__ll2float_rn(nt), frac));
+    if (nt < 2) {
+        res = a[0];
+    } else {
+        int64_t left = 0, right = nt;
+        int guard = 0;
+        while (true) {
+            float u = __fdiv_rn(__int2float_rn(rand_r_glibc(&seed) % 2147483647), 2147483648.0f);
+            float pf = fadd(__ll2float_rn(left), fmul(u, __ll2float_rn(right - left)));
+            int64_t pi = (int64_t)__float2ll_rz(pf);
+            if (pi >= right) pi = right - 1;  // keeps the access in range (u == 1 edge)
+            float piv = a[pi], t;
+            t = a[pi]; a[pi] = a[right - 1]; a[right - 1] = t;
+            int64_t si = right - 2, i;
+            for (i = left; i < si; i++)
+                if (a[i] > piv) {
+                    t = a[i]; a[i] = a[si]; a[si] = t;
+                    si--;
+                    i--;
+                }
+            if (a[si] <= piv) si++;
+            t = a[right - 1]; a[right - 1] = a[si]; a[si] = t;
+            int64_t p = si;
+            if (kk == p || (a[left] == a[right - 1])) {
+                res = a[kk];
+                break;
+            }
+            if (kk < p) right = p;
+            else left = p + 1;
+            if (++guard > 100000000) {
+                res = a[kk];
+                break;
+            }
+        }
+    }
+    N.target_r[node] = res;
+}
+
+// element -> level-local node index for the nodes [base, base + count)
+__global__ void k_fill_eln(HierNodes N, int32_t base, int32_t *eln) {
+    int k = blockIdx.x;
+    int s = N.start[base + k], n = N.n[base + k];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) eln[s + i] = k;
+}
+
+__device__ __forceinline__ int uf_find2(int *par, int x) {
+    int p = par[x];
+    while (p != x) {
+        int gp = par[p];
+        if (gp != p) par[x] = gp;
+        x = p;
+        p = par[x];
+    }
+    return x;
+}
+__device__ __forceinline__ void uf_unite2(int *par, int a, int b) {
+    while (true) {
+        a = uf_find2(par, a);
+        b = uf_find2(par, b);
+        if (a == b) return;
+        if (a < b) { int t = a; a = b; b = t; }
+        if (atomicCAS(&par[a], a, b) == a) return;
+    }
+}
+
+// _find_subfofs_at_r (src/groupies.c:274-284): every particle links to
+// itself and to the later particles within target_r (6D, strict <).  This
+// kernel lists those later neighbours in ascending order (the order the
+// skip search returns them); count pass when nbr == nullptr.
+__global__ void k_fof6(const KNode<6> *nodes, const Rec *W, int64_t M, HierNodes N,
+                       int32_t base, const int32_t *eln, const int32_t *noff, int32_t *ncnt,
+                       int32_t *nbr, int *err) {
+    int64_t i64 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i64 >= M) return;
+    int i = (int)i64;
+    int k = eln[i];
+    if (k < 0) return;
+    float r = N.target_r[base + k];
+    const float r2 = fmul(r, r);
+    float c[6];
+#pragma unroll
+    for (int d = 0; d < 6; d++) c[d] = W[i].pos[d];
+    int stack[RSG_STACK6];
+    int sp = 0, cnt = 0;
+    int o = nbr ? noff[i] : 0;
+    stack[sp++] = k;
+    while (sp) {
+        const KNode<6> &x = nodes[stack[--sp]];
+        if (x.start + x.n <= i) continue;
+        if (box_out6(x, c, r)) continue;
+        if (x.div < 0) {
+            int j0 = x.start > i + 1 ? x.start : i + 1;
+            for (int j = j0; j < x.start + x.n; j++)
+                if (dist6(c, W[j].pos) < r2) {
+                    if (nbr) nbr[o + cnt] = j;
+                    cnt++;
+                }
+            continue;
+        }
+        if (sp + 2 > RSG_STACK6) {
+            atomicExch(err, 1);
+            return;
+        }
+        stack[sp++] = x.left + 1;
+        stack[sp++] = x.left;
+    }
+    if (!nbr) ncnt[i] = cnt;
+}
+
+// Union-find labels exactly as link_particle_to_fof / merge_smallfofs build
+// them (src/fof.c:46-170): particles in array order, a new set takes the
+// next integer, and when a link's set meets the current set the link's root
+// survives.  Sequential per node (one thread), so the labels -- and thus the
+// partition order and the subgroup order -- are the reference's.
+__device__ __forceinline__ int sf_find(int32_t *R, int a) {
+    int r = a;
+    while (R[r] != r) r = R[r];
+    while (R[a] != r) {
+        int nx = R[a];
+        R[a] = r;
+        a = nx;
+    }
+    return r;
+}
+__global__ void k_replay6(HierNodes N, int32_t base, int32_t count, const int32_t *noff,
+                          const int32_t *nbr, int32_t *lab, int32_t *R) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    int s = N.start[node], n = N.n[node];
+    int32_t *RR = R + s;
+    int nsf = 0;
+    for (int i = s; i < s + n; i++) lab[i] = -1;
+    for (int i = s; i < s + n; i++) {
+        int e0 = noff[i], e1 = noff[i + 1];
+        if (e0 == e1) continue;
+        int f = lab[i];
+        if (f < 0) {
+            for (int e = e0; e < e1; e++)
+                if (lab[nbr[e]] != -1) {
+                    f = lab[nbr[e]];
+                    break;
+                }
+            if (f < 0) {
+                f = nsf++;
+                RR[f] = f;
+            }
+        }
+        for (int e = e0 - 1; e < e1; e++) {
+            int j = (e < e0) ? i : nbr[e];
+            if (lab[j] == -1) {
+                lab[j] = f;
+            } else {
+                int rl = sf_find(RR, lab[j]), rc = sf_find(RR, f);
+                if (rl != rc) RR[rc] = rl;
+            }
+        }
+    }
+    for (int i = s; i < s + n; i++)
+        if (lab[i] >= 0) lab[i] = sf_find(RR, lab[i]);
+}
+
+// Runs of equal labels after the partition sort: the kept ones (>= 0 and at
+// least MIN_HALO_PARTICLES long) are the subgroups of build_fullfofs
+// (src/fof.c:226-255), in array order.
+__global__ void k_run_heads(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
+                            const int32_t *lab, int32_t *flag) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    int f = 0;
+    if (k >= 0) {
+        int s = N.start[base + k];
+        f = (i == s) || lab[i] != lab[i - 1];
+    }
+    flag[i] = f;
+}
+__global__ void k_run_children(const int32_t *heads, int32_t nh, const int32_t *eln,
+                               HierNodes N, int32_t base, const int32_t *lab, int64_t minsz,
+                               int32_t *cflag, int32_t *clen) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nh) return;
+    int p = heads[t];
+    int k = eln[p];
+    int node = base + k;
+    int end = N.start[node] + N.n[node];
+    if (t + 1 < nh && heads[t + 1] < end) end = heads[t + 1];
+    int len = end - p;
+    clen[t] = len;
+    cflag[t] = lab[p] >= 0 && len >= minsz && len > minsz && len < N.n[node];
+}
+__global__ void k_make_children2(const int32_t *cidx, int32_t nc, const int32_t *heads,
+                                 const int32_t *clen, const int32_t *eln, HierNodes N,
+                                 int32_t base, int32_t nbase) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nc) return;
+    int h = cidx[t];
+    int p = heads[h];
+    int par = base + eln[p];
+    int c = nbase + t;
+    N.start[c] = p;
+    N.n[c] = clen[h];
+    N.parent[c] = par;
+    N.group[c] = N.group[par];
+    N.level[c] = N.level[par] + 1;
+    N.nchild[c] = 0;
+    atomicAdd(&N.nchild[par], 1);
+}
+
+__global__ void k_init_par(const int32_t *eln, int64_t M, int *par, int *size) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    par[i] = (int)i;
+    size[i] = 0;
+}
+
+__global__ void k_comp_size(const int32_t *eln, int64_t M, int *par, int *root, int *size) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M || eln[i] < 0) return;
+    int rt = uf_find2(par, (int)i);
+    root[i] = rt;
+    atomicAdd(&size[rt], 1);
+}
+
+// Sort keys that regroup each level node's range: particles outside kept
+// subgroups first, then subgroups by first position (stable inside).
+__global__ void k_subkeys(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
+                          const int *root, const int *size, int64_t minsz, uint64_t *key,
+                          uint32_t *val) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    uint64_t kk;
+    if (k < 0) {
+        kk = (uint64_t)i << 32;
+    } else {
+        int s = N.start[base + k];
+        int rt = root[i];
+        bool kept = size[rt] >= minsz && size[rt] >= 2;
+        kk = ((uint64_t)s << 32) | (uint64_t)(kept ? (rt - s + 1) : 0);
+    }
+    key[i] = kk;
+    val[i] = (uint32_t)i;
+}
+
+template <class T>
+__global__ void k_gather(const T *src, const uint32_t *perm, int64_t M, T *dst) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < M) dst[i] = src[perm[i]];
+}
+
+// Heads of kept subgroups after regrouping: candidates for level L+1.
+__global__ void k_child_heads(const int32_t *eln_sorted, const uint64_t *key, int64_t M,
+                              HierNodes N, int32_t base, const int *size, int64_t minsz,
+                              int32_t *flag) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int f = 0;
+    uint64_t kk = key[i];
+    uint32_t lo = (uint32_t)(kk & 0xffffffffu);
+    int k = eln_sorted[i];
+    if (k >= 0 && lo != 0 && (i == 0 || key[i - 1] != kk)) {
+        int s = N.start[base + k], pn = N.n[base + k];
+        int rt = (int)lo - 1 + s;
+        int sz = size[rt];
+        if (sz > minsz && sz < pn) f = 1;
+    }
+    flag[i] = f;
+}
+
+__global__ void k_make_children(const int32_t *heads, const int *nheads, const int32_t *eln,
+                                const uint64_t *key, HierNodes N, int32_t base, int32_t nbase,
+                                const int *size) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= *nheads) return;
+    int i = heads[t];
+    int k = eln[i];
+    int par = base + k;
+    int s = N.start[par];
+    int rt = (int)(key[i] & 0xffffffffu) - 1 + s;
+    int c = nbase + t;
+    N.start[c] = i;
+    N.n[c] = size[rt];
+    N.parent[c] = par;
+    N.group[c] = N.group[par];
+    N.level[c] = N.level[par] + 1;
+    N.nchild[c] = 0;
+    atomicAdd(&N.nchild[par], 1);
+}
+
+// ---- halos -----------------------------------------------------------------
+
+__global__ void k_leaf_flags(HierNodes N, int32_t nn, int32_t *flag) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nn) flag[i] = N.nchild[i] == 0;
+}
+__global__ void k_leaf_keys(HierNodes N, const int32_t *leaves, int32_t nl, int32_t *key) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nl) key[i] = N.start[leaves[i]];
+}
+__device__ int lower_bound_i(const int32_t *a, int n, int v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+__global__ void k_halo_ranges(HierNodes N, int32_t nn, const int32_t *lstart, int32_t nl) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    N.h0[i] = lower_bound_i(lstart, nl, N.start[i]);
+    N.h1[i] = lower_bound_i(lstart, nl, N.start[i] + N.n[i]);
+}
+// add_new_halo (src/groupies.c:164-187)
+__global__ void k_halo_init(rsg_halo *H, rsg_extra_halo_info *E, int32_t nh) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= nh) return;
+    rsg_halo z;
+    memset(&z, 0, sizeof(z));
+    z.flags = RSG_GROWING;
+    H[h] = z;
+    E[h].child = E[h].next_cochild = E[h].ph = E[h].prev_cochild = E[h].sub_of = -1;
+    E[h].max_metric = 0;
+}
+
+// src/groupies.c:542-551: particle -> halo from the children's halos, and
+// real coordinates restored from the caller's particles.
+__global__ void k_asc_mark(Rec *W, const rsg_particle *P, HierNodes N, int32_t base,
+                           const rsg_halo *H, int32_t *phalo) {
+    int node = base + blockIdx.x;
+    int s = N.start[node], n = N.n[node];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        phalo[s + i] = -1;
+        const rsg_particle &q = P[W[s + i].ridx];
+#pragma unroll
+        for (int d = 0; d < 6; d++) W[s + i].pos[d] = q.pos[d];
+    }
+    __syncthreads();
+    for (int h = N.h0[node]; h < N.h1[node]; h++) {
+        int ps = (int)H[h].p_start, np = (int)H[h].num_p;
+        for (int j = threadIdx.x; j < np; j += blockDim.x) phalo[ps + j] = h;
+    }
+}
+
+// _find_biggest_parent without temporal information (src/groupies.c:362-380)
+__device__ int biggest(const rsg_halo *H, int h0, int h1, int growing_only, int first) {
+    int mi = growing_only ? first : h0;
+    for (int i = h0; i < h1; i++) {
+        if (growing_only && !(H[i].flags & RSG_GROWING)) continue;
+        if (H[i].vmax > H[mi].vmax) mi = i;
+        if (H[i].vmax == H[mi].vmax && H[i].num_p > H[mi].num_p) mi = i;
+    }
+    return mi;
+}
+
+// src/groupies.c:553-582: biggest seed, Poisson/force-resolution merges,
+// growing list.  One thread per node.
+__global__ void k_asc_seed(HierNodes N, int32_t base, int32_t count, rsg_halo *H,
+                           rsg_extra_halo_info *E, int32_t *glist, int32_t *redirect,
+                           double force_res) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    int h0 = N.h0[node], h1 = N.h1[node];
+    int mi = biggest(H, h0, h1, 0, 0);
+    H[mi].flags |= RSG_GROWING;
+    E[mi].sub_of = -1;
+    int ng = 0;
+    glist[h0 + ng++] = mi;
+    for (int i = h0; i < h1; i++) {
+        redirect[i] = -1;
+        if (i == mi || !(H[i].flags & RSG_GROWING)) continue;
+        int force;
+        if (poisson_or_force(H[i], H[mi], force_res, &force)) {
+            H[i].flags -= (H[i].flags & RSG_GROWING);
+            E[i].sub_of = mi;
+            if (!force) {
+                redirect[i] = mi;
+                H[i].num_p = 0;
+            }
+            continue;
+        }
+        glist[h0 + ng++] = i;
+    }
+    N.maxi[node] = mi;
+    N.ng[node] = ng;
+}
+
+// src/groupies.c:584-609: particles of merged seeds go to the biggest halo;
+// unassigned particles go to the halo of smallest phase-space metric among
+// the growing ones, then up the sub_of chain while the metric exceeds the
+// halo's max_metric.
+__global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_halo *H,
+                             const rsg_extra_halo_info *E, const int32_t *glist,
+                             const int32_t *redirect, int32_t *phalo) {
+    int node = base + blockIdx.x;
+    int s = N.start[node], n = N.n[node];
+    int mi = N.maxi[node], ng = N.ng[node], h0 = N.h0[node];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int ph = phalo[s + i];
+        if (ph >= 0) {
+            if (redirect[ph] >= 0) phalo[s + i] = redirect[ph];
+            continue;
+        }
+        if (ng == 1) {
+            phalo[s + i] = mi;
+            continue;
+        }
+        const float *pos = W[s + i].pos;
+        float best = pdist(H[mi], pos);
+        int bh = mi;
+        for (int g = 0; g < ng; g++) {
+            int h = glist[h0 + g];
+            float m = pdist(H[h], pos);
+            if (m < best) {
+                best = m;
+                bh = h;
+            }
+        }
+        int h = bh;
+        for (int guard = 0; guard < 100000 && E[h].sub_of > -1; guard++) {
+            if (pdist(H[h], pos) > E[h].max_metric) h = (int)E[h].sub_of;
+            else break;
+        }
+        phalo[s + i] = h;
+    }
+}
+
+// Regroup keys for reassign_halo_particles (src/groupies.c:316-331) and the
+// core sort of src/fun_times.c:204-227 (by squared distance to the halo).
+__global__ void k_halokeys(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
+                           const int32_t *phalo, uint64_t *key, uint32_t *val) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    uint64_t kk;
+    if (k < 0) kk = (uint64_t)i << 32;
+    else {
+        int s = N.start[base + k], h0 = N.h0[base + k];
+        kk = ((uint64_t)s << 32) | (uint64_t)(phalo[i] - h0);
+    }
+    key[i] = kk;
+    val[i] = (uint32_t)i;
+}
+__global__ void k_halo_heads(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
+                             const int32_t *phalo, rsg_halo *H) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    if (k < 0) return;
+    int s = N.start[base + k];
+    if (i == s || phalo[i] != phalo[i - 1]) H[phalo[i]].p_start = i;
+}
+__global__ void k_halo_tails(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
+                             const int32_t *phalo, rsg_halo *H) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    if (k < 0) return;
+    int s = N.start[base + k], n = N.n[base + k];
+    if (i == s + n - 1 || phalo[i] != phalo[i + 1]) H[phalo[i]].num_p = i + 1 - H[phalo[i]].p_start;
+}
+
+// calc_basic_halo_props + estimate_vmax (src/properties.c:39-125); one
+// block per listed halo.
+__global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, const DevCfg *C) {
+    __shared__ double sm[40];
+    __shared__ double mean[6], p2[6];
+    __shared__ int bins[50];
+    int h = list[blockIdx.x];
+    rsg_halo &hh = H[h];
+    int ps = (int)hh.p_start, np = (int)hh.num_p;
+    if (np <= RSG_SEQ_MAX) {
+        // sequential, in array order (src/properties.c:76-87)
+        if (threadIdx.x == 0) {
+            double a[6] = {0, 0, 0, 0, 0, 0}, b[6] = {0, 0, 0, 0, 0, 0};
+            for (int i = 0; i < np; i++)
+                for (int d = 0; d < 6; d++) a[d] += (double)W[ps + i].pos[d];
+            for (int d = 0; d < 6; d++) mean[d] = a[d] / (double)np;
+            for (int i = 0; i < np; i++)
+                for (int d = 0; d < 6; d++) {
+                    double x = (double)W[ps + i].pos[d] - mean[d];
+                    b[d] += x * x;
+                }
+            for (int d = 0; d < 6; d++) p2[d] = b[d];
+        }
+        __syncthreads();
+    } else {
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < np; i += blockDim.x)
+#pragma unroll
+        for (int d = 0; d < 6; d++) acc[d] += (double)W[ps + i].pos[d];
+    for (int d = 0; d < 6; d++) {
+        double t = block_sum_d(acc[d], sm);
+        if (threadIdx.x == 0) mean[d] = t / (double)np;
+    }
+    __syncthreads();
+    for (int d = 0; d < 6; d++) acc[d] = 0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x)
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            double x = (double)W[ps + i].pos[d] - mean[d];
+            acc[d] += x * x;
+        }
+    for (int d = 0; d < 6; d++) {
+        double t = block_sum_d(acc[d], sm);
+        if (threadIdx.x == 0) p2[d] = t;
+    }
+    }
+    if (threadIdx.x < 50) bins[threadIdx.x] = 0;
+    __shared__ float rsc_s;
+    __shared__ int do_bins;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        hh.r = hh.vrms = 0;
+        for (int k = 0; k < 6; k++) {
+            if (k < 3) hh.r = (float)((double)hh.r + p2[k] / (double)np);
+            else hh.vrms = (float)((double)hh.vrms + p2[k] / (double)np);
+        }
+        double pe = (double)hh.r / (double)np, ve = (double)hh.vrms / (double)np;
+        if ((!hh.min_pos_err) || ((double)hh.min_pos_err > pe)) {
+            hh.min_pos_err = (float)pe;
+            hh.n_core = hh.num_p;
+            for (int k = 0; k < 3; k++) hh.pos[k] = (float)mean[k];
+        }
+        if ((!hh.min_vel_err) || ((double)hh.min_vel_err > ve)) {
+            hh.min_vel_err = (float)ve;
+            for (int k = 3; k < 6; k++) hh.pos[k] = (float)mean[k];
+        }
+        for (int k = 3; k < 6; k++) hh.bulkvel[k - 3] = (float)mean[k];
+        hh.m = (float)hh.num_p;
+        if (!hh.num_child_particles) hh.num_child_particles = hh.num_p;
+        hh.r = (float)cbrt((double)hh.num_p / ((4.0 * M_PI / 3.0) * C->rvir_dens));
+        hh.child_r = (float)cbrt((double)hh.num_child_particles / ((4.0 * M_PI / 3.0) * C->rvir_dens));
+        hh.vmax = hh.vmax_r = 0;
+        do_bins = (hh.child_r > 0);
+        rsc_s = (float)(50.0 / (double)hh.child_r);
+    }
+    __syncthreads();
+    if (do_bins) {
+        float rsc = rsc_s;
+        float c0 = hh.pos[0], c1 = hh.pos[1], c2 = hh.pos[2];
+        for (int i = threadIdx.x; i < np; i += blockDim.x) {
+            float dx, ds = 0.f;
+            dx = fsub(c0, W[ps + i].pos[0]); ds = fadd(ds, fmul(dx, dx));
+            dx = fsub(c1, W[ps + i].pos[1]); ds = fadd(ds, fmul(dx, dx));
+            dx = fsub(c2, W[ps + i].pos[2]); ds = fadd(ds, fmul(dx, dx));
+            int64_t b = (int64_t)(sqrt((double)ds) * (double)rsc);
+            if (b < 50) atomicAdd(&bins[b], 1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (do_bins) {
+            float rsc = rsc_s, vm = 0.f;
+            int64_t tp = 0;
+            for (int i = 0; i < 50; i++) {
+                float r = (float)((i + 1.0) / (double)rsc);
+                if ((double)r < C->force_res) r = (float)C->force_res;
+                tp += bins[i];
+                float vc = __fdiv_rn(__ll2float_rn(tp), r);
+                if (vc > vm) vm = vc;
+            }
+            float sn = (float)C->scale_now;
+            float v = (float)sqrt(RSG_GC * (double)vm * C->particle_mass / (double)sn);
+            hh.vmax = v;
+            hh.vmax_r = (float)(sqrt((double)sn) * (double)v * C->dyn_time);
+        }
+        if (hh.vmax_r) hh.r = hh.vmax_r;
+        hh.vrms = (float)sqrt((double)hh.vrms);
+    }
+}
+
+// growing-halo list of a level: node glist entries concatenated
+__global__ void k_list_growing(HierNodes N, int32_t base, int32_t count, const int32_t *goff,
+                               const int32_t *glist, int32_t *list) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    for (int g = 0; g < N.ng[node]; g++) list[goff[k] + g] = glist[N.h0[node] + g];
+}
+__global__ void k_ng(HierNodes N, int32_t base, int32_t count, int32_t *out, int all) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > count) return;
+    if (k == count) { out[k] = 0; return; }
+    int node = base + k;
+    out[k] = all ? N.h1[node] - N.h0[node] : N.ng[node];
+}
+__global__ void k_list_all(HierNodes N, int32_t base, int32_t count, const int32_t *off,
+                           int32_t *list) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    for (int h = N.h0[node]; h < N.h1[node]; h++) list[off[k] + h - N.h0[node]] = h;
+}
+
+// Biggest halo among growing ones (all = 0) or all halos (all = 1).
+__global__ void k_maxi(HierNodes N, int32_t base, int32_t count, const rsg_halo *H,
+                       const int32_t *glist, int all) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    int h0 = N.h0[node];
+    N.maxi[node] = all ? biggest(H, h0, N.h1[node], 0, 0)
+                       : biggest(H, h0, N.h1[node], 1, glist[h0]);
+}
+
+// find_best_parent (src/subhalo_metric.c:185-191) over the node's listed halos.
+__global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const int32_t *loff,
+                              const int32_t *list, const int32_t *hnode, rsg_halo *H,
+                              rsg_extra_halo_info *E) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int tot = loff[count];
+    if (t >= tot) return;
+    int h = list[t];
+    int k = hnode[t];
+    int node = base + k;
+    int mi = N.maxi[node];
+    int res = h;
+    if (h != mi) {
+        float best = hdist(H[mi], H[h]);
+        res = mi;
+        for (int g = loff[k]; g < loff[k + 1]; g++) {
+            int c = list[g];
+            float m = hdist(H[c], H[h]);
+            if (m < best) {
+                best = m;
+                res = c;
+            }
+        }
+    }
+    E[h].sub_of = res;
+}
+__global__ void k_list_node(int32_t count, const int32_t *loff, int32_t *hnode) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    for (int g = loff[k]; g < loff[k + 1]; g++) hnode[g] = k;
+}
+
+// _fix_parents (src/groupies.c:425-485) and calc_num_child_particles
+// (src/properties.c:139-163) for the node's halo range; one thread per node.
+__device__ void fix_parents_dev(rsg_halo *H, rsg_extra_halo_info *E, int h0, int h1) {
+    for (int i = h0; i < h1; i++) {
+        E[i].next_cochild = E[i].prev_cochild = E[i].child = -1;
+        if (E[i].sub_of == i) E[i].sub_of = -1;
+    }
+    for (int i = h0; i < h1; i++) {
+        E[i].max_metric = 1e10f;
+        int64_t so = E[i].sub_of;
+        if (so < 0) continue;
+        E[i].max_metric = pdist(H[i], H[so].pos);
+        int64_t nx = E[so].child;
+        E[i].next_cochild = nx;
+        E[i].prev_cochild = -1;
+        E[so].child = i;
+        if (nx > -1) E[nx].prev_cochild = i;
+    }
+}
+__device__ void num_child_dev(rsg_halo *H, const rsg_extra_halo_info *E, int h0, int h1,
+                              int32_t *stk) {
+    for (int i = h0; i < h1; i++) H[i].num_child_particles = 0;
+    for (int i = h0; i < h1; i++) {
+        if (H[i].num_child_particles) continue;
+        // iterative post-order walk of the child lists from i
+        int sp = 0;
+        stk[sp++] = i;
+        H[i].num_child_particles = H[i].num_p;
+        int guard = 0;
+        while (sp && ++guard < 100000000) {
+            int h = stk[sp - 1];
+            // find the first child not yet accumulated: children are
+            // accumulated in list order, marked by a cursor kept in stk
+            // entries above the halo; use the sign of flags bit 30 as visited
+            int64_t c = E[h].child;
+            bool pushed = false;
+            while (c > -1) {
+                if (!(H[c].flags & (1 << 30))) {
+                    H[c].flags |= (1 << 30);
+                    if (!H[c].num_child_particles) {
+                        H[c].num_child_particles = H[c].num_p;
+                        stk[sp++] = (int)c;
+                        pushed = true;
+                        break;
+                    }
+                    H[h].num_child_particles += H[c].num_child_particles;
+                }
+                c = E[c].next_cochild;
+            }
+            if (pushed) continue;
+            sp--;
+            if (sp) H[stk[sp - 1]].num_child_particles += H[h].num_child_particles;
+        }
+    }
+    for (int i = h0; i < h1; i++) H[i].flags &= ~(int64_t)(1 << 30);
+}
+__global__ void k_fix_parents(HierNodes N, int32_t base, int32_t count, rsg_halo *H,
+                              rsg_extra_halo_info *E, int32_t *stk) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    fix_parents_dev(H, E, N.h0[node], N.h1[node]);
+    num_child_dev(H, E, N.h0[node], N.h1[node], stk + N.h0[node]);
+}
+__global__ void k_num_child(HierNodes N, int32_t base, int32_t count, rsg_halo *H,
+                            const rsg_extra_halo_info *E, int32_t *stk) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int node = base + k;
+    num_child_dev(H, E, N.h0[node], N.h1[node], stk + N.h0[node]);
+}
+
+// core sort keys: within each halo of the level-0 nodes, by float squared
+// distance to the halo position (src/fun_times.c:204-214)
+__global__ void k_corekeys(const Rec *W, const int32_t *eln, int64_t M, const int32_t *phalo,
+                           const rsg_halo *H, uint64_t *key, uint32_t *val) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    uint64_t kk;
+    if (eln[i] < 0) kk = ((uint64_t)i << 32);
+    else {
+        const rsg_halo &h = H[phalo[i]];
+        float dx = 0.f, ds;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            ds = fsub(h.pos[j], W[i].pos[j]);
+            dx = fadd(dx, fmul(ds, ds));
+        }
+        kk = ((uint64_t)h.p_start << 32) | (uint64_t)f2ord(dx);
+    }
+    key[i] = kk;
+    val[i] = (uint32_t)i;
+}
+
+// Output: caller particles in the final order, halo p_start relative to it.
+__global__ void k_write_back(const Rec *W, int64_t M, const int32_t *wgroup,
+                             const int64_t *goff, const int64_t *woff, const rsg_particle *Pin,
+                             rsg_particle *Pout) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int g = wgroup[i];
+    Pout[goff[g] + (i - woff[g])] = Pin[W[i].ridx];
+}
+__global__ void k_halo_out(rsg_halo *H, rsg_extra_halo_info *E, int32_t nh, const int32_t *hgrp,
+                           const int64_t *goff, const int64_t *woff) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= nh) return;
+    int g = hgrp[h];
+    H[h].p_start = goff[g] + (H[h].p_start - woff[g]);
+}
+__global__ void k_halo_group(HierNodes N, const int32_t *leaves, int32_t nl, int32_t *hgrp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nl) hgrp[i] = N.group[leaves[i]];
+}
+__global__ void k_make_w(const rsg_particle *P, int64_t ng, const int64_t *goff,
+                         const int64_t *woff, const int64_t *gsz, Rec *W, int32_t *wgroup,
+                         HierNodes N) {
+    int g = blockIdx.x;
+    if (g >= ng) return;
+    int64_t s = woff[g], n = gsz[g], o = goff[g];
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        Rec r;
+#pragma unroll
+        for (int d = 0; d < 6; d++) r.pos[d] = P[o + i].pos[d];
+        r.ridx = (int32_t)(o + i);
+        r.aux = 0;
+        W[s + i] = r;
+        wgroup[s + i] = g;
+    }
+    if (threadIdx.x == 0) {
+        N.start[g] = (int32_t)s;
+        N.n[g] = (int32_t)n;
+        N.parent[g] = -1;
+        N.group[g] = g;
+        N.level[g] = 0;
+        N.nchild[g] = 0;
+    }
+}
+
+// ---- host driver ------------------------------------------------------------
+
+template <class K, class V>
+static void sort_pairs(Arena &ar, K *k, K *k2, V *v, V *v2, int64_t n, int bits, cudaStream_t st) {
+    size_t b = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, b, k, k2, v, v2, (int)n, 0, bits, st);
+    size_t m = ar.used;
+    void *t = ar.take(b + 256);
+    cub::DeviceRadixSort::SortPairs(t, b, k, k2, v, v2, (int)n, 0, bits, st);
+    RSG_CHECK_LAUNCH();
+    ar.used = m;
+}
+template <class T>
+static int32_t excl_scan(Arena &ar, const T *in, T *out, int32_t n, cudaStream_t st) {
+    size_t b = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, b, in, out, n, st);
+    size_t m = ar.used;
+    void *t = ar.take(b + 256);
+    cub::DeviceScan::ExclusiveSum(t, b, in, out, n, st);
+    RSG_CHECK_LAUNCH();
+    ar.used = m;
+    T last = 0;
+    RSG_CUDA(cudaMemcpyAsync(&last, out + n - 1, sizeof(T), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    return (int32_t)last;
+}
+static int32_t select_flagged(Arena &ar, const int32_t *flag, int32_t *out, int64_t n,
+                              int32_t first, cudaStream_t st) {
+    int *cnt = ar.get<int>(1);
+    size_t b = 0;
+    cub::DeviceSelect::Flagged(nullptr, b, thrust::counting_iterator<int32_t>(first), flag, out,
+                               cnt, (int)n, st);
+    size_t m = ar.used;
+    void *t = ar.take(b + 256);
+    cub::DeviceSelect::Flagged(t, b, thrust::counting_iterator<int32_t>(first), flag, out, cnt,
+                               (int)n, st);
+    RSG_CHECK_LAUNCH();
+    ar.used = m;
+    int h = 0;
+    RSG_CUDA(cudaMemcpyAsync(&h, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    return h;
+}
+
+DevCfg make_devcfg(const rsg_config &c) {
+    DevCfg d;
+    d.particle_mass = c.particle_mass;
+    d.force_res = c.force_res;
+    d.scale_now = c.scale_now;
+    d.initial_metric_scaling = c.initial_metric_scaling;
+    d.include_host_potential_ratio = c.include_host_potential_ratio;
+    d.fof_fraction = c.fof_fraction;
+    for (int i = 0; i < 5; i++) d.thresh_dens[i] = c.particle_thresh_dens[i];
+    d.rvir_dens = c.particle_rvir_dens;
+    d.rvir_dens_z0 = c.particle_rvir_dens_z0;
+    d.dyn_time = c.dynamical_time;
+    d.om = c.om;
+    d.ol = c.ol;
+    d.w0 = c.w0;
+    d.wa = c.wa;
+    d.min_halo_particles = c.min_halo_particles;
+    d.bound_props = c.bound_props;
+    d.shape_iterations = c.shape_iterations;
+    d.weighted_shapes = c.weighted_shapes;
+    d.exact_ll_calc = c.exact_ll_calc;
+    return d;
+}
+
+SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int64_t *goff_h,
+                         const int64_t *gsz_h, int64_t ngroups, const rsg_config &cfg,
+                         rsg_halo *d_halos, rsg_extra_halo_info *d_extra, int64_t max_halos,
+                         cudaStream_t st) {
+    SubsOut out{0};
+    const int T = 256;
+    // groups with particles, their working offsets
+    std::vector<int64_t> goff, gsz, woff;
+    int64_t M = 0;
+    for (int64_t g = 0; g < ngroups; g++) {
+        if (gsz_h[g] <= 0) continue;
+        if (goff_h[g] < 0 || goff_h[g] + gsz_h[g] > num_p) {
+            set_error(RSG_ERR_ARGS, "group %lld out of range", (long long)g);
+            throw Failure();
+        }
+        goff.push_back(goff_h[g]);
+        gsz.push_back(gsz_h[g]);
+        woff.push_back(M);
+        M += gsz_h[g];
+    }
+    int64_t G = (int64_t)goff.size();
+    if (G == 0) return out;
+    if (M >= (1ll << 31) - 1) {
+        set_error(RSG_ERR_ARGS, "find_subs supports up to 2^31-2 particles per call");
+        throw Failure();
+    }
+    DevCfg dc = make_devcfg(cfg);
+    DevCfg *d_dc = ar.get<DevCfg>(1);
+    RSG_CUDA(cudaMemcpyAsync(d_dc, &dc, sizeof(dc), cudaMemcpyHostToDevice, st));
+    int64_t *d_goff = ar.get<int64_t>(G), *d_gsz = ar.get<int64_t>(G), *d_woff = ar.get<int64_t>(G);
+    RSG_CUDA(cudaMemcpyAsync(d_goff, goff.data(), 8 * G, cudaMemcpyHostToDevice, st));
+    RSG_CUDA(cudaMemcpyAsync(d_gsz, gsz.data(), 8 * G, cudaMemcpyHostToDevice, st));
+    RSG_CUDA(cudaMemcpyAsync(d_woff, woff.data(), 8 * G, cudaMemcpyHostToDevice, st));
+
+    // hierarchy node table
+    int64_t cap = G + (M / 10) * 2 + 4096;
+    HierNodes N;
+    N.cap = (int32_t)cap;
+    N.start = ar.get<int32_t>(cap); N.n = ar.get<int32_t>(cap); N.parent = ar.get<int32_t>(cap);
+    N.group = ar.get<int32_t>(cap); N.level = ar.get<int32_t>(cap); N.nchild = ar.get<int32_t>(cap);
+    N.h0 = ar.get<int32_t>(cap); N.h1 = ar.get<int32_t>(cap); N.maxi = ar.get<int32_t>(cap);
+    N.ng = ar.get<int32_t>(cap); N.target_r = ar.get<float>(cap);
+
+    Rec *W = ar.get<Rec>(M), *W2 = ar.get<Rec>(M);
+    int32_t *wgroup = ar.get<int32_t>(M);
+    int32_t *eln = ar.get<int32_t>(M), *eln2 = ar.get<int32_t>(M);
+    int32_t *phalo = ar.get<int32_t>(M), *phalo2 = ar.get<int32_t>(M);
+    uint64_t *key = ar.get<uint64_t>(M), *key2 = ar.get<uint64_t>(M);
+    uint32_t *val = ar.get<uint32_t>(M), *val2 = ar.get<uint32_t>(M);
+    int *par = ar.get<int>(M + 1), *root = ar.get<int>(M + 1), *csize = ar.get<int>(M + 1);
+    int32_t *hflag = ar.get<int32_t>(M + 1);
+    int *err = ar.get<int>(4);
+    RSG_CUDA(cudaMemsetAsync(err, 0, 16, st));
+    k_make_w<<<(int)G, T, 0, st>>>(d_p, G, d_goff, d_woff, d_gsz, W, wgroup, N);
+    RSG_CHECK_LAUNCH();
+
+    // ---------------- descending ----------------
+    std::vector<int32_t> lvl_base{0}, lvl_cnt{(int32_t)G};
+    int32_t nn = (int32_t)G;
+    int keybits = 32 + 1;
+    while ((1ll << (keybits - 32)) <= M) keybits++;
+    for (int L = 0;; L++) {
+        int32_t base = lvl_base[L], cnt = lvl_cnt[L];
+        if (cnt == 0) break;
+        if (L > 100000) {
+            set_error(RSG_ERR_LIMIT, "subgroup hierarchy too deep");
+            throw Failure();
+        }
+        size_t mark = ar.used;
+        {
+            double *sig = ar.get<double>(2 * (int64_t)cnt);
+            k_norm_seq<<<nblk(cnt, 32), 32, 0, st>>>(W, N, base, cnt, L == 0,
+                                                     cfg.initial_metric_scaling, sig);
+            k_norm_par<<<cnt, T, 0, st>>>(W, N, base, L == 0, cfg.initial_metric_scaling, sig);
+            k_norm_div<<<cnt, T, 0, st>>>(W, N, base, sig);
+            RSG_CHECK_LAUNCH();
+        }
+        int32_t *rst = N.start + base, *rn = N.n + base;
+        std::vector<int32_t> hs(cnt), hn(cnt);
+        RSG_CUDA(cudaMemcpyAsync(hn.data(), rn, 4 * cnt, cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaMemcpyAsync(hs.data(), rst, 4 * cnt, cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        int64_t nin = 0;
+        std::vector<int32_t> so(cnt);
+        int64_t tot = 0;
+        for (int k = 0; k < cnt; k++) {
+            so[k] = (int32_t)tot;
+            int nt = cfg.exact_ll_calc ? hn[k] : (hn[k] < 10000 ? hn[k] : 10000);
+            tot += nt;
+            nin += hn[k];
+        }
+        // 6D kd-forest over this level's nodes (src/groupies.c:294)
+        Forest<6> F = build_forest<6, Rec>(ar, W, M, rst, rn, cnt, nin, 40, st);
+        int32_t *soff = ar.get<int32_t>(cnt);
+        RSG_CUDA(cudaMemcpyAsync(soff, so.data(), 4 * cnt, cudaMemcpyHostToDevice, st));
+        int32_t *sidx = ar.get<int32_t>(tot + 1);
+        float *prad = ar.get<float>(tot + 1);
+        unsigned *seeds = ar.get<unsigned>(cnt);
+        k_sample<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, soff, sidx, seeds,
+                                               (int)cfg.exact_ll_calc);
+        k_nn<<<cnt, 128, 0, st>>>(F.nodes, W, N, base, soff, sidx, prad, (int)cfg.exact_ll_calc,
+                                  err);
+        k_target<<<nblk(cnt, 32), 32, 0, st>>>(N, base, cnt, soff, prad, seeds,
+                                               (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
+        RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
+        k_fill_eln<<<cnt, T, 0, st>>>(N, base, eln);
+        // later neighbours within target_r, as CSR lists
+        int32_t *ncnt = par, *noff = root;
+        RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
+        k_fof6<<<nblk(M, T), T, 0, st>>>(F.nodes, W, M, N, base, eln, nullptr, ncnt, nullptr, err);
+        int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
+        int32_t *nbr = ar.get<int32_t>(ne + 1);
+        k_fof6<<<nblk(M, T), T, 0, st>>>(F.nodes, W, M, N, base, eln, noff, ncnt, nbr, err);
+        // reference labels, then the reference's partition sort by label
+        k_replay6<<<nblk(cnt, 32), 32, 0, st>>>(N, base, cnt, noff, nbr, phalo, csize);
+        RSG_CHECK_LAUNCH();
+        partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
+        k_run_heads<<<nblk(M, T), T, 0, st>>>(eln, M, N, base, phalo, hflag);
+        int32_t *heads = ar.get<int32_t>(M);
+        int32_t nh = select_flagged(ar, hflag, heads, M, 0, st);
+        int32_t *cflag = ar.get<int32_t>(nh + 1), *clen = ar.get<int32_t>(nh + 1);
+        int32_t *cidx = ar.get<int32_t>(nh + 1);
+        int32_t nc = 0;
+        if (nh) {
+            k_run_children<<<nblk(nh, T), T, 0, st>>>(heads, nh, eln, N, base, phalo,
+                                                      cfg.min_halo_particles, cflag, clen);
+            nc = select_flagged(ar, cflag, cidx, nh, 0, st);
+        }
+        if (nn + (int64_t)nc > cap) {
+            set_error(RSG_ERR_LIMIT, "subgroup node capacity exceeded");
+            throw Failure();
+        }
+        if (nc) k_make_children2<<<nblk(nc, T), T, 0, st>>>(cidx, nc, heads, clen, eln, N, base, nn);
+        RSG_CHECK_LAUNCH();
+        ar.used = mark;
+        lvl_base.push_back(nn);
+        lvl_cnt.push_back(nc);
+        nn += nc;
+    }
+    int nlev = (int)lvl_base.size() - 1;  // the last entry has count 0
+    {
+        g_dbg_level.resize(nn);
+        g_dbg_start.resize(nn);
+        g_dbg_n.resize(nn);
+        g_dbg_target.resize(nn);
+        RSG_CUDA(cudaMemcpyAsync(g_dbg_level.data(), N.level, 4 * nn, cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaMemcpyAsync(g_dbg_start.data(), N.start, 4 * nn, cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaMemcpyAsync(g_dbg_n.data(), N.n, 4 * nn, cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaMemcpyAsync(g_dbg_target.data(), N.target_r, 4 * nn, cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+    }
+
+    // ---------------- halos ----------------
+    int32_t *nflag = ar.get<int32_t>(nn), *leaves = ar.get<int32_t>(nn);
+    k_leaf_flags<<<nblk(nn, T), T, 0, st>>>(N, nn, nflag);
+    int32_t NH = select_flagged(ar, nflag, leaves, nn, 0, st);
+    if (NH > max_halos) {
+        set_error(RSG_ERR_ARGS, "%d halos exceed max_halos %lld", NH, (long long)max_halos);
+        throw Failure();
+    }
+    {
+        int32_t *lk = ar.get<int32_t>(NH), *lk2 = ar.get<int32_t>(NH), *lv2 = ar.get<int32_t>(NH);
+        k_leaf_keys<<<nblk(NH, T), T, 0, st>>>(N, leaves, NH, lk);
+        sort_pairs(ar, lk, lk2, leaves, lv2, NH, 32, st);
+        RSG_CUDA(cudaMemcpyAsync(leaves, lv2, 4 * NH, cudaMemcpyDeviceToDevice, st));
+        k_halo_ranges<<<nblk(nn, T), T, 0, st>>>(N, nn, lk2, NH);
+    }
+    rsg_halo *H = d_halos;
+    rsg_extra_halo_info *E = d_extra;
+    k_halo_init<<<nblk(NH, T), T, 0, st>>>(H, E, NH);
+    int32_t *glist = ar.get<int32_t>(NH), *redirect = ar.get<int32_t>(NH);
+    int32_t *stk = ar.get<int32_t>(NH + 1);
+    RSG_CHECK_LAUNCH();
+
+    // ---------------- ascending ----------------
+    for (int L = nlev - 1; L >= 0; L--) {
+        int32_t base = lvl_base[L], cnt = lvl_cnt[L];
+        if (cnt == 0) continue;
+        size_t mark = ar.used;
+        k_asc_mark<<<cnt, T, 0, st>>>(W, d_p, N, base, H, phalo);
+        k_asc_seed<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, H, E, glist, redirect, cfg.force_res);
+        k_asc_assign<<<cnt, T, 0, st>>>(W, N, base, H, E, glist, redirect, phalo);
+        RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
+        k_fill_eln<<<cnt, T, 0, st>>>(N, base, eln);
+        RSG_CHECK_LAUNCH();
+        {
+            // reassign_halo_particles: the reference's partition by halo index
+            std::vector<int32_t> hs(cnt), hn(cnt);
+            RSG_CUDA(cudaMemcpyAsync(hn.data(), N.n + base, 4 * cnt, cudaMemcpyDeviceToHost, st));
+            RSG_CUDA(cudaMemcpyAsync(hs.data(), N.start + base, 4 * cnt, cudaMemcpyDeviceToHost, st));
+            RSG_CUDA(cudaStreamSynchronize(st));
+            partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
+        }
+        k_halo_heads<<<nblk(M, T), T, 0, st>>>(eln, M, N, base, phalo, H);
+        k_halo_tails<<<nblk(M, T), T, 0, st>>>(eln, M, N, base, phalo, H);
+        // growing list of the level
+        int32_t *goffs = ar.get<int32_t>(cnt + 1);
+        k_ng<<<nblk(cnt + 1, T), T, 0, st>>>(N, base, cnt, goffs, 0);
+        int32_t ngr = excl_scan(ar, goffs, goffs, cnt + 1, st);
+        int32_t *glv = ar.get<int32_t>(ngr + 1), *gnode = ar.get<int32_t>(ngr + 1);
+        k_list_growing<<<nblk(cnt, T), T, 0, st>>>(N, base, cnt, goffs, glist, glv);
+        k_list_node<<<nblk(cnt, T), T, 0, st>>>(cnt, goffs, gnode);
+        if (ngr) k_basic_props<<<ngr, T, 0, st>>>(W, H, glv, d_dc);
+        k_maxi<<<nblk(cnt, T), T, 0, st>>>(N, base, cnt, H, glist, 0);
+        k_best_parent<<<nblk(ngr, T), T, 0, st>>>(N, base, cnt, goffs, glv, gnode, H, E);
+        k_fix_parents<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, H, E, stk);
+        if (ngr) k_basic_props<<<ngr, T, 0, st>>>(W, H, glv, d_dc);
+        RSG_CHECK_LAUNCH();
+        if (L == 0) {
+            int32_t *aoff = ar.get<int32_t>(cnt + 1);
+            k_ng<<<nblk(cnt + 1, T), T, 0, st>>>(N, base, cnt, aoff, 1);
+            int32_t na = excl_scan(ar, aoff, aoff, cnt + 1, st);
+            int32_t *alist = ar.get<int32_t>(na + 1), *anode = ar.get<int32_t>(na + 1);
+            k_list_all<<<nblk(cnt, T), T, 0, st>>>(N, base, cnt, aoff, alist);
+            k_list_node<<<nblk(cnt, T), T, 0, st>>>(cnt, aoff, anode);
+            if (na) k_basic_props<<<na, T, 0, st>>>(W, H, alist, d_dc);
+            k_corekeys<<<nblk(M, T), T, 0, st>>>(W, eln, M, phalo, H, key, val);
+            sort_pairs(ar, key, key2, val, val2, M, keybits, st);
+            k_gather<Rec><<<nblk(M, T), T, 0, st>>>(W, val2, M, W2);
+            k_gather<int32_t><<<nblk(M, T), T, 0, st>>>(phalo, val2, M, phalo2);
+            std::swap(W, W2);
+            std::swap(phalo, phalo2);
+            k_maxi<<<nblk(cnt, T), T, 0, st>>>(N, base, cnt, H, glist, 1);
+            k_best_parent<<<nblk(na, T), T, 0, st>>>(N, base, cnt, aoff, alist, anode, H, E);
+            k_fix_parents<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, H, E, stk);
+            RSG_CHECK_LAUNCH();
+            // find_subs tail (src/groupies.c:697-703): child counts and basic
+            // properties for every halo, then the additional properties.
+            k_num_child<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, H, E, stk);
+            if (na) k_basic_props<<<na, T, 0, st>>>(W, H, alist, d_dc);
+            RSG_CHECK_LAUNCH();
+        }
+        ar.used = mark;
+    }
+    additional_props(ar, dc, d_dc, W, M, H, E, NH, st);
+
+    // outputs
+    int32_t *hgrp = ar.get<int32_t>(NH + 1);
+    k_halo_group<<<nblk(NH, T), T, 0, st>>>(N, leaves, NH, hgrp);
+    k_halo_out<<<nblk(NH, T), T, 0, st>>>(H, E, NH, hgrp, d_goff, d_woff);
+    rsg_particle *Pcopy = ar.get<rsg_particle>(num_p);
+    RSG_CUDA(cudaMemcpyAsync(Pcopy, d_p, sizeof(rsg_particle) * num_p, cudaMemcpyDeviceToDevice, st));
+    k_write_back<<<nblk(M, T), T, 0, st>>>(W, M, wgroup, d_goff, d_woff, Pcopy, d_p);
+    RSG_CHECK_LAUNCH();
+    int herr[4];
+    RSG_CUDA(cudaMemcpyAsync(herr, err, 16, cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    if (herr[0]) {
+        set_error(RSG_ERR_LIMIT, "6D kd-tree traversal stack overflow");
+        throw Failure();
+    }
+    out.nhalos = NH;
+    return out;
+}
+
+}  // namespace rsg

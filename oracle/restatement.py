@@ -59,6 +59,8 @@ def lib():
         h.oracle_compute_potential.argtypes = [vp, i64]
         h.oracle_kinetic_energy.argtypes = [vp, i64, vp, vp, C.c_float]
         h.oracle_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
+        h.oracle_hierarchy.restype = i64
+        h.oracle_hierarchy.argtypes = [vp, vp, vp, i64]
         _lib = h
     return _lib
 
@@ -118,3 +120,13 @@ def tree_order(parts, dim, leaf):
     pa = np.array(parts, dtype=L.PARTICLE, copy=True)
     lib().oracle_tree_order(pa.ctypes.data, len(pa), dim, leaf)
     return pa
+
+
+def hierarchy():
+    """(level, size, target_r) of every 6D FOF call of the last find_subs."""
+    cap = 1 << 22
+    lv = np.zeros(cap, np.int64)
+    n = np.zeros(cap, np.int64)
+    tr = np.zeros(cap, np.float32)
+    k = min(lib().oracle_hierarchy(lv.ctypes.data, n.ctypes.data, tr.ctypes.data, cap), cap)
+    return lv[:k].copy(), n[:k].copy(), tr[:k].copy()

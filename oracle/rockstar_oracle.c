@@ -565,6 +565,18 @@ static float kth_radius(float *a, int64_t n, float frac, unsigned *seed) {
 }
 
 static struct ktree ptree6;
+/* test hook: (level, n, target_r) of every 6D FOF call, in call order */
+static int64_t *rec_level, *rec_n; static float *rec_tr; static int64_t rec_cnt, rec_cap, cur_level;
+static void rec_push(int64_t n, float tr) {
+    if (rec_cnt == rec_cap) { rec_cap = rec_cap * 2 + 1024;
+        rec_level = realloc(rec_level, 8 * rec_cap); rec_n = realloc(rec_n, 8 * rec_cap);
+        rec_tr = realloc(rec_tr, 4 * rec_cap); }
+    rec_level[rec_cnt] = cur_level; rec_n[rec_cnt] = n; rec_tr[rec_cnt] = tr; rec_cnt++;
+}
+int64_t oracle_hierarchy(int64_t *level, int64_t *n, float *tr, int64_t cap) {
+    for (int64_t i = 0; i < rec_cnt && i < cap; i++) { level[i] = rec_level[i]; n[i] = rec_n[i]; tr[i] = rec_tr[i]; }
+    return rec_cnt;
+}
 static struct ilist qres;
 static struct uf fuf;
 
@@ -588,6 +600,7 @@ static void find_subgroups(struct fofrec *f, float thresh, float *target_out) {
     }
     float tr = kth_radius(prad, nt, thresh, &seed);
     if (target_out) *target_out = tr;
+    rec_push(n, tr);
     /* 6D FOF at tr: every particle links to itself and later neighbours */
     int64_t *lab = malloc(sizeof(int64_t) * (n ? n : 1));
     for (int64_t i = 0; i < n; i++) lab[i] = -1;
@@ -850,6 +863,7 @@ static void find_subs_rec(struct fofrec *f0, int64_t fi, int64_t level, struct h
     int64_t p0 = f.particles - cp, fnp = f.num_p, i, j, mi;
     int force;
     int64_t fs = nsubf;
+    cur_level = level;
     find_subgroups(&f, (float)C.fof_fraction, NULL);
     int64_t fe = nsubf;
     int64_t h0 = hi->n;
@@ -1408,6 +1422,7 @@ static void find_subs_one(struct particle *pa, int64_t off, int64_t n, struct hi
 int64_t oracle_find_subs(struct particle *pa, const int64_t *off, const int64_t *sz, int64_t nf,
                          struct halo **ho, struct extra **eo) {
     struct hinfo hi = {0};
+    rec_cnt = 0;
     for (int64_t i = 0; i < nf; i++) find_subs_one(pa, off[i], sz[i], &hi);
     *ho = hi.h; *eo = hi.e;
     return hi.n;
