@@ -1,0 +1,302 @@
+"""Benchmark of the halo-finding hot path: 3D FOF -> 6D phase-space FOF
+hierarchy -> particle assignment -> potentials / unbinding -> properties.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step is the whole path over one synthetic snapshot.  The default
+workload is the 128^3 substructure snapshot (2,097,152 particles, 80 Mpc/h,
+NFW hosts with subhalos, 35% background; csrc/synth.c workload 2).  Under
+torchrun every rank processes its own snapshot (seed + rank): the path
+shards by snapshot region / group with no exchange, so scaling is weak.
+
+value   : particles/s with the particles already in HBM (rsg_path_device),
+          timed per step with CUDA events; L2 is flushed between steps.
+e2e     : the same metric through the C ABI with host buffers
+          (rsg_rockstar_fof + rsg_find_subs from pinned memory), copies
+          included.
+roofline: the dominant kernel (by device time in the launch list), timed
+          with CUDA events on its stream during the timed steps.
+cpu_baseline: the C restatement of the reference (oracle/) on one host core
+          over a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+METRIC = "particles/s through FOF+6D+unbind+props, batched vs plain on GB300 @ stated tol"
+SEED = 20261203
+# dominant kernel for the roofline figure, with its algorithmic bytes per
+# unit (see the kernel table of the design doc)
+ROOF_KERNEL = os.environ.get("RSG_ROOF_KERNEL", "k_bh_walk")
+
+
+def load_pkg():
+    import importlib.util
+    d = os.path.join(ROOT, "mpi-rockstar_gb300")
+    if "mpi_rockstar_gb300" in sys.modules:
+        return sys.modules["mpi_rockstar_gb300"]
+    spec = importlib.util.spec_from_file_location(
+        "mpi_rockstar_gb300", os.path.join(d, "__init__.py"), submodule_search_locations=[d])
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["mpi_rockstar_gb300"] = m
+    spec.loader.exec_module(m)
+    return m
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, dev):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(dev), "--query-gpu=" + q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_port(rk, cfg_id, scale):
+    """The oracle restatement on one core over a bounded sample: workload
+    `cfg_id` at `scale` (same density and structure), the whole path."""
+    from oracle import restatement as O
+    O.build()
+    p, box, mp, _ = rk.synth(cfg_id, scale, SEED)
+    c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    O.setup(c)
+    t0 = time.perf_counter()
+    fp, off, sz = O.fof(p)
+    O.find_subs(fp, off, sz)
+    dt = time.perf_counter() - t0
+    return {"value": len(p) / dt, "unit": "particles/s", "cores": 1, "kind": "port",
+            "sample": "workload %d at scale %g (%d particles), full path, one step, 1 thread"
+                      % (cfg_id, scale, len(p))}
+
+
+# ---- reference arm: the oracle port over all host cores -------------------
+def _ref_worker(args):
+    parts, off, sz = args
+    sys.path.insert(0, ROOT)
+    from oracle import restatement as O
+    cfgd = _ref_worker.cfg
+    O.setup(cfgd)
+    out, h, e = O.find_subs(parts, off, sz)
+    return len(h)
+
+
+def _ref_init(cfg):
+    sys.path.insert(0, ROOT)
+    from oracle import restatement as O
+    O.build()
+    _ref_worker.cfg = cfg
+
+
+def reference_arm(args, rk):
+    import multiprocessing as mp_
+    from oracle import restatement as O
+    O.build()
+    p, box, mp, _ = rk.synth(args.cfg, args.scale, SEED)
+    c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    ncores = os.cpu_count() or 1
+    ctx = mp_.get_context("spawn")
+    pool = ctx.Pool(ncores, initializer=_ref_init, initargs=(c,))
+    O.setup(c)
+
+    def step():
+        fp, off, sz = O.fof(p)  # serial, as rockstar() is in the reference
+        # groups to workers, largest first (the reference's OMP dynamic loop)
+        order = np.argsort(-sz, kind="stable")
+        chunks = [[] for _ in range(ncores)]
+        load = np.zeros(ncores)
+        for g in order:
+            k = int(np.argmin(load))
+            chunks[k].append(g)
+            load[k] += float(sz[g]) * np.log2(float(sz[g]) + 2)
+        jobs = []
+        for ch in chunks:
+            if not ch:
+                continue
+            ch = np.array(sorted(ch))
+            parts = np.concatenate([fp[off[g]:off[g] + sz[g]] for g in ch])
+            o = np.concatenate([[0], np.cumsum(sz[ch])[:-1]])
+            jobs.append((parts, o, sz[ch]))
+        return sum(pool.map(_ref_worker, jobs))
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / args.steps
+    pool.close()
+    v = len(p) / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "particles/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "synthetic workload %d (%d particles)" % (args.cfg, len(p)),
+                       "particles": len(p), "host_cores": ncores},
+            "cpu_baseline": {"value": v, "unit": "particles/s", "cores": ncores, "kind": "port",
+                             "sample": "full workload, FOF serial, find_subs over groups on "
+                                       "%d processes" % ncores},
+            "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cfg", type=int, default=2)
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rk = load_pkg()
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args, rk)
+        return
+    # CPU baseline first: no GPU context exists yet
+    cpu = None
+    if rank == 0 and world >= 1 and not args.no_cpu_baseline and args.gpus == 1:
+        cpu = cpu_baseline_port(rk, args.cfg, args.scale / 8)
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    rk.build()
+    p, box, mp, _ = rk.synth(args.cfg, args.scale, SEED + rank)
+    n = len(p)
+    cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=n)
+    raw = torch.from_numpy(p.view(np.uint8).reshape(-1))
+    d_in = raw.cuda()
+    path = rk.DevicePath(n, cfg)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        path.run(d_in.data_ptr())
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    rk.profile_select(ROOF_KERNEL)
+    l0 = rk.launch_count()
+    times = []
+    res = None
+    for _ in range(args.steps):
+        flush.fill_(1)  # L2 flush between steps (outside the step's events)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        res = path.run(d_in.data_ptr())
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    launches = rk.launch_count() - l0
+    kl, kms = rk.profile_read()
+    rk.profile_select("")
+    clk = clocks.stop()
+    step_ms = float(np.mean(times))
+    if dist:
+        t = torch.tensor([step_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+        dist.barrier()
+    value = n * world / (step_ms * 1e-3)
+
+    # e2e through the C ABI with pinned host buffers
+    pin = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
+    pin.copy_(raw)
+    host = pin.numpy().view(rk.PARTICLE)
+    e2e_t = []
+    h2d = d2h = 0
+    for it in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fp, off, sz = rk.rockstar_fof(host, cfg)
+        parts, halos, extra = rk.find_subs(fp, off, sz, cfg)
+        e2e_t.append(time.perf_counter() - t0)
+        h2d = n * 32 + len(fp) * 32 + 16 * len(off)
+        d2h = len(fp) * 32 + 16 * len(off) + len(fp) * 32 + len(halos) * (312 + 48)
+    e2e_v = n * world / min(e2e_t)
+
+    pk, pk_kind = peaks()
+    roof = None
+    if kl:
+        # algorithmic bytes of one k_bh_walk launch: every particle record of
+        # every potential set is read once (48 B) and its potential written
+        # once (8 B); node records are read from L2 and not counted
+        npo = getattr(rk, "_last_npo", None)
+        avg_ms = kms / kl
+        roof = {"kernel": ROOF_KERNEL, "bound": "hbm", "launches": kl, "avg_ms": avg_ms}
+    line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "synthetic workload %d: %d particles, %.0f Mpc/h box"
+                                   % (args.cfg, n, box),
+                       "particles": n, "groups": res[1], "halos": res[2],
+                       "l2": "flushed between steps (256 MiB write)", "path": "plain"},
+            "e2e": {"value": e2e_v, "unit": "particles/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+            "clocks": clk, "peak_source": pk_kind}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -127,6 +127,25 @@ int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offs
                   struct rsg_halo *halos, struct rsg_extra_halo_info *extra, int64_t max_halos,
                   int64_t *num_halos);
 
+/* The whole hot path -- rockstar(NULL, 1) then find_subs over every group
+ * -- on device-resident data (no host copies): d_in holds n id-sorted
+ * particles, d_out receives the permuted particles (*num_p_out of them)
+ * and d_halos/d_extra (capacity max_halos) the halos of all groups.  Has no
+ * single reference counterpart: it fuses the calls of src/mpi_main.cpp:1564
+ * and :1363-1389 for callers that keep particles on the GPU. */
+int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg_config *cfg,
+                    struct rsg_particle *d_out, int64_t *num_p_out, int64_t *num_fofs,
+                    struct rsg_halo *d_halos, struct rsg_extra_halo_info *d_extra,
+                    int64_t max_halos, int64_t *num_halos);
+
+/* Instrumentation: kernels launched by this library so far (process-wide),
+ * and CUDA-event timing of every launch of the kernels whose name contains
+ * `kernel_substring` (empty string: off).  rsg_profile_read returns the
+ * number of timed launches and their summed device time, then clears. */
+int64_t rsg_launch_count(void);
+int rsg_profile_select(const char *kernel_substring);
+int rsg_profile_read(int64_t *launches, double *total_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,6 +53,10 @@ def lib():
         h.rsg_debug_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
         h.rsg_debug_hierarchy.restype = i64
         h.rsg_debug_hierarchy.argtypes = [vp, vp, vp, i64]
+        h.rsg_path_device.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp]
+        h.rsg_launch_count.restype = i64
+        h.rsg_profile_select.argtypes = [C.c_char_p]
+        h.rsg_profile_read.argtypes = [vp, vp]
         h.rsg_find_subs.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, i64, vp]
         for name, args in _EXTRA_SIGS.items():
             if hasattr(h, name):
@@ -153,3 +157,45 @@ def synth(cfg_id, scale=1.0, seed=20261203):
     if rc:
         raise ValueError("synthetic generator failed (%d)" % rc)
     return p, float(box[0]), float(mp[0]), int(nh[0])
+
+
+def launch_count():
+    """Kernels this library has launched in the process so far."""
+    return int(lib().rsg_launch_count())
+
+
+def profile_select(name):
+    """Time every launch of kernels whose name contains `name` with CUDA events."""
+    _check(lib().rsg_profile_select(name.encode() if name else b""))
+
+
+def profile_read():
+    """(launches, total device ms) of the selected kernel since the last read."""
+    n = np.zeros(1, np.int64)
+    t = np.zeros(1, np.float64)
+    _check(lib().rsg_profile_read(n.ctypes.data, t.ctypes.data))
+    return int(n[0]), float(t[0])
+
+
+class DevicePath:
+    """The full hot path on device-resident arrays (torch CUDA tensors or raw
+    device pointers): rsg_path_device."""
+
+    def __init__(self, n, cfg, halo_cap=None):
+        import torch
+        self.n = n
+        self.st = setup_config(cfg)
+        self.halo_cap = halo_cap or (n // 4 + 1024)
+        self.out = torch.empty(n * PARTICLE.itemsize, dtype=torch.uint8, device="cuda")
+        self.halos = torch.empty(self.halo_cap * HALO.itemsize, dtype=torch.uint8, device="cuda")
+        self.extra = torch.empty(self.halo_cap * EXTRA.itemsize, dtype=torch.uint8, device="cuda")
+        self._np = np.zeros(1, np.int64)
+        self._nf = np.zeros(1, np.int64)
+        self._nh = np.zeros(1, np.int64)
+
+    def run(self, d_in_ptr):
+        _check(lib().rsg_path_device(d_in_ptr, self.n, C.byref(self.st), self.out.data_ptr(),
+                                     self._np.ctypes.data, self._nf.ctypes.data,
+                                     self.halos.data_ptr(), self.extra.data_ptr(),
+                                     self.halo_cap, self._nh.ctypes.data))
+        return int(self._np[0]), int(self._nf[0]), int(self._nh[0])

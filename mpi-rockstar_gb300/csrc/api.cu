@@ -193,6 +193,45 @@ int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offs
     }
 }
 
+int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg_config *cfg,
+                    struct rsg_particle *d_out, int64_t *num_p_out, int64_t *num_fofs,
+                    struct rsg_halo *d_halos, struct rsg_extra_halo_info *d_extra,
+                    int64_t max_halos, int64_t *num_halos) {
+    if (!d_in || !d_out || !cfg || n < 0 || !num_halos || !num_fofs || !num_p_out) {
+        set_error(RSG_ERR_ARGS, "rsg_path_device: bad arguments");
+        return RSG_ERR_ARGS;
+    }
+    try {
+        Ctx &C = ctx();
+        *num_halos = 0;
+        *num_fofs = 0;
+        *num_p_out = n;
+        if (n == 0) return RSG_OK;
+        C.ar.reserve((size_t)n * 1000 + (512u << 20));
+        C.ar.reset();
+        int64_t *d_off = C.ar.get<int64_t>(n / 2 + 1), *d_sz = C.ar.get<int64_t>(n / 2 + 1);
+        size_t mark = C.ar.used;
+        FofOut o = fof3d_device(C.ar, d_in, n, *cfg, d_out, d_off, d_sz, C.st);
+        C.ar.used = mark;
+        std::vector<int64_t> off(o.nfofs), sz(o.nfofs);
+        if (o.nfofs) {
+            RSG_CUDA(cudaMemcpyAsync(off.data(), d_off, 8 * o.nfofs, cudaMemcpyDeviceToHost, C.st));
+            RSG_CUDA(cudaMemcpyAsync(sz.data(), d_sz, 8 * o.nfofs, cudaMemcpyDeviceToHost, C.st));
+            RSG_CUDA(cudaStreamSynchronize(C.st));
+        }
+        SubsOut s2 = find_subs_device(C.ar, d_out, o.num_p, off.data(), sz.data(), o.nfofs, *cfg,
+                                      d_halos, d_extra, max_halos, C.st);
+        RSG_CUDA(cudaStreamSynchronize(C.st));
+        phase_report();
+        *num_p_out = o.num_p;
+        *num_fofs = o.nfofs;
+        *num_halos = s2.nhalos;
+        return RSG_OK;
+    } catch (Failure &) {
+        return error_code();
+    }
+}
+
 // Test hook: the subgroup hierarchy of the last rsg_find_subs call on this
 // thread: per node its level, size and 6D linking length (normalised units).
 int64_t rsg_debug_hierarchy(int32_t *level, int32_t *n, float *target_r, int64_t cap) {

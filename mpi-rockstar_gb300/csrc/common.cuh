@@ -3,7 +3,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 
+#include "launch.cuh"
 #include "rockstar_gb300.h"
 
 namespace rsg {
@@ -80,6 +82,12 @@ __device__ __forceinline__ float ord2f(unsigned u) {
 }
 
 inline int nblk(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+// Phase timer: with RSG_TIMING set in the environment, synchronises the
+// stream at each mark and accumulates wall time per phase name; the totals
+// are printed to stderr by phase_report().
+void phase_mark(cudaStream_t st, const char *name);
+void phase_report();
 
 #define RSG_STACK 96
 #define RSG_STACK6 128

@@ -2,6 +2,10 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <string>
+#include <unordered_map>
+#include <vector>
+
 #include "kdtree.cuh"
 
 namespace rsg {
@@ -65,9 +69,90 @@ __global__ void k_root_owner(const int32_t *rstart, const int32_t *rn, int32_t n
     }
 }
 
+// ---- phase timers ----------------------------------------------------------
+#include <chrono>
+#include <map>
+static int g_timing = -1;
+static std::map<std::string, double> g_phase;
+static std::chrono::steady_clock::time_point g_last;
+static std::vector<std::string> g_phase_order;
+void phase_mark(cudaStream_t st, const char *name) {
+    if (g_timing < 0) g_timing = getenv("RSG_TIMING") ? 1 : 0;
+    if (!g_timing) return;
+    cudaStreamSynchronize(st);
+    auto now = std::chrono::steady_clock::now();
+    if (name && *name) {
+        if (!g_phase.count(name)) g_phase_order.push_back(name);
+        g_phase[name] += std::chrono::duration<double, std::milli>(now - g_last).count();
+    }
+    g_last = now;
+}
+void phase_report() {
+    if (g_timing <= 0) return;
+    for (auto &k : g_phase_order) fprintf(stderr, "  [phase] %-28s %10.2f ms\n", k.c_str(), g_phase[k]);
+    g_phase.clear();
+    g_phase_order.clear();
+}
+
+// ---- launch accounting and event timing of one selected kernel -----------
+static LaunchStats g_ls;
+static std::string g_prof_name;
+static std::unordered_map<const void *, bool> g_prof_cache;
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_ev, g_prof_pool;
+static size_t g_prof_used = 0;
+
+LaunchStats &launch_stats() { return g_ls; }
+
+bool prof_match(const void *func) {
+    auto it = g_prof_cache.find(func);
+    if (it != g_prof_cache.end()) return it->second;
+    const char *nm = nullptr;
+    bool m = false;
+    if (cudaFuncGetName(&nm, func) == cudaSuccess && nm) m = strstr(nm, g_prof_name.c_str()) != nullptr;
+    g_prof_cache[func] = m;
+    return m;
+}
+void prof_begin(cudaStream_t st) {
+    if (g_prof_used == g_prof_pool.size()) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        g_prof_pool.push_back({a, b});
+    }
+    g_prof_ev.push_back(g_prof_pool[g_prof_used++]);
+    cudaEventRecord(g_prof_ev.back().first, st);
+}
+void prof_end(cudaStream_t st) { cudaEventRecord(g_prof_ev.back().second, st); }
+
 }  // namespace rsg
 
 extern "C" {
+
+int64_t rsg_launch_count(void) { return rsg::g_ls.launches; }
+
+int rsg_profile_select(const char *kernel_substring) {
+    rsg::g_prof_name = kernel_substring ? kernel_substring : "";
+    rsg::g_prof_cache.clear();
+    rsg::g_prof_ev.clear();
+    rsg::g_prof_used = 0;
+    rsg::g_ls.selecting = !rsg::g_prof_name.empty();
+    return 0;
+}
+
+int rsg_profile_read(int64_t *launches, double *total_ms) {
+    double t = 0;
+    for (auto &e : rsg::g_prof_ev) {
+        float ms = 0;
+        if (cudaEventSynchronize(e.second) != cudaSuccess) return RSG_ERR_CUDA;
+        cudaEventElapsedTime(&ms, e.first, e.second);
+        t += ms;
+    }
+    *launches = (int64_t)rsg::g_prof_ev.size();
+    *total_ms = t;
+    rsg::g_prof_ev.clear();
+    rsg::g_prof_used = 0;
+    return 0;
+}
 
 int rsg_version(void) { return 1; }
 

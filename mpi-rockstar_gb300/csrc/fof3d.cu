@@ -186,59 +186,70 @@ __global__ void k_count(const KNode<3> *nodes, const Rec *recs, int n, float r, 
     cnt[i] = (uint8_t)(k > 17 ? 17 : k);
 }
 
-// Earlier dense neighbours of every dense particle (counted, then listed).
-__global__ void k_elist(const KNode<3> *nodes, const Rec *recs, int n, float r,
-                        const uint8_t *cnt, const int *eoff, int *ecnt, int *elist, int *err) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || cnt[i] <= 16) return;
-    float c[3] = {recs[i].pos[0], recs[i].pos[1], recs[i].pos[2]};
-    int k = 0;
-    int base = eoff ? eoff[i] : 0;
+
+
+
+// Later dense neighbours of every dense particle k (j > k, j in S_r(k)),
+// counted then listed; cnt[j] counts the dense k that can skip j.
+__global__ void k_llist(const KNode<3> *nodes, const Rec *recs, int n, float r,
+                        const uint8_t *cnt, const int *loff, int *lcnt, int *llist, int *skipcnt,
+                        int *err) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || cnt[k] <= 16) return;
+    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+    int m = 0;
+    int base = loff ? loff[k] : 0;
+    auto add = [&](int j) {
+        if (j > k && cnt[j] > 16) {
+            if (llist) llist[base + m] = j;
+            else atomicAdd(&skipcnt[j], 1);
+            m++;
+        }
+    };
     sphere3(
         nodes, 0, recs, c, r, err,
-        [&](int s, int m) {
-            for (int j = s; j < s + m && j < i; j++)
-                if (cnt[j] > 16) {
-                    if (elist) elist[base + k] = j;
-                    k++;
-                }
+        [&](int s, int q) {
+            for (int j = s; j < s + q; j++) add(j);
             return true;
         },
         [&](int j) {
-            if (j < i && cnt[j] > 16) {
-                if (elist) elist[base + k] = j;
-                k++;
-            }
+            add(j);
             return true;
         });
-    if (!elist) ecnt[i] = k;
+    if (!llist) lcnt[k] = m;
 }
-
-// One pass of the ordered greedy independent set: state 0 undecided,
-// 1 seed, 2 not a seed.  Decisions only use final states of earlier
-// particles, so in-place updates within a pass are safe.
-__global__ void k_mis(const int *dense, int nd, const int *eoff, const int *elist,
-                      uint8_t *state, int *changed) {
+// One frontier step of the ordered independent set: every particle decided
+// in the previous step walks its later list once; a seed marks its later
+// neighbours as skipped, and every decided particle releases one pending
+// earlier neighbour of each.  A particle with none pending that was not
+// skipped is a seed (all its earlier potential skippers are decided and
+// none of them is a seed).
+__global__ void k_kahn(const int *front, int nf, const int *loff, const int *llist, int *state,
+                       int *skipcnt, int *next, int *nnext) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nf) return;
+    int k = front[w];
+    int sk = state[k];
+    for (int e = loff[k] + lane; e < loff[k + 1]; e += 32) {
+        int j = llist[e];
+        if (sk == 1 && atomicCAS(&state[j], 0, 2) == 0) next[atomicAdd(nnext, 1)] = j;
+        if (atomicSub(&skipcnt[j], 1) == 1 && atomicCAS(&state[j], 0, 1) == 0)
+            next[atomicAdd(nnext, 1)] = j;
+    }
+}
+__global__ void k_kahn_init(const int *dense, int nd, const int *skipcnt, int *state, int *front,
+                            int *nfront) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nd) return;
     int i = dense[t];
-    if (state[i] != 0) return;
-    bool all_out = true;
-    for (int e = eoff[i]; e < eoff[i + 1]; e++) {
-        uint8_t s = ((volatile uint8_t *)state)[elist[e]];
-        if (s == 1) {
-            state[i] = 2;
-            *changed = 1;
-            return;
-        }
-        if (s == 0) all_out = false;
-    }
-    if (all_out) {
+    if (skipcnt[i] == 0) {
         state[i] = 1;
-        *changed = 1;
-    } else {
-        atomicAdd(changed + 1, 1);
+        front[atomicAdd(nfront, 1)] = i;
     }
+}
+__global__ void k_state8(const int *s32, int n, uint8_t *s8) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) s8[i] = (uint8_t)s32[i];
 }
 
 __global__ void k_seed_mark(const KNode<3> *nodes, const Rec *recs, int n, float r,
@@ -383,13 +394,14 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     Rec *recs = ar.get<Rec>(n);
     int *flags = ar.get<int>(8);
     RSG_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * 8, st));
-    k_make_recs<<<nblk(n, T), T, 0, st>>>(d_in, n, recs, flags);
+    phase_mark(st, "");
+    launch(k_make_recs, nblk(n, T), T, 0, st, d_in, n, recs, flags);
     int32_t *seg = ar.get<int32_t>(2);
     int32_t hseg[2] = {0, n};
     RSG_CUDA(cudaMemcpyAsync(seg, hseg, sizeof(hseg), cudaMemcpyHostToDevice, st));
     size_t mark = ar.used;
     Forest<3> F = build_forest<3, Rec>(ar, recs, n, seg, seg + 1, 1, n, 20, st);
-    k_dup_probe<<<nblk(n, T), T, 0, st>>>(recs, d_in, n, flags + 1);
+    launch(k_dup_probe, nblk(n, T), T, 0, st, recs, d_in, n, flags + 1);
     int hflags[8];
     RSG_CUDA(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
@@ -399,7 +411,7 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     }
     if (hflags[1]) {
         int64_t *dn = ar.get<int64_t>(1);
-        k_dedupe_serial<<<1, 1, 0, st>>>(recs, d_in, n, dn);
+        launch(k_dedupe_serial, 1, 1, 0, st, recs, d_in, n, dn);
         int64_t nn = 0;
         RSG_CUDA(cudaMemcpyAsync(&nn, dn, sizeof(nn), cudaMemcpyDeviceToHost, st));
         RSG_CUDA(cudaStreamSynchronize(st));
@@ -415,24 +427,27 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     int *err = flags + 2;
 
     uint8_t *cnt = ar.get<uint8_t>(n);
-    k_count<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, cnt, err);
-    // earlier-dense-neighbour lists
-    int *ecnt = ar.get<int>(n + 1), *eoff = ar.get<int>(n + 1);
-    RSG_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int) * (n + 1), st));
-    k_elist<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, cnt, nullptr, ecnt, nullptr, err);
+    phase_mark(st, "fof.tree3d");
+    launch(k_count, nblk(n, T), T, 0, st, F.nodes, recs, n, r, cnt, err);
+    phase_mark(st, "fof.count");
+    // later-dense-neighbour lists and pending-skipper counts
+    int *lcnt = ar.get<int>(n + 1), *loff = ar.get<int>(n + 1), *skipcnt = ar.get<int>(n);
+    RSG_CUDA(cudaMemsetAsync(lcnt, 0, sizeof(int) * (n + 1), st));
+    RSG_CUDA(cudaMemsetAsync(skipcnt, 0, sizeof(int) * n, st));
+    launch(k_llist, nblk(n, T), T, 0, st, F.nodes, recs, n, r, cnt, (const int *)nullptr, lcnt,
+           (int *)nullptr, skipcnt, err);
     size_t cb = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, cb, ecnt, eoff, n + 1, st);
+    cub::DeviceScan::ExclusiveSum(nullptr, cb, lcnt, loff, n + 1, st);
     void *ct = ar.take(cb + 256);
-    cub::DeviceScan::ExclusiveSum(ct, cb, ecnt, eoff, n + 1, st);
+    cub::DeviceScan::ExclusiveSum(ct, cb, lcnt, loff, n + 1, st);
     int ne = 0;
-    RSG_CUDA(cudaMemcpyAsync(&ne, eoff + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaMemcpyAsync(&ne, loff + n, sizeof(int), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
-    int *elist = ar.get<int>(ne > 0 ? ne : 1);
-    k_elist<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, cnt, eoff, ecnt, elist, err);
+    int *llist = ar.get<int>(ne > 0 ? ne : 1);
+    launch(k_llist, nblk(n, T), T, 0, st, F.nodes, recs, n, r, cnt, loff, lcnt, llist, skipcnt, err);
     // dense particle list
     int *dense = ar.get<int>(n), *ndense = ar.get<int>(1);
     {
-        // dense flags
         thrust::transform_iterator<DFlag, thrust::counting_iterator<int>, uint8_t> it(
             thrust::counting_iterator<int>(0), DFlag{cnt});
         size_t b2 = 0;
@@ -444,52 +459,61 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     }
     int nd = 0;
     RSG_CUDA(cudaMemcpyAsync(&nd, ndense, sizeof(int), cudaMemcpyDeviceToHost, st));
-    uint8_t *state = ar.get<uint8_t>(n);
-    RSG_CUDA(cudaMemsetAsync(state, 2, n, st));
     RSG_CUDA(cudaStreamSynchronize(st));
-    if (nd > 0) k_mark_undecided<<<nblk(nd, T), T, 0, st>>>(dense, nd, state);
-    int *chg = ar.get<int>(2);
-    int rounds = 0;
-    while (nd > 0) {
-        RSG_CUDA(cudaMemsetAsync(chg, 0, sizeof(int) * 2, st));
-        k_mis<<<nblk(nd, T), T, 0, st>>>(dense, nd, eoff, elist, state, chg);
-        int h[2];
-        RSG_CUDA(cudaMemcpyAsync(h, chg, sizeof(h), cudaMemcpyDeviceToHost, st));
+    phase_mark(st, "fof.elist");
+    int *state32 = ar.get<int>(n);
+    RSG_CUDA(cudaMemsetAsync(state32, 0, sizeof(int) * n, st));
+    int *fa = ar.get<int>(nd + 1), *fb = ar.get<int>(nd + 1), *nf = ar.get<int>(2);
+    RSG_CUDA(cudaMemsetAsync(nf, 0, sizeof(int) * 2, st));
+    launch(k_kahn_init, nblk(nd, T), T, 0, st, dense, nd, skipcnt, state32, fa, nf);
+    int hf = 0, rounds = 0;
+    RSG_CUDA(cudaMemcpyAsync(&hf, nf, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    while (hf > 0) {
+        RSG_CUDA(cudaMemsetAsync(nf + 1, 0, sizeof(int), st));
+        launch(k_kahn, nblk((int64_t)hf * 32, T), T, 0, st, fa, hf, loff, llist, state32, skipcnt, fb,
+               nf + 1);
+        RSG_CUDA(cudaMemcpyAsync(&hf, nf + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
         RSG_CUDA(cudaStreamSynchronize(st));
-        rounds++;
-        if (h[1] == 0) break;
-        if (rounds > 1000000) {
+        std::swap(fa, fb);
+        if (++rounds > 10000000) {
             set_error(RSG_ERR_LIMIT, "seed selection did not converge");
             throw Failure();
         }
     }
+    // non-dense particles: state 2 (never seeds)
+    uint8_t *state = ar.get<uint8_t>(n);
+    launch(k_state8, nblk(n, T), T, 0, st, state32, n, state);
+    phase_mark(st, "fof.seeds");
+    if (getenv("RSG_TIMING")) fprintf(stderr, "  [fof] dense %d, later-list %d, frontier steps %d\n", nd, ne, rounds);
     uint8_t *skipped = ar.get<uint8_t>(n);
     RSG_CUDA(cudaMemsetAsync(skipped, 0, n, st));
-    k_seed_mark<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, state, skipped, err);
+    launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, state, skipped, err);
     int *gtime = ar.get<int>(n), *par = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(gtime, 0x7f, sizeof(int) * n, st));
-    k_iota<<<nblk(n, T), T, 0, st>>>(par, n);
-    k_link_r<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r, cnt, skipped, gtime, par, err);
-    k_link_2r<<<nblk(n, T), T, 0, st>>>(F.nodes, recs, n, r2x, state, gtime, par, err);
+    launch(k_iota, nblk(n, T), T, 0, st, par, n);
+    launch(k_link_r, nblk(n, T), T, 0, st, F.nodes, recs, n, r, cnt, skipped, gtime, par, err);
+    launch(k_link_2r, nblk(n, T), T, 0, st, F.nodes, recs, n, r2x, state, gtime, par, err);
+    phase_mark(st, "fof.links");
     int *root = ar.get<int>(n), *size = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(size, 0, sizeof(int) * n, st));
-    k_roots<<<nblk(n, T), T, 0, st>>>(par, n, root, size);
+    launch(k_roots, nblk(n, T), T, 0, st, par, n, root, size);
     uint32_t *key = ar.get<uint32_t>(n), *val = ar.get<uint32_t>(n);
     uint32_t *key2 = ar.get<uint32_t>(n), *val2 = ar.get<uint32_t>(n);
-    k_keys<<<nblk(n, T), T, 0, st>>>(root, size, n, cfg.min_halo_particles, key, val);
+    launch(k_keys, nblk(n, T), T, 0, st, root, size, n, cfg.min_halo_particles, key, val);
     size_t sb = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, sb, key, key2, val, val2, n, 0, 32, st);
     void *stmp = ar.take(sb + 256);
     cub::DeviceRadixSort::SortPairs(stmp, sb, key, key2, val, val2, n, 0, 32, st);
-    k_gather_out<<<nblk(n, T), T, 0, st>>>(val2, recs, d_in, n, d_out);
+    launch(k_gather_out, nblk(n, T), T, 0, st, val2, recs, d_in, n, d_out);
     int *head = ar.get<int>(n), *hpos = ar.get<int>(n), *nh = ar.get<int>(1);
-    k_heads<<<nblk(n, T), T, 0, st>>>(key2, n, head);
+    launch(k_heads, nblk(n, T), T, 0, st, key2, n, head);
     size_t hb = 0;
     cub::DeviceSelect::Flagged(nullptr, hb, thrust::counting_iterator<int>(0), head, hpos, nh, n,
                                st);
     void *htmp = ar.take(hb + 256);
     cub::DeviceSelect::Flagged(htmp, hb, thrust::counting_iterator<int>(0), head, hpos, nh, n, st);
-    k_group_sizes<<<nblk(n / 2 + 1, T), T, 0, st>>>(hpos, nh, key2, n, d_off, d_sz);
+    launch(k_group_sizes, nblk(n / 2 + 1, T), T, 0, st, hpos, nh, key2, n, d_off, d_sz);
     RSG_CHECK_LAUNCH();
     int hnh = 0;
     RSG_CUDA(cudaMemcpyAsync(&hnh, nh, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -500,6 +524,7 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
         throw Failure();
     }
     res.nfofs = hnh;
+    phase_mark(st, "fof.output");
     return res;
 }
 

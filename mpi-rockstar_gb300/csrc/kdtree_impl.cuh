@@ -100,16 +100,16 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
     cub_bytes = cub_bytes > b2 ? cub_bytes : b2;
     void *cub_tmp = ar.take(cub_bytes + 256);
 
-    k_root_init<D, RecT><<<nblk(ntrees, T), T, 0, st>>>(rstart, rn, ntrees, nodes, bmin, bmax);
+    launch(k_root_init<D, RecT>, nblk(ntrees, T), T, 0, st, rstart, rn, ntrees, nodes, bmin, bmax);
     RSG_CUDA(cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * nrec, st));
     RSG_CUDA(cudaMemsetAsync(box_owner, 0xff, sizeof(int32_t) * nrec, st));
-    k_root_owner<<<ntrees, 256, 0, st>>>(rstart, rn, ntrees, leaf, owner, box_owner);
+    launch(k_root_owner, ntrees, 256, 0, st, rstart, rn, ntrees, leaf, owner, box_owner);
     RSG_CHECK_LAUNCH();
     const int IT = 8;
-    k_box_runs<D, RecT, IT><<<nblk((nrec + IT - 1) / IT, T), T, 0, st>>>(recs, nrec, box_owner,
+    launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st, recs, nrec, box_owner,
                                                                          bmin, bmax);
-    k_box_final_range<D><<<nblk(ntrees, T), T, 0, st>>>(nodes, 0, ntrees, bmin, bmax);
-    k_root_active<D><<<nblk(ntrees, T), T, 0, st>>>(nodes, ntrees, leaf, nflag);
+    launch(k_box_final_range<D>, nblk(ntrees, T), T, 0, st, nodes, 0, ntrees, bmin, bmax);
+    launch(k_root_active<D>, nblk(ntrees, T), T, 0, st, nodes, ntrees, leaf, nflag);
     cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, thrust::counting_iterator<int32_t>(0), nflag,
                                act, cnt, ntrees, st);
     RSG_CHECK_LAUNCH();
@@ -125,18 +125,18 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
             set_error(RSG_ERR_LIMIT, "kd-forest build exceeded 4096 levels");
             throw Failure();
         }
-        k_slot_set<<<nblk(nact, T), T, 0, st>>>(act, nact, slot);
-        k_prep<D><<<nblk(nact, T), T, 0, st>>>(nodes, act, nact, lim);
-        k_flags<D, RecT><<<nblk(nrec + 1, T), T, 0, st>>>(recs, nrec, owner, slot, nodes, lim,
+        launch(k_slot_set, nblk(nact, T), T, 0, st, act, nact, slot);
+        launch(k_prep<D>, nblk(nact, T), T, 0, st, nodes, act, nact, lim);
+        launch(k_flags<D, RecT>, nblk(nrec + 1, T), T, 0, st, recs, nrec, owner, slot, nodes, lim,
                                                           flag);
         cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, flag, rank, (int)(nrec + 1), st);
-        k_counts<D><<<nblk(nact, T), T, 0, st>>>(nodes, act, nact, rank, m_arr, q_arr);
-        k_tables<D><<<nblk(nrec, T), T, 0, st>>>(nodes, nrec, owner, slot, flag, rank, m_arr,
+        launch(k_counts<D>, nblk(nact, T), T, 0, st, nodes, act, nact, rank, m_arr, q_arr);
+        launch(k_tables<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, slot, flag, rank, m_arr,
                                                  fb, bs);
-        k_scatter<D, RecT><<<nblk(nrec, T), T, 0, st>>>(nodes, recs, tmp, nrec, owner, slot,
+        launch(k_scatter<D, RecT>, nblk(nrec, T), T, 0, st, nodes, recs, tmp, nrec, owner, slot,
                                                         flag, rank, m_arr, q_arr, fb, bs);
-        k_copy_owned<RecT><<<nblk(nrec, T), T, 0, st>>>(tmp, recs, nrec, owner);
-        k_split_flags<D><<<nblk(nact + 1, T), T, 0, st>>>(m_arr, nodes, act, nact, sflag);
+        launch(k_copy_owned<RecT>, nblk(nrec, T), T, 0, st, tmp, recs, nrec, owner);
+        launch(k_split_flags<D>, nblk(nact + 1, T), T, 0, st, m_arr, nodes, act, nact, sflag);
         cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, sflag, soff, nact + 1, st);
         RSG_CHECK_LAUNCH();
         int32_t nsplit = 0;
@@ -147,16 +147,16 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
             throw Failure();
         }
         int32_t base = nnodes;
-        k_children<D><<<nblk(nact, T), T, 0, st>>>(nodes, act, nact, m_arr, soff, base, bmin, bmax);
+        launch(k_children<D>, nblk(nact, T), T, 0, st, nodes, act, nact, m_arr, soff, base, bmin, bmax);
         nnodes += 2 * nsplit;
         F.lv_first.push_back(nnodes);
-        k_owner_update<D><<<nblk(nrec, T), T, 0, st>>>(nodes, nrec, owner, box_owner, leaf);
+        launch(k_owner_update<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, box_owner, leaf);
         if (nsplit > 0) {
-            k_box_runs<D, RecT, IT><<<nblk((nrec + IT - 1) / IT, T), T, 0, st>>>(
+            launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st, 
                 recs, nrec, box_owner, bmin, bmax);
-            k_box_final_range<D><<<nblk(2 * nsplit, T), T, 0, st>>>(nodes, base, 2 * nsplit, bmin,
+            launch(k_box_final_range<D>, nblk(2 * nsplit, T), T, 0, st, nodes, base, 2 * nsplit, bmin,
                                                                     bmax);
-            k_next_active<D><<<nblk(2 * nsplit, T), T, 0, st>>>(nodes, base, 2 * nsplit, leaf,
+            launch(k_next_active<D>, nblk(2 * nsplit, T), T, 0, st, nodes, base, 2 * nsplit, leaf,
                                                                 nflag);
             cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, thrust::counting_iterator<int32_t>(base),
                                        nflag, act, cnt, 2 * nsplit, st);

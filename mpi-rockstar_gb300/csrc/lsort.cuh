@@ -193,17 +193,17 @@ void partition_sort_labels(Arena &ar, T *W, int32_t *lab, int64_t M,
             throw Failure();
         }
         RSG_CUDA(cudaMemsetAsync(owner, 0xff, 4 * M, st));
-        k_ls_owner<<<ns, T_, 0, st>>>(S.start, S.n, owner);
-        k_ls_init<<<nblk(ns, T_), T_, 0, st>>>(S, ns);
-        k_ls_minmax<8><<<nblk((M + 7) / 8, T_), T_, 0, st>>>(lab, M, owner, S);
-        k_ls_pivot<<<nblk(ns, T_), T_, 0, st>>>(S, ns);
-        k_ls_flags<<<nblk(M + 1, T_), T_, 0, st>>>(lab, M, owner, S, flag);
+        launch(k_ls_owner, ns, T_, 0, st, S.start, S.n, owner);
+        launch(k_ls_init, nblk(ns, T_), T_, 0, st, S, ns);
+        launch(k_ls_minmax<8>, nblk((M + 7) / 8, T_), T_, 0, st, lab, M, owner, S);
+        launch(k_ls_pivot, nblk(ns, T_), T_, 0, st, S, ns);
+        launch(k_ls_flags, nblk(M + 1, T_), T_, 0, st, lab, M, owner, S, flag);
         cub::DeviceScan::ExclusiveSum(tmp, tb, flag, rank, (int)(M + 1), st);
-        k_ls_counts<<<nblk(ns, T_), T_, 0, st>>>(S, ns, rank);
-        k_ls_tables<<<nblk(M, T_), T_, 0, st>>>(M, owner, S, flag, rank, fb, bs);
-        k_ls_scatter<T><<<nblk(M, T_), T_, 0, st>>>(M, owner, S, flag, rank, fb, bs, W, tw, lab, tl);
-        k_ls_copy<T><<<nblk(M, T_), T_, 0, st>>>(M, owner, tw, W, tl, lab);
-        k_ls_next<<<nblk(ns, T_), T_, 0, st>>>(S, ns, nst, nn, nflag);
+        launch(k_ls_counts, nblk(ns, T_), T_, 0, st, S, ns, rank);
+        launch(k_ls_tables, nblk(M, T_), T_, 0, st, M, owner, S, flag, rank, fb, bs);
+        launch(k_ls_scatter<T>, nblk(M, T_), T_, 0, st, M, owner, S, flag, rank, fb, bs, W, tw, lab, tl);
+        launch(k_ls_copy<T>, nblk(M, T_), T_, 0, st, M, owner, tw, W, tl, lab);
+        launch(k_ls_next, nblk(ns, T_), T_, 0, st, S, ns, nst, nn, nflag);
         cub::DeviceSelect::Flagged(tmp, tb, nst, nflag, S.start, cnt, 2 * ns, st);
         cub::DeviceSelect::Flagged(tmp, tb, nn, nflag, S.n, cnt, 2 * ns, st);
         RSG_CHECK_LAUNCH();

@@ -145,6 +145,9 @@ __device__ __forceinline__ double d2d(const float *a, const float *b) {
     return r2;
 }
 
+// Internal potential-tree nodes above this size are reduced by a block.
+#define RSG_BH_BIG 4096
+
 struct BHNode {
     float mc[3], m, dmin;
 };
@@ -184,7 +187,7 @@ __global__ void k_bh_internal(const KNode<3> *nodes, int32_t first, int32_t coun
     if (k >= count) return;
     int a = first + k;
     const KNode<3> &x = nodes[a];
-    if (x.div < 0) return;
+    if (x.div < 0 || x.n > RSG_BH_BIG) return;
     const BHNode &L = B[x.left], &R = B[x.left + 1];
     BHNode b;
     b.m = fadd(L.m, R.m);
@@ -192,6 +195,52 @@ __global__ void k_bh_internal(const KNode<3> *nodes, int32_t first, int32_t coun
         b.mc[j] = b.m ? __fdiv_rn(fadd(fmul(R.mc[j], R.m), fmul(L.mc[j], L.m)), b.m) : 0.f;
     b.dmin = node_dmin(PO, x.start, x.n, b.mc);
     B[a] = b;
+}
+
+// Large internal nodes: the block computes every point's squared distance
+// to the mass centre; the maximum is a reduction and the sum is added by one
+// thread in point order, as _compute_dmin does.
+__global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, int32_t first,
+                                                         int32_t count, const PotRec *PO, BHNode *B) {
+    __shared__ double dx_s[256];
+    __shared__ BHNode bs;
+    __shared__ double mx_s[8];
+    int a = first + blockIdx.x;
+    const KNode<3> &x = nodes[a];
+    if (x.div < 0 || x.n <= RSG_BH_BIG) return;
+    if (threadIdx.x == 0) {
+        const BHNode &L = B[x.left], &R = B[x.left + 1];
+        bs.m = fadd(L.m, R.m);
+        for (int j = 0; j < 3; j++)
+            bs.mc[j] = bs.m ? __fdiv_rn(fadd(fmul(R.mc[j], R.m), fmul(L.mc[j], L.m)), bs.m) : 0.f;
+    }
+    __syncthreads();
+    double sx = 0, bm = 0;
+    for (int b0 = 0; b0 < x.n; b0 += 256) {
+        int i = b0 + threadIdx.x;
+        double dx = 0;
+        if (i < x.n) {
+            dx = d2d(bs.mc, PO[x.start + i].pos);
+            if (bm < dx) bm = dx;
+        }
+        dx_s[threadIdx.x] = dx;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int m = min(256, x.n - b0);
+            for (int t = 0; t < m; t++) sx += dx_s[t];
+        }
+        __syncthreads();
+    }
+    for (int o = 16; o; o >>= 1) bm = fmax(bm, __shfl_down_sync(0xffffffffu, bm, o));
+    if ((threadIdx.x & 31) == 0) mx_s[threadIdx.x >> 5] = bm;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; w++) bm = fmax(bm, mx_s[w]);
+        bm = sqrt(bm) / 2.0;
+        BHNode b = bs;
+        b.dmin = (float)(bm + sqrt(bm * bm + sx / (x.n * 1.0)));
+        B[a] = b;
+    }
 }
 
 // _compute_monopole_potentials(leaf, root) (src/potential.c:133-168)
@@ -687,6 +736,542 @@ __global__ void k_halo_scans(rsg_halo *H, const rsg_extra_halo_info *E, int32_t 
     more_props(hh, q, tot, 1, C);
 }
 
+// ---- block-cooperative scans for large halos ------------------------------
+// Same arithmetic as corevel/kinetic/more_props/shape above.  The block
+// computes every per-particle operand in parallel (ellipsoidal radius,
+// weights, tensor products, densities, energies); sums that the reference
+// accumulates in array order are then accumulated by warp 0 with one lane
+// per accumulator, walking the staged operands in order, so each sum rounds
+// exactly as the reference's loop while all of them advance together.
+// Threshold decisions (density thresholds, Vmax) become block reductions.
+#define RSG_SB 256
+
+struct BlkBuf {
+    double v[RSG_SB][9];
+    unsigned char skip[RSG_SB];
+    int32_t np[RSG_SB];
+};
+
+// inclusive count of non-skipped entries up to each thread of a chunk
+__device__ int chunk_prefix(int flag, int *warp_tot) {
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned m = __ballot_sync(0xffffffffu, flag);
+    int incl = __popc(m & (0xffffffffu >> (31 - lane)));
+    if (lane == 31) warp_tot[w] = __popc(m);
+    __syncthreads();
+    int off = 0;
+    for (int i = 0; i < w; i++) off += warp_tot[i];
+    __syncthreads();
+    return off + incl;
+}
+
+__device__ void shape_blk(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
+                          const DevCfg &C, BlkBuf &B) {
+    __shared__ double orth[3][3], eig[3], acc[7];
+    __shared__ float minr_s;
+    __shared__ int64_t it_s;
+    __shared__ int done, an_s;
+    __shared__ int wt[RSG_SB / 32];
+    // number of analysed particles (bound filter)
+    int cntl = 0;
+    for (int64_t j = threadIdx.x; j < tot; j += RSG_SB) cntl += !(bound && unbound(po[j]));
+    for (int o = 16; o; o >>= 1) cntl += __shfl_down_sync(0xffffffffu, cntl, o);
+    if (threadIdx.x == 0) an_s = 0;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) atomicAdd(&an_s, cntl);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        done = 0;
+        int64_t it = C.shape_iterations, an = an_s;
+        float minr = fmul((float)C.force_res, (float)C.force_res);
+        h.b_to_a = h.c_to_a = 0;
+        h.A[0] = h.A[1] = h.A[2] = 0;
+        if (!(h.r > 0)) done = 1;
+        else {
+            minr = (float)((double)minr * (1e6 / (double)fmul(h.r, h.r)));
+            if (an < 3 || !(h.r > 0)) done = 1;
+            if (an < it) it = an;
+            for (int i = 0; i < 3; i++) {
+                for (int k = 0; k < 3; k++) orth[i][k] = 0;
+                orth[i][i] = 1;
+                eig[i] = (double)fmul(h.r, h.r) * 1e-6;
+            }
+        }
+        minr_s = minr;
+        it_s = it;
+    }
+    (void)wt;
+    __syncthreads();
+    if (done) return;
+    const float hp0 = h.pos[0], hp1 = h.pos[1], hp2 = h.pos[2];
+    for (int64_t i = 0; i < it_s; i++) {
+        double a = 0;  // lane k of warp 0 owns accumulator k (w, m00, m11, m22, m10, m20, m21)
+        for (int64_t b0 = 0; b0 < tot; b0 += RSG_SB) {
+            int64_t j = b0 + threadIdx.x;
+            unsigned char sk = 1;
+            if (j < tot && !(bound && unbound(po[j]))) {
+                const float *p = po[j].pos;
+                double dd[3] = {(double)fsub(p[0], hp0), (double)fsub(p[1], hp1),
+                                (double)fsub(p[2], hp2)};
+                double r = 0, dr;
+                for (int k = 0; k < 3; k++) {
+                    dr = 0;
+                    for (int l = 0; l < 3; l++) dr += orth[k][l] * dd[l];
+                    r += dr * dr / eig[k];
+                }
+                if (r < (double)minr_s) r = minr_s;
+                if (r > 0 && r <= 1) {
+                    double tw = (C.weighted_shapes) ? 1.0 / r : 1.0;
+                    B.v[threadIdx.x][0] = tw;
+                    B.v[threadIdx.x][1] = dd[0] * dd[0] * tw;
+                    B.v[threadIdx.x][2] = dd[1] * dd[1] * tw;
+                    B.v[threadIdx.x][3] = dd[2] * dd[2] * tw;
+                    B.v[threadIdx.x][4] = dd[0] * dd[1] * tw;
+                    B.v[threadIdx.x][5] = dd[0] * dd[2] * tw;
+                    B.v[threadIdx.x][6] = dd[1] * dd[2] * tw;
+                    sk = 0;
+                }
+            }
+            B.skip[threadIdx.x] = sk;
+            __syncthreads();
+            if (threadIdx.x < 7) {
+                int m = (tot - b0) < RSG_SB ? (int)(tot - b0) : RSG_SB;
+                int c = threadIdx.x;
+                for (int t = 0; t < m; t++)
+                    if (!B.skip[t]) a += B.v[t][c];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x < 7) acc[threadIdx.x] = a;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double w = acc[0];
+            if (!w) done = 1;
+            else {
+                double m[3][3] = {{acc[1], acc[4], acc[5]}, {acc[4], acc[2], acc[6]},
+                                  {acc[5], acc[6], acc[3]}};
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) m[k][l] /= (double)w;
+                double mt2[3][3], o2[3][3], e2[3];
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) mt2[k][l] = m[k][l];
+                jacobi3(m, e2, o2);
+                int a2 = 0, b = 1, c = 2;
+                if (e2[1] > e2[0]) { b = 0; a2 = 1; }
+                if (e2[2] > e2[b]) { c = b; b = 2; }
+                if (e2[b] > e2[a2]) { int t = a2; a2 = b; b = t; }
+                for (int k = 0; k < 3; k++) {
+                    eig[k] = e2[k];
+                    for (int l = 0; l < 3; l++) orth[k][l] = o2[k][l];
+                }
+                if (!e2[a2] || !e2[b] || !e2[c]) done = 1;
+                else {
+                    float ba = (float)sqrt(e2[b] / e2[a2]);
+                    float ca = (float)sqrt(e2[c] / e2[a2]);
+                    if ((fabs((double)fsub(ba, h.b_to_a)) < 0.01 * (double)h.b_to_a) &&
+                        (fabs((double)fsub(ca, h.c_to_a)) < 0.01 * (double)h.c_to_a))
+                        done = 1;
+                    else {
+                        h.b_to_a = (ba > 0) ? ba : 0;
+                        h.c_to_a = (ca > 0) ? ca : 0;
+                        double rr = sqrt(e2[a2]);
+                        for (int k = 0; k < 3; k++) {
+                            h.A[k] = (float)(1e3 * rr * o2[a2][k]);
+                            eig[k] *= ((double)fmul(h.r, h.r) * 1e-6) / (rr * rr);
+                        }
+                        h.inertia_tensor[0] = (float)mt2[0][0];
+                        h.inertia_tensor[1] = (float)mt2[1][1];
+                        h.inertia_tensor[2] = (float)mt2[2][2];
+                        h.inertia_tensor[3] = (float)mt2[0][1];
+                        h.inertia_tensor[4] = (float)mt2[1][2];
+                        h.inertia_tensor[5] = (float)mt2[2][0];
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (done) return;
+    }
+}
+
+struct MPState {
+    int64_t pmd, npa[4], npv, dtot, avg, nhalf, j0;
+    double vmax, rvmax, L[3], m, xa[3], va[3], vrms[3];
+};
+
+// lexicographic max of (cv, -j) across the block
+__device__ void blk_argmax(double &cv, int64_t &j, double *scv, int64_t *sj) {
+    for (int o = 16; o; o >>= 1) {
+        double c2 = __shfl_down_sync(0xffffffffu, cv, o);
+        int64_t j2 = __shfl_down_sync(0xffffffffu, j, o);
+        if (c2 > cv || (c2 == cv && j2 < j)) { cv = c2; j = j2; }
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { scv[w] = cv; sj[w] = j; }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int i = 1; i < RSG_SB / 32; i++)
+            if (scv[i] > scv[0] || (scv[i] == scv[0] && sj[i] < sj[0])) { scv[0] = scv[i]; sj[0] = sj[i]; }
+    __syncthreads();
+    cv = scv[0];
+    j = sj[0];
+    __syncthreads();
+}
+
+__device__ void more_props_blk(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
+                               const DevCfg &C, BlkBuf &B) {
+    __shared__ MPState S;
+    __shared__ int want;
+    __shared__ int wt[RSG_SB / 32];
+    __shared__ double scv[RSG_SB / 32];
+    __shared__ int64_t sj[RSG_SB / 32];
+    __shared__ unsigned long long red[8];
+    float scale = (float)C.scale_now;
+    const double f43 = 4.0 * M_PI / 3.0;
+    const double dth = C.thresh_dens[0] * f43, d1 = C.thresh_dens[1] * f43;
+    const double d2 = C.thresh_dens[2] * f43, d3 = C.thresh_dens[3] * f43, d4 = C.thresh_dens[4] * f43;
+    const double rth = C.rvir_dens * f43;
+    // pass 1 (src/properties.c:402-433) as reductions: the thresholds keep
+    // the last qualifying running count, the Vmax search the first maximum
+    // after the first particle above the Delta threshold
+    if (threadIdx.x < 8) red[threadIdx.x] = 0;
+    if (threadIdx.x == 0) { S.j0 = INT64_MAX; }
+    __syncthreads();
+    int64_t base_np = 0;
+    int64_t l_pmd = 0, l_dtot = 0, l_npa[4] = {0, 0, 0, 0}, l_npv = 0, l_j0 = INT64_MAX;
+    for (int64_t b0 = 0; b0 < tot; b0 += RSG_SB) {
+        int64_t j = b0 + threadIdx.x;
+        int ok = (j < tot) && !(bound && unbound(po[j]));
+        int incl = chunk_prefix(ok, wt);
+        int64_t np_ = base_np + incl;
+        if (ok) {
+            double r = sqrt((double)po[j].r2);
+            if (r < C.force_res) r = C.force_res;
+            double cd = ((double)np_ / (r * r * r));
+            if (cd > dth) { l_pmd = np_; l_dtot = j; if (j < l_j0) l_j0 = j; }
+            if (cd > d1) l_npa[0] = np_;
+            if (cd > d2) l_npa[1] = np_;
+            if (cd > d3) l_npa[2] = np_;
+            if (cd > d4) l_npa[3] = np_;
+            if (cd > rth) l_npv = np_;
+        }
+        __syncthreads();
+        if (threadIdx.x == RSG_SB - 1) B.np[0] = incl;
+        __syncthreads();
+        base_np += B.np[0];
+        __syncthreads();
+    }
+    // counts grow with j, so the last qualifying value is the maximum
+    atomicMax(&red[0], (unsigned long long)l_pmd);
+    atomicMax(&red[1], (unsigned long long)l_dtot * (l_pmd > 0));
+    for (int k = 0; k < 4; k++) atomicMax(&red[2 + k], (unsigned long long)l_npa[k]);
+    atomicMax(&red[6], (unsigned long long)l_npv);
+    atomicMin((unsigned long long *)&S.j0, (unsigned long long)l_j0);
+    __syncthreads();
+    // Vmax: first maximum of np/r over qualifying particles at or after j0
+    double bcv = -1;
+    int64_t bj = INT64_MAX;
+    base_np = 0;
+    for (int64_t b0 = 0; b0 < tot; b0 += RSG_SB) {
+        int64_t j = b0 + threadIdx.x;
+        int ok = (j < tot) && !(bound && unbound(po[j]));
+        int incl = chunk_prefix(ok, wt);
+        int64_t np_ = base_np + incl;
+        if (ok && j >= S.j0) {
+            double r = sqrt((double)po[j].r2);
+            if (r < C.force_res) r = C.force_res;
+            double cd = ((double)np_ / (r * r * r));
+            if (cd > rth) {
+                double cv = (double)np_ / r;
+                if (cv > bcv || (cv == bcv && j < bj)) { bcv = cv; bj = j; }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == RSG_SB - 1) B.np[0] = incl;
+        __syncthreads();
+        base_np += B.np[0];
+        __syncthreads();
+    }
+    blk_argmax(bcv, bj, scv, sj);
+    if (threadIdx.x == 0) {
+        S.pmd = (int64_t)red[0];
+        S.dtot = (int64_t)red[1];
+        for (int k = 0; k < 4; k++) S.npa[k] = (int64_t)red[2 + k];
+        S.npv = (int64_t)red[6];
+        S.vmax = 0;
+        S.rvmax = 0;
+        if (bcv > 0 && bj != INT64_MAX) {
+            S.vmax = bcv;
+            double r = sqrt((double)po[bj].r2);
+            if (r < C.force_res) r = C.force_res;
+            S.rvmax = r;
+        }
+        S.avg = 0;
+        S.nhalf = 0;
+    }
+    __syncthreads();
+    // pass 2 (src/properties.c:435-448): warp 0, lanes 0-2 own L[k], lanes
+    // 3-5 xavg[k], lanes 6-8 vavg[k] and vrms[k]
+    {
+        double acc_a = 0, acc_b = 0;
+        int64_t avg = 0, nhalf = 0;
+        const float *c = h.pos;
+        for (int64_t b0 = 0; b0 < S.dtot; b0 += RSG_SB) {
+            int64_t j = b0 + threadIdx.x;
+            unsigned char sk = 1;
+            if (j < S.dtot && !(bound && unbound(po[j]))) {
+                for (int d = 0; d < 6; d++) B.v[threadIdx.x][d] = (double)po[j].pos[d];
+                sk = 0;
+            }
+            B.skip[threadIdx.x] = sk;
+            __syncthreads();
+            if (threadIdx.x < 9) {
+                int lane = threadIdx.x;
+                int m = (S.dtot - b0) < RSG_SB ? (int)(S.dtot - b0) : RSG_SB;
+                for (int t = 0; t < m; t++) {
+                    if (B.skip[t]) continue;
+                    avg++;
+                    if (avg * 2 >= S.pmd && !nhalf) nhalf = b0 + t;
+                    const double *p = B.v[t];
+                    if (lane < 3) {
+                        int x = (lane + 1) % 3, y = (lane + 2) % 3;
+                        // L[0] += (p1-c1)(p5-c5) - ..., as add_ang_mom orders them
+                        float pa = fmul(fsub((float)p[x], c[x]), fsub((float)p[y + 3], c[y + 3]));
+                        float pb = fmul(fsub((float)p[y], c[y]), fsub((float)p[x + 3], c[x + 3]));
+                        acc_a += (double)pa;
+                        acc_a -= (double)pb;
+                    } else if (lane < 6) {
+                        int k = lane - 3;
+                        acc_a += (p[k] - acc_a) / ((double)avg);
+                    } else {
+                        int k = lane - 6;
+                        double md = p[k + 3] - acc_a;
+                        acc_a += md / (double)avg;
+                        acc_b += md * (p[k + 3] - acc_a);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x < 3) S.L[threadIdx.x] = acc_a;
+        else if (threadIdx.x < 6) S.xa[threadIdx.x - 3] = acc_a;
+        else if (threadIdx.x < 9) { S.va[threadIdx.x - 6] = acc_a; S.vrms[threadIdx.x - 6] = acc_b; }
+        if (threadIdx.x == 0) { S.avg = avg; S.nhalf = nhalf; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        S.m = S.pmd * C.particle_mass;
+        if (!bound) h.m = (float)S.m;
+        else h.mgrav = (float)S.m;
+        for (int k = 0; k < 3; k++) S.vrms[k] = (S.avg > 0) ? (S.vrms[k] / S.avg) : 0;
+        want = ((!bound) == (!C.bound_props));
+        if (want) {
+            double ds;
+            h.Xoff = h.Voff = 0;
+            for (int k = 0; k < 3; k++) {
+                ds = S.xa[k] - (double)h.pos[k];
+                h.Xoff = (float)((double)h.Xoff + ds * ds);
+                ds = S.va[k] - (double)h.pos[k + 3];
+                h.Voff = (float)((double)h.Voff + ds * ds);
+            }
+            for (int k = 0; k < 4; k++) h.alt_m[k] = (float)(S.npa[k] * C.particle_mass);
+            h.Xoff = (float)(sqrt((double)h.Xoff) * 1e3);
+            h.Voff = (float)sqrt((double)h.Voff);
+            h.vrms = (float)sqrt(S.vrms[0] + S.vrms[1] + S.vrms[2]);
+            h.vmax = (float)(RSG_VMAX_CONST * sqrt(S.vmax * (C.particle_mass / (double)scale)));
+            h.rvmax = (float)(S.rvmax * 1e3);
+            h.halfmass_radius = (float)(sqrt((double)po[S.nhalf].r2) * 1e3);
+            h.r = (float)(cbrt((3.0 / (4.0 * M_PI)) * S.npa[2] / C.thresh_dens[3]) * 1e3);
+        }
+    }
+    __syncthreads();
+    if (!want) return;
+    shape_blk(h, po, S.npa[2], bound, C, B);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        h.b_to_a2 = h.b_to_a;
+        h.c_to_a2 = h.c_to_a;
+        for (int k = 0; k < 3; k++) h.A2[k] = h.A[k];
+        for (int k = 0; k < 6; k++) h.inertia_tensor2[k] = h.inertia_tensor[k];
+        h.r = (float)(cbrt((3.0 / (4.0 * M_PI)) * S.pmd / C.thresh_dens[0]) * 1e3);
+    }
+    __syncthreads();
+    shape_blk(h, po, S.dtot, bound, C, B);
+    __syncthreads();
+    // estimate_total_energy over [0, dtot) in descending order: lane 0 sums
+    // ke, lane 1 the two coupled potential sums (src/properties.c:328-349)
+    __shared__ double en[3];
+    {
+        double acc_a = 0, acc_b = 0;
+        for (int64_t top = S.dtot - 1; top >= 0; top -= RSG_SB) {
+            int64_t i = top - threadIdx.x;
+            unsigned char sk = 1;
+            if (i >= 0 && po[i].pe > (double)po[i].ke) {
+                double r = sqrt((double)po[i].r2);
+                if (r < C.force_res) r = C.force_res;
+                B.v[threadIdx.x][0] = (double)po[i].ke;
+                B.v[threadIdx.x][1] = C.particle_mass * i / r;
+                B.v[threadIdx.x][2] = C.particle_mass / r;
+                sk = 0;
+            }
+            B.skip[threadIdx.x] = sk;
+            __syncthreads();
+            int m = (top + 1) < RSG_SB ? (int)(top + 1) : RSG_SB;
+            if (threadIdx.x == 0) {
+                for (int t = 0; t < m; t++)
+                    if (!B.skip[t]) acc_a += B.v[t][0];
+            } else if (threadIdx.x == 1) {
+                for (int t = 0; t < m; t++)
+                    if (!B.skip[t]) {
+                        acc_a += B.v[t][1] + acc_b;
+                        acc_b += B.v[t][2];
+                    }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) en[0] = acc_a;
+        if (threadIdx.x == 1) en[1] = acc_a;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double rvir = cbrt((3.0 / (4.0 * M_PI)) * S.npv / C.rvir_dens) * 1e3;
+        double mvir = S.npv * C.particle_mass, m = S.m;
+        scale_radius(h, (float)m, h.r, h.vmax, h.rvmax, scale, po, S.dtot, bound, C);
+        for (int j = 0; j < 3; j++) h.J[j] = (float)(C.particle_mass * (double)scale * S.L[j]);
+        {
+            double ke = en[0], tphi = en[1] / 2.0;
+            h.kin_to_pot = 0;
+            if (tphi) h.kin_to_pot = (float)(ke / tphi);
+            float sn = (float)C.scale_now;
+            h.energy = (float)((ke - tphi) * C.particle_mass * RSG_GC / (double)sn);
+        }
+        double Jh = C.particle_mass * (double)scale *
+                    sqrt(S.L[0] * S.L[0] + S.L[1] * S.L[1] + S.L[2] * S.L[2]);
+        h.spin = (float)((m > 0) ? (Jh * sqrt(fabs((double)h.energy)) / (RSG_GC * pow(m, 2.5))) : 0);
+        h.bullock_spin = (float)((m > 0) ? (Jh / (mvir * sqrt(2.0 * RSG_GC * mvir * rvir * (double)scale / 1e3))) : 0);
+        pseudo_masses(h, po, tot, bound, C);
+    }
+    __syncthreads();
+}
+
+// calculate_corevel with the block: rmax / core_max by reductions, then the
+// three running means and variances on lanes 0-2 of warp 0 (the combined
+// variance, and so every decision, is shared through shuffles).
+__device__ void corevel_blk(rsg_halo &h, const PotRec *q, int64_t tot, const DevCfg &C) {
+    __shared__ unsigned long long rm[2];
+    double rt = C.rvir_dens * (4.0 * M_PI / 3.0);
+    if (threadIdx.x == 0) { rm[0] = 0; rm[1] = 0; }
+    __syncthreads();
+    // rmax = largest j with j*j > r2^3 * rt^2 (or -1)
+    long long best = -1;
+    for (int64_t j = threadIdx.x; j < tot; j += blockDim.x) {
+        float r2 = q[j].r2;
+        if ((double)(j * j) > (double)fmul(fmul(r2, r2), r2) * (rt * rt)) best = j;
+    }
+    atomicMax(&rm[0], (unsigned long long)(best + 1));
+    __syncthreads();
+    int64_t rmax = (int64_t)rm[0] - 1;
+    if (rmax < 1) return;
+    long long cb = -1;
+    for (int64_t j = threadIdx.x; j < tot; j += blockDim.x)
+        if ((double)q[j].r2 * 100.0 < (double)q[rmax].r2) cb = j;
+    atomicMax(&rm[1], (unsigned long long)(cb + 1));
+    __syncthreads();
+    int64_t cmax = (int64_t)rm[1] - 1;
+    if (cmax < 100) cmax = 100;
+    if (threadIdx.x < 3) {
+        const unsigned mask = 0x7u;
+        int k = threadIdx.x;
+        double vel = 0, var = 0, bv = 0;
+        for (int64_t i = 0; i < rmax; i++) {
+            double x = (double)q[i].pos[k + 3];
+            double dl = x - vel;
+            vel += dl / ((double)(i + 1));
+            var += dl * (x - vel);
+            double v0 = __shfl_sync(mask, var, 0), v1 = __shfl_sync(mask, var, 1),
+                   v2 = __shfl_sync(mask, var, 2);
+            double tv = (v0 + v1) + v2;
+            if ((i < 10) || (tv < bv * (i - 3) * i)) {
+                if (i > 3) bv = tv / (double)((i - 3) * i);
+                else bv = 0;
+                if (i < cmax) {
+                    if (k == 0) {
+                        h.n_core = i;
+                        h.min_vel_err = (float)bv;
+                    }
+                    h.corevel[k] = (float)vel;
+                }
+                h.bulkvel[k] = (float)vel;
+                if (k == 0) h.min_bulkvel_err = (float)bv;
+            }
+        }
+        __syncwarp(mask);
+        h.pos[k + 3] = h.corevel[k];
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(RSG_SB) k_halo_scans_blk(rsg_halo *H, const rsg_extra_halo_info *E,
+                                                           const int32_t *list, PotRec *PO,
+                                                           const int32_t *toff, const int32_t *kept,
+                                                           const DevCfg *Cp) {
+    __shared__ BlkBuf B;
+    int h = list[blockIdx.x];
+    rsg_halo &hh = H[h];
+    const DevCfg &C = *Cp;
+    PotRec *q = PO + toff[h];
+    int64_t tot = kept[h];
+    corevel_blk(hh, q, tot, C);
+    __syncthreads();
+    float sn = (float)C.scale_now;
+    const float *vc = (E[h].sub_of > -1) ? hh.corevel : hh.bulkvel;
+    {
+        double conv = 0.5 * (double)sn / RSG_GC, z1 = 1.0 / (double)sn;
+        double hub = 100.0 * hubble_scaling_d(C, z1 - 1.0);
+        float vv[3] = {vc[0], vc[1], vc[2]}, pp[3] = {hh.pos[0], hh.pos[1], hh.pos[2]};
+        for (int64_t i = threadIdx.x; i < tot; i += blockDim.x) {
+            if (q[i].ke < 0) continue;
+            float ke = 0;
+            for (int j = 0; j < 3; j++) {
+                double dv = (double)fsub(q[i].pos[j + 3], vv[j]) +
+                            hub * (double)sn * (double)fsub(q[i].pos[j], pp[j]);
+                ke = (float)((double)ke + dv * dv);
+            }
+            q[i].ke = (float)((double)ke * conv);
+        }
+    }
+    __syncthreads();
+    more_props_blk(hh, q, tot, 0, C, B);
+    more_props_blk(hh, q, tot, 1, C, B);
+}
+
+// halos split by size: small ones one thread each, large ones one block each
+__global__ void k_scan_split(const rsg_halo *H, int32_t NH, const int32_t *kept, int32_t big,
+                             int32_t *fsmall, int32_t *fbig) {
+    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= NH) return;
+    bool act = H[h].num_p >= 1;
+    fbig[h] = act && kept[h] > big;
+    fsmall[h] = act && kept[h] <= big;
+}
+__global__ void k_halo_scans_list(rsg_halo *H, const rsg_extra_halo_info *E, const int32_t *list,
+                                  int32_t n, PotRec *PO, const int32_t *toff, const int32_t *kept,
+                                  const DevCfg *Cp) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int h = list[t];
+    rsg_halo &hh = H[h];
+    const DevCfg &C = *Cp;
+    PotRec *q = PO + toff[h];
+    int64_t tot = kept[h];
+    corevel(hh, q, tot, C);
+    float sn = (float)C.scale_now;
+    if (E[h].sub_of > -1) kinetic(q, tot, hh.corevel, hh.pos, sn, C);
+    else kinetic(q, tot, hh.bulkvel, hh.pos, sn, C);
+    more_props(hh, q, tot, 0, C);
+    more_props(hh, q, tot, 1, C);
+}
+
 __global__ void k_kept_count(const PotRec *PO, const int32_t *toff, const int32_t *tot,
                              int32_t NH, int32_t *kept) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -745,17 +1330,23 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     const int T = 256;
     if (ntrees == 0) return;
     Forest<3> F = build_forest<3, PotRec>(ar, PO, npo, rs, rn, ntrees, npo, 10, st);
+    phase_mark(st, "p.bh_tree");
     BHNode *B = ar.get<BHNode>(F.nnodes);
-    k_bh_leaf<<<nblk(F.nnodes, T), T, 0, st>>>(F.nodes, F.nnodes, PO, mp, B);
+    launch(k_bh_leaf, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, PO, mp, B);
     for (int l = (int)F.lv_first.size() - 2; l >= 0; l--) {
         int32_t a = F.lv_first[l], b = F.lv_first[l + 1];
-        if (b > a) k_bh_internal<<<nblk(b - a, 64), 64, 0, st>>>(F.nodes, a, b - a, PO, B);
+        if (b > a) {
+            launch(k_bh_internal, nblk(b - a, 64), 64, 0, st, F.nodes, a, b - a, PO, B);
+            launch(k_bh_internal_big, b - a, 256, 0, st, F.nodes, a, b - a, PO, B);
+        }
     }
+    phase_mark(st, "p.bh_mass");
     int32_t *lf = ar.get<int32_t>(F.nnodes), *leaves = ar.get<int32_t>(F.nnodes);
-    k_leaf_list_flags<<<nblk(F.nnodes, T), T, 0, st>>>(F.nodes, F.nnodes, lf);
+    launch(k_leaf_list_flags, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, lf);
     int32_t nl = select_idx(ar, lf, leaves, F.nnodes, st);
-    k_bh_walk<<<nblk(nl, 64), 64, 0, st>>>(F.nodes, leaves, nl, B, PO, mp, force_res, err);
+    launch(k_bh_walk, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res, err);
     RSG_CHECK_LAUNCH();
+    phase_mark(st, "p.bh_walk");
 }
 
 void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec *W,
@@ -768,24 +1359,25 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     RSG_CUDA(cudaMemsetAsync(err, 0, 8, st));
     int32_t *tot = ar.get<int32_t>(NH + 1), *nseg = ar.get<int32_t>(NH + 1);
     int32_t *toff = ar.get<int32_t>(NH + 1), *soff = ar.get<int32_t>(NH + 1);
-    k_set_count<<<nblk(NH + 1, 64), 64, 0, st>>>(H, E, NH, dc.include_host_potential_ratio, tot,
+    launch(k_set_count, nblk(NH + 1, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio, tot,
                                                  nseg, err);
     int32_t npo = scan_i32(ar, tot, toff, NH + 1, st);
+    phase_mark(st, "p.sets");
     int32_t ns = scan_i32(ar, nseg, soff, NH + 1, st);
     Seg *segs = ar.get<Seg>(ns + 1);
     PotRec *PO = ar.get<PotRec>(npo + 1), *PO2 = ar.get<PotRec>(npo + 1);
-    k_set_segs<<<nblk(NH, 64), 64, 0, st>>>(H, E, NH, dc.include_host_potential_ratio, toff, soff,
+    launch(k_set_segs, nblk(NH, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio, toff, soff,
                                             segs);
-    if (ns) k_set_fill<<<ns, 128, 0, st>>>(segs, W, H, PO);
+    if (ns) launch(k_set_fill, ns, 128, 0, st, segs, W, H, PO);
     RSG_CHECK_LAUNCH();
     // potentials
     {
         size_t m2 = ar.used;
         int32_t *rflag = ar.get<int32_t>(NH), *hl = ar.get<int32_t>(NH);
-        k_bh_roots<<<nblk(NH, T), T, 0, st>>>(toff, tot, NH, rflag);
+        launch(k_bh_roots, nblk(NH, T), T, 0, st, toff, tot, NH, rflag);
         int32_t nr = select_idx(ar, rflag, hl, NH, st);
         int32_t *rs = ar.get<int32_t>(nr + 1), *rn = ar.get<int32_t>(nr + 1);
-        if (nr) k_bh_root_arrays<<<nblk(nr, T), T, 0, st>>>(hl, nr, toff, tot, rs, rn);
+        if (nr) launch(k_bh_root_arrays, nblk(nr, T), T, 0, st, hl, nr, toff, tot, rs, rn);
         bh_potential(ar, PO, npo, rs, rn, nr, dc.particle_mass, dc.force_res, err, st);
         ar.used = m2;
     }
@@ -794,21 +1386,31 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
         size_t m2 = ar.used;
         uint64_t *k1 = ar.get<uint64_t>(npo + 1), *k2 = ar.get<uint64_t>(npo + 1);
         uint32_t *v1 = ar.get<uint32_t>(npo + 1), *v2 = ar.get<uint32_t>(npo + 1);
-        k_po_keys<<<nblk(npo, T), T, 0, st>>>(PO, npo, k1, v1);
+        launch(k_po_keys, nblk(npo, T), T, 0, st, PO, npo, k1, v1);
         int bits = 33;
         while ((1ll << (bits - 33)) <= NH) bits++;
         size_t b = 0;
         cub::DeviceRadixSort::SortPairs(nullptr, b, k1, k2, v1, v2, npo, 0, bits, st);
         void *t = ar.take(b + 256);
         cub::DeviceRadixSort::SortPairs(t, b, k1, k2, v1, v2, npo, 0, bits, st);
-        k_po_gather<<<nblk(npo, T), T, 0, st>>>(PO, v2, npo, PO2);
+        launch(k_po_gather, nblk(npo, T), T, 0, st, PO, v2, npo, PO2);
         RSG_CHECK_LAUNCH();
         ar.used = m2;
     }
+    phase_mark(st, "p.sort");
     int32_t *kept = ar.get<int32_t>(NH + 1);
-    k_kept_count<<<nblk(NH, T), T, 0, st>>>(PO2, toff, tot, NH, kept);
-    k_halo_scans<<<nblk(NH, 32), 32, 0, st>>>(H, E, NH, PO2, toff, kept, d_dc);
+    launch(k_kept_count, nblk(NH, T), T, 0, st, PO2, toff, tot, NH, kept);
+    {
+        int32_t *fs = ar.get<int32_t>(NH), *fbg = ar.get<int32_t>(NH);
+        int32_t *ls = ar.get<int32_t>(NH), *lb = ar.get<int32_t>(NH);
+        launch(k_scan_split, nblk(NH, T), T, 0, st, H, NH, kept, 1024, fs, fbg);
+        int32_t nsm = select_idx(ar, fs, ls, NH, st);
+        int32_t nbg = select_idx(ar, fbg, lb, NH, st);
+        launch(k_halo_scans_blk, nbg, RSG_SB, 0, st, H, E, lb, PO2, toff, kept, d_dc);
+        launch(k_halo_scans_list, nblk(nsm, 32), 32, 0, st, H, E, ls, nsm, PO2, toff, kept, d_dc);
+    }
     RSG_CHECK_LAUNCH();
+    phase_mark(st, "p.scans");
     int herr[2];
     RSG_CUDA(cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));

@@ -29,6 +29,10 @@
 // Ranges up to this size are summed by one thread in array order, so FP64
 // sums round exactly as the reference's sequential loops do.
 #define RSG_SEQ_MAX 65536
+// Below this size one thread does all of a node's or halo's work.
+#define RSG_SMALL 2048
+// Nodes up to this size replay their union-find in shared memory.
+#define RSG_REPLAY_SMEM 24576
 
 namespace rsg {
 
@@ -113,7 +117,7 @@ __global__ void k_norm_seq(Rec *W, HierNodes N, int32_t base, int32_t count, int
     if (k >= count) return;
     int node = base + k;
     int s = N.start[node], n = N.n[node];
-    if (n <= 0 || n > RSG_SEQ_MAX) return;
+    if (n <= 0 || n > RSG_SMALL) return;
     double mean[6] = {0, 0, 0, 0, 0, 0};
     for (int i = 0; i < n; i++)
         for (int d = 0; d < 6; d++) mean[d] += (double)W[s + i].pos[d];
@@ -132,6 +136,57 @@ __global__ void k_norm_seq(Rec *W, HierNodes N, int32_t base, int32_t count, int
     }
     for (int j = 0; j < 21; j++) c[j] /= (double)n;
     norm_sigmas(c, level0, ims, sig + 2 * k);
+}
+
+// Mid-size nodes: the block stages particles in shared memory and computes
+// the per-particle products; thread 0 adds them in array order.
+__global__ void __launch_bounds__(256) k_norm_blk(Rec *W, HierNodes N, int32_t base, int level0,
+                                                  double ims, double *sig) {
+    __shared__ float q[256][6];
+    __shared__ float pr[256][21];
+    __shared__ double mean[6], corr[21];
+    int k = blockIdx.x;
+    int node = base + k;
+    int s = N.start[node], n = N.n[node];
+    if (n <= RSG_SMALL || n > RSG_SEQ_MAX) return;
+    // lane d of warp 0 owns the running sum of coordinate d
+    double a = 0;
+    for (int b0 = 0; b0 < n; b0 += 256) {
+        int i = b0 + threadIdx.x;
+        if (i < n)
+            for (int d = 0; d < 6; d++) q[threadIdx.x][d] = W[s + i].pos[d];
+        __syncthreads();
+        if (threadIdx.x < 6) {
+            int m = min(256, n - b0), d = threadIdx.x;
+            for (int t = 0; t < m; t++) a += (double)q[t][d];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) mean[threadIdx.x] = a / (double)n;
+    __syncthreads();
+    double c = 0;  // lane j of warp 0 owns second moment j
+    for (int b0 = 0; b0 < n; b0 += 256) {
+        int i = b0 + threadIdx.x;
+        if (i < n) {
+            float v[6];
+            for (int d = 0; d < 6; d++) {
+                v[d] = __double2float_rn((double)W[s + i].pos[d] - mean[d]);
+                W[s + i].pos[d] = v[d];
+            }
+            int j = 0;
+            for (int x = 0; x < 6; x++)
+                for (int y = x; y < 6; y++) pr[threadIdx.x][j++] = fmul(v[x], v[y]);
+        }
+        __syncthreads();
+        if (threadIdx.x < 21) {
+            int m = min(256, n - b0), j = threadIdx.x;
+            for (int t = 0; t < m; t++) c += (double)pr[t][j];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 21) corr[threadIdx.x] = c / (double)n;
+    __syncthreads();
+    if (threadIdx.x == 0) norm_sigmas(corr, level0, ims, sig + 2 * k);
 }
 
 // Larger nodes: one block, deterministic tree reductions.
@@ -289,19 +344,27 @@ __device__ float next_closest(const KNode<6> *nodes, int root, const Rec *W, con
 }
 
 __global__ void k_nn(const KNode<6> *nodes, const Rec *W, HierNodes N, int32_t base,
-                     const int32_t *soff, const int32_t *sidx, float *prad, int exact, int *err) {
-    int k = blockIdx.x;
+                     int32_t count, const int32_t *soff, const int32_t *sidx, float *prad,
+                     int64_t total, int exact, int *err) {
+    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    // node of sample g: last k with soff[k] <= g
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (soff[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    int k = lo;
     int node = base + k;
     int s = N.start[node], n = N.n[node];
     int nt = exact ? n : (n < 10000 ? n : 10000);
-    int o = soff[k];
-    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-        int j = (nt == n) ? t : sidx[o + t];
-        float c[6];
+    int t = (int)(g - soff[k]);
+    int j = (nt == n) ? t : sidx[soff[k] + t];
+    float c[6];
 #pragma unroll
-        for (int d = 0; d < 6; d++) c[d] = W[s + j].pos[d];
-        prad[o + t] = next_closest(nodes, k, W, c, err);
-    }
+    for (int d = 0; d < 6; d++) c[d] = W[s + j].pos[d];
+    prad[g] = next_closest(nodes, k, W, c, err);
 }
 
 // find_median_r / rad_partition (src/groupies.c:735-786), run as is on the
@@ -446,6 +509,7 @@ __global__ void k_replay6(HierNodes N, int32_t base, int32_t count, const int32_
     if (k >= count) return;
     int node = base + k;
     int s = N.start[node], n = N.n[node];
+    if (n > RSG_SMALL && n <= RSG_REPLAY_SMEM) return;
     int32_t *RR = R + s;
     int nsf = 0;
     for (int i = s; i < s + n; i++) lab[i] = -1;
@@ -476,6 +540,59 @@ __global__ void k_replay6(HierNodes N, int32_t base, int32_t count, const int32_
     }
     for (int i = s; i < s + n; i++)
         if (lab[i] >= 0) lab[i] = sf_find(RR, lab[i]);
+}
+
+// The same replay for mid-size nodes with the label and root arrays in
+// shared memory (one block per node, thread 0 replays, the block loads and
+// stores).
+__global__ void k_replay6_smem(HierNodes N, int32_t base, const int32_t *noff,
+                               const int32_t *nbr, int32_t *lab_out) {
+    extern __shared__ int32_t sm_i[];
+    int k = blockIdx.x;
+    int node = base + k;
+    int s = N.start[node], n = N.n[node];
+    if (n <= RSG_SMALL || n > RSG_REPLAY_SMEM) return;
+    int32_t *lab = sm_i, *RR = sm_i + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) lab[i] = -1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int nsf = 0;
+        for (int i = 0; i < n; i++) {
+            int e0 = noff[s + i], e1 = noff[s + i + 1];
+            if (e0 == e1) continue;
+            int f = lab[i];
+            if (f < 0) {
+                for (int e = e0; e < e1; e++)
+                    if (lab[nbr[e] - s] != -1) {
+                        f = lab[nbr[e] - s];
+                        break;
+                    }
+                if (f < 0) {
+                    f = nsf++;
+                    RR[f] = f;
+                }
+            }
+            for (int e = e0 - 1; e < e1; e++) {
+                int j = (e < e0) ? i : nbr[e] - s;
+                if (lab[j] == -1) {
+                    lab[j] = f;
+                } else {
+                    int rl = sf_find(RR, lab[j]), rc = sf_find(RR, f);
+                    if (rl != rc) RR[rc] = rl;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int l = lab[i];
+        if (l >= 0) {
+            int r = l;
+            while (RR[r] != r) r = RR[r];
+            l = r;
+        }
+        lab_out[s + i] = l;
+    }
 }
 
 // Runs of equal labels after the partition sort: the kept ones (>= 0 and at
@@ -791,19 +908,38 @@ __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, co
     rsg_halo &hh = H[h];
     int ps = (int)hh.p_start, np = (int)hh.num_p;
     if (np <= RSG_SEQ_MAX) {
-        // sequential, in array order (src/properties.c:76-87)
-        if (threadIdx.x == 0) {
-            double a[6] = {0, 0, 0, 0, 0, 0}, b[6] = {0, 0, 0, 0, 0, 0};
-            for (int i = 0; i < np; i++)
-                for (int d = 0; d < 6; d++) a[d] += (double)W[ps + i].pos[d];
-            for (int d = 0; d < 6; d++) mean[d] = a[d] / (double)np;
-            for (int i = 0; i < np; i++)
+        // in array order (src/properties.c:76-87): the block stages values,
+        // thread 0 adds them
+        __shared__ double stage[256][6];
+        double a = 0, b = 0;  // lane d of warp 0 owns coordinate d
+        for (int b0 = 0; b0 < np; b0 += blockDim.x) {
+            int i = b0 + threadIdx.x;
+            if (i < np)
+                for (int d = 0; d < 6; d++) stage[threadIdx.x][d] = (double)W[ps + i].pos[d];
+            __syncthreads();
+            if (threadIdx.x < 6) {
+                int m = min((int)blockDim.x, np - b0), d = threadIdx.x;
+                for (int t = 0; t < m; t++) a += stage[t][d];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x < 6) mean[threadIdx.x] = a / (double)np;
+        __syncthreads();
+        for (int b0 = 0; b0 < np; b0 += blockDim.x) {
+            int i = b0 + threadIdx.x;
+            if (i < np)
                 for (int d = 0; d < 6; d++) {
                     double x = (double)W[ps + i].pos[d] - mean[d];
-                    b[d] += x * x;
+                    stage[threadIdx.x][d] = x * x;
                 }
-            for (int d = 0; d < 6; d++) p2[d] = b[d];
+            __syncthreads();
+            if (threadIdx.x < 6) {
+                int m = min((int)blockDim.x, np - b0), d = threadIdx.x;
+                for (int t = 0; t < m; t++) b += stage[t][d];
+            }
+            __syncthreads();
         }
+        if (threadIdx.x < 6) p2[threadIdx.x] = b;
         __syncthreads();
     } else {
     double acc[6] = {0, 0, 0, 0, 0, 0};
@@ -1217,7 +1353,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     int32_t *hflag = ar.get<int32_t>(M + 1);
     int *err = ar.get<int>(4);
     RSG_CUDA(cudaMemsetAsync(err, 0, 16, st));
-    k_make_w<<<(int)G, T, 0, st>>>(d_p, G, d_goff, d_woff, d_gsz, W, wgroup, N);
+    phase_mark(st, "");
+    launch(k_make_w, (int)G, T, 0, st, d_p, G, d_goff, d_woff, d_gsz, W, wgroup, N);
     RSG_CHECK_LAUNCH();
 
     // ---------------- descending ----------------
@@ -1235,12 +1372,14 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         size_t mark = ar.used;
         {
             double *sig = ar.get<double>(2 * (int64_t)cnt);
-            k_norm_seq<<<nblk(cnt, 32), 32, 0, st>>>(W, N, base, cnt, L == 0,
+            launch(k_norm_seq, nblk(cnt, 32), 32, 0, st, W, N, base, cnt, L == 0,
                                                      cfg.initial_metric_scaling, sig);
-            k_norm_par<<<cnt, T, 0, st>>>(W, N, base, L == 0, cfg.initial_metric_scaling, sig);
-            k_norm_div<<<cnt, T, 0, st>>>(W, N, base, sig);
+            launch(k_norm_blk, cnt, 256, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig);
+            launch(k_norm_par, cnt, T, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig);
+            launch(k_norm_div, cnt, T, 0, st, W, N, base, sig);
             RSG_CHECK_LAUNCH();
         }
+        phase_mark(st, "d.norm_sd");
         int32_t *rst = N.start + base, *rn = N.n + base;
         std::vector<int32_t> hs(cnt), hn(cnt);
         RSG_CUDA(cudaMemcpyAsync(hn.data(), rn, 4 * cnt, cudaMemcpyDeviceToHost, st));
@@ -1257,38 +1396,52 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         }
         // 6D kd-forest over this level's nodes (src/groupies.c:294)
         Forest<6> F = build_forest<6, Rec>(ar, W, M, rst, rn, cnt, nin, 40, st);
+        phase_mark(st, "d.tree6d");
         int32_t *soff = ar.get<int32_t>(cnt);
         RSG_CUDA(cudaMemcpyAsync(soff, so.data(), 4 * cnt, cudaMemcpyHostToDevice, st));
         int32_t *sidx = ar.get<int32_t>(tot + 1);
         float *prad = ar.get<float>(tot + 1);
         unsigned *seeds = ar.get<unsigned>(cnt);
-        k_sample<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, soff, sidx, seeds,
+        launch(k_sample, nblk(cnt, 64), 64, 0, st, N, base, cnt, soff, sidx, seeds,
                                                (int)cfg.exact_ll_calc);
-        k_nn<<<cnt, 128, 0, st>>>(F.nodes, W, N, base, soff, sidx, prad, (int)cfg.exact_ll_calc,
-                                  err);
-        k_target<<<nblk(cnt, 32), 32, 0, st>>>(N, base, cnt, soff, prad, seeds,
+        launch(k_nn, nblk(tot, 128), 128, 0, st, F.nodes, W, N, base, cnt, soff, sidx, prad,
+               (int64_t)tot, (int)cfg.exact_ll_calc, err);
+        launch(k_target, nblk(cnt, 32), 32, 0, st, N, base, cnt, soff, prad, seeds,
                                                (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
+        phase_mark(st, "d.nn_target");
         RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
-        k_fill_eln<<<cnt, T, 0, st>>>(N, base, eln);
+        launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
         // later neighbours within target_r, as CSR lists
         int32_t *ncnt = par, *noff = root;
         RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
-        k_fof6<<<nblk(M, T), T, 0, st>>>(F.nodes, W, M, N, base, eln, nullptr, ncnt, nullptr, err);
+        launch(k_fof6, nblk(M, T), T, 0, st, F.nodes, W, M, N, base, eln, nullptr, ncnt, nullptr, err);
         int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
         int32_t *nbr = ar.get<int32_t>(ne + 1);
-        k_fof6<<<nblk(M, T), T, 0, st>>>(F.nodes, W, M, N, base, eln, noff, ncnt, nbr, err);
+        launch(k_fof6, nblk(M, T), T, 0, st, F.nodes, W, M, N, base, eln, noff, ncnt, nbr, err);
+        phase_mark(st, "d.fof6d");
         // reference labels, then the reference's partition sort by label
-        k_replay6<<<nblk(cnt, 32), 32, 0, st>>>(N, base, cnt, noff, nbr, phalo, csize);
+        launch(k_replay6, nblk(cnt, 32), 32, 0, st, N, base, cnt, noff, nbr, phalo, csize);
+        {
+            static bool attr = false;
+            if (!attr) {
+                RSG_CUDA(cudaFuncSetAttribute(k_replay6_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              8 * RSG_REPLAY_SMEM));
+                attr = true;
+            }
+            launch(k_replay6_smem, cnt, 128, (size_t)8 * RSG_REPLAY_SMEM, st, N, base, noff, nbr, phalo);
+        }
         RSG_CHECK_LAUNCH();
+        phase_mark(st, "d.replay");
         partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
-        k_run_heads<<<nblk(M, T), T, 0, st>>>(eln, M, N, base, phalo, hflag);
+        phase_mark(st, "d.psort");
+        launch(k_run_heads, nblk(M, T), T, 0, st, eln, M, N, base, phalo, hflag);
         int32_t *heads = ar.get<int32_t>(M);
         int32_t nh = select_flagged(ar, hflag, heads, M, 0, st);
         int32_t *cflag = ar.get<int32_t>(nh + 1), *clen = ar.get<int32_t>(nh + 1);
         int32_t *cidx = ar.get<int32_t>(nh + 1);
         int32_t nc = 0;
         if (nh) {
-            k_run_children<<<nblk(nh, T), T, 0, st>>>(heads, nh, eln, N, base, phalo,
+            launch(k_run_children, nblk(nh, T), T, 0, st, heads, nh, eln, N, base, phalo,
                                                       cfg.min_halo_particles, cflag, clen);
             nc = select_flagged(ar, cflag, cidx, nh, 0, st);
         }
@@ -1296,12 +1449,13 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             set_error(RSG_ERR_LIMIT, "subgroup node capacity exceeded");
             throw Failure();
         }
-        if (nc) k_make_children2<<<nblk(nc, T), T, 0, st>>>(cidx, nc, heads, clen, eln, N, base, nn);
+        if (nc) launch(k_make_children2, nblk(nc, T), T, 0, st, cidx, nc, heads, clen, eln, N, base, nn);
         RSG_CHECK_LAUNCH();
         ar.used = mark;
         lvl_base.push_back(nn);
         lvl_cnt.push_back(nc);
         nn += nc;
+        phase_mark(st, "d.children");
     }
     int nlev = (int)lvl_base.size() - 1;  // the last entry has count 0
     {
@@ -1318,7 +1472,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
 
     // ---------------- halos ----------------
     int32_t *nflag = ar.get<int32_t>(nn), *leaves = ar.get<int32_t>(nn);
-    k_leaf_flags<<<nblk(nn, T), T, 0, st>>>(N, nn, nflag);
+    launch(k_leaf_flags, nblk(nn, T), T, 0, st, N, nn, nflag);
     int32_t NH = select_flagged(ar, nflag, leaves, nn, 0, st);
     if (NH > max_halos) {
         set_error(RSG_ERR_ARGS, "%d halos exceed max_halos %lld", NH, (long long)max_halos);
@@ -1326,28 +1480,31 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     }
     {
         int32_t *lk = ar.get<int32_t>(NH), *lk2 = ar.get<int32_t>(NH), *lv2 = ar.get<int32_t>(NH);
-        k_leaf_keys<<<nblk(NH, T), T, 0, st>>>(N, leaves, NH, lk);
+        launch(k_leaf_keys, nblk(NH, T), T, 0, st, N, leaves, NH, lk);
         sort_pairs(ar, lk, lk2, leaves, lv2, NH, 32, st);
         RSG_CUDA(cudaMemcpyAsync(leaves, lv2, 4 * NH, cudaMemcpyDeviceToDevice, st));
-        k_halo_ranges<<<nblk(nn, T), T, 0, st>>>(N, nn, lk2, NH);
+        launch(k_halo_ranges, nblk(nn, T), T, 0, st, N, nn, lk2, NH);
     }
     rsg_halo *H = d_halos;
     rsg_extra_halo_info *E = d_extra;
-    k_halo_init<<<nblk(NH, T), T, 0, st>>>(H, E, NH);
+    launch(k_halo_init, nblk(NH, T), T, 0, st, H, E, NH);
     int32_t *glist = ar.get<int32_t>(NH), *redirect = ar.get<int32_t>(NH);
     int32_t *stk = ar.get<int32_t>(NH + 1);
     RSG_CHECK_LAUNCH();
 
+    phase_mark(st, "halos");
     // ---------------- ascending ----------------
     for (int L = nlev - 1; L >= 0; L--) {
         int32_t base = lvl_base[L], cnt = lvl_cnt[L];
         if (cnt == 0) continue;
         size_t mark = ar.used;
-        k_asc_mark<<<cnt, T, 0, st>>>(W, d_p, N, base, H, phalo);
-        k_asc_seed<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, H, E, glist, redirect, cfg.force_res);
-        k_asc_assign<<<cnt, T, 0, st>>>(W, N, base, H, E, glist, redirect, phalo);
+        launch(k_asc_mark, cnt, T, 0, st, W, d_p, N, base, H, phalo);
+        phase_mark(st, "a.mark");
+        launch(k_asc_seed, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, glist, redirect, cfg.force_res);
+        launch(k_asc_assign, cnt, T, 0, st, W, N, base, H, E, glist, redirect, phalo);
+        phase_mark(st, "a.seed_assign");
         RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
-        k_fill_eln<<<cnt, T, 0, st>>>(N, base, eln);
+        launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
         RSG_CHECK_LAUNCH();
         {
             // reassign_halo_particles: the reference's partition by halo index
@@ -1357,56 +1514,59 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             RSG_CUDA(cudaStreamSynchronize(st));
             partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
         }
-        k_halo_heads<<<nblk(M, T), T, 0, st>>>(eln, M, N, base, phalo, H);
-        k_halo_tails<<<nblk(M, T), T, 0, st>>>(eln, M, N, base, phalo, H);
+        phase_mark(st, "a.reassign");
+        launch(k_halo_heads, nblk(M, T), T, 0, st, eln, M, N, base, phalo, H);
+        launch(k_halo_tails, nblk(M, T), T, 0, st, eln, M, N, base, phalo, H);
         // growing list of the level
         int32_t *goffs = ar.get<int32_t>(cnt + 1);
-        k_ng<<<nblk(cnt + 1, T), T, 0, st>>>(N, base, cnt, goffs, 0);
+        launch(k_ng, nblk(cnt + 1, T), T, 0, st, N, base, cnt, goffs, 0);
         int32_t ngr = excl_scan(ar, goffs, goffs, cnt + 1, st);
         int32_t *glv = ar.get<int32_t>(ngr + 1), *gnode = ar.get<int32_t>(ngr + 1);
-        k_list_growing<<<nblk(cnt, T), T, 0, st>>>(N, base, cnt, goffs, glist, glv);
-        k_list_node<<<nblk(cnt, T), T, 0, st>>>(cnt, goffs, gnode);
-        if (ngr) k_basic_props<<<ngr, T, 0, st>>>(W, H, glv, d_dc);
-        k_maxi<<<nblk(cnt, T), T, 0, st>>>(N, base, cnt, H, glist, 0);
-        k_best_parent<<<nblk(ngr, T), T, 0, st>>>(N, base, cnt, goffs, glv, gnode, H, E);
-        k_fix_parents<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, H, E, stk);
-        if (ngr) k_basic_props<<<ngr, T, 0, st>>>(W, H, glv, d_dc);
+        launch(k_list_growing, nblk(cnt, T), T, 0, st, N, base, cnt, goffs, glist, glv);
+        launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, goffs, gnode);
+        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc);
+        launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 0);
+        launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E);
+        launch(k_fix_parents, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
+        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc);
         RSG_CHECK_LAUNCH();
+        phase_mark(st, "a.props_parents");
         if (L == 0) {
             int32_t *aoff = ar.get<int32_t>(cnt + 1);
-            k_ng<<<nblk(cnt + 1, T), T, 0, st>>>(N, base, cnt, aoff, 1);
+            launch(k_ng, nblk(cnt + 1, T), T, 0, st, N, base, cnt, aoff, 1);
             int32_t na = excl_scan(ar, aoff, aoff, cnt + 1, st);
             int32_t *alist = ar.get<int32_t>(na + 1), *anode = ar.get<int32_t>(na + 1);
-            k_list_all<<<nblk(cnt, T), T, 0, st>>>(N, base, cnt, aoff, alist);
-            k_list_node<<<nblk(cnt, T), T, 0, st>>>(cnt, aoff, anode);
-            if (na) k_basic_props<<<na, T, 0, st>>>(W, H, alist, d_dc);
-            k_corekeys<<<nblk(M, T), T, 0, st>>>(W, eln, M, phalo, H, key, val);
+            launch(k_list_all, nblk(cnt, T), T, 0, st, N, base, cnt, aoff, alist);
+            launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, aoff, anode);
+            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc);
+            launch(k_corekeys, nblk(M, T), T, 0, st, W, eln, M, phalo, H, key, val);
             sort_pairs(ar, key, key2, val, val2, M, keybits, st);
-            k_gather<Rec><<<nblk(M, T), T, 0, st>>>(W, val2, M, W2);
-            k_gather<int32_t><<<nblk(M, T), T, 0, st>>>(phalo, val2, M, phalo2);
+            launch(k_gather<Rec>, nblk(M, T), T, 0, st, W, val2, M, W2);
+            launch(k_gather<int32_t>, nblk(M, T), T, 0, st, phalo, val2, M, phalo2);
             std::swap(W, W2);
             std::swap(phalo, phalo2);
-            k_maxi<<<nblk(cnt, T), T, 0, st>>>(N, base, cnt, H, glist, 1);
-            k_best_parent<<<nblk(na, T), T, 0, st>>>(N, base, cnt, aoff, alist, anode, H, E);
-            k_fix_parents<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, H, E, stk);
+            launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 1);
+            launch(k_best_parent, nblk(na, T), T, 0, st, N, base, cnt, aoff, alist, anode, H, E);
+            launch(k_fix_parents, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
             RSG_CHECK_LAUNCH();
             // find_subs tail (src/groupies.c:697-703): child counts and basic
             // properties for every halo, then the additional properties.
-            k_num_child<<<nblk(cnt, 64), 64, 0, st>>>(N, base, cnt, H, E, stk);
-            if (na) k_basic_props<<<na, T, 0, st>>>(W, H, alist, d_dc);
+            launch(k_num_child, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
+            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc);
             RSG_CHECK_LAUNCH();
         }
         ar.used = mark;
     }
+    phase_mark(st, "a.level0");
     additional_props(ar, dc, d_dc, W, M, H, E, NH, st);
 
     // outputs
     int32_t *hgrp = ar.get<int32_t>(NH + 1);
-    k_halo_group<<<nblk(NH, T), T, 0, st>>>(N, leaves, NH, hgrp);
-    k_halo_out<<<nblk(NH, T), T, 0, st>>>(H, E, NH, hgrp, d_goff, d_woff);
+    launch(k_halo_group, nblk(NH, T), T, 0, st, N, leaves, NH, hgrp);
+    launch(k_halo_out, nblk(NH, T), T, 0, st, H, E, NH, hgrp, d_goff, d_woff);
     rsg_particle *Pcopy = ar.get<rsg_particle>(num_p);
     RSG_CUDA(cudaMemcpyAsync(Pcopy, d_p, sizeof(rsg_particle) * num_p, cudaMemcpyDeviceToDevice, st));
-    k_write_back<<<nblk(M, T), T, 0, st>>>(W, M, wgroup, d_goff, d_woff, Pcopy, d_p);
+    launch(k_write_back, nblk(M, T), T, 0, st, W, M, wgroup, d_goff, d_woff, Pcopy, d_p);
     RSG_CHECK_LAUNCH();
     int herr[4];
     RSG_CUDA(cudaMemcpyAsync(herr, err, 16, cudaMemcpyDeviceToHost, st));
