@@ -221,33 +221,38 @@ def main():
     cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=n)
     raw = torch.from_numpy(p.view(np.uint8).reshape(-1))
     d_in = raw.cuda()
-    path = rk.DevicePath(n, cfg)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    for _ in range(args.warmup):
-        path.run(d_in.data_ptr())
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+
+    def timed(path, steps, prof):
+        for _ in range(args.warmup):
+            path.run(d_in.data_ptr())
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        if prof:
+            rk.profile_select(ROOF_KERNEL)
+        l0 = rk.launch_count()
+        times, res = [], None
+        for _ in range(steps):
+            flush.fill_(1)  # L2 flush between steps (outside the step's events)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            res = path.run(d_in.data_ptr())
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        launches = rk.launch_count() - l0
+        kl, kms = rk.profile_read() if prof else (0, 0.0)
+        rk.profile_select("")
+        return float(np.mean(times)), res, launches, kl, kms
+
+    # plain drop-in (the reference's results bit for bit), then the batched form
+    plain_ms, plain_res, _, _, _ = timed(rk.DevicePath(n, cfg, batched=False), args.steps, False)
     clocks = Clocks(local)
-    rk.profile_select(ROOF_KERNEL)
-    l0 = rk.launch_count()
-    times = []
-    res = None
-    for _ in range(args.steps):
-        flush.fill_(1)  # L2 flush between steps (outside the step's events)
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        res = path.run(d_in.data_ptr())
-        e1.record()
-        torch.cuda.synchronize()
-        times.append(e0.elapsed_time(e1))
-    launches = rk.launch_count() - l0
-    kl, kms = rk.profile_read()
-    rk.profile_select("")
+    step_ms, res, launches, kl, kms = timed(rk.DevicePath(n, cfg, batched=True), args.steps, True)
     clk = clocks.stop()
-    step_ms = float(np.mean(times))
     if dist:
         t = torch.tensor([step_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -265,7 +270,7 @@ def main():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         fp, off, sz = rk.rockstar_fof(host, cfg)
-        parts, halos, extra = rk.find_subs(fp, off, sz, cfg)
+        parts, halos, extra = rk.find_subs(fp, off, sz, cfg, batched=True)
         e2e_t.append(time.perf_counter() - t0)
         h2d = n * 32 + len(fp) * 32 + 16 * len(off)
         d2h = len(fp) * 32 + 16 * len(off) + len(fp) * 32 + len(halos) * (312 + 48)
@@ -287,7 +292,9 @@ def main():
             "config": {"workload": "synthetic workload %d: %d particles, %.0f Mpc/h box"
                                    % (args.cfg, n, box),
                        "particles": n, "groups": res[1], "halos": res[2],
-                       "l2": "flushed between steps (256 MiB write)", "path": "plain"},
+                       "l2": "flushed between steps (256 MiB write)", "form": "batched",
+                       "plain_particles_per_s": n * world / (plain_ms * 1e-3),
+                       "plain_ms_per_step": plain_ms, "plain_halos": plain_res[2]},
             "e2e": {"value": e2e_v, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,

@@ -127,16 +127,29 @@ int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offs
                   struct rsg_halo *halos, struct rsg_extra_halo_info *extra, int64_t max_halos,
                   int64_t *num_halos);
 
+/* Batched form of rsg_find_subs (same arguments), replacing the same OpenMP
+ * loop (src/mpi_main.cpp:1363-1389): subgroup labels come from a parallel
+ * union-find and large sums from tree reductions, so halo membership and
+ * properties are the reference's up to FP64 rounding except where a
+ * subgroup of more than 10000 particles samples its linking length (the
+ * sample depends on the reference's particle order, which this form does
+ * not reproduce); halo order within a group may differ. */
+int rsg_find_subs_batch(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offsets,
+                        const int64_t *fof_sizes, int64_t num_fofs, const struct rsg_config *cfg,
+                        struct rsg_halo *halos, struct rsg_extra_halo_info *extra,
+                        int64_t max_halos, int64_t *num_halos);
+
 /* The whole hot path -- rockstar(NULL, 1) then find_subs over every group
  * -- on device-resident data (no host copies): d_in holds n id-sorted
  * particles, d_out receives the permuted particles (*num_p_out of them)
- * and d_halos/d_extra (capacity max_halos) the halos of all groups.  Has no
+ * and d_halos/d_extra (capacity max_halos) the halos of all groups;
+ * batched selects the rsg_find_subs_batch form for the substructure step.  Has no
  * single reference counterpart: it fuses the calls of src/mpi_main.cpp:1564
  * and :1363-1389 for callers that keep particles on the GPU. */
 int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg_config *cfg,
                     struct rsg_particle *d_out, int64_t *num_p_out, int64_t *num_fofs,
                     struct rsg_halo *d_halos, struct rsg_extra_halo_info *d_extra,
-                    int64_t max_halos, int64_t *num_halos);
+                    int64_t max_halos, int64_t *num_halos, int32_t batched);
 
 /* Instrumentation: kernels launched by this library so far (process-wide),
  * and CUDA-event timing of every launch of the kernels whose name contains

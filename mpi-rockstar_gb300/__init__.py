@@ -53,7 +53,8 @@ def lib():
         h.rsg_debug_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
         h.rsg_debug_hierarchy.restype = i64
         h.rsg_debug_hierarchy.argtypes = [vp, vp, vp, i64]
-        h.rsg_path_device.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp]
+        h.rsg_path_device.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp, C.c_int32]
+        h.rsg_find_subs_batch.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, i64, vp]
         h.rsg_launch_count.restype = i64
         h.rsg_profile_select.argtypes = [C.c_char_p]
         h.rsg_profile_read.argtypes = [vp, vp]
@@ -96,9 +97,10 @@ def rockstar_fof(parts, cfg):
     return pa[:n[0]].copy(), off[:k].copy(), sz[:k].copy()
 
 
-def find_subs(parts, offsets, sizes, cfg):
-    """Substructure + halo properties for every group (batched).  Returns
-    (particles after find_subs, halos, extra)."""
+def find_subs(parts, offsets, sizes, cfg, batched=False):
+    """Substructure + halo properties for every group.  batched=False is the
+    plain drop-in (the reference's results bit for bit); batched=True the
+    batched form (rsg_find_subs_batch).  Returns (particles, halos, extra)."""
     st = setup_config(cfg)
     pa = np.array(parts, dtype=PARTICLE, copy=True)
     off = np.ascontiguousarray(offsets, np.int64)
@@ -107,8 +109,9 @@ def find_subs(parts, offsets, sizes, cfg):
     h = np.zeros(cap, HALO)
     e = np.zeros(cap, EXTRA)
     nh = np.zeros(1, np.int64)
-    _check(lib().rsg_find_subs(pa.ctypes.data, len(pa), off.ctypes.data, sz.ctypes.data, len(sz),
-                               C.byref(st), h.ctypes.data, e.ctypes.data, cap, nh.ctypes.data))
+    fn = lib().rsg_find_subs_batch if batched else lib().rsg_find_subs
+    _check(fn(pa.ctypes.data, len(pa), off.ctypes.data, sz.ctypes.data, len(sz),
+              C.byref(st), h.ctypes.data, e.ctypes.data, cap, nh.ctypes.data))
     k = int(nh[0])
     return pa, h[:k].copy(), e[:k].copy()
 
@@ -181,9 +184,10 @@ class DevicePath:
     """The full hot path on device-resident arrays (torch CUDA tensors or raw
     device pointers): rsg_path_device."""
 
-    def __init__(self, n, cfg, halo_cap=None):
+    def __init__(self, n, cfg, halo_cap=None, batched=False):
         import torch
         self.n = n
+        self.batched = 1 if batched else 0
         self.st = setup_config(cfg)
         self.halo_cap = halo_cap or (n // 4 + 1024)
         self.out = torch.empty(n * PARTICLE.itemsize, dtype=torch.uint8, device="cuda")
@@ -197,5 +201,5 @@ class DevicePath:
         _check(lib().rsg_path_device(d_in_ptr, self.n, C.byref(self.st), self.out.data_ptr(),
                                      self._np.ctypes.data, self._nf.ctypes.data,
                                      self.halos.data_ptr(), self.extra.data_ptr(),
-                                     self.halo_cap, self._nh.ctypes.data))
+                                     self.halo_cap, self._nh.ctypes.data, self.batched))
         return int(self._np[0]), int(self._nf[0]), int(self._nh[0])

@@ -151,10 +151,11 @@ int rsg_rockstar_fof(struct rsg_particle *p, int64_t *num_p, const struct rsg_co
     }
 }
 
-int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offsets,
-                  const int64_t *fof_sizes, int64_t num_fofs, const struct rsg_config *cfg,
-                  struct rsg_halo *halos, struct rsg_extra_halo_info *extra, int64_t max_halos,
-                  int64_t *num_halos) {
+static int find_subs_host(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offsets,
+                          const int64_t *fof_sizes, int64_t num_fofs,
+                          const struct rsg_config *cfg, struct rsg_halo *halos,
+                          struct rsg_extra_halo_info *extra, int64_t max_halos,
+                          int64_t *num_halos, int exact) {
     if (!p || !cfg || !num_halos || num_p < 0 || num_fofs < 0 ||
         (num_fofs && (!fof_offsets || !fof_sizes))) {
         set_error(RSG_ERR_ARGS, "rsg_find_subs: bad arguments");
@@ -174,7 +175,7 @@ int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offs
         rsg_extra_halo_info *d_e = C.ar.get<rsg_extra_halo_info>(hcap);
         RSG_CUDA(cudaMemcpyAsync(d_p, p, sizeof(rsg_particle) * num_p, cudaMemcpyHostToDevice, C.st));
         SubsOut o = find_subs_device(C.ar, d_p, num_p, fof_offsets, fof_sizes, num_fofs, *cfg,
-                                     d_h, d_e, hcap, C.st);
+                                     d_h, d_e, hcap, C.st, exact);
         if (o.nhalos > max_halos) {
             set_error(RSG_ERR_ARGS, "rsg_find_subs: %lld halos exceed max_halos %lld",
                       (long long)o.nhalos, (long long)max_halos);
@@ -193,10 +194,26 @@ int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offs
     }
 }
 
+int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offsets,
+                  const int64_t *fof_sizes, int64_t num_fofs, const struct rsg_config *cfg,
+                  struct rsg_halo *halos, struct rsg_extra_halo_info *extra, int64_t max_halos,
+                  int64_t *num_halos) {
+    return find_subs_host(p, num_p, fof_offsets, fof_sizes, num_fofs, cfg, halos, extra,
+                          max_halos, num_halos, 1);
+}
+
+int rsg_find_subs_batch(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offsets,
+                        const int64_t *fof_sizes, int64_t num_fofs, const struct rsg_config *cfg,
+                        struct rsg_halo *halos, struct rsg_extra_halo_info *extra,
+                        int64_t max_halos, int64_t *num_halos) {
+    return find_subs_host(p, num_p, fof_offsets, fof_sizes, num_fofs, cfg, halos, extra,
+                          max_halos, num_halos, 0);
+}
+
 int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg_config *cfg,
                     struct rsg_particle *d_out, int64_t *num_p_out, int64_t *num_fofs,
                     struct rsg_halo *d_halos, struct rsg_extra_halo_info *d_extra,
-                    int64_t max_halos, int64_t *num_halos) {
+                    int64_t max_halos, int64_t *num_halos, int32_t batched) {
     if (!d_in || !d_out || !cfg || n < 0 || !num_halos || !num_fofs || !num_p_out) {
         set_error(RSG_ERR_ARGS, "rsg_path_device: bad arguments");
         return RSG_ERR_ARGS;
@@ -220,7 +237,7 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
             RSG_CUDA(cudaStreamSynchronize(C.st));
         }
         SubsOut s2 = find_subs_device(C.ar, d_out, o.num_p, off.data(), sz.data(), o.nfofs, *cfg,
-                                      d_halos, d_extra, max_halos, C.st);
+                                      d_halos, d_extra, max_halos, C.st, batched ? 0 : 1);
         RSG_CUDA(cudaStreamSynchronize(C.st));
         phase_report();
         *num_p_out = o.num_p;

@@ -201,7 +201,8 @@ __global__ void k_bh_internal(const KNode<3> *nodes, int32_t first, int32_t coun
 // to the mass centre; the maximum is a reduction and the sum is added by one
 // thread in point order, as _compute_dmin does.
 __global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, int32_t first,
-                                                         int32_t count, const PotRec *PO, BHNode *B) {
+                                                         int32_t count, const PotRec *PO, BHNode *B,
+                                                         int exact) {
     __shared__ double dx_s[256];
     __shared__ BHNode bs;
     __shared__ double mx_s[8];
@@ -223,11 +224,26 @@ __global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, 
             dx = d2d(bs.mc, PO[x.start + i].pos);
             if (bm < dx) bm = dx;
         }
+        if (!exact) {
+            sx += dx;
+            continue;
+        }
         dx_s[threadIdx.x] = dx;
         __syncthreads();
         if (threadIdx.x == 0) {
             int m = min(256, x.n - b0);
             for (int t = 0; t < m; t++) sx += dx_s[t];
+        }
+        __syncthreads();
+    }
+    if (!exact) {
+        for (int o = 16; o; o >>= 1) sx += __shfl_down_sync(0xffffffffu, sx, o);
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) dx_s[threadIdx.x >> 5] = sx;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            sx = 0;
+            for (int w = 0; w < 8; w++) sx += dx_s[w];
         }
         __syncthreads();
     }
@@ -765,8 +781,26 @@ __device__ int chunk_prefix(int flag, int *warp_tot) {
     return off + incl;
 }
 
+// deterministic block sum of one double (all threads call; result in all)
+__device__ double bsum(double v, double *sm) {
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int i = 0; i < RSG_SB / 32; i++) t += sm[i];
+        sm[RSG_SB / 32] = t;
+    }
+    __syncthreads();
+    double r = sm[RSG_SB / 32];
+    __syncthreads();
+    return r;
+}
+
 __device__ void shape_blk(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
-                          const DevCfg &C, BlkBuf &B) {
+                          const DevCfg &C, BlkBuf &B, int exact) {
+    __shared__ double red_s[RSG_SB / 32 + 1];
     __shared__ double orth[3][3], eig[3], acc[7];
     __shared__ float minr_s;
     __shared__ int64_t it_s;
@@ -806,9 +840,11 @@ __device__ void shape_blk(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
     const float hp0 = h.pos[0], hp1 = h.pos[1], hp2 = h.pos[2];
     for (int64_t i = 0; i < it_s; i++) {
         double a = 0;  // lane k of warp 0 owns accumulator k (w, m00, m11, m22, m10, m20, m21)
+        double part[7] = {0, 0, 0, 0, 0, 0, 0};  // batched mode: per-thread partial sums
         for (int64_t b0 = 0; b0 < tot; b0 += RSG_SB) {
             int64_t j = b0 + threadIdx.x;
             unsigned char sk = 1;
+            double vv[7];
             if (j < tot && !(bound && unbound(po[j]))) {
                 const float *p = po[j].pos;
                 double dd[3] = {(double)fsub(p[0], hp0), (double)fsub(p[1], hp1),
@@ -822,16 +858,23 @@ __device__ void shape_blk(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
                 if (r < (double)minr_s) r = minr_s;
                 if (r > 0 && r <= 1) {
                     double tw = (C.weighted_shapes) ? 1.0 / r : 1.0;
-                    B.v[threadIdx.x][0] = tw;
-                    B.v[threadIdx.x][1] = dd[0] * dd[0] * tw;
-                    B.v[threadIdx.x][2] = dd[1] * dd[1] * tw;
-                    B.v[threadIdx.x][3] = dd[2] * dd[2] * tw;
-                    B.v[threadIdx.x][4] = dd[0] * dd[1] * tw;
-                    B.v[threadIdx.x][5] = dd[0] * dd[2] * tw;
-                    B.v[threadIdx.x][6] = dd[1] * dd[2] * tw;
+                    vv[0] = tw;
+                    vv[1] = dd[0] * dd[0] * tw;
+                    vv[2] = dd[1] * dd[1] * tw;
+                    vv[3] = dd[2] * dd[2] * tw;
+                    vv[4] = dd[0] * dd[1] * tw;
+                    vv[5] = dd[0] * dd[2] * tw;
+                    vv[6] = dd[1] * dd[2] * tw;
                     sk = 0;
                 }
             }
+            if (!exact) {
+                if (!sk)
+                    for (int c = 0; c < 7; c++) part[c] += vv[c];
+                continue;
+            }
+            if (!sk)
+                for (int c = 0; c < 7; c++) B.v[threadIdx.x][c] = vv[c];
             B.skip[threadIdx.x] = sk;
             __syncthreads();
             if (threadIdx.x < 7) {
@@ -842,6 +885,11 @@ __device__ void shape_blk(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
             }
             __syncthreads();
         }
+        if (!exact)
+            for (int c = 0; c < 7; c++) {
+                double t = bsum(part[c], red_s);
+                if (threadIdx.x == c) a = t;
+            }
         if (threadIdx.x < 7) acc[threadIdx.x] = a;
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -919,7 +967,8 @@ __device__ void blk_argmax(double &cv, int64_t &j, double *scv, int64_t *sj) {
 }
 
 __device__ void more_props_blk(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
-                               const DevCfg &C, BlkBuf &B) {
+                               const DevCfg &C, BlkBuf &B, int exact) {
+    __shared__ double red_m[RSG_SB / 32 + 1];
     __shared__ MPState S;
     __shared__ int want;
     __shared__ int wt[RSG_SB / 32];
@@ -1012,7 +1061,69 @@ __device__ void more_props_blk(rsg_halo &h, const PotRec *po, int64_t tot, int b
     __syncthreads();
     // pass 2 (src/properties.c:435-448): warp 0, lanes 0-2 own L[k], lanes
     // 3-5 xavg[k], lanes 6-8 vavg[k] and vrms[k]
-    {
+    if (!exact) {
+        // batched mode: block sums; running means become plain means and the
+        // running second moments a two-pass sum about the mean
+        double lp[3] = {0, 0, 0}, xs[3] = {0, 0, 0}, vs[3] = {0, 0, 0};
+        int64_t cnt = 0, nh = INT64_MAX;
+        const float *c = h.pos;
+        int64_t base = 0;
+        for (int64_t b0 = 0; b0 < S.dtot; b0 += RSG_SB) {
+            int64_t j = b0 + threadIdx.x;
+            int ok = j < S.dtot && !(bound && unbound(po[j]));
+            int incl = chunk_prefix(ok, wt);
+            if (ok) {
+                const float *p = po[j].pos;
+                for (int k = 0; k < 3; k++) {
+                    int x = (k + 1) % 3, y = (k + 2) % 3;
+                    lp[k] += (double)fmul(fsub(p[x], c[x]), fsub(p[y + 3], c[y + 3]));
+                    lp[k] -= (double)fmul(fsub(p[y], c[y]), fsub(p[x + 3], c[x + 3]));
+                    xs[k] += (double)p[k];
+                    vs[k] += (double)p[k + 3];
+                }
+                cnt++;
+                int64_t run = base + incl;
+                if (j >= 1 && run * 2 >= S.pmd && j < nh) nh = j;
+            }
+            __syncthreads();
+            if (threadIdx.x == RSG_SB - 1) B.np[0] = incl;
+            __syncthreads();
+            base += B.np[0];
+            __syncthreads();
+        }
+        double tot_c = bsum((double)cnt, red_m);
+        for (int k = 0; k < 3; k++) {
+            double t = bsum(lp[k], red_m);
+            if (threadIdx.x == 0) S.L[k] = t;
+            t = bsum(xs[k], red_m);
+            if (threadIdx.x == 0) S.xa[k] = tot_c > 0 ? t / tot_c : 0;
+            t = bsum(vs[k], red_m);
+            if (threadIdx.x == 0) S.va[k] = tot_c > 0 ? t / tot_c : 0;
+        }
+        __syncthreads();
+        double v2[3] = {0, 0, 0};
+        for (int64_t j = threadIdx.x; j < S.dtot; j += RSG_SB) {
+            if (bound && unbound(po[j])) continue;
+            for (int k = 0; k < 3; k++) {
+                double d = (double)po[j].pos[k + 3] - S.va[k];
+                v2[k] += d * d;
+            }
+        }
+        for (int k = 0; k < 3; k++) {
+            double t = bsum(v2[k], red_m);
+            if (threadIdx.x == 0) S.vrms[k] = t;
+        }
+        __shared__ unsigned long long nhs;
+        if (threadIdx.x == 0) nhs = (unsigned long long)INT64_MAX;
+        __syncthreads();
+        atomicMin(&nhs, (unsigned long long)nh);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            S.avg = (int64_t)tot_c;
+            S.nhalf = (nhs == (unsigned long long)INT64_MAX) ? 0 : (int64_t)nhs;
+        }
+        __syncthreads();
+    } else {
         double acc_a = 0, acc_b = 0;
         int64_t avg = 0, nhalf = 0;
         const float *c = h.pos;
@@ -1086,7 +1197,7 @@ __device__ void more_props_blk(rsg_halo &h, const PotRec *po, int64_t tot, int b
     }
     __syncthreads();
     if (!want) return;
-    shape_blk(h, po, S.npa[2], bound, C, B);
+    shape_blk(h, po, S.npa[2], bound, C, B, exact);
     __syncthreads();
     if (threadIdx.x == 0) {
         h.b_to_a2 = h.b_to_a;
@@ -1096,12 +1207,35 @@ __device__ void more_props_blk(rsg_halo &h, const PotRec *po, int64_t tot, int b
         h.r = (float)(cbrt((3.0 / (4.0 * M_PI)) * S.pmd / C.thresh_dens[0]) * 1e3);
     }
     __syncthreads();
-    shape_blk(h, po, S.dtot, bound, C, B);
+    shape_blk(h, po, S.dtot, bound, C, B, exact);
     __syncthreads();
     // estimate_total_energy over [0, dtot) in descending order: lane 0 sums
     // ke, lane 1 the two coupled potential sums (src/properties.c:328-349)
     __shared__ double en[3];
-    {
+    if (!exact) {
+        // tphi = sum a_i + sum b_i * (number of qualifying particles before i)
+        double kes = 0, ts = 0;
+        int64_t base = 0;
+        for (int64_t b0 = 0; b0 < S.dtot; b0 += RSG_SB) {
+            int64_t i = b0 + threadIdx.x;
+            int ok = i < S.dtot && po[i].pe > (double)po[i].ke;
+            int incl = chunk_prefix(ok, wt);
+            if (ok) {
+                double r = sqrt((double)po[i].r2);
+                if (r < C.force_res) r = C.force_res;
+                kes += (double)po[i].ke;
+                ts += C.particle_mass * i / r + (C.particle_mass / r) * (double)(base + incl - 1);
+            }
+            __syncthreads();
+            if (threadIdx.x == RSG_SB - 1) B.np[0] = incl;
+            __syncthreads();
+            base += B.np[0];
+            __syncthreads();
+        }
+        double t1 = bsum(kes, red_m), t2 = bsum(ts, red_m);
+        if (threadIdx.x == 0) { en[0] = t1; en[1] = t2; }
+        __syncthreads();
+    } else {
         double acc_a = 0, acc_b = 0;
         for (int64_t top = S.dtot - 1; top >= 0; top -= RSG_SB) {
             int64_t i = top - threadIdx.x;
@@ -1214,7 +1348,7 @@ __device__ void corevel_blk(rsg_halo &h, const PotRec *q, int64_t tot, const Dev
 __global__ void __launch_bounds__(RSG_SB) k_halo_scans_blk(rsg_halo *H, const rsg_extra_halo_info *E,
                                                            const int32_t *list, PotRec *PO,
                                                            const int32_t *toff, const int32_t *kept,
-                                                           const DevCfg *Cp) {
+                                                           const DevCfg *Cp, int exact) {
     __shared__ BlkBuf B;
     int h = list[blockIdx.x];
     rsg_halo &hh = H[h];
@@ -1241,8 +1375,8 @@ __global__ void __launch_bounds__(RSG_SB) k_halo_scans_blk(rsg_halo *H, const rs
         }
     }
     __syncthreads();
-    more_props_blk(hh, q, tot, 0, C, B);
-    more_props_blk(hh, q, tot, 1, C, B);
+    more_props_blk(hh, q, tot, 0, C, B, exact);
+    more_props_blk(hh, q, tot, 1, C, B, exact);
 }
 
 // halos split by size: small ones one thread each, large ones one block each
@@ -1326,7 +1460,8 @@ static int32_t select_idx(Arena &ar, const int32_t *flag, int32_t *out, int32_t 
 
 // Barnes-Hut potentials for the segments (rs[k], rn[k]) of PO.
 void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const int32_t *rn,
-                  int32_t ntrees, double mp, double force_res, int *err, cudaStream_t st) {
+                  int32_t ntrees, double mp, double force_res, int *err, cudaStream_t st,
+                  int exact) {
     const int T = 256;
     if (ntrees == 0) return;
     Forest<3> F = build_forest<3, PotRec>(ar, PO, npo, rs, rn, ntrees, npo, 10, st);
@@ -1337,7 +1472,7 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
         int32_t a = F.lv_first[l], b = F.lv_first[l + 1];
         if (b > a) {
             launch(k_bh_internal, nblk(b - a, 64), 64, 0, st, F.nodes, a, b - a, PO, B);
-            launch(k_bh_internal_big, b - a, 256, 0, st, F.nodes, a, b - a, PO, B);
+            launch(k_bh_internal_big, b - a, 256, 0, st, F.nodes, a, b - a, PO, B, exact);
         }
     }
     phase_mark(st, "p.bh_mass");
@@ -1351,7 +1486,7 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
 
 void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec *W,
                       int64_t M, rsg_halo *H, rsg_extra_halo_info *E, int32_t NH,
-                      cudaStream_t st) {
+                      cudaStream_t st, int exact) {
     const int T = 256;
     if (NH == 0) return;
     size_t mark = ar.used;
@@ -1378,7 +1513,7 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
         int32_t nr = select_idx(ar, rflag, hl, NH, st);
         int32_t *rs = ar.get<int32_t>(nr + 1), *rn = ar.get<int32_t>(nr + 1);
         if (nr) launch(k_bh_root_arrays, nblk(nr, T), T, 0, st, hl, nr, toff, tot, rs, rn);
-        bh_potential(ar, PO, npo, rs, rn, nr, dc.particle_mass, dc.force_res, err, st);
+        bh_potential(ar, PO, npo, rs, rn, nr, dc.particle_mass, dc.force_res, err, st, exact);
         ar.used = m2;
     }
     // drop potential-only records and sort every halo's records by r^2
@@ -1406,7 +1541,7 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
         launch(k_scan_split, nblk(NH, T), T, 0, st, H, NH, kept, 1024, fs, fbg);
         int32_t nsm = select_idx(ar, fs, ls, NH, st);
         int32_t nbg = select_idx(ar, fbg, lb, NH, st);
-        launch(k_halo_scans_blk, nbg, RSG_SB, 0, st, H, E, lb, PO2, toff, kept, d_dc);
+        launch(k_halo_scans_blk, nbg, RSG_SB, 0, st, H, E, lb, PO2, toff, kept, d_dc, exact);
         launch(k_halo_scans_list, nblk(nsm, 32), 32, 0, st, H, E, ls, nsm, PO2, toff, kept, d_dc);
     }
     RSG_CHECK_LAUNCH();

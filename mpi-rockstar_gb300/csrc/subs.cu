@@ -43,7 +43,7 @@ std::vector<float> g_dbg_target;
 
 void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec *W,
                       int64_t M, rsg_halo *H, rsg_extra_halo_info *E, int32_t NH,
-                      cudaStream_t st);
+                      cudaStream_t st, int exact);
 
 // ---- reductions -------------------------------------------------------------
 __device__ __forceinline__ double warp_sum_d(double v) {
@@ -141,7 +141,7 @@ __global__ void k_norm_seq(Rec *W, HierNodes N, int32_t base, int32_t count, int
 // Mid-size nodes: the block stages particles in shared memory and computes
 // the per-particle products; thread 0 adds them in array order.
 __global__ void __launch_bounds__(256) k_norm_blk(Rec *W, HierNodes N, int32_t base, int level0,
-                                                  double ims, double *sig) {
+                                                  double ims, double *sig, int seq_max) {
     __shared__ float q[256][6];
     __shared__ float pr[256][21];
     __shared__ double mean[6], corr[21];
@@ -191,13 +191,13 @@ __global__ void __launch_bounds__(256) k_norm_blk(Rec *W, HierNodes N, int32_t b
 
 // Larger nodes: one block, deterministic tree reductions.
 __global__ void k_norm_par(Rec *W, HierNodes N, int32_t base, int level0, double ims,
-                           double *sig) {
+                           double *sig, int seq_max) {
     __shared__ double sm[40];
     __shared__ double mean[6], corr[21];
     int k = blockIdx.x;
     int node = base + k;
     int s = N.start[node], n = N.n[node];
-    if (n <= RSG_SEQ_MAX) return;
+    if (n <= seq_max) return;
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int i = threadIdx.x; i < n; i += blockDim.x)
         for (int d = 0; d < 6; d++) acc[d] += (double)W[s + i].pos[d];
@@ -595,6 +595,30 @@ __global__ void k_replay6_smem(HierNodes N, int32_t base, const int32_t *noff,
     }
 }
 
+// Batched mode: subgroup labels from a parallel union-find over the same
+// links (components are the same sets; the label is the component's first
+// position, -1 for particles without links), so the partition order is
+// deterministic but not the reference's.
+__global__ void k_uf6(const int32_t *eln, int64_t M, const int32_t *noff, const int32_t *nbr,
+                      int *par) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M || eln[i] < 0) return;
+    for (int e = noff[i]; e < noff[i + 1]; e++) uf_unite2(par, (int)i, nbr[e]);
+}
+__global__ void k_uf6_size(const int32_t *eln, int64_t M, int *par, int *root, int *size) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M || eln[i] < 0) return;
+    int r = uf_find2(par, (int)i);
+    root[i] = r;
+    atomicAdd(&size[r], 1);
+}
+__global__ void k_uf6_label(const int32_t *eln, int64_t M, const int *root, const int *size,
+                            int32_t *lab) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M || eln[i] < 0) return;
+    lab[i] = size[root[i]] > 1 ? root[i] : -1;
+}
+
 // Runs of equal labels after the partition sort: the kept ones (>= 0 and at
 // least MIN_HALO_PARTICLES long) are the subgroups of build_fullfofs
 // (src/fof.c:226-255), in array order.
@@ -900,14 +924,15 @@ __global__ void k_halo_tails(const int32_t *eln, int64_t M, HierNodes N, int32_t
 
 // calc_basic_halo_props + estimate_vmax (src/properties.c:39-125); one
 // block per listed halo.
-__global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, const DevCfg *C) {
+__global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, const DevCfg *C,
+                              int seq_max) {
     __shared__ double sm[40];
     __shared__ double mean[6], p2[6];
     __shared__ int bins[50];
     int h = list[blockIdx.x];
     rsg_halo &hh = H[h];
     int ps = (int)hh.p_start, np = (int)hh.num_p;
-    if (np <= RSG_SEQ_MAX) {
+    if (np <= seq_max) {
         // in array order (src/properties.c:76-87): the block stages values,
         // thread 0 adds them
         __shared__ double stage[256][6];
@@ -1303,8 +1328,10 @@ DevCfg make_devcfg(const rsg_config &c) {
 SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int64_t *goff_h,
                          const int64_t *gsz_h, int64_t ngroups, const rsg_config &cfg,
                          rsg_halo *d_halos, rsg_extra_halo_info *d_extra, int64_t max_halos,
-                         cudaStream_t st) {
+                         cudaStream_t st, int exact) {
     SubsOut out{0};
+    // ordered (bit-exact) FP64 sums up to this size; tree reductions above
+    const int seq_max = exact ? RSG_SEQ_MAX : RSG_SMALL;
     const int T = 256;
     // groups with particles, their working offsets
     std::vector<int64_t> goff, gsz, woff;
@@ -1374,8 +1401,10 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             double *sig = ar.get<double>(2 * (int64_t)cnt);
             launch(k_norm_seq, nblk(cnt, 32), 32, 0, st, W, N, base, cnt, L == 0,
                                                      cfg.initial_metric_scaling, sig);
-            launch(k_norm_blk, cnt, 256, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig);
-            launch(k_norm_par, cnt, T, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig);
+            launch(k_norm_blk, cnt, 256, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig,
+                   seq_max);
+            launch(k_norm_par, cnt, T, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig,
+                   seq_max);
             launch(k_norm_div, cnt, T, 0, st, W, N, base, sig);
             RSG_CHECK_LAUNCH();
         }
@@ -1420,8 +1449,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         launch(k_fof6, nblk(M, T), T, 0, st, F.nodes, W, M, N, base, eln, noff, ncnt, nbr, err);
         phase_mark(st, "d.fof6d");
         // reference labels, then the reference's partition sort by label
-        launch(k_replay6, nblk(cnt, 32), 32, 0, st, N, base, cnt, noff, nbr, phalo, csize);
-        {
+        if (exact) {
+            launch(k_replay6, nblk(cnt, 32), 32, 0, st, N, base, cnt, noff, nbr, phalo, csize);
             static bool attr = false;
             if (!attr) {
                 RSG_CUDA(cudaFuncSetAttribute(k_replay6_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1429,6 +1458,12 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                 attr = true;
             }
             launch(k_replay6_smem, cnt, 128, (size_t)8 * RSG_REPLAY_SMEM, st, N, base, noff, nbr, phalo);
+        } else {
+            int *ufp = csize, *ufr = key2 ? (int *)key2 : nullptr, *ufs = (int *)val2;
+            launch(k_init_par, nblk(M, T), T, 0, st, eln, M, ufp, ufs);
+            launch(k_uf6, nblk(M, T), T, 0, st, eln, M, noff, nbr, ufp);
+            launch(k_uf6_size, nblk(M, T), T, 0, st, eln, M, ufp, ufr, ufs);
+            launch(k_uf6_label, nblk(M, T), T, 0, st, eln, M, ufr, ufs, phalo);
         }
         RSG_CHECK_LAUNCH();
         phase_mark(st, "d.replay");
@@ -1524,11 +1559,11 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         int32_t *glv = ar.get<int32_t>(ngr + 1), *gnode = ar.get<int32_t>(ngr + 1);
         launch(k_list_growing, nblk(cnt, T), T, 0, st, N, base, cnt, goffs, glist, glv);
         launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, goffs, gnode);
-        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc);
+        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc, seq_max);
         launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 0);
         launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E);
         launch(k_fix_parents, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
-        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc);
+        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc, seq_max);
         RSG_CHECK_LAUNCH();
         phase_mark(st, "a.props_parents");
         if (L == 0) {
@@ -1538,7 +1573,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             int32_t *alist = ar.get<int32_t>(na + 1), *anode = ar.get<int32_t>(na + 1);
             launch(k_list_all, nblk(cnt, T), T, 0, st, N, base, cnt, aoff, alist);
             launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, aoff, anode);
-            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc);
+            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc, seq_max);
             launch(k_corekeys, nblk(M, T), T, 0, st, W, eln, M, phalo, H, key, val);
             sort_pairs(ar, key, key2, val, val2, M, keybits, st);
             launch(k_gather<Rec>, nblk(M, T), T, 0, st, W, val2, M, W2);
@@ -1552,13 +1587,13 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             // find_subs tail (src/groupies.c:697-703): child counts and basic
             // properties for every halo, then the additional properties.
             launch(k_num_child, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
-            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc);
+            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc, seq_max);
             RSG_CHECK_LAUNCH();
         }
         ar.used = mark;
     }
     phase_mark(st, "a.level0");
-    additional_props(ar, dc, d_dc, W, M, H, E, NH, st);
+    additional_props(ar, dc, d_dc, W, M, H, E, NH, st, exact);
 
     // outputs
     int32_t *hgrp = ar.get<int32_t>(NH + 1);

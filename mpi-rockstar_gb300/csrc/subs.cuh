@@ -24,9 +24,11 @@ struct SubsOut {
 //  d_p      : caller particles (num_p), permuted in place on return
 //  goff/gsz : groups (host arrays, ng groups); groups must not overlap
 //  d_halos/d_extra : outputs (capacity max_halos)
+//  exact    : 1 = the reference's labels, orders and sums (plain drop-in);
+//             0 = batched mode (parallel labels and reductions)
 SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int64_t *goff,
                          const int64_t *gsz, int64_t ngroups, const rsg_config &cfg,
                          rsg_halo *d_halos, rsg_extra_halo_info *d_extra, int64_t max_halos,
-                         cudaStream_t st);
+                         cudaStream_t st, int exact);
 
 }  // namespace rsg

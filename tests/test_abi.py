@@ -1,0 +1,53 @@
+"""The C ABI library loads and exports every function declared in
+include/*.h (no GPU calls)."""
+import ctypes
+import glob
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[\w ]+?[\s\*]+(rsg_\w+)\s*\(", src, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_exports_every_declared_symbol(rk):
+    lib = ctypes.CDLL(rk.LIB)
+    names = declared_functions()
+    assert {"rsg_rockstar_fof", "rsg_find_subs", "rsg_find_subs_batch",
+            "rsg_path_device", "rsg_config_setup"} <= names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_config_setup_matches_oracle(rk, oracle):
+    """AVG_PARTICLE_SPACING and the density thresholds, host side."""
+    import numpy as np
+    c = rk.Config(particle_mass=2.03e10, box_size=80.0, total_particles=2097152)
+    st = rk.setup_config(c)
+    sp = oracle.setup(c)
+    th = oracle.thresholds()
+    assert st.avg_particle_spacing == sp
+    assert np.array_equal(np.array(list(st.particle_thresh_dens)), th[:5])
+    assert (st.particle_rvir_dens, st.particle_rvir_dens_z0, st.dynamical_time) == tuple(th[5:8])
+
+
+def test_errors_without_gpu(rk):
+    """Without a GPU every compute entry fails with a code, never silently."""
+    import numpy as np
+    import torch
+    if torch.cuda.is_available():
+        return
+    p = np.zeros(10, rk.PARTICLE)
+    try:
+        rk.rockstar_fof(p, rk.Config())
+    except rk.RockstarError as e:
+        assert e.code in (-2, -3)
+    else:
+        raise AssertionError("expected an error without a GPU")
