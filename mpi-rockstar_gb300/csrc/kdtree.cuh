@@ -61,13 +61,18 @@ struct PosOf<MetricRec, D> {
     __device__ static float get(const MetricRec &r, int d) { return r.pos[d]; }
 };
 
+#define RSG_FOREST_LEVELS 4096  // deepest build accepted (checked by build_forest)
+
 template <int D>
 struct Forest {
     KNode<D> *nodes = nullptr;  // nodes[t] is the root of tree t
     int32_t nnodes = 0;
     int32_t ntrees = 0;
-    // nodes created by level l of the build are [lv_first[l], lv_first[l+1])
-    std::vector<int32_t> lv_first;
+    // nodes created by level l of the build are [lv_first[l], lv_first[l+1]),
+    // l < nlv - 1; a fixed table so a build touches no host heap
+    int32_t lv_first[RSG_FOREST_LEVELS + 2];
+    int32_t nlv = 0;
+    void level_end(int32_t first) { lv_first[nlv++] = first; }
 };
 
 // ---- kernels ------------------------------------------------------------

@@ -117,12 +117,12 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
     RSG_CUDA(cudaMemcpyAsync(&nact, cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     int32_t nnodes = ntrees;
-    F.lv_first.push_back(0);
-    F.lv_first.push_back(ntrees);
+    F.level_end(0);
+    F.level_end(ntrees);
     int level = 0;
     while (nact > 0) {
-        if (++level > 4096) {
-            set_error(RSG_ERR_LIMIT, "kd-forest build exceeded 4096 levels");
+        if (++level > RSG_FOREST_LEVELS) {
+            set_error(RSG_ERR_LIMIT, "kd-forest build exceeded %d levels", RSG_FOREST_LEVELS);
             throw Failure();
         }
         launch(k_slot_set, nblk(nact, T), T, 0, st, act, nact, slot);
@@ -149,7 +149,7 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
         int32_t base = nnodes;
         launch(k_children<D>, nblk(nact, T), T, 0, st, nodes, act, nact, m_arr, soff, base, bmin, bmax);
         nnodes += 2 * nsplit;
-        F.lv_first.push_back(nnodes);
+        F.level_end(nnodes);
         launch(k_owner_update<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, box_owner, leaf);
         if (nsplit > 0) {
             launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st, 

@@ -1468,7 +1468,7 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     phase_mark(st, "p.bh_tree");
     BHNode *B = ar.get<BHNode>(F.nnodes);
     launch(k_bh_leaf, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, PO, mp, B);
-    for (int l = (int)F.lv_first.size() - 2; l >= 0; l--) {
+    for (int l = F.nlv - 2; l >= 0; l--) {
         int32_t a = F.lv_first[l], b = F.lv_first[l + 1];
         if (b > a) {
             launch(k_bh_internal, nblk(b - a, 64), 64, 0, st, F.nodes, a, b - a, PO, B);
