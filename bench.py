@@ -33,9 +33,36 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 METRIC = "particles/s through FOF+6D+unbind+props, batched vs plain on GB300 @ stated tol"
 SEED = 20261203
-# dominant kernel for the roofline figure, with its algorithmic bytes per
-# unit (see the kernel table of the design doc)
-ROOF_KERNEL = os.environ.get("RSG_ROOF_KERNEL", "k_bh_walk")
+# Algorithmic (compulsory) bytes of ONE launch of a kernel, from the work
+# counters the library reports for the step (rsg_last_stats): every input
+# record read once, every output written once; node data held in L2 is not
+# counted.  Kernels without an entry get no roofline figure.
+ALGO_BYTES = {
+    "k_halo_scans_blk": lambda st, L: 52.0 * st["kept_big"],
+    "k_halo_scans_list": lambda st, L: 52.0 * st["kept_small"],
+    "k_bh_walk": lambda st, L: 56.0 * st["pot_records"],     # read 48 B, write 8 B pe
+    # two launches (count, fill): positions read by both, entries written once
+    "k_llist": lambda st, L: (32.0 * st["particles"] + 4.0 * st["later_list"]) / max(L, 1),
+}
+
+
+def short_name(mangled):
+    """rsg kernel name from its mangled symbol (_ZN3rsg<len><name>...)."""
+    import re
+    m = re.match(r"_ZN3rsg(\d+)", mangled)
+    if not m:
+        return mangled
+    k = int(m.group(1))
+    return mangled[m.end():m.end() + k]
+
+
+def parse_table(txt):
+    rows = []
+    for line in txt.splitlines():
+        parts = line.split("\t")
+        if len(parts) == 3:
+            rows.append((short_name(parts[0]), int(parts[1]), float(parts[2])))
+    return rows
 
 
 def load_pkg():
@@ -196,6 +223,9 @@ def main():
     ap.add_argument("--cfg", type=int, default=2)
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel-table", default="",
+                    help="write per-kernel CUDA-event times of one extra (untimed) step of "
+                         "each form to this file")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -207,7 +237,7 @@ def main():
     # CPU baseline first: no GPU context exists yet
     cpu = None
     if rank == 0 and world >= 1 and not args.no_cpu_baseline and args.gpus == 1:
-        cpu = cpu_baseline_port(rk, args.cfg, args.scale / 8)
+        cpu = cpu_baseline_port(rk, args.cfg, args.scale)
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
@@ -223,6 +253,20 @@ def main():
     d_in = raw.cuda()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
+    def event_table(path):
+        """One untimed step with CUDA events around every kernel."""
+        torch.cuda.synchronize()
+        rk.profile_select("*")
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        path.run(d_in.data_ptr())
+        e1.record()
+        torch.cuda.synchronize()
+        tab = rk.profile_table()
+        rk.profile_select("")
+        return e0.elapsed_time(e1), tab
+
     def timed(path, steps, prof):
         for _ in range(args.warmup):
             path.run(d_in.data_ptr())
@@ -230,7 +274,7 @@ def main():
         if dist:
             dist.barrier()
         if prof:
-            rk.profile_select(ROOF_KERNEL)
+            rk.profile_select(prof)
         l0 = rk.launch_count()
         times, res = [], None
         for _ in range(steps):
@@ -249,16 +293,33 @@ def main():
         return float(np.mean(times)), res, launches, kl, kms
 
     # plain drop-in (the reference's results bit for bit), then the batched form
-    plain_ms, plain_res, _, _, _ = timed(rk.DevicePath(n, cfg, batched=False), args.steps, False)
+    plain_path = rk.DevicePath(n, cfg, batched=False)
+    plain_ms, plain_res, plain_launches, _, _ = timed(plain_path, args.steps, None)
+    batched_path = rk.DevicePath(n, cfg, batched=True)
+    batched_path.run(d_in.data_ptr())
+    # the dominant kernel of the batched step, by device time
+    tab_ms, tab = event_table(batched_path)
+    rows = parse_table(tab)
+    top = rows[0][0] if rows else None
     clocks = Clocks(local)
-    step_ms, res, launches, kl, kms = timed(rk.DevicePath(n, cfg, batched=True), args.steps, True)
+    step_ms, res, launches, kl, kms = timed(batched_path, args.steps, top)
     clk = clocks.stop()
+    stats = rk.last_stats()
     if dist:
         t = torch.tensor([step_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         step_ms = float(t.item())
         dist.barrier()
     value = n * world / (step_ms * 1e-3)
+
+    if args.kernel_table and rank == 0:
+        # the batched table above and one extra step of the plain form
+        with open(args.kernel_table, "w") as f:
+            f.write("# form batched: step %.3f ms (events around every kernel)\n" % tab_ms)
+            f.write(tab)
+            pms, ptab = event_table(plain_path)
+            f.write("# form plain: step %.3f ms (events around every kernel)\n" % pms)
+            f.write(ptab)
 
     # e2e through the C ABI with pinned host buffers
     pin = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
@@ -279,12 +340,21 @@ def main():
     pk, pk_kind = peaks()
     roof = None
     if kl:
-        # algorithmic bytes of one k_bh_walk launch: every particle record of
-        # every potential set is read once (48 B) and its potential written
-        # once (8 B); node records are read from L2 and not counted
-        npo = getattr(rk, "_last_npo", None)
         avg_ms = kms / kl
-        roof = {"kernel": ROOF_KERNEL, "bound": "hbm", "launches": kl, "avg_ms": avg_ms}
+        per_step = kl / max(args.steps, 1)
+        model = ALGO_BYTES.get(top)
+        algo = model(stats, per_step) if model else None
+        ach = algo / (avg_ms * 1e-3) / 1e9 if algo else None
+        peak = float(pk["hbm_gbs"])
+        share = None
+        if rows:
+            share = sum(r[2] for r in rows if r[0] == top) / tab_ms
+        roof = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": (ach / peak) if ach else None, "traffic": None,
+                "algorithmic_bytes_per_launch": algo, "launches": kl, "avg_ms": avg_ms,
+                "share_of_step": share,
+                "peak_kind": "measured copy (MEASURED_PEAKS.json hbm_gbs)"
+                             if pk_kind == "measured" else "fallback 6.8 TB/s"}
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -294,10 +364,12 @@ def main():
                        "particles": n, "groups": res[1], "halos": res[2],
                        "l2": "flushed between steps (256 MiB write)", "form": "batched",
                        "plain_particles_per_s": n * world / (plain_ms * 1e-3),
-                       "plain_ms_per_step": plain_ms, "plain_halos": plain_res[2]},
+                       "plain_ms_per_step": plain_ms, "plain_halos": plain_res[2],
+                       "plain_gpu_launches": plain_launches},
             "e2e": {"value": e2e_v, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+            "work": stats,
             "clocks": clk, "peak_source": pk_kind}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -151,6 +151,22 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
                     struct rsg_halo *d_halos, struct rsg_extra_halo_info *d_extra,
                     int64_t max_halos, int64_t *num_halos, int32_t batched);
 
+/* Work counters of the last rsg_path_device / rsg_find_subs* /
+ * rsg_rockstar_fof call on the calling thread (vals[0..n), n <=
+ * RSG_STAT_COUNT), for throughput and roofline accounting. */
+#define RSG_STAT_PARTICLES 0     /* particles after dedupe */
+#define RSG_STAT_GROUPS 1        /* 3D FOF groups */
+#define RSG_STAT_HALOS 2         /* halos written */
+#define RSG_STAT_POT_RECORDS 3   /* potential records over all halos */
+#define RSG_STAT_KEPT_BIG 4      /* kept records of block-processed halos */
+#define RSG_STAT_KEPT_SMALL 5    /* kept records of thread-processed halos */
+#define RSG_STAT_HALOS_BIG 6
+#define RSG_STAT_HALOS_SMALL 7
+#define RSG_STAT_DENSE 8         /* 3D FOF particles with > 16 neighbours */
+#define RSG_STAT_LATER_LIST 9    /* 3D FOF later-dense-neighbour entries */
+#define RSG_STAT_COUNT 10
+int rsg_last_stats(int64_t *vals, int32_t n);
+
 /* Instrumentation: kernels launched by this library so far (process-wide),
  * and CUDA-event timing of every launch of the kernels whose name contains
  * `kernel_substring` (empty string: off).  rsg_profile_read returns the
@@ -158,6 +174,11 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
 int64_t rsg_launch_count(void);
 int rsg_profile_select(const char *kernel_substring);
 int rsg_profile_read(int64_t *launches, double *total_ms);
+/* Per-kernel table of the timed launches ("*" selects every kernel):
+ * lines "name<TAB>launches<TAB>total_ms", largest total first, written to
+ * buf (capacity cap, NUL-terminated); returns the table's length, then
+ * clears the timed launches. */
+int64_t rsg_profile_table(char *buf, int64_t cap);
 
 #ifdef __cplusplus
 }

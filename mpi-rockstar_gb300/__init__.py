@@ -58,6 +58,9 @@ def lib():
         h.rsg_launch_count.restype = i64
         h.rsg_profile_select.argtypes = [C.c_char_p]
         h.rsg_profile_read.argtypes = [vp, vp]
+        h.rsg_last_stats.argtypes = [vp, C.c_int32]
+        h.rsg_profile_table.restype = i64
+        h.rsg_profile_table.argtypes = [C.c_char_p, i64]
         h.rsg_find_subs.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, i64, vp]
         for name, args in _EXTRA_SIGS.items():
             if hasattr(h, name):
@@ -178,6 +181,27 @@ def profile_read():
     t = np.zeros(1, np.float64)
     _check(lib().rsg_profile_read(n.ctypes.data, t.ctypes.data))
     return int(n[0]), float(t[0])
+
+
+STAT_NAMES = ("particles", "groups", "halos", "pot_records", "kept_big", "kept_small",
+              "halos_big", "halos_small", "dense", "later_list")
+
+
+def last_stats():
+    """Work counters of the last call on this thread (rsg_last_stats)."""
+    v = np.zeros(len(STAT_NAMES), np.int64)
+    _check(lib().rsg_last_stats(v.ctypes.data, len(v)))
+    return dict(zip(STAT_NAMES, (int(x) for x in v)))
+
+
+def profile_table():
+    """Per-kernel "name\tlaunches\ttotal_ms" lines of the launches timed since
+    profile_select (largest first); clears them."""
+    buf = C.create_string_buffer(1 << 20)
+    need = lib().rsg_profile_table(buf, 1 << 20)
+    if need < 0:
+        _check(int(need))
+    return buf.value.decode()
 
 
 class DevicePath:

@@ -188,6 +188,7 @@ static int find_subs_host(struct rsg_particle *p, int64_t num_p, const int64_t *
         }
         RSG_CUDA(cudaStreamSynchronize(C.st));
         *num_halos = o.nhalos;
+        last_stats()[RSG_STAT_HALOS] = o.nhalos;
         return RSG_OK;
     } catch (Failure &) {
         return error_code();
@@ -243,6 +244,7 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
         *num_p_out = o.num_p;
         *num_fofs = o.nfofs;
         *num_halos = s2.nhalos;
+        last_stats()[RSG_STAT_HALOS] = s2.nhalos;
         return RSG_OK;
     } catch (Failure &) {
         return error_code();

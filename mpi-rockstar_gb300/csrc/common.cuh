@@ -89,6 +89,10 @@ inline int nblk(int64_t n, int t) { return (int)((n + t - 1) / t); }
 void phase_mark(cudaStream_t st, const char *name);
 void phase_report();
 
+// Counters of the last call on the calling thread (rsg_last_stats); the
+// indices are the RSG_STAT_* constants of the public header.
+int64_t *last_stats();
+
 #define RSG_STACK 96
 #define RSG_STACK6 128
 

@@ -2,6 +2,7 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -11,6 +12,9 @@
 namespace rsg {
 
 static thread_local Error g_err = {0, ""};
+static thread_local int64_t g_stats[RSG_STAT_COUNT];
+
+int64_t *last_stats() { return g_stats; }
 
 void set_error(int code, const char *fmt, ...) {
     g_err.code = code;
@@ -98,7 +102,12 @@ void phase_report() {
 static LaunchStats g_ls;
 static std::string g_prof_name;
 static std::unordered_map<const void *, bool> g_prof_cache;
-static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_ev, g_prof_pool;
+struct ProfRec {
+    cudaEvent_t a, b;
+    const void *func;
+};
+static std::vector<ProfRec> g_prof_ev;
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_pool;
 static size_t g_prof_used = 0;
 
 LaunchStats &launch_stats() { return g_ls; }
@@ -108,21 +117,24 @@ bool prof_match(const void *func) {
     if (it != g_prof_cache.end()) return it->second;
     const char *nm = nullptr;
     bool m = false;
-    if (cudaFuncGetName(&nm, func) == cudaSuccess && nm) m = strstr(nm, g_prof_name.c_str()) != nullptr;
+    if (g_prof_name == "*") m = true;  // every kernel
+    else if (cudaFuncGetName(&nm, func) == cudaSuccess && nm)
+        m = strstr(nm, g_prof_name.c_str()) != nullptr;
     g_prof_cache[func] = m;
     return m;
 }
-void prof_begin(cudaStream_t st) {
+void prof_begin(cudaStream_t st, const void *func) {
     if (g_prof_used == g_prof_pool.size()) {
         cudaEvent_t a, b;
         cudaEventCreate(&a);
         cudaEventCreate(&b);
         g_prof_pool.push_back({a, b});
     }
-    g_prof_ev.push_back(g_prof_pool[g_prof_used++]);
-    cudaEventRecord(g_prof_ev.back().first, st);
+    auto &e = g_prof_pool[g_prof_used++];
+    g_prof_ev.push_back({e.first, e.second, func});
+    cudaEventRecord(g_prof_ev.back().a, st);
 }
-void prof_end(cudaStream_t st) { cudaEventRecord(g_prof_ev.back().second, st); }
+void prof_end(cudaStream_t st) { cudaEventRecord(g_prof_ev.back().b, st); }
 
 }  // namespace rsg
 
@@ -143,8 +155,8 @@ int rsg_profile_read(int64_t *launches, double *total_ms) {
     double t = 0;
     for (auto &e : rsg::g_prof_ev) {
         float ms = 0;
-        if (cudaEventSynchronize(e.second) != cudaSuccess) return RSG_ERR_CUDA;
-        cudaEventElapsedTime(&ms, e.first, e.second);
+        if (cudaEventSynchronize(e.b) != cudaSuccess) return RSG_ERR_CUDA;
+        cudaEventElapsedTime(&ms, e.a, e.b);
         t += ms;
     }
     *launches = (int64_t)rsg::g_prof_ev.size();
@@ -152,6 +164,44 @@ int rsg_profile_read(int64_t *launches, double *total_ms) {
     rsg::g_prof_ev.clear();
     rsg::g_prof_used = 0;
     return 0;
+}
+
+int64_t rsg_profile_table(char *buf, int64_t cap) {
+    std::unordered_map<std::string, std::pair<int64_t, double>> agg;
+    for (auto &e : rsg::g_prof_ev) {
+        float ms = 0;
+        if (cudaEventSynchronize(e.b) != cudaSuccess) return RSG_ERR_CUDA;
+        cudaEventElapsedTime(&ms, e.a, e.b);
+        const char *nm = nullptr;
+        std::string name = (cudaFuncGetName(&nm, e.func) == cudaSuccess && nm) ? nm : "?";
+        auto &r = agg[name];
+        r.first++;
+        r.second += ms;
+    }
+    std::vector<std::pair<double, std::string>> rows;
+    for (auto &kv : agg) {
+        char line[1024];
+        snprintf(line, sizeof(line), "%s\t%lld\t%.6f\n", kv.first.c_str(),
+                 (long long)kv.second.first, kv.second.second);
+        rows.push_back({kv.second.second, line});
+    }
+    std::sort(rows.begin(), rows.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
+    std::string out;
+    for (auto &r : rows) out += r.second;
+    rsg::g_prof_ev.clear();
+    rsg::g_prof_used = 0;
+    if (buf && cap > 0) {
+        size_t n = out.size() < (size_t)cap - 1 ? out.size() : (size_t)cap - 1;
+        memcpy(buf, out.data(), n);
+        buf[n] = 0;
+    }
+    return (int64_t)out.size();
+}
+
+int rsg_last_stats(int64_t *vals, int32_t n) {
+    if (!vals || n < 0) return RSG_ERR_ARGS;
+    for (int32_t i = 0; i < n && i < RSG_STAT_COUNT; i++) vals[i] = rsg::g_stats[i];
+    return RSG_OK;
 }
 
 int rsg_version(void) { return 1; }

@@ -486,6 +486,8 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     launch(k_state8, nblk(n, T), T, 0, st, state32, n, state);
     phase_mark(st, "fof.seeds");
     if (getenv("RSG_TIMING")) fprintf(stderr, "  [fof] dense %d, later-list %d, frontier steps %d\n", nd, ne, rounds);
+    last_stats()[RSG_STAT_DENSE] = nd;
+    last_stats()[RSG_STAT_LATER_LIST] = ne;
     uint8_t *skipped = ar.get<uint8_t>(n);
     RSG_CUDA(cudaMemsetAsync(skipped, 0, n, st));
     launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, state, skipped, err);
@@ -524,6 +526,8 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
         throw Failure();
     }
     res.nfofs = hnh;
+    last_stats()[RSG_STAT_PARTICLES] = n;
+    last_stats()[RSG_STAT_GROUPS] = hnh;
     phase_mark(st, "fof.output");
     return res;
 }

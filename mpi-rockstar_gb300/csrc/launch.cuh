@@ -16,7 +16,7 @@ struct LaunchStats {
 };
 LaunchStats &launch_stats();
 bool prof_match(const void *func);
-void prof_begin(cudaStream_t st);
+void prof_begin(cudaStream_t st, const void *func);
 void prof_end(cudaStream_t st);
 
 template <class... KA, class... A>
@@ -24,7 +24,7 @@ inline void launch(void (*k)(KA...), dim3 g, dim3 b, size_t sm, cudaStream_t st,
     if (g.x == 0 || g.y == 0 || g.z == 0) return;
     LaunchStats &S = launch_stats();
     bool prof = S.selecting && prof_match((const void *)k);
-    if (prof) prof_begin(st);
+    if (prof) prof_begin(st, (const void *)k);
     k<<<g, b, sm, st>>>(std::forward<A>(a)...);
     S.launches++;
     if (prof) prof_end(st);

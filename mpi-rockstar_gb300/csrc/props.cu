@@ -1381,12 +1381,17 @@ __global__ void __launch_bounds__(RSG_SB) k_halo_scans_blk(rsg_halo *H, const rs
 
 // halos split by size: small ones one thread each, large ones one block each
 __global__ void k_scan_split(const rsg_halo *H, int32_t NH, const int32_t *kept, int32_t big,
-                             int32_t *fsmall, int32_t *fbig) {
+                             int32_t *fsmall, int32_t *fbig, unsigned long long *work) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= NH) return;
     bool act = H[h].num_p >= 1;
     fbig[h] = act && kept[h] > big;
     fsmall[h] = act && kept[h] <= big;
+    if (act) {
+        int b = kept[h] > big ? 0 : 1;
+        atomicAdd(&work[b], (unsigned long long)kept[h]);
+        atomicAdd(&work[2 + b], 1ull);
+    }
 }
 __global__ void k_halo_scans_list(rsg_halo *H, const rsg_extra_halo_info *E, const int32_t *list,
                                   int32_t n, PotRec *PO, const int32_t *toff, const int32_t *kept,
@@ -1492,6 +1497,8 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     size_t mark = ar.used;
     int *err = ar.get<int>(2);
     RSG_CUDA(cudaMemsetAsync(err, 0, 8, st));
+    unsigned long long *work = ar.get<unsigned long long>(4);
+    RSG_CUDA(cudaMemsetAsync(work, 0, 32, st));
     int32_t *tot = ar.get<int32_t>(NH + 1), *nseg = ar.get<int32_t>(NH + 1);
     int32_t *toff = ar.get<int32_t>(NH + 1), *soff = ar.get<int32_t>(NH + 1);
     launch(k_set_count, nblk(NH + 1, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio, tot,
@@ -1538,7 +1545,7 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     {
         int32_t *fs = ar.get<int32_t>(NH), *fbg = ar.get<int32_t>(NH);
         int32_t *ls = ar.get<int32_t>(NH), *lb = ar.get<int32_t>(NH);
-        launch(k_scan_split, nblk(NH, T), T, 0, st, H, NH, kept, 1024, fs, fbg);
+        launch(k_scan_split, nblk(NH, T), T, 0, st, H, NH, kept, 1024, fs, fbg, work);
         int32_t nsm = select_idx(ar, fs, ls, NH, st);
         int32_t nbg = select_idx(ar, fbg, lb, NH, st);
         launch(k_halo_scans_blk, nbg, RSG_SB, 0, st, H, E, lb, PO2, toff, kept, d_dc, exact);
@@ -1547,8 +1554,16 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     RSG_CHECK_LAUNCH();
     phase_mark(st, "p.scans");
     int herr[2];
+    unsigned long long hwork[4];
     RSG_CUDA(cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaMemcpyAsync(hwork, work, 32, cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
+    int64_t *S = last_stats();
+    S[RSG_STAT_POT_RECORDS] = npo;
+    S[RSG_STAT_KEPT_BIG] = (int64_t)hwork[0];
+    S[RSG_STAT_KEPT_SMALL] = (int64_t)hwork[1];
+    S[RSG_STAT_HALOS_BIG] = (int64_t)hwork[2];
+    S[RSG_STAT_HALOS_SMALL] = (int64_t)hwork[3];
     if (herr[0]) {
         set_error(RSG_ERR_LIMIT, "halo walk or potential tree traversal exceeded its bound");
         throw Failure();
