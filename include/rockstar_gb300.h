@@ -32,6 +32,7 @@ extern "C" {
 #define RSG_ERR_NO_DEVICE (-3)  /* no usable GPU */
 #define RSG_ERR_LIMIT (-4)      /* a bounded device loop hit its limit */
 #define RSG_ERR_INPUT (-5)      /* non-finite particle data */
+#define RSG_ERR_BUSY (-6)       /* a call that shares fixed scratch is in progress */
 
 struct rsg_particle { int64_t id; float pos[6]; };
 struct rsg_fof { int64_t num_p; struct rsg_particle *particles; };
@@ -150,6 +151,32 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
                     struct rsg_particle *d_out, int64_t *num_p_out, int64_t *num_fofs,
                     struct rsg_halo *d_halos, struct rsg_extra_halo_info *d_extra,
                     int64_t max_halos, int64_t *num_halos, int32_t batched);
+
+/* Allocation-free 3D FOF of one chunk: rsg_rockstar_fof on device buffers,
+ * with no counterpart in the reference (whose fof.c grows its buffers with
+ * realloc).  It allocates nothing: every scratch buffer is carved from one
+ * fixed device array of RSG_NOALLOC_SCRATCH_BYTES per device, reserved when
+ * the library's module for it loads at the first call on a device (make
+ * that call before any stream capture).  For callers that cannot let a
+ * library allocate or free device memory while their own kernels run.
+ *   d_in  : num_p particles on the device (num_p <= RSG_NOALLOC_MAX_PARTICLES,
+ *           else RSG_ERR_LIMIT); not modified.
+ *   d_out : device, capacity num_p, must not overlap d_in; receives the
+ *           permuted, deduplicated particles (*num_p_out of them).
+ *   d_fof_offsets / d_fof_sizes : device, capacity max_fofs; groups as
+ *           rsg_rockstar_fof returns them (same groups, same order).
+ *   stream: a cudaStream_t (NULL = the legacy default stream); the call
+ *           returns after the stream has drained.
+ * Very dense chunks can need more scratch than the array holds (the FOF's
+ * neighbour lists grow with density): the call then fails with
+ * RSG_ERR_LIMIT.  Calls on one device must not overlap in time; a call made
+ * while another is in progress on the same device returns RSG_ERR_BUSY. */
+#define RSG_NOALLOC_MAX_PARTICLES 65536
+#define RSG_NOALLOC_SCRATCH_BYTES (64u << 20)
+int rsg_rockstar_fof_noalloc(const struct rsg_particle *d_in, int64_t num_p,
+                             const struct rsg_config *cfg, struct rsg_particle *d_out,
+                             int64_t *num_p_out, int64_t *d_fof_offsets, int64_t *d_fof_sizes,
+                             int64_t max_fofs, int64_t *num_fofs, void *stream);
 
 /* Work counters of the last rsg_path_device / rsg_find_subs* /
  * rsg_rockstar_fof call on the calling thread (vals[0..n), n <=

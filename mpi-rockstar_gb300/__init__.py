@@ -62,6 +62,7 @@ def lib():
         h.rsg_profile_table.restype = i64
         h.rsg_profile_table.argtypes = [C.c_char_p, i64]
         h.rsg_find_subs.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, i64, vp]
+        h.rsg_rockstar_fof_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, vp, i64, vp, vp]
         for name, args in _EXTRA_SIGS.items():
             if hasattr(h, name):
                 getattr(h, name).argtypes = args
@@ -202,6 +203,21 @@ def profile_table():
     if need < 0:
         _check(int(need))
     return buf.value.decode()
+
+
+NOALLOC_MAX_PARTICLES = 65536
+NOALLOC_SCRATCH_BYTES = 64 << 20
+
+
+def rockstar_fof_noalloc(d_in, n, cfg_struct, d_out, d_off, d_sz, max_fofs, stream=0):
+    """rsg_rockstar_fof_noalloc on caller-owned device buffers (raw device
+    pointers; cfg_struct from setup_config).  Returns (num_p, num_fofs)."""
+    np_out = np.zeros(1, np.int64)
+    nf = np.zeros(1, np.int64)
+    _check(lib().rsg_rockstar_fof_noalloc(d_in, n, C.byref(cfg_struct), d_out,
+                                          np_out.ctypes.data, d_off, d_sz, max_fofs,
+                                          nf.ctypes.data, stream))
+    return int(np_out[0]), int(nf[0])
 
 
 class DevicePath:
