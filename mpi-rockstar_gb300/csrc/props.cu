@@ -752,6 +752,10 @@ __global__ void k_halo_scans(rsg_halo *H, const rsg_extra_halo_info *E, int32_t 
     more_props(hh, q, tot, 1, C);
 }
 
+}  // namespace rsg
+#include "props_seg.cuh"
+namespace rsg {
+
 // ---- block-cooperative scans for large halos ------------------------------
 // Same arithmetic as corevel/kinetic/more_props/shape above.  The block
 // computes every per-particle operand in parallel (ellipsoidal radius,
@@ -1489,6 +1493,82 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     phase_mark(st, "p.bh_walk");
 }
 
+// Batched property scans of every halo (kernels in props_seg.cuh).
+static void seg_count(const Chunk *CH, int32_t nc, int32_t NH, const int32_t *c0,
+                      const int32_t *nch, const uint8_t *flag, CP *cp, int32_t *cnt,
+                      cudaStream_t st) {
+    launch(k_sg_cnt_chunk, nc, RSG_CT, 0, st, CH, flag, cp);
+    launch(k_sg_cnt_off, nblk(NH, 128), 128, 0, st, NH, c0, nch, cp);
+    launch(k_sg_cnt_scan, nc, RSG_CT, 0, st, CH, flag, (const CP *)cp, cnt);
+}
+
+static void seg_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, PotRec *PO, int32_t npo,
+                      rsg_halo *H, const rsg_extra_halo_info *E, int32_t NH,
+                      const int32_t *toff, const int32_t *kept, cudaStream_t st) {
+    const int HT = 128;
+    const int HB = nblk(NH, HT);
+    size_t mark = ar.used;
+    int32_t *nch = ar.get<int32_t>(NH + 1), *c0 = ar.get<int32_t>(NH + 1);
+    launch(k_sg_nch, nblk(NH + 1, HT), HT, 0, st, H, NH, kept, nch);
+    int32_t nc = scan_i32(ar, nch, c0, NH + 1, st);
+    HS *S = ar.get<HS>(NH);
+    Chunk *CH = ar.get<Chunk>(nc + 1);
+    CP *cp = ar.get<CP>(nc + 1);
+    uint8_t *flag = ar.get<uint8_t>(npo + 1), *flag2 = ar.get<uint8_t>(npo + 1);
+    int32_t *cnt = ar.get<int32_t>(npo + 1), *cnt2 = ar.get<int32_t>(npo + 1);
+    double *g = ar.get<double>(npo + 1);
+    float *vel = ar.get<float>(3 * (size_t)npo + 3);
+    launch(k_sg_fill, HB, HT, 0, st, NH, toff, kept, c0, nch, CH);
+    // calculate_corevel, then the kinetic energies
+    launch(k_cv_rmax, nc, RSG_CT, 0, st, CH, PO, d_dc, cp);
+    launch(k_cv_fin1, HB, HT, 0, st, NH, H, c0, nch, cp, S);
+    launch(k_cv_cmax, nc, RSG_CT, 0, st, CH, PO, toff, S, cp);
+    launch(k_cv_fin2, HB, HT, 0, st, NH, H, c0, nch, cp, PO, toff, S);
+    launch(k_cv_sums, nc, RSG_CT, 0, st, CH, PO, S, cp);
+    launch(k_cv_off, HB, HT, 0, st, NH, H, c0, nch, S, cp);
+    launch(k_cv_scan, nc, RSG_CT, 0, st, CH, PO, S, cp, g, vel);
+    launch(k_cv_fin3, HB, HT, 0, st, NH, H, c0, nch, cp, S, toff, g, vel);
+    launch(k_sg_kinetic, nc, RSG_CT, 0, st, CH, PO, H, E, d_dc);
+    phase_mark(st, "p.corevel");
+    // _calc_additional_halo_props for bound = 0 and 1; only the pass whose
+    // fields are kept ((!bound) == (!BOUND_PROPS)) runs beyond the masses
+    for (int bound = 0; bound < 2; bound++) {
+        bool want = ((!bound) == (!dc.bound_props));
+        launch(k_sg_flag, nc, RSG_CT, 0, st, CH, PO, S, bound, 0, flag);
+        seg_count(CH, nc, NH, c0, nch, flag, cp, cnt, st);
+        launch(k_sg_p1, nc, RSG_CT, 0, st, CH, PO, flag, cnt, d_dc, cp);
+        launch(k_sg_p1_fin, HB, HT, 0, st, NH, H, c0, nch, cp, d_dc, bound, S);
+        if (!want) continue;
+        launch(k_sg_vmax, nc, RSG_CT, 0, st, CH, PO, flag, cnt, S, d_dc, cp);
+        launch(k_sg_vmax_fin, HB, HT, 0, st, NH, H, c0, nch, cp, PO, toff, d_dc, S);
+        launch(k_sg_p2, nc, RSG_CT, 0, st, CH, PO, H, flag, cnt, S, cp);
+        launch(k_sg_p2_fin, HB, HT, 0, st, NH, H, c0, nch, cp, S);
+        launch(k_sg_v2, nc, RSG_CT, 0, st, CH, PO, flag, S, cp);
+        launch(k_sg_v2_fin, HB, HT, 0, st, NH, H, c0, nch, cp, PO, toff, d_dc, S);
+        phase_mark(st, "p.passes");
+        for (int which = 0; which < 2; which++) {
+            launch(k_sh_init, HB, HT, 0, st, NH, H, cnt, toff, d_dc, which, S);
+            for (int64_t i = 0; i < dc.shape_iterations; i++) {
+                launch(k_sh_sum, nc, RSG_CT, 0, st, CH, PO, H, flag, S, d_dc, cp);
+                launch(k_sh_fin, HB, HT, 0, st, NH, H, c0, nch, cp, S);
+            }
+        }
+        phase_mark(st, "p.shape");
+        launch(k_sg_flag, nc, RSG_CT, 0, st, CH, PO, S, bound, 1, flag2);
+        seg_count(CH, nc, NH, c0, nch, flag2, cp, cnt2, st);
+        launch(k_sg_energy, nc, RSG_CT, 0, st, CH, PO, flag2, cnt2, d_dc, cp);
+        launch(k_sg_energy_fin, HB, HT, 0, st, NH, H, c0, nch, cp, S);
+        launch(k_nfw_init, HB, HT, 0, st, NH, H, cnt, toff, d_dc, S);
+        launch(k_nfw_bins, nc, RSG_CT, 0, st, CH, PO, flag, cnt, S);
+        launch(k_nfw_fit, HB, HT, 0, st, NH, H, d_dc, S);
+        launch(k_sg_pseudo, nc, RSG_CT, 0, st, CH, PO, H, flag, cnt, cp);
+        launch(k_sg_final, HB, HT, 0, st, NH, H, c0, nch, cp, d_dc, S);
+        phase_mark(st, "p.final");
+    }
+    RSG_CHECK_LAUNCH();
+    ar.used = mark;
+}
+
 void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec *W,
                       int64_t M, rsg_halo *H, rsg_extra_halo_info *E, int32_t NH,
                       cudaStream_t st, int exact) {
@@ -1546,10 +1626,15 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
         int32_t *fs = ar.get<int32_t>(NH), *fbg = ar.get<int32_t>(NH);
         int32_t *ls = ar.get<int32_t>(NH), *lb = ar.get<int32_t>(NH);
         launch(k_scan_split, nblk(NH, T), T, 0, st, H, NH, kept, 1024, fs, fbg, work);
-        int32_t nsm = select_idx(ar, fs, ls, NH, st);
-        int32_t nbg = select_idx(ar, fbg, lb, NH, st);
-        launch(k_halo_scans_blk, nbg, RSG_SB, 0, st, H, E, lb, PO2, toff, kept, d_dc, exact);
-        launch(k_halo_scans_list, nblk(nsm, 32), 32, 0, st, H, E, ls, nsm, PO2, toff, kept, d_dc);
+        if (exact) {
+            int32_t nsm = select_idx(ar, fs, ls, NH, st);
+            int32_t nbg = select_idx(ar, fbg, lb, NH, st);
+            launch(k_halo_scans_blk, nbg, RSG_SB, 0, st, H, E, lb, PO2, toff, kept, d_dc, exact);
+            launch(k_halo_scans_list, nblk(nsm, 32), 32, 0, st, H, E, ls, nsm, PO2, toff, kept,
+                   d_dc);
+        } else {
+            seg_props(ar, dc, d_dc, PO2, npo, H, E, NH, toff, kept, st);
+        }
     }
     RSG_CHECK_LAUNCH();
     phase_mark(st, "p.scans");
