@@ -152,6 +152,17 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
                     struct rsg_halo *d_halos, struct rsg_extra_halo_info *d_extra,
                     int64_t max_halos, int64_t *num_halos, int32_t batched);
 
+/* Barnes-Hut potentials of one particle set: replaces compute_potential(po,
+ * num_po) (src/potential.h:23, src/potential.c:183-192) with PARTICLE_MASS
+ * and FORCE_RES taken from cfg.  As in the reference, po is permuted in
+ * place into the potential tree's order and every po[i].pe is overwritten.
+ *   form 0: the reference's arithmetic (FP64 distances and sums),
+ *           bit-identical potentials;
+ *   form 1: the batched precision form (FP32 distances and 1/r, FP32
+ *           Kahan-compensated sums; the same tree and opening decisions). */
+int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct rsg_config *cfg,
+                          int32_t form);
+
 /* Allocation-free 3D FOF of one chunk: rsg_rockstar_fof on device buffers,
  * with no counterpart in the reference (whose fof.c grows its buffers with
  * realloc).  It allocates nothing: every scratch buffer is carved from one

@@ -59,6 +59,7 @@ def lib():
         h.rsg_profile_select.argtypes = [C.c_char_p]
         h.rsg_profile_read.argtypes = [vp, vp]
         h.rsg_last_stats.argtypes = [vp, C.c_int32]
+        h.rsg_compute_potential.argtypes = [vp, i64, vp, C.c_int32]
         h.rsg_profile_table.restype = i64
         h.rsg_profile_table.argtypes = [C.c_char_p, i64]
         h.rsg_find_subs.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, i64, vp]
@@ -118,6 +119,15 @@ def find_subs(parts, offsets, sizes, cfg, batched=False):
               C.byref(st), h.ctypes.data, e.ctypes.data, cap, nh.ctypes.data))
     k = int(nh[0])
     return pa, h[:k].copy(), e[:k].copy()
+
+
+def compute_potential(po, cfg, form=0):
+    """Barnes-Hut potentials of one set of POTENTIAL records (permuted into
+    tree order, pe filled): form 0 reference arithmetic, 1 FP32 form."""
+    st = setup_config(cfg)
+    q = np.array(po, dtype=POTENTIAL, copy=True)
+    _check(lib().rsg_compute_potential(q.ctypes.data, len(q), C.byref(st), form))
+    return q
 
 
 def debug_hierarchy():

@@ -20,6 +20,15 @@ struct FofOut {
 FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n, const rsg_config &cfg,
                     rsg_particle *d_out, int64_t *d_off, int64_t *d_sz, cudaStream_t st);
 
+__global__ void k_zero_pe(PotRec *PO, int64_t n) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) PO[i].pe = 0;
+}
+
+void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const int32_t *rn,
+                  int32_t ntrees, double mp, double force_res, int *err, cudaStream_t st,
+                  int exact);
+
 // One device context per host thread: a stream and a scratch arena that is
 // reused across calls (the role the reference's threadprivate scratch
 // buffers play, src/groupies.c:52-57).
@@ -245,6 +254,47 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
         *num_fofs = o.nfofs;
         *num_halos = s2.nhalos;
         last_stats()[RSG_STAT_HALOS] = s2.nhalos;
+        return RSG_OK;
+    } catch (Failure &) {
+        return error_code();
+    }
+}
+
+int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct rsg_config *cfg,
+                          int32_t form) {
+    if (!cfg || num_po < 0 || (num_po > 0 && !po) || (form != 0 && form != 1)) {
+        set_error(RSG_ERR_ARGS, "rsg_compute_potential: bad arguments");
+        return RSG_ERR_ARGS;
+    }
+    if (num_po >= (1ll << 31) - 2) {
+        set_error(RSG_ERR_ARGS, "rsg_compute_potential: at most 2^31-2 records");
+        return RSG_ERR_ARGS;
+    }
+    try {
+        Ctx &C = ctx();
+        if (num_po == 0) return RSG_OK;
+        C.ar.reserve((size_t)num_po * 400 + (64u << 20));
+        C.ar.reset();
+        static_assert(sizeof(PotRec) == sizeof(rsg_potential), "potential record layout");
+        PotRec *d = C.ar.get<PotRec>(num_po);
+        int32_t *seg = C.ar.get<int32_t>(2);
+        int *err = C.ar.get<int>(2);
+        int32_t hseg[2] = {0, (int32_t)num_po};
+        RSG_CUDA(cudaMemcpyAsync(d, po, sizeof(PotRec) * num_po, cudaMemcpyHostToDevice, C.st));
+        RSG_CUDA(cudaMemcpyAsync(seg, hseg, sizeof(hseg), cudaMemcpyHostToDevice, C.st));
+        RSG_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), C.st));
+        launch(k_zero_pe, nblk(num_po, 256), 256, 0, C.st, d, num_po);
+        bh_potential(C.ar, d, num_po, seg, seg + 1, 1, cfg->particle_mass, cfg->force_res, err,
+                     C.st, form == 0 ? 1 : 0);
+        int herr[2];
+        RSG_CUDA(cudaMemcpyAsync(po, d, sizeof(PotRec) * num_po, cudaMemcpyDeviceToHost, C.st));
+        RSG_CUDA(cudaMemcpyAsync(herr, err, sizeof(herr), cudaMemcpyDeviceToHost, C.st));
+        RSG_CUDA(cudaStreamSynchronize(C.st));
+        if (herr[0]) {
+            set_error(RSG_ERR_LIMIT, "potential tree traversal exceeded its stack");
+            return RSG_ERR_LIMIT;
+        }
+        last_stats()[RSG_STAT_POT_RECORDS] = num_po;
         return RSG_OK;
     } catch (Failure &) {
         return error_code();

@@ -259,62 +259,138 @@ __global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, 
     }
 }
 
-// _compute_monopole_potentials(leaf, root) (src/potential.c:133-168)
-__global__ void k_bh_walk(const KNode<3> *nodes, const int32_t *leaves, int32_t nl,
-                          const BHNode *B, PotRec *PO, double mp, double force_res, int *err) {
+// _compute_monopole_potentials(leaf, root) (src/potential.c:133-168): one
+// thread per leaf walks the tree from the root, in groups of RSG_BH_G of the
+// leaf's particles whose sums stay in registers.  A particle's potential
+// receives the same terms in the same order as in the reference (the self
+// leaf's pairs in ascending partner order, opened leaves in point order,
+// monopoles as visited), so the FP64 form is bit-identical to it.
+//   F32 = false: r = max(sqrt(r2), FORCE_RES) and m / r in FP64, as the
+//                reference computes them;
+//   F32 = true:  the batched precision form: squared distance and 1/r in
+//                FP32 (rsqrtf), each particle's sum Kahan-compensated in
+//                FP32.  The opening test stays in FP64 so that the same
+//                nodes are opened.
+#define RSG_BH_G 16
+template <bool F32>
+__global__ void __launch_bounds__(64) k_bh_walk(const KNode<3> *nodes, const int32_t *leaves,
+                                                int32_t nl, const BHNode *B, PotRec *PO,
+                                                double mp, double force_res, int *err) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl) return;
     int a = leaves[t];
     const KNode<3> &n = nodes[a];
     const BHNode bn = B[a];
-    int stack[RSG_STACK];
-    int sp = 0;
-    stack[sp++] = n.tree;
-    while (sp) {
-        int b = stack[--sp];
-        const KNode<3> &n2 = nodes[b];
-        if (b == a) {
-            if (n.n > 20) continue;  // degenerate leaf
-            for (int i = 0; i < n.n; i++)
-                for (int j = i + 1; j < n.n; j++) {
-                    double r = sqrt(d2d(PO[n.start + i].pos, PO[n.start + j].pos));
-                    if (r < force_res) r = force_res;
-                    double dpo = mp * (1.0 / r);
-                    PO[n.start + i].pe += dpo;
-                    PO[n.start + j].pe += dpo;
-                }
-            continue;
-        }
-        int i;
-        for (i = 0; i < 3; i++)
-            if (n.mn[i] < n2.mn[i] || n.mx[i] > n2.mx[i]) break;
-        bool open = (i == 3);
-        if (!open) {
-            float r2 = (float)d2d(bn.mc, B[b].mc);
-            open = !(r2 > fmul(B[b].dmin, B[b].dmin));
-        }
-        if (open) {
-            if (n2.div < 0) {
-                for (int p = 0; p < n.n; p++)
-                    for (int q = 0; q < n2.n; q++) {
-                        double r = sqrt(d2d(PO[n.start + p].pos, PO[n2.start + q].pos));
-                        if (r < force_res) r = force_res;
-                        PO[n.start + p].pe += mp * (1.0 / r);
-                    }
+    const float mpf = (float)mp, fr2f = (float)(force_res * force_res);
+    for (int p0 = 0; p0 < n.n; p0 += RSG_BH_G) {
+        int np_ = min(RSG_BH_G, n.n - p0);
+        float px[RSG_BH_G][3];
+        double acc[RSG_BH_G];
+        float s[RSG_BH_G], c[RSG_BH_G];
+#pragma unroll
+        for (int p = 0; p < RSG_BH_G; p++) {
+            acc[p] = 0;
+            s[p] = c[p] = 0.f;
+            if (p < np_) {
+                const PotRec &r = PO[n.start + p0 + p];
+                px[p][0] = r.pos[0];
+                px[p][1] = r.pos[1];
+                px[p][2] = r.pos[2];
+                acc[p] = r.pe;
             } else {
-                if (sp + 2 > RSG_STACK) {
-                    atomicExch(err, 1);
-                    return;
-                }
-                stack[sp++] = n2.left + 1;
-                stack[sp++] = n2.left;
-            }
-        } else {
-            for (int p = 0; p < n.n; p++) {
-                float r = (float)sqrt(d2d(PO[n.start + p].pos, B[b].mc));
-                PO[n.start + p].pe += (double)__fdiv_rn(B[b].m, r);
+                px[p][0] = px[p][1] = px[p][2] = 0.f;
             }
         }
+        // adds one term to particle p's sum
+#define RSG_BH_ADD(p, term64, term32)                  \
+    do {                                                \
+        if (F32) {                                      \
+            float y_ = (term32) - c[p];                 \
+            float t_ = s[p] + y_;                       \
+            c[p] = (t_ - s[p]) - y_;                    \
+            s[p] = t_;                                  \
+        } else {                                        \
+            acc[p] += (term64);                         \
+        }                                               \
+    } while (0)
+        // direct pair with point q (softened)
+#define RSG_BH_PAIR(p, q)                                                              \
+    do {                                                                               \
+        if (F32) {                                                                     \
+            float dx = px[p][0] - q[0], dy = px[p][1] - q[1], dz = px[p][2] - q[2];    \
+            float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));                  \
+            RSG_BH_ADD(p, 0.0, mpf * rsqrtf(fmaxf(r2, fr2f)));                         \
+        } else {                                                                       \
+            double r = sqrt(d2d(px[p], q));                                            \
+            if (r < force_res) r = force_res;                                          \
+            RSG_BH_ADD(p, mp * (1.0 / r), 0.f);                                        \
+        }                                                                              \
+    } while (0)
+        int stack[RSG_STACK];
+        int sp = 0;
+        stack[sp++] = n.tree;
+        while (sp) {
+            int b = stack[--sp];
+            const KNode<3> &n2 = nodes[b];
+            if (b == a) {
+                if (n.n > 20) continue;  // degenerate leaf
+                for (int qi = 0; qi < n.n; qi++) {
+                    const float *qp = PO[n.start + qi].pos;
+                    float q[3] = {qp[0], qp[1], qp[2]};
+#pragma unroll
+                    for (int p = 0; p < RSG_BH_G; p++)
+                        if (p < np_ && p0 + p != qi) RSG_BH_PAIR(p, q);
+                }
+                continue;
+            }
+            int i;
+            for (i = 0; i < 3; i++)
+                if (n.mn[i] < n2.mn[i] || n.mx[i] > n2.mx[i]) break;
+            bool open = (i == 3);
+            if (!open) {
+                float r2 = (float)d2d(bn.mc, B[b].mc);
+                open = !(r2 > fmul(B[b].dmin, B[b].dmin));
+            }
+            if (open) {
+                if (n2.div < 0) {
+                    for (int qi = 0; qi < n2.n; qi++) {
+                        const float *qp = PO[n2.start + qi].pos;
+                        float q[3] = {qp[0], qp[1], qp[2]};
+#pragma unroll
+                        for (int p = 0; p < RSG_BH_G; p++)
+                            if (p < np_) RSG_BH_PAIR(p, q);
+                    }
+                } else {
+                    if (sp + 2 > RSG_STACK) {
+                        atomicExch(err, 1);
+                        return;
+                    }
+                    stack[sp++] = n2.left + 1;
+                    stack[sp++] = n2.left;
+                }
+            } else {
+                const BHNode &m = B[b];
+#pragma unroll
+                for (int p = 0; p < RSG_BH_G; p++) {
+                    if (p >= np_) continue;
+                    if (F32) {
+                        float dx = px[p][0] - m.mc[0], dy = px[p][1] - m.mc[1],
+                              dz = px[p][2] - m.mc[2];
+                        float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+                        RSG_BH_ADD(p, 0.0, m.m * rsqrtf(r2));
+                    } else {
+                        float r = (float)sqrt(d2d(px[p], m.mc));
+                        RSG_BH_ADD(p, (double)__fdiv_rn(m.m, r), 0.f);
+                    }
+                }
+            }
+        }
+#undef RSG_BH_PAIR
+#undef RSG_BH_ADD
+#pragma unroll
+        for (int p = 0; p < RSG_BH_G; p++)
+            if (p < np_)
+                PO[n.start + p0 + p].pe = F32 ? acc[p] + ((double)s[p] - (double)c[p]) : acc[p];
     }
 }
 
@@ -1488,7 +1564,12 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     int32_t *lf = ar.get<int32_t>(F.nnodes), *leaves = ar.get<int32_t>(F.nnodes);
     launch(k_leaf_list_flags, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, lf);
     int32_t nl = select_idx(ar, lf, leaves, F.nnodes, st);
-    launch(k_bh_walk, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res, err);
+    if (exact)
+        launch(k_bh_walk<false>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
+               err);
+    else
+        launch(k_bh_walk<true>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
+               err);
     RSG_CHECK_LAUNCH();
     phase_mark(st, "p.bh_walk");
 }

@@ -1,0 +1,64 @@
+"""rsg_compute_potential (the reference's compute_potential) against the
+oracle: form 0 must be bit-identical (same tree permutation, same FP64 sums);
+form 1, the FP32 Kahan form, within 1e-5 relative of form 0.  Both are also
+measured against an FP64 direct sum (the Barnes-Hut error itself)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def nfw_like(n, seed, centre=(10.0, 10.0, 10.0), scale=0.3, dup=0):
+    rng = np.random.default_rng(seed)
+    po = np.zeros(n, dtype=[("pos", "<f4", (6,)), ("r2", "<f4"), ("_pad", "<f4"),
+                            ("pe", "<f8"), ("ke", "<f4"), ("flags", "<i4")])
+    r = scale * rng.random(n) ** 2.0
+    v = rng.normal(size=(n, 3))
+    v /= np.linalg.norm(v, axis=1)[:, None]
+    po["pos"][:, :3] = (np.asarray(centre) + r[:, None] * v).astype(np.float32)
+    po["pos"][:, 3:] = rng.normal(scale=200.0, size=(n, 3)).astype(np.float32)
+    if dup:
+        po["pos"][1:dup + 1, :3] = po["pos"][0, :3]
+    return po
+
+
+def direct_fp64(po, mp, fr):
+    x = po["pos"][:, :3].astype(np.float64)
+    pe = np.zeros(len(po))
+    for i in range(0, len(po), 512):
+        d = np.sqrt(((x[i:i + 512, None, :] - x[None, :, :]) ** 2).sum(-1))
+        d = np.maximum(d, fr)
+        inv = mp / d
+        for k in range(d.shape[0]):
+            inv[k, i + k] = 0.0
+        pe[i:i + 512] = inv.sum(1)
+    return pe
+
+
+@pytest.mark.parametrize("n,seed,dup", [(2000, 1, 0), (30000, 2, 0), (5000, 3, 40)])
+def test_potential_form0_equals_oracle(rk, oracle, n, seed, dup):
+    po = nfw_like(n, seed, dup=dup).view(rk.POTENTIAL)
+    cfg = rk.Config(particle_mass=1e9, force_res=0.003)
+    oracle.setup(cfg)
+    ref = oracle.compute_potential(po)
+    got = rk.compute_potential(po, cfg, form=0)
+    assert np.array_equal(got["pos"], ref["pos"])     # same tree permutation
+    assert got["pe"].tobytes() == ref["pe"].tobytes()  # same FP64 sums
+
+
+@pytest.mark.parametrize("n,seed", [(2000, 4), (30000, 5)])
+def test_potential_fp32_form(rk, n, seed):
+    po = nfw_like(n, seed).view(rk.POTENTIAL)
+    cfg = rk.Config(particle_mass=1e9, force_res=0.003)
+    a = rk.compute_potential(po, cfg, form=0)
+    b = rk.compute_potential(po, cfg, form=1)
+    assert np.array_equal(a["pos"], b["pos"])
+    rel = np.abs(b["pe"] - a["pe"]) / np.abs(a["pe"])
+    assert rel.max() <= 1e-5, rel.max()
+    # both against the FP64 direct sum: the Barnes-Hut approximation error
+    if n <= 5000:
+        d = direct_fp64(a, cfg.particle_mass, cfg.force_res)
+        e0 = np.abs(a["pe"] - d) / d
+        e1 = np.abs(b["pe"] - d) / d
+        assert np.median(e0) < 1e-2 and np.median(e1) < 1e-2
+        assert abs(np.median(e1) - np.median(e0)) < 1e-5
