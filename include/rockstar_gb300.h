@@ -159,7 +159,8 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
  *   form 0: the reference's arithmetic (FP64 distances and sums),
  *           bit-identical potentials;
  *   form 1: the batched precision form (FP32 distances and 1/r, FP32
- *           Kahan-compensated sums; the same tree and opening decisions). */
+ *           Kahan-compensated sums; node sizes from parallel sums; the same
+ *           tree and opening rule). */
 int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct rsg_config *cfg,
                           int32_t form);
 

@@ -34,16 +34,19 @@ struct TravStatus {
 // Sphere search (src/fast3tree.c:377-414) on tree `root` of a 3D forest.
 // on_range(start, n) receives nodes that lie entirely inside the sphere
 // (shortcut of :386-392), on_point(j) leaf points with dist < r^2.  Either
-// returns false to stop the walk.
+// returns false to stop the walk.  Callers that only want points after
+// index `after` skip the nodes that hold none (the tests of every other node
+// are unchanged, so the points found after `after` are the same).
 template <class FR, class FP>
 __device__ bool sphere3(const KNode<3> *nodes, int root, const Rec *recs, const float *c,
-                        float r, int *errflag, FR on_range, FP on_point) {
+                        float r, int *errflag, FR on_range, FP on_point, int after = -1) {
     int stack[RSG_STACK];
     int sp = 0;
     stack[sp++] = root;
     const float r2 = fmul(r, r);
     while (sp) {
         const KNode<3> &nd = nodes[stack[--sp]];
+        if (nd.start + nd.n <= after + 1) continue;
         // _fast3tree_box_not_intersect_sphere
         float d = 0.f, e;
         bool out = false;
@@ -215,7 +218,8 @@ __global__ void k_llist(const KNode<3> *nodes, const Rec *recs, int n, float r,
         [&](int j) {
             add(j);
             return true;
-        });
+        },
+        k);
     if (!llist) lcnt[k] = m;
 }
 // One frontier step of the ordered independent set: every particle decided
@@ -267,7 +271,8 @@ __global__ void k_seed_mark(const KNode<3> *nodes, const Rec *recs, int n, float
         [&](int j) {
             if (j > s) skipped[j] = 1;
             return true;
-        });
+        },
+        s);
 }
 
 __global__ void k_link_r(const KNode<3> *nodes, const Rec *recs, int n, float r,

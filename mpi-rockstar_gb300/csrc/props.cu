@@ -197,6 +197,37 @@ __global__ void k_bh_internal(const KNode<3> *nodes, int32_t first, int32_t coun
     B[a] = b;
 }
 
+// Batched form: one warp per internal node of at most RSG_BH_BIG points,
+// the sum of squared distances reduced by shuffles.
+__global__ void k_bh_internal_warp(const KNode<3> *nodes, int32_t first, int32_t count,
+                                   const PotRec *PO, BHNode *B) {
+    int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (k >= count) return;
+    int a = first + k;
+    const KNode<3> &x = nodes[a];
+    if (x.div < 0 || x.n > RSG_BH_BIG) return;
+    const BHNode &L = B[x.left], &R = B[x.left + 1];
+    BHNode b;
+    b.m = fadd(L.m, R.m);
+    for (int j = 0; j < 3; j++)
+        b.mc[j] = b.m ? __fdiv_rn(fadd(fmul(R.mc[j], R.m), fmul(L.mc[j], L.m)), b.m) : 0.f;
+    double sx = 0, bm = 0;
+    for (int i = lane; i < x.n; i += 32) {
+        double dx = d2d(b.mc, PO[x.start + i].pos);
+        if (bm < dx) bm = dx;
+        sx += dx;
+    }
+    for (int o = 16; o; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        bm = fmax(bm, __shfl_xor_sync(0xffffffffu, bm, o));
+    }
+    if (lane == 0) {
+        bm = sqrt(bm) / 2.0;
+        b.dmin = (float)(bm + sqrt(bm * bm + sx / (x.n * 1.0)));
+        B[a] = b;
+    }
+}
+
 // Large internal nodes: the block computes every point's squared distance
 // to the mass centre; the maximum is a reduction and the sum is added by one
 // thread in point order, as _compute_dmin does.
@@ -269,8 +300,7 @@ __global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, 
 //                reference computes them;
 //   F32 = true:  the batched precision form: squared distance and 1/r in
 //                FP32 (rsqrtf), each particle's sum Kahan-compensated in
-//                FP32.  The opening test stays in FP64 so that the same
-//                nodes are opened.
+//                FP32.  The opening test itself stays in FP64.
 #define RSG_BH_G 16
 template <bool F32>
 __global__ void __launch_bounds__(64) k_bh_walk(const KNode<3> *nodes, const int32_t *leaves,
@@ -1556,7 +1586,11 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     for (int l = F.nlv - 2; l >= 0; l--) {
         int32_t a = F.lv_first[l], b = F.lv_first[l + 1];
         if (b > a) {
-            launch(k_bh_internal, nblk(b - a, 64), 64, 0, st, F.nodes, a, b - a, PO, B);
+            if (exact)
+                launch(k_bh_internal, nblk(b - a, 64), 64, 0, st, F.nodes, a, b - a, PO, B);
+            else
+                launch(k_bh_internal_warp, nblk((int64_t)(b - a) * 32, 256), 256, 0, st, F.nodes, a,
+                       b - a, PO, B);
             launch(k_bh_internal_big, b - a, 256, 0, st, F.nodes, a, b - a, PO, B, exact);
         }
     }

@@ -138,6 +138,41 @@ __global__ void k_norm_seq(Rec *W, HierNodes N, int32_t base, int32_t count, int
     norm_sigmas(c, level0, ims, sig + 2 * k);
 }
 
+// Batched form, nodes up to RSG_SMALL particles: one warp per node, sums in
+// lane-strided order reduced by shuffles (deterministic).
+__global__ void k_norm_warp(Rec *W, HierNodes N, int32_t base, int32_t count, int level0,
+                            double ims, double *sig) {
+    int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (k >= count) return;
+    int node = base + k;
+    int s = N.start[node], n = N.n[node];
+    if (n <= 0 || n > RSG_SMALL) return;
+    double mean[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = lane; i < n; i += 32)
+        for (int d = 0; d < 6; d++) mean[d] += (double)W[s + i].pos[d];
+    for (int d = 0; d < 6; d++) {
+        for (int o = 16; o; o >>= 1) mean[d] += __shfl_xor_sync(0xffffffffu, mean[d], o);
+        mean[d] /= (double)n;
+    }
+    double c[21];
+    for (int j = 0; j < 21; j++) c[j] = 0;
+    for (int i = lane; i < n; i += 32) {
+        float q[6];
+        for (int d = 0; d < 6; d++) {
+            q[d] = __double2float_rn((double)W[s + i].pos[d] - mean[d]);
+            W[s + i].pos[d] = q[d];
+        }
+        int j = 0;
+        for (int x = 0; x < 6; x++)
+            for (int y = x; y < 6; y++) c[j++] += (double)fmul(q[x], q[y]);
+    }
+    for (int j = 0; j < 21; j++) {
+        for (int o = 16; o; o >>= 1) c[j] += __shfl_xor_sync(0xffffffffu, c[j], o);
+        c[j] /= (double)n;
+    }
+    if (lane == 0) norm_sigmas(c, level0, ims, sig + 2 * k);
+}
+
 // Mid-size nodes: the block stages particles in shared memory and computes
 // the per-particle products; thread 0 adds them in array order.
 __global__ void __launch_bounds__(256) k_norm_blk(Rec *W, HierNodes N, int32_t base, int level0,
@@ -148,7 +183,7 @@ __global__ void __launch_bounds__(256) k_norm_blk(Rec *W, HierNodes N, int32_t b
     int k = blockIdx.x;
     int node = base + k;
     int s = N.start[node], n = N.n[node];
-    if (n <= RSG_SMALL || n > RSG_SEQ_MAX) return;
+    if (n <= RSG_SMALL || n > seq_max) return;
     // lane d of warp 0 owns the running sum of coordinate d
     double a = 0;
     for (int b0 = 0; b0 < n; b0 += 256) {
@@ -445,47 +480,71 @@ __device__ __forceinline__ void uf_unite2(int *par, int a, int b) {
 }
 
 // _find_subfofs_at_r (src/groupies.c:274-284): every particle links to
-// itself and to the later particles within target_r (6D, strict <).  This
-// kernel lists those later neighbours in ascending order (the order the
-// skip search returns them); count pass when nbr == nullptr.
-__global__ void k_fof6(const KNode<6> *nodes, const Rec *W, int64_t M, HierNodes N,
-                       int32_t base, const int32_t *eln, const int32_t *noff, int32_t *ncnt,
-                       int32_t *nbr, int *err) {
-    int64_t i64 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i64 >= M) return;
-    int i = (int)i64;
-    int k = eln[i];
-    if (k < 0) return;
-    float r = N.target_r[base + k];
-    const float r2 = fmul(r, r);
+// itself and to the later particles within target_r (6D, strict <), which
+// the skip search returns in ascending order.
+// The search runs for 32 consecutive particles at a time: the warp walks
+// each node's tree once with a shared stack, entering a node when any
+// lane's own box test admits it; at a leaf every lane tests
+// every point with its own distance test.  A lane meets exactly the points
+// of its own search, in ascending order.  MODE 0 counts, 1 fills the CSR
+// lists (exact form), 2 unites at once (batched form).
+template <int MODE>
+__global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec *W, int64_t M,
+                                                HierNodes N, int32_t base, const int32_t *eln,
+                                                const int32_t *noff, int32_t *ncnt, int32_t *nbr,
+                                                int *par, int *err) {
+    const unsigned FULL = 0xffffffffu;
+    int64_t w0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * 32;
+    int lane = threadIdx.x & 31;
+    if (w0 >= M) return;
+    int i = (int)(w0 + lane);
+    bool valid = w0 + lane < M;
+    int k = valid ? eln[i] : -1;
     float c[6];
 #pragma unroll
-    for (int d = 0; d < 6; d++) c[d] = W[i].pos[d];
+    for (int d = 0; d < 6; d++) c[d] = (valid && k >= 0) ? W[i].pos[d] : 0.f;
+    int cnt = 0;
+    int o = (MODE == 1 && valid && k >= 0) ? noff[i] : 0;
+    unsigned pending = __ballot_sync(FULL, valid && k >= 0);
     int stack[RSG_STACK6];
-    int sp = 0, cnt = 0;
-    int o = nbr ? noff[i] : 0;
-    stack[sp++] = k;
-    while (sp) {
-        const KNode<6> &x = nodes[stack[--sp]];
-        if (x.start + x.n <= i) continue;
-        if (box_out6(x, c, r)) continue;
-        if (x.div < 0) {
-            int j0 = x.start > i + 1 ? x.start : i + 1;
-            for (int j = j0; j < x.start + x.n; j++)
-                if (dist6(c, W[j].pos) < r2) {
-                    if (nbr) nbr[o + cnt] = j;
-                    cnt++;
+    while (pending) {
+        int leader = __ffs(pending) - 1;
+        int kk = __shfl_sync(FULL, k, leader);
+        bool mine = valid && k == kk;
+        pending &= ~__ballot_sync(FULL, mine);
+        int imin = (int)w0 + leader;  // the segment's first particle
+        float r = N.target_r[base + kk];
+        const float r2 = fmul(r, r);
+        int sp = 0;
+        stack[sp++] = kk;
+        while (sp) {
+            const KNode<6> &x = nodes[stack[--sp]];
+            if (x.start + x.n <= imin + 1) continue;
+            bool need = mine && (x.start + x.n > i + 1) && !box_out6(x, c, r);
+            if (!__ballot_sync(FULL, need)) continue;
+            if (x.div < 0) {
+                int j0 = x.start > imin + 1 ? x.start : imin + 1;
+                for (int j = j0; j < x.start + x.n; j++) {
+                    float q[6];
+#pragma unroll
+                    for (int d = 0; d < 6; d++) q[d] = W[j].pos[d];
+                    if (need && j > i && dist6(c, q) < r2) {
+                        if (MODE == 1) nbr[o + cnt] = j;
+                        if (MODE == 2) uf_unite2(par, i, j);
+                        cnt++;
+                    }
                 }
-            continue;
+                continue;
+            }
+            if (sp + 2 > RSG_STACK6) {
+                if (lane == 0) atomicExch(err, 1);
+                return;
+            }
+            stack[sp++] = x.left + 1;
+            stack[sp++] = x.left;
         }
-        if (sp + 2 > RSG_STACK6) {
-            atomicExch(err, 1);
-            return;
-        }
-        stack[sp++] = x.left + 1;
-        stack[sp++] = x.left;
     }
-    if (!nbr) ncnt[i] = cnt;
+    if (MODE == 0 && valid && k >= 0) ncnt[i] = cnt;
 }
 
 // Union-find labels exactly as link_particle_to_fof / merge_smallfofs build
@@ -595,16 +654,10 @@ __global__ void k_replay6_smem(HierNodes N, int32_t base, const int32_t *noff,
     }
 }
 
-// Batched mode: subgroup labels from a parallel union-find over the same
-// links (components are the same sets; the label is the component's first
+// Batched mode: subgroup labels from the parallel union-find of k_fof6_w<2>
+// (components are the same sets; the label is the component's first
 // position, -1 for particles without links), so the partition order is
 // deterministic but not the reference's.
-__global__ void k_uf6(const int32_t *eln, int64_t M, const int32_t *noff, const int32_t *nbr,
-                      int *par) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M || eln[i] < 0) return;
-    for (int e = noff[i]; e < noff[i + 1]; e++) uf_unite2(par, (int)i, nbr[e]);
-}
 __global__ void k_uf6_size(const int32_t *eln, int64_t M, int *par, int *root, int *size) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= M || eln[i] < 0) return;
@@ -1399,8 +1452,12 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         size_t mark = ar.used;
         {
             double *sig = ar.get<double>(2 * (int64_t)cnt);
-            launch(k_norm_seq, nblk(cnt, 32), 32, 0, st, W, N, base, cnt, L == 0,
-                                                     cfg.initial_metric_scaling, sig);
+            if (exact)
+                launch(k_norm_seq, nblk(cnt, 32), 32, 0, st, W, N, base, cnt, L == 0,
+                       cfg.initial_metric_scaling, sig);
+            else
+                launch(k_norm_warp, nblk((int64_t)cnt * 32, 256), 256, 0, st, W, N, base, cnt,
+                       L == 0, cfg.initial_metric_scaling, sig);
             launch(k_norm_blk, cnt, 256, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig,
                    seq_max);
             launch(k_norm_par, cnt, T, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig,
@@ -1440,16 +1497,18 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         phase_mark(st, "d.nn_target");
         RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
         launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
-        // later neighbours within target_r, as CSR lists
-        int32_t *ncnt = par, *noff = root;
-        RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
-        launch(k_fof6, nblk(M, T), T, 0, st, F.nodes, W, M, N, base, eln, nullptr, ncnt, nullptr, err);
-        int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
-        int32_t *nbr = ar.get<int32_t>(ne + 1);
-        launch(k_fof6, nblk(M, T), T, 0, st, F.nodes, W, M, N, base, eln, noff, ncnt, nbr, err);
-        phase_mark(st, "d.fof6d");
-        // reference labels, then the reference's partition sort by label
         if (exact) {
+            // later neighbours within target_r, as CSR lists
+            int32_t *ncnt = par, *noff = root;
+            RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
+            launch(k_fof6_w<0>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
+                   (const int32_t *)nullptr, ncnt, (int32_t *)nullptr, (int *)nullptr, err);
+            int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
+            int32_t *nbr = ar.get<int32_t>(ne + 1);
+            launch(k_fof6_w<1>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
+                   (const int32_t *)noff, ncnt, nbr, (int *)nullptr, err);
+            phase_mark(st, "d.fof6d");
+            // reference labels, then the reference's partition sort by label
             launch(k_replay6, nblk(cnt, 32), 32, 0, st, N, base, cnt, noff, nbr, phalo, csize);
             static bool attr = false;
             if (!attr) {
@@ -1461,7 +1520,9 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         } else {
             int *ufp = csize, *ufr = key2 ? (int *)key2 : nullptr, *ufs = (int *)val2;
             launch(k_init_par, nblk(M, T), T, 0, st, eln, M, ufp, ufs);
-            launch(k_uf6, nblk(M, T), T, 0, st, eln, M, noff, nbr, ufp);
+            launch(k_fof6_w<2>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
+                   (const int32_t *)nullptr, (int32_t *)nullptr, (int32_t *)nullptr, ufp, err);
+            phase_mark(st, "d.fof6d");
             launch(k_uf6_size, nblk(M, T), T, 0, st, eln, M, ufp, ufr, ufs);
             launch(k_uf6_label, nblk(M, T), T, 0, st, eln, M, ufr, ufs, phalo);
         }
