@@ -20,6 +20,8 @@
 // Sphere searches walk the same kd-tree with the same float tests as
 // src/fast3tree.c:293-414, so S_r is the reference's set, node shortcut
 // included.
+#include <limits.h>
+
 #include <cub/cub.cuh>
 
 #include "kdtree_impl.cuh"
@@ -106,6 +108,98 @@ __device__ bool sphere3(const KNode<3> *nodes, int root, const Rec *recs, const 
     return true;
 }
 
+// The same search for the 32 queries of a warp (one per lane, `active`
+// lanes only) with one shared walk: a stack entry carries the lanes that
+// still need the subtree and each lane applies its own tests, so every lane meets exactly
+// the nodes and points of its own walk, in the same order.  A callback
+// returning false ends that lane's walk; nodes holding no index after the
+// lane's `after` are dropped for that lane (the points it finds after
+// `after` are unchanged).
+template <class FR, class FP>
+__device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float *c, bool active,
+                             float r, int after, int *errflag, FR on_range, FP on_point) {
+    const unsigned FULL = 0xffffffffu;
+    const unsigned bit = 1u << (threadIdx.x & 31);
+    const float r2 = fmul(r, r);
+    int sn[RSG_STACK];
+    unsigned sm[RSG_STACK];
+    unsigned live = __ballot_sync(FULL, active);
+    if (!live) return;
+    int sp = 0;
+    sn[sp] = 0;
+    sm[sp++] = live;
+    while (sp) {
+        --sp;
+        const int xi = sn[sp];
+        const unsigned m = sm[sp] & live;
+        if (!m) continue;
+        const KNode<3> &nd = nodes[xi];
+        int kind = 0;  // 1 out, 2 inside, 3 leaf points, 4 descend
+        if (m & bit) {
+            kind = 1;
+            if (nd.start + nd.n > after + 1) {
+                float d = 0.f, e;
+                bool out = false;
+#pragma unroll
+                for (int i = 0; i < 3; i++) {
+                    if ((e = fsub(c[i], nd.mn[i])) < 0) {
+                        d = fadd(d, fmul(e, e));
+                        if (d >= r2) { out = true; break; }
+                    } else if ((e = fsub(c[i], nd.mx[i])) > 0) {
+                        d = fadd(d, fmul(e, e));
+                        if (d >= r2) { out = true; break; }
+                    }
+                }
+                if (!out) {
+                    bool inside = true;
+                    if (fabsf(fsub(c[0], nd.mn[0])) > r) inside = false;
+                    else {
+                        float dist = 0.f;
+#pragma unroll
+                        for (int i = 0; i < 3; i++) {
+                            float dx = fsub(nd.mn[i], c[i]);
+                            dx = fmul(dx, dx);
+                            float dx2 = fsub(c[i], nd.mx[i]);
+                            dx2 = fmul(dx2, dx2);
+                            if (dx2 > dx) dx = dx2;
+                            dist = fadd(dist, dx);
+                            if (dist > r2) { inside = false; break; }
+                        }
+                    }
+                    kind = inside ? 2 : (nd.div < 0 ? 3 : 4);
+                }
+            }
+        }
+        bool stop = false;
+        if (kind == 2) stop = !on_range(nd.start, nd.n);
+        if (__any_sync(FULL, kind == 3)) {
+            for (int k = 0; k < nd.n; k++) {
+                int j = nd.start + k;
+                float q0 = recs[j].pos[0], q1 = recs[j].pos[1], q2 = recs[j].pos[2];
+                if (kind == 3 && !stop) {
+                    float dist = 0.f, dx;
+                    dx = fsub(c[0], q0); dist = fadd(dist, fmul(dx, dx));
+                    dx = fsub(c[1], q1); dist = fadd(dist, fmul(dx, dx));
+                    dx = fsub(c[2], q2); dist = fadd(dist, fmul(dx, dx));
+                    if (dist < r2) stop = !on_point(j);
+                }
+            }
+        }
+        live &= ~__ballot_sync(FULL, stop);
+        unsigned down = __ballot_sync(FULL, kind == 4) & live;
+        if (down) {
+            if (sp + 2 > RSG_STACK) {
+                if (bit == 1u) atomicExch(errflag, 1);
+                return;
+            }
+            sn[sp] = nd.left + 1;
+            sm[sp++] = down;
+            sn[sp] = nd.left;
+            sm[sp++] = down;
+        }
+    }
+}
+
 // ---- union-find (lock-free, root = smallest index) ----------------------
 __device__ __forceinline__ int uf_find(int *par, int x) {
     int p = par[x];
@@ -176,32 +270,45 @@ __global__ void k_dedupe_serial(Rec *recs, const rsg_particle *p, int64_t n, int
     *n_out = n;
 }
 
-__global__ void k_count(const KNode<3> *nodes, const Rec *recs, int n, float r, uint8_t *cnt,
-                        int *err) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float c[3] = {recs[i].pos[0], recs[i].pos[1], recs[i].pos[2]};
+// Warp forms of the searches: queries are list[0..nq) (ascending particle
+// indices, so a warp's queries are neighbours in the tree), or all
+// particles when list is null.
+__device__ __forceinline__ bool warp_query(const int *list, int nq, int *q) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    *q = (t < nq) ? (list ? list[t] : t) : -1;
+    return *q >= 0;
+}
+__device__ __forceinline__ bool warp_idle(int nq) {
+    return (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u) >= nq;
+}
+// |S_r(i)| capped at 17 (the reference only asks whether it exceeds 16)
+__global__ void __launch_bounds__(128) k_count_w(const KNode<3> *nodes, const Rec *recs, int n,
+                                                 float r, uint8_t *cnt, int *err) {
+    if (warp_idle(n)) return;
+    int i;
+    bool act = warp_query(nullptr, n, &i);
+    float c[3] = {0, 0, 0};
+    if (act) { c[0] = recs[i].pos[0]; c[1] = recs[i].pos[1]; c[2] = recs[i].pos[2]; }
     int k = 0;
-    sphere3(
-        nodes, 0, recs, c, r, err,
+    sphere3_warp(
+        nodes, recs, c, act, r, -1, err,
         [&](int s, int m) { k += m; return k <= 16; },
         [&](int j) { k++; return k <= 16; });
-    cnt[i] = (uint8_t)(k > 17 ? 17 : k);
+    if (act) cnt[i] = (uint8_t)(k > 17 ? 17 : k);
 }
-
-
-
-
 // Later dense neighbours of every dense particle k (j > k, j in S_r(k)),
-// counted then listed; cnt[j] counts the dense k that can skip j.
-__global__ void k_llist(const KNode<3> *nodes, const Rec *recs, int n, float r,
-                        const uint8_t *cnt, const int *loff, int *lcnt, int *llist, int *skipcnt,
-                        int *err) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n || cnt[k] <= 16) return;
-    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+// counted then listed; skipcnt[j] counts the dense k that can skip j.
+__global__ void __launch_bounds__(128) k_llist_w(const KNode<3> *nodes, const Rec *recs,
+                                                 const int *dense, int nd, float r,
+                                                 const uint8_t *cnt, const int *loff, int *lcnt,
+                                                 int *llist, int *skipcnt, int *err) {
+    if (warp_idle(nd)) return;
+    int k;
+    bool act = warp_query(dense, nd, &k);
+    float c[3] = {0, 0, 0};
+    if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
     int m = 0;
-    int base = loff ? loff[k] : 0;
+    int base = (loff && act) ? loff[k] : 0;
     auto add = [&](int j) {
         if (j > k && cnt[j] > 16) {
             if (llist) llist[base + m] = j;
@@ -209,8 +316,8 @@ __global__ void k_llist(const KNode<3> *nodes, const Rec *recs, int n, float r,
             m++;
         }
     };
-    sphere3(
-        nodes, 0, recs, c, r, err,
+    sphere3_warp(
+        nodes, recs, c, act, r, act ? k : INT_MAX - 1, err,
         [&](int s, int q) {
             for (int j = s; j < s + q; j++) add(j);
             return true;
@@ -218,44 +325,12 @@ __global__ void k_llist(const KNode<3> *nodes, const Rec *recs, int n, float r,
         [&](int j) {
             add(j);
             return true;
-        },
-        k);
-    if (!llist) lcnt[k] = m;
+        });
+    if (act && !llist) lcnt[k] = m;
 }
-// One frontier step of the ordered independent set: every particle decided
-// in the previous step walks its later list once; a seed marks its later
-// neighbours as skipped, and every decided particle releases one pending
-// earlier neighbour of each.  A particle with none pending that was not
-// skipped is a seed (all its earlier potential skippers are decided and
-// none of them is a seed).
-__global__ void k_kahn(const int *front, int nf, const int *loff, const int *llist, int *state,
-                       int *skipcnt, int *next, int *nnext) {
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= nf) return;
-    int k = front[w];
-    int sk = state[k];
-    for (int e = loff[k] + lane; e < loff[k + 1]; e += 32) {
-        int j = llist[e];
-        if (sk == 1 && atomicCAS(&state[j], 0, 2) == 0) next[atomicAdd(nnext, 1)] = j;
-        if (atomicSub(&skipcnt[j], 1) == 1 && atomicCAS(&state[j], 0, 1) == 0)
-            next[atomicAdd(nnext, 1)] = j;
-    }
-}
-__global__ void k_kahn_init(const int *dense, int nd, const int *skipcnt, int *state, int *front,
-                            int *nfront) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nd) return;
-    int i = dense[t];
-    if (skipcnt[i] == 0) {
-        state[i] = 1;
-        front[atomicAdd(nfront, 1)] = i;
-    }
-}
-__global__ void k_state8(const int *s32, int n, uint8_t *s8) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) s8[i] = (uint8_t)s32[i];
-}
-
+// Searches with atomic updates on the points found keep one thread per
+// query: neighbouring queries of one warp would update the same points at
+// the same moment.
 __global__ void k_seed_mark(const KNode<3> *nodes, const Rec *recs, int n, float r,
                             const uint8_t *state, uint8_t *skipped, int *err) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -313,6 +388,40 @@ __global__ void k_link_2r(const KNode<3> *nodes, const Rec *recs, int n, float r
             if (gtime[j] <= s) uf_unite(par, s, j);
             return true;
         });
+}
+
+// One frontier step of the ordered independent set: every particle decided
+// in the previous step walks its later list once; a seed marks its later
+// neighbours as skipped, and every decided particle releases one pending
+// earlier neighbour of each.  A particle with none pending that was not
+// skipped is a seed (all its earlier potential skippers are decided and
+// none of them is a seed).
+__global__ void k_kahn(const int *front, int nf, const int *loff, const int *llist, int *state,
+                       int *skipcnt, int *next, int *nnext) {
+    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nf) return;
+    int k = front[w];
+    int sk = state[k];
+    for (int e = loff[k] + lane; e < loff[k + 1]; e += 32) {
+        int j = llist[e];
+        if (sk == 1 && atomicCAS(&state[j], 0, 2) == 0) next[atomicAdd(nnext, 1)] = j;
+        if (atomicSub(&skipcnt[j], 1) == 1 && atomicCAS(&state[j], 0, 1) == 0)
+            next[atomicAdd(nnext, 1)] = j;
+    }
+}
+__global__ void k_kahn_init(const int *dense, int nd, const int *skipcnt, int *state, int *front,
+                            int *nfront) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nd) return;
+    int i = dense[t];
+    if (skipcnt[i] == 0) {
+        state[i] = 1;
+        front[atomicAdd(nfront, 1)] = i;
+    }
+}
+__global__ void k_state8(const int *s32, int n, uint8_t *s8) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) s8[i] = (uint8_t)s32[i];
 }
 
 __global__ void k_roots(int *par, int n, int *root, int *size) {
@@ -378,6 +487,24 @@ struct DFlag {
     const uint8_t *c;
     __device__ uint8_t operator()(int i) const { return c[i] > 16; }
 };
+// Indices i < n with pred(i), ascending, into out; returns their number.
+template <class Pred>
+static int select_where(Arena &ar, int n, Pred pred, int *out, cudaStream_t st) {
+    thrust::transform_iterator<Pred, thrust::counting_iterator<int>, uint8_t> it(
+        thrust::counting_iterator<int>(0), pred);
+    size_t mark = ar.used;
+    int *cnt = ar.get<int>(1);
+    size_t b = 0;
+    cub::DeviceSelect::Flagged(nullptr, b, thrust::counting_iterator<int>(0), it, out, cnt, n, st);
+    void *t = ar.take(b + 256);
+    cub::DeviceSelect::Flagged(t, b, thrust::counting_iterator<int>(0), it, out, cnt, n, st);
+    RSG_CHECK_LAUNCH();
+    int h = 0;
+    RSG_CUDA(cudaMemcpyAsync(&h, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    ar.used = mark;
+    return h;
+}
 
 struct FofOut {
     int64_t num_p;
@@ -433,14 +560,18 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
 
     uint8_t *cnt = ar.get<uint8_t>(n);
     phase_mark(st, "fof.tree3d");
-    launch(k_count, nblk(n, T), T, 0, st, F.nodes, recs, n, r, cnt, err);
+    const int TW = 128;
+    launch(k_count_w, nblk(n, TW), TW, 0, st, F.nodes, recs, n, r, cnt, err);
     phase_mark(st, "fof.count");
+    // dense particles (more than 16 neighbours), in tree order
+    int *dense = ar.get<int>(n);
+    int nd = select_where(ar, n, DFlag{cnt}, dense, st);
     // later-dense-neighbour lists and pending-skipper counts
     int *lcnt = ar.get<int>(n + 1), *loff = ar.get<int>(n + 1), *skipcnt = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(lcnt, 0, sizeof(int) * (n + 1), st));
     RSG_CUDA(cudaMemsetAsync(skipcnt, 0, sizeof(int) * n, st));
-    launch(k_llist, nblk(n, T), T, 0, st, F.nodes, recs, n, r, cnt, (const int *)nullptr, lcnt,
-           (int *)nullptr, skipcnt, err);
+    launch(k_llist_w, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
+           (const uint8_t *)cnt, (const int *)nullptr, lcnt, (int *)nullptr, skipcnt, err);
     size_t cb = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, cb, lcnt, loff, n + 1, st);
     void *ct = ar.take(cb + 256);
@@ -449,22 +580,8 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     RSG_CUDA(cudaMemcpyAsync(&ne, loff + n, sizeof(int), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     int *llist = ar.get<int>(ne > 0 ? ne : 1);
-    launch(k_llist, nblk(n, T), T, 0, st, F.nodes, recs, n, r, cnt, loff, lcnt, llist, skipcnt, err);
-    // dense particle list
-    int *dense = ar.get<int>(n), *ndense = ar.get<int>(1);
-    {
-        thrust::transform_iterator<DFlag, thrust::counting_iterator<int>, uint8_t> it(
-            thrust::counting_iterator<int>(0), DFlag{cnt});
-        size_t b2 = 0;
-        cub::DeviceSelect::Flagged(nullptr, b2, thrust::counting_iterator<int>(0), it, dense,
-                                   ndense, n, st);
-        void *t2 = ar.take(b2 + 256);
-        cub::DeviceSelect::Flagged(t2, b2, thrust::counting_iterator<int>(0), it, dense, ndense,
-                                   n, st);
-    }
-    int nd = 0;
-    RSG_CUDA(cudaMemcpyAsync(&nd, ndense, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RSG_CUDA(cudaStreamSynchronize(st));
+    launch(k_llist_w, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
+           (const uint8_t *)cnt, (const int *)loff, lcnt, llist, skipcnt, err);
     phase_mark(st, "fof.elist");
     int *state32 = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(state32, 0, sizeof(int) * n, st));
@@ -490,17 +607,21 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     uint8_t *state = ar.get<uint8_t>(n);
     launch(k_state8, nblk(n, T), T, 0, st, state32, n, state);
     phase_mark(st, "fof.seeds");
-    if (getenv("RSG_TIMING")) fprintf(stderr, "  [fof] dense %d, later-list %d, frontier steps %d\n", nd, ne, rounds);
+    if (getenv("RSG_TIMING"))
+        fprintf(stderr, "  [fof] dense %d, later-list %d, frontier steps %d\n", nd, ne, rounds);
     last_stats()[RSG_STAT_DENSE] = nd;
     last_stats()[RSG_STAT_LATER_LIST] = ne;
     uint8_t *skipped = ar.get<uint8_t>(n);
     RSG_CUDA(cudaMemsetAsync(skipped, 0, n, st));
-    launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, state, skipped, err);
+    launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)state, skipped,
+           err);
     int *gtime = ar.get<int>(n), *par = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(gtime, 0x7f, sizeof(int) * n, st));
     launch(k_iota, nblk(n, T), T, 0, st, par, n);
-    launch(k_link_r, nblk(n, T), T, 0, st, F.nodes, recs, n, r, cnt, skipped, gtime, par, err);
-    launch(k_link_2r, nblk(n, T), T, 0, st, F.nodes, recs, n, r2x, state, gtime, par, err);
+    launch(k_link_r, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
+           (const uint8_t *)skipped, gtime, par, err);
+    launch(k_link_2r, nblk(n, T), T, 0, st, F.nodes, recs, n, r2x, (const uint8_t *)state,
+           (const int *)gtime, par, err);
     phase_mark(st, "fof.links");
     int *root = ar.get<int>(n), *size = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(size, 0, sizeof(int) * n, st));
