@@ -1521,13 +1521,16 @@ __global__ void k_halo_scans_list(rsg_halo *H, const rsg_extra_halo_info *E, con
     more_props(hh, q, tot, 1, C);
 }
 
+// records of every halo kept after dropping the potential-only ones; one
+// warp per halo
 __global__ void k_kept_count(const PotRec *PO, const int32_t *toff, const int32_t *tot,
                              int32_t NH, int32_t *kept) {
-    int h = blockIdx.x * blockDim.x + threadIdx.x;
+    int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (h >= NH) return;
     int c = 0;
-    for (int i = 0; i < tot[h]; i++) c += PO[toff[h] + i].ke >= 0;
-    kept[h] = c;
+    for (int i = lane; i < tot[h]; i += 32) c += PO[toff[h] + i].ke >= 0;
+    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) kept[h] = c;
 }
 __global__ void k_bh_roots(const int32_t *toff, const int32_t *tot, int32_t NH, int32_t *rflag) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1736,7 +1739,7 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     }
     phase_mark(st, "p.sort");
     int32_t *kept = ar.get<int32_t>(NH + 1);
-    launch(k_kept_count, nblk(NH, T), T, 0, st, PO2, toff, tot, NH, kept);
+    launch(k_kept_count, nblk((int64_t)NH * 32, T), T, 0, st, PO2, toff, tot, NH, kept);
     {
         int32_t *fs = ar.get<int32_t>(NH), *fbg = ar.get<int32_t>(NH);
         int32_t *ls = ar.get<int32_t>(NH), *lb = ar.get<int32_t>(NH);

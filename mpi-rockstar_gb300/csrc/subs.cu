@@ -273,27 +273,56 @@ __global__ void k_norm_div(Rec *W, HierNodes N, int32_t base, const double *sig)
             W[s + i].pos[d] = __double2float_rn((double)W[s + i].pos[d] / (d < 3 ? sx : sv));
 }
 
+// x advanced by m steps of rand_r's generator (x <- 1103515245 x + 12345
+// mod 2^32), by squaring the affine step.
+__device__ __forceinline__ unsigned lcg_jump(unsigned x, uint64_t m) {
+    unsigned a = 1103515245u, c = 12345u, ra = 1u, rc = 0u;
+    while (m) {
+        if (m & 1) {
+            ra = a * ra;
+            rc = a * rc + c;
+        }
+        c = a * c + c;
+        a = a * a;
+        m >>= 1;
+    }
+    return ra * x + rc;
+}
+
 // Sample list (src/groupies.c:295-308): all particles when n <= 10000
-// (or EXACT_LL_CALC), else 10000 indices from rand_r seeded with n.
-__global__ void k_sample(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
-                         int32_t *sidx, unsigned *seed_out, int exact) {
+// (or EXACT_LL_CALC), else 10000 indices drawn by two rand_r calls each
+// from a stream seeded with n.  A rand_r call is three generator steps, so
+// sample t starts from the seed advanced by 6 t steps: every sample is
+// drawn on its own thread.  The node's stream continues into
+// find_median_r from the state after all its samples.
+__global__ void k_sample_seed(HierNodes N, int32_t base, int32_t count, unsigned *seed_out,
+                              int exact) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= count) return;
-    int node = base + k;
-    int n = N.n[node];
+    int n = N.n[base + k];
     int nt = exact ? n : (n < 10000 ? n : 10000);
-    unsigned seed = (unsigned)n;
-    if (nt != n) {
-        int o = soff[k];
-        for (int i = 0; i < nt; i++) {
-            int64_t j = rand_r_glibc(&seed);
-            j <<= 31;
-            j += rand_r_glibc(&seed);
-            j %= n;
-            sidx[o + i] = (int32_t)j;
-        }
+    seed_out[k] = (nt != n) ? lcg_jump((unsigned)n, 6ull * (uint64_t)nt) : (unsigned)n;
+}
+__global__ void k_sample_idx(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
+                             int32_t *sidx, int64_t total, int exact) {
+    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = count - 1;  // node of sample g: last k with soff[k] <= g
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (soff[mid] <= g) lo = mid;
+        else hi = mid - 1;
     }
-    seed_out[k] = seed;
+    int n = N.n[base + lo];
+    int nt = exact ? n : (n < 10000 ? n : 10000);
+    if (nt == n) return;
+    int64_t t = g - soff[lo];
+    unsigned seed = lcg_jump((unsigned)n, 6ull * (uint64_t)t);
+    int64_t j = rand_r_glibc(&seed);
+    j <<= 31;
+    j += rand_r_glibc(&seed);
+    j %= n;
+    sidx[g] = (int32_t)j;
 }
 
 __device__ __forceinline__ float dist6(const float *c, const float *p) {
@@ -404,6 +433,51 @@ __global__ void k_nn(const KNode<6> *nodes, const Rec *W, HierNodes N, int32_t b
 
 // find_median_r / rad_partition (src/groupies.c:735-786), run as is on the
 // sample's distances in sample order with the continuing rand_r stream.
+__device__ float median_r(float *a, int nt, unsigned seed, float frac) {
+    int64_t kk = (int64_t)__float2ll_rz(fmul(__ll2float_rn(nt), frac));
+    if (nt < 2) return a[0];
+    int64_t left = 0, right = nt;
+    int guard = 0;
+    while (true) {
+        float u = __fdiv_rn(__int2float_rn(rand_r_glibc(&seed) % 2147483647), 2147483648.0f);
+        float pf = fadd(__ll2float_rn(left), fmul(u, __ll2float_rn(right - left)));
+        int64_t pi = (int64_t)__float2ll_rz(pf);
+        if (pi >= right) pi = right - 1;  // keeps the access in range (u == 1 edge)
+        float piv = a[pi], t;
+        t = a[pi]; a[pi] = a[right - 1]; a[right - 1] = t;
+        int64_t si = right - 2, i;
+        for (i = left; i < si; i++)
+            if (a[i] > piv) {
+                t = a[i]; a[i] = a[si]; a[si] = t;
+                si--;
+                i--;
+            }
+        if (a[si] <= piv) si++;
+        t = a[right - 1]; a[right - 1] = a[si]; a[si] = t;
+        int64_t p = si;
+        if (kk == p || (a[left] == a[right - 1])) return a[kk];
+        if (kk < p) right = p;
+        else left = p + 1;
+        if (++guard > 100000000) return a[kk];
+    }
+}
+// Nodes whose sample fits in shared memory (RSG_TARGET_SMEM distances): one
+// block per node stages the distances, one thread selects.
+#define RSG_TARGET_SMEM 10000
+__global__ void k_target_smem(HierNodes N, int32_t base, const int32_t *soff, const float *prad,
+                              const unsigned *seed_in, float frac, int exact) {
+    extern __shared__ float a_s[];
+    int k = blockIdx.x;
+    int node = base + k;
+    int n = N.n[node];
+    int nt = exact ? n : (n < 10000 ? n : 10000);
+    if (nt > RSG_TARGET_SMEM) return;
+    const float *a = prad + soff[k];
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) a_s[i] = a[i];
+    __syncthreads();
+    if (threadIdx.x == 0) N.target_r[node] = median_r(a_s, nt, seed_in[k], frac);
+}
+// Larger samples (EXACT_LL_CALC): in place in global memory.
 __global__ void k_target(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
                          float *prad, const unsigned *seed_in, float frac, int exact) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -411,45 +485,8 @@ __global__ void k_target(HierNodes N, int32_t base, int32_t count, const int32_t
     int node = base + k;
     int n = N.n[node];
     int nt = exact ? n : (n < 10000 ? n : 10000);
-    float *a = prad + soff[k];
-    unsigned seed = seed_in[k];
-    float res;
-    int64_t kk = (int64_t)__float2ll_rz(fmul(__ll2float_rn(nt), frac));
-    if (nt < 2) {
-        res = a[0];
-    } else {
-        int64_t left = 0, right = nt;
-        int guard = 0;
-        while (true) {
-            float u = __fdiv_rn(__int2float_rn(rand_r_glibc(&seed) % 2147483647), 2147483648.0f);
-            float pf = fadd(__ll2float_rn(left), fmul(u, __ll2float_rn(right - left)));
-            int64_t pi = (int64_t)__float2ll_rz(pf);
-            if (pi >= right) pi = right - 1;  // keeps the access in range (u == 1 edge)
-            float piv = a[pi], t;
-            t = a[pi]; a[pi] = a[right - 1]; a[right - 1] = t;
-            int64_t si = right - 2, i;
-            for (i = left; i < si; i++)
-                if (a[i] > piv) {
-                    t = a[i]; a[i] = a[si]; a[si] = t;
-                    si--;
-                    i--;
-                }
-            if (a[si] <= piv) si++;
-            t = a[right - 1]; a[right - 1] = a[si]; a[si] = t;
-            int64_t p = si;
-            if (kk == p || (a[left] == a[right - 1])) {
-                res = a[kk];
-                break;
-            }
-            if (kk < p) right = p;
-            else left = p + 1;
-            if (++guard > 100000000) {
-                res = a[kk];
-                break;
-            }
-        }
-    }
-    N.target_r[node] = res;
+    if (nt <= RSG_TARGET_SMEM) return;
+    N.target_r[node] = median_r(prad + soff[k], nt, seed_in[k], frac);
 }
 
 // element -> level-local node index for the nodes [base, base + count)
@@ -1488,12 +1525,24 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         int32_t *sidx = ar.get<int32_t>(tot + 1);
         float *prad = ar.get<float>(tot + 1);
         unsigned *seeds = ar.get<unsigned>(cnt);
-        launch(k_sample, nblk(cnt, 64), 64, 0, st, N, base, cnt, soff, sidx, seeds,
-                                               (int)cfg.exact_ll_calc);
+        launch(k_sample_seed, nblk(cnt, 64), 64, 0, st, N, base, cnt, seeds,
+               (int)cfg.exact_ll_calc);
+        launch(k_sample_idx, nblk(tot, 256), 256, 0, st, N, base, cnt, (const int32_t *)soff, sidx,
+               (int64_t)tot, (int)cfg.exact_ll_calc);
         launch(k_nn, nblk(tot, 128), 128, 0, st, F.nodes, W, N, base, cnt, soff, sidx, prad,
                (int64_t)tot, (int)cfg.exact_ll_calc, err);
-        launch(k_target, nblk(cnt, 32), 32, 0, st, N, base, cnt, soff, prad, seeds,
-                                               (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
+        {
+            int ntmax = 0;
+            for (int32_t k = 0; k < cnt; k++) {
+                int nt = cfg.exact_ll_calc ? hn[k] : (hn[k] < 10000 ? hn[k] : 10000);
+                if (nt <= RSG_TARGET_SMEM && nt > ntmax) ntmax = nt;
+            }
+            launch(k_target_smem, cnt, 64, (size_t)4 * (ntmax > 0 ? ntmax : 1), st, N, base,
+                   (const int32_t *)soff, (const float *)prad, (const unsigned *)seeds,
+                   (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
+            launch(k_target, nblk(cnt, 32), 32, 0, st, N, base, cnt, soff, prad, seeds,
+                   (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
+        }
         phase_mark(st, "d.nn_target");
         RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
         launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
