@@ -940,13 +940,60 @@ __global__ void k_asc_seed(HierNodes N, int32_t base, int32_t count, rsg_halo *H
 // src/groupies.c:584-609: particles of merged seeds go to the biggest halo;
 // unassigned particles go to the halo of smallest phase-space metric among
 // the growing ones, then up the sub_of chain while the metric exceeds the
-// halo's max_metric.
+// halo's max_metric.  The metric is calc_particle_dist's
+// (float)sqrt((double)x) of the float sum x = r^2/h.r^2 + v^2/h.vrms^2,
+// which is monotone in x: a candidate whose x is not below the best one's
+// cannot win the strict comparison, so the square root is only taken for
+// candidates that might (same choice, ties included).  The block stages the
+// growing halos' centres and scales in shared memory.
+struct AscHalo {
+    float pos[6];
+    float r, vrms;
+};
+#define RSG_ASC_SMEM 1024
+__device__ __forceinline__ bool asc_valid(const AscHalo &h) { return !(h.vrms <= 0 || h.r <= 0); }
+__device__ __forceinline__ float asc_x(const AscHalo &h, const float *pos) {
+    float r2 = 0.f, v2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float dx = fsub(h.pos[i], pos[i]);
+        r2 = fadd(r2, fmul(dx, dx));
+    }
+#pragma unroll
+    for (int i = 3; i < 6; i++) {
+        float dx = fsub(h.pos[i], pos[i]);
+        v2 = fadd(v2, fmul(dx, dx));
+    }
+    float a = __fdiv_rn(r2, fmul(h.r, h.r));
+    float b = __fdiv_rn(v2, fmul(h.vrms, h.vrms));
+    return fadd(a, b);
+}
 __global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_halo *H,
                              const rsg_extra_halo_info *E, const int32_t *glist,
                              const int32_t *redirect, int32_t *phalo) {
+    __shared__ AscHalo gs[RSG_ASC_SMEM];
     int node = base + blockIdx.x;
     int s = N.start[node], n = N.n[node];
     int mi = N.maxi[node], ng = N.ng[node], h0 = N.h0[node];
+    const bool staged = ng <= RSG_ASC_SMEM;
+    if (staged)
+        for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+            const rsg_halo &hh = H[glist[h0 + g]];
+            for (int d = 0; d < 3; d++) {
+                gs[g].pos[d] = hh.pos[d];
+                gs[g].pos[d + 3] = hh.bulkvel[d];
+            }
+            gs[g].r = hh.r;
+            gs[g].vrms = hh.vrms;
+        }
+    __syncthreads();
+    AscHalo hm;
+    for (int d = 0; d < 3; d++) {
+        hm.pos[d] = H[mi].pos[d];
+        hm.pos[d + 3] = H[mi].bulkvel[d];
+    }
+    hm.r = H[mi].r;
+    hm.vrms = H[mi].vrms;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         int ph = phalo[s + i];
         if (ph >= 0) {
@@ -957,15 +1004,44 @@ __global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_
             phalo[s + i] = mi;
             continue;
         }
-        const float *pos = W[s + i].pos;
-        float best = pdist(H[mi], pos);
+        float pos[6];
+#pragma unroll
+        for (int d = 0; d < 6; d++) pos[d] = W[s + i].pos[d];
+        // the running best: its metric and, when valid, its x
+        bool bvalid = asc_valid(hm);
+        float bx = bvalid ? asc_x(hm, pos) : 0.f;
+        float best = bvalid ? (float)sqrt((double)bx) : 1e20f;
         int bh = mi;
         for (int g = 0; g < ng; g++) {
-            int h = glist[h0 + g];
-            float m = pdist(H[h], pos);
+            AscHalo c;
+            if (staged) c = gs[g];
+            else {
+                const rsg_halo &hh = H[glist[h0 + g]];
+                for (int d = 0; d < 3; d++) {
+                    c.pos[d] = hh.pos[d];
+                    c.pos[d + 3] = hh.bulkvel[d];
+                }
+                c.r = hh.r;
+                c.vrms = hh.vrms;
+            }
+            float m;
+            if (!asc_valid(c)) {
+                m = 1e20f;
+                if (m < best) {
+                    best = m;
+                    bh = glist[h0 + g];
+                    bvalid = false;
+                }
+                continue;
+            }
+            float x = asc_x(c, pos);
+            if (bvalid && !(x < bx)) continue;  // metric >= best
+            m = (float)sqrt((double)x);
             if (m < best) {
                 best = m;
-                bh = h;
+                bx = x;
+                bvalid = true;
+                bh = glist[h0 + g];
             }
         }
         int h = bh;
