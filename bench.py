@@ -144,37 +144,47 @@ def cpu_baseline_port(rk, cfg_id, scale):
 
 
 # ---- reference arm: the oracle port over all host cores -------------------
-def _ref_worker(args):
-    parts, off, sz = args
+_REF_CFG = None
+
+
+def _ref_init(cfg_fields):
+    global _REF_CFG
     sys.path.insert(0, ROOT)
+    from oracle import layouts as OL
     from oracle import restatement as O
-    cfgd = _ref_worker.cfg
-    O.setup(cfgd)
+    O.build()
+    _REF_CFG = OL.Config(**cfg_fields)
+    O.setup(_REF_CFG)
+
+
+def _ref_worker(args):
+    from oracle import restatement as O
+    parts, off, sz = args
     out, h, e = O.find_subs(parts, off, sz)
     return len(h)
 
 
-def _ref_init(cfg):
-    sys.path.insert(0, ROOT)
-    from oracle import restatement as O
-    O.build()
-    _ref_worker.cfg = cfg
-
-
 def reference_arm(args, rk):
+    """The reference's algorithm on the host cores: the C restatement (pinned
+    bit-exact to the reference's sources) with the FOF serial, as rockstar()
+    runs it, and find_subs over the groups on one process per core, largest
+    groups first, as the reference's dynamic OpenMP loop deals them."""
+    import dataclasses
     import multiprocessing as mp_
+    from concurrent.futures import ProcessPoolExecutor
+    from oracle import layouts as OL
     from oracle import restatement as O
     O.build()
     p, box, mp, _ = rk.synth(args.cfg, args.scale, SEED)
-    c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    fields = {f.name: getattr(rk.Config(particle_mass=mp, box_size=box, total_particles=len(p)),
+                              f.name) for f in dataclasses.fields(OL.Config)}
+    O.setup(OL.Config(**fields))
     ncores = os.cpu_count() or 1
-    ctx = mp_.get_context("spawn")
-    pool = ctx.Pool(ncores, initializer=_ref_init, initargs=(c,))
-    O.setup(c)
+    pool = ProcessPoolExecutor(ncores, mp_context=mp_.get_context("spawn"),
+                               initializer=_ref_init, initargs=(fields,))
 
     def step():
         fp, off, sz = O.fof(p)  # serial, as rockstar() is in the reference
-        # groups to workers, largest first (the reference's OMP dynamic loop)
         order = np.argsort(-sz, kind="stable")
         chunks = [[] for _ in range(ncores)]
         load = np.zeros(ncores)
@@ -198,7 +208,7 @@ def reference_arm(args, rk):
     for _ in range(args.steps):
         step()
     dt = (time.perf_counter() - t0) / args.steps
-    pool.close()
+    pool.shutdown()
     v = len(p) / dt
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "particles/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,

@@ -300,15 +300,15 @@ __global__ void __launch_bounds__(128) k_count_w(const KNode<3> *nodes, const Re
 // counted then listed; skipcnt[j] counts the dense k that can skip j.
 __global__ void __launch_bounds__(128) k_llist_w(const KNode<3> *nodes, const Rec *recs,
                                                  const int *dense, int nd, float r,
-                                                 const uint8_t *cnt, const int *loff, int *lcnt,
-                                                 int *llist, int *skipcnt, int *err) {
+                                                 const uint8_t *cnt, const int64_t *loff,
+                                                 int *lcnt, int *llist, int *skipcnt, int *err) {
     if (warp_idle(nd)) return;
     int k;
     bool act = warp_query(dense, nd, &k);
     float c[3] = {0, 0, 0};
     if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
     int m = 0;
-    int base = (loff && act) ? loff[k] : 0;
+    int64_t base = (loff && act) ? loff[k] : 0;
     auto add = [&](int j) {
         if (j > k && cnt[j] > 16) {
             if (llist) llist[base + m] = j;
@@ -396,13 +396,13 @@ __global__ void k_link_2r(const KNode<3> *nodes, const Rec *recs, int n, float r
 // earlier neighbour of each.  A particle with none pending that was not
 // skipped is a seed (all its earlier potential skippers are decided and
 // none of them is a seed).
-__global__ void k_kahn(const int *front, int nf, const int *loff, const int *llist, int *state,
+__global__ void k_kahn(const int *front, int nf, const int64_t *loff, const int *llist, int *state,
                        int *skipcnt, int *next, int *nnext) {
     int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nf) return;
     int k = front[w];
     int sk = state[k];
-    for (int e = loff[k] + lane; e < loff[k + 1]; e += 32) {
+    for (int64_t e = loff[k] + lane; e < loff[k + 1]; e += 32) {
         int j = llist[e];
         if (sk == 1 && atomicCAS(&state[j], 0, 2) == 0) next[atomicAdd(nnext, 1)] = j;
         if (atomicSub(&skipcnt[j], 1) == 1 && atomicCAS(&state[j], 0, 1) == 0)
@@ -567,21 +567,24 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     int *dense = ar.get<int>(n);
     int nd = select_where(ar, n, DFlag{cnt}, dense, st);
     // later-dense-neighbour lists and pending-skipper counts
-    int *lcnt = ar.get<int>(n + 1), *loff = ar.get<int>(n + 1), *skipcnt = ar.get<int>(n);
+    // (64-bit offsets: the lists can hold more than 2^31 entries)
+    int *lcnt = ar.get<int>(n + 1), *skipcnt = ar.get<int>(n);
+    int64_t *loff = ar.get<int64_t>(n + 1);
     RSG_CUDA(cudaMemsetAsync(lcnt, 0, sizeof(int) * (n + 1), st));
     RSG_CUDA(cudaMemsetAsync(skipcnt, 0, sizeof(int) * n, st));
     launch(k_llist_w, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
-           (const uint8_t *)cnt, (const int *)nullptr, lcnt, (int *)nullptr, skipcnt, err);
+           (const uint8_t *)cnt, (const int64_t *)nullptr, lcnt, (int *)nullptr, skipcnt, err);
     size_t cb = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, cb, lcnt, loff, n + 1, st);
+    thrust::transform_iterator<ToI64, const int32_t *, int64_t> lc64((const int32_t *)lcnt, ToI64{});
+    cub::DeviceScan::ExclusiveSum(nullptr, cb, lc64, loff, n + 1, st);
     void *ct = ar.take(cb + 256);
-    cub::DeviceScan::ExclusiveSum(ct, cb, lcnt, loff, n + 1, st);
-    int ne = 0;
-    RSG_CUDA(cudaMemcpyAsync(&ne, loff + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    cub::DeviceScan::ExclusiveSum(ct, cb, lc64, loff, n + 1, st);
+    int64_t ne = 0;
+    RSG_CUDA(cudaMemcpyAsync(&ne, loff + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     int *llist = ar.get<int>(ne > 0 ? ne : 1);
     launch(k_llist_w, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
-           (const uint8_t *)cnt, (const int *)loff, lcnt, llist, skipcnt, err);
+           (const uint8_t *)cnt, (const int64_t *)loff, lcnt, llist, skipcnt, err);
     phase_mark(st, "fof.elist");
     int *state32 = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(state32, 0, sizeof(int) * n, st));
@@ -608,7 +611,8 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     launch(k_state8, nblk(n, T), T, 0, st, state32, n, state);
     phase_mark(st, "fof.seeds");
     if (getenv("RSG_TIMING"))
-        fprintf(stderr, "  [fof] dense %d, later-list %d, frontier steps %d\n", nd, ne, rounds);
+        fprintf(stderr, "  [fof] dense %d, later-list %lld, frontier steps %d\n", nd,
+                (long long)ne, rounds);
     last_stats()[RSG_STAT_DENSE] = nd;
     last_stats()[RSG_STAT_LATER_LIST] = ne;
     uint8_t *skipped = ar.get<uint8_t>(n);

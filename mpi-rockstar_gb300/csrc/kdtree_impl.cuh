@@ -4,6 +4,33 @@
 
 namespace rsg {
 
+struct ToI64 {
+    __device__ int64_t operator()(int32_t v) const { return (int64_t)v; }
+};
+// Fails with RSG_ERR_LIMIT when the int32 counts in[0..n) add up to more
+// than an int32 offset can address: the callers scan such counts into
+// int32 offsets.
+inline void check_i32_total(Arena &ar, const int32_t *in, int64_t n, const char *what,
+                            cudaStream_t st) {
+    thrust::transform_iterator<ToI64, const int32_t *, int64_t> it(in, ToI64{});
+    size_t mark = ar.used;
+    int64_t *tot = ar.get<int64_t>(1);
+    size_t b = 0;
+    cub::DeviceReduce::Sum(nullptr, b, it, tot, (int)n, st);
+    void *t = ar.take(b + 256);
+    cub::DeviceReduce::Sum(t, b, it, tot, (int)n, st);
+    RSG_CHECK_LAUNCH();
+    int64_t h = 0;
+    RSG_CUDA(cudaMemcpyAsync(&h, tot, sizeof(h), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    ar.used = mark;
+    if (h > (int64_t)0x7fffffff - 1) {
+        set_error(RSG_ERR_LIMIT, "%s: %lld entries exceed the 2^31 limit of one call", what,
+                  (long long)h);
+        throw Failure();
+    }
+}
+
 // Box accumulation with per-thread runs: each thread walks ITEMS consecutive
 // elements, keeps a running min/max while the owner stays the same and
 // flushes with ordered atomics when it changes, so a node spanning millions

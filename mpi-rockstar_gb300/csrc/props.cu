@@ -1701,6 +1701,7 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     int32_t *toff = ar.get<int32_t>(NH + 1), *soff = ar.get<int32_t>(NH + 1);
     launch(k_set_count, nblk(NH + 1, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio, tot,
                                                  nseg, err);
+    check_i32_total(ar, tot, NH + 1, "potential records", st);
     int32_t npo = scan_i32(ar, tot, toff, NH + 1, st);
     phase_mark(st, "p.sets");
     int32_t ns = scan_i32(ar, nseg, soff, NH + 1, st);

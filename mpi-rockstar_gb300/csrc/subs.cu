@@ -1628,6 +1628,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
             launch(k_fof6_w<0>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
                    (const int32_t *)nullptr, ncnt, (int32_t *)nullptr, (int *)nullptr, err);
+            check_i32_total(ar, ncnt, M + 1, "6D neighbour lists", st);
             int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
             int32_t *nbr = ar.get<int32_t>(ne + 1);
             launch(k_fof6_w<1>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
