@@ -38,11 +38,39 @@ SEED = 20261203
 # record read once, every output written once; node data held in L2 is not
 # counted.  Kernels without an entry get no roofline figure.
 ALGO_BYTES = {
+    # 6D FOF: each level's particles read once (24 B of the 32 B record), one
+    # union-find parent written (4 B)
+    "k_fof6_w": lambda st, L: 28.0 * st["items_6d"] / max(L, 1),
+    # assignment: position read, label read and written
+    "k_asc_assign": lambda st, L: 32.0 * st["items_6d"] / max(L, 1),
+    # basic halo properties: two passes over the halo's positions
+    "k_basic_props": lambda st, L: 48.0 * st["items_6d"] / max(L, 1),
+    # norm_sd: positions read and written back
+    "k_norm_par": lambda st, L: 48.0 * st["items_6d"] / max(L, 1),
+    "k_norm_warp": lambda st, L: 48.0 * st["items_6d"] / max(L, 1),
+    # next-closest search: sample position read, distance written
+    "k_nn": lambda st, L: 28.0 * st["samples_6d"] / max(L, 1),
+    # median selection: every sample distance read once
+    "k_target_smem": lambda st, L: 4.0 * st["samples_6d"] / max(L, 1),
+    # later-dense lists: positions of the dense particles in both launches,
+    # every entry written once
+    "k_llist_w": lambda st, L: (32.0 * st["dense"] + 4.0 * st["later_list"]) / max(L, 1),
+    # seed selection: every list entry read, its pending count updated
+    "k_kahn": lambda st, L: 12.0 * st["later_list"] / max(L, 1),
+    # potentials: record read (48 B), potential written (8 B)
+    "k_bh_walk": lambda st, L: 56.0 * st["pot_records"] / max(L, 1),
+    # property scans: record read, kinetic energy written
     "k_halo_scans_blk": lambda st, L: 52.0 * st["kept_big"],
     "k_halo_scans_list": lambda st, L: 52.0 * st["kept_small"],
-    "k_bh_walk": lambda st, L: 56.0 * st["pot_records"],     # read 48 B, write 8 B pe
-    # two launches (count, fill): positions read by both, entries written once
-    "k_llist": lambda st, L: (32.0 * st["particles"] + 4.0 * st["later_list"]) / max(L, 1),
+}
+
+
+# DRAM bytes per work unit from one ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum of the captured launch over the units it processed),
+# scaled to the timed launches by their units
+NCU_TRAFFIC = {
+    "k_fof6_w": (62.18e6 / 1364736.0, "items_6d",
+                 "profiles/k_fof6_w_workload2_level0.md (level-0 launch, scaled by particles)"),
 }
 
 
@@ -359,8 +387,13 @@ def main():
         share = None
         if rows:
             share = sum(r[2] for r in rows if r[0] == top) / tab_ms
+        traffic, tsrc = None, None
+        if top in NCU_TRAFFIC:
+            per_unit, unit_key, tsrc = NCU_TRAFFIC[top]
+            traffic = per_unit * stats[unit_key] / max(per_step, 1)
         roof = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
-                "frac": (ach / peak) if ach else None, "traffic": None,
+                "frac": (ach / peak) if ach else None, "traffic": traffic,
+                "traffic_source": tsrc,
                 "algorithmic_bytes_per_launch": algo, "launches": kl, "avg_ms": avg_ms,
                 "share_of_step": share,
                 "peak_kind": "measured copy (MEASURED_PEAKS.json hbm_gbs)"

@@ -195,7 +195,7 @@ def profile_read():
 
 
 STAT_NAMES = ("particles", "groups", "halos", "pot_records", "kept_big", "kept_small",
-              "halos_big", "halos_small", "dense", "later_list")
+              "halos_big", "halos_small", "dense", "later_list", "items_6d", "samples_6d")
 
 
 def last_stats():

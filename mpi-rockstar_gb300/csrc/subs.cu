@@ -1496,6 +1496,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                          rsg_halo *d_halos, rsg_extra_halo_info *d_extra, int64_t max_halos,
                          cudaStream_t st, int exact) {
     SubsOut out{0};
+    last_stats()[RSG_STAT_6D_ITEMS] = 0;
+    last_stats()[RSG_STAT_6D_SAMPLES] = 0;
     // ordered (bit-exact) FP64 sums up to this size; tree reductions above
     const int seq_max = exact ? RSG_SEQ_MAX : RSG_SMALL;
     const int T = 256;
@@ -1593,6 +1595,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             tot += nt;
             nin += hn[k];
         }
+        last_stats()[RSG_STAT_6D_ITEMS] += nin;
+        last_stats()[RSG_STAT_6D_SAMPLES] += tot;
         // 6D kd-forest over this level's nodes (src/groupies.c:294)
         Forest<6> F = build_forest<6, Rec>(ar, W, M, rst, rn, cnt, nin, 40, st);
         phase_mark(st, "d.tree6d");
