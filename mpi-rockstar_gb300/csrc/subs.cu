@@ -1053,6 +1053,21 @@ __global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_
     }
 }
 
+// Batched form: the records of every node grouped by label with one stable
+// radix sort on (node start, label + 1); records outside the level's nodes
+// keep their places.  (The plain form reproduces the reference's recursive
+// midpoint partition instead, whose record order the reference's later
+// sampling depends on.)
+__global__ void k_lsort_keys(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
+                             const int32_t *lab, uint64_t *key, uint32_t *val) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    uint64_t hi = (k >= 0) ? (uint64_t)N.start[base + k] : (uint64_t)i;
+    key[i] = (hi << 32) | (uint64_t)(uint32_t)(k >= 0 ? lab[i] + 1 : 0);
+    val[i] = (uint32_t)i;
+}
+
 // Regroup keys for reassign_halo_particles (src/groupies.c:316-331) and the
 // core sort of src/fun_times.c:204-227 (by squared distance to the halo).
 __global__ void k_halokeys(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
@@ -1435,6 +1450,30 @@ static void sort_pairs(Arena &ar, K *k, K *k2, V *v, V *v2, int64_t n, int bits,
     RSG_CHECK_LAUNCH();
     ar.used = m;
 }
+static void label_sort_stable(Arena &ar, Rec *W, int32_t *lab, const int32_t *eln, HierNodes N,
+                              int32_t base, int64_t M, cudaStream_t st) {
+    const int T = 256;
+    size_t mark = ar.used;
+    uint64_t *k1 = ar.get<uint64_t>(M), *k2 = ar.get<uint64_t>(M);
+    uint32_t *v1 = ar.get<uint32_t>(M), *v2 = ar.get<uint32_t>(M);
+    Rec *wt = ar.get<Rec>(M);
+    int32_t *lt = ar.get<int32_t>(M);
+    launch(k_lsort_keys, nblk(M, T), T, 0, st, eln, M, N, base, (const int32_t *)lab, k1, v1);
+    int bits = 33;
+    while (bits < 64 && (1ll << (bits - 32)) <= M) bits++;
+    size_t b = 0;
+    RSG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, b, k1, k2, v1, v2, (int)M, 0, bits, st));
+    void *t = ar.take(b + 256);
+    RSG_CUDA(cub::DeviceRadixSort::SortPairs(t, b, k1, k2, v1, v2, (int)M, 0, bits, st));
+    launch(k_gather<Rec>, nblk(M, T), T, 0, st, (const Rec *)W, (const uint32_t *)v2, M, wt);
+    launch(k_gather<int32_t>, nblk(M, T), T, 0, st, (const int32_t *)lab, (const uint32_t *)v2, M,
+           lt);
+    RSG_CUDA(cudaMemcpyAsync(W, wt, sizeof(Rec) * M, cudaMemcpyDeviceToDevice, st));
+    RSG_CUDA(cudaMemcpyAsync(lab, lt, sizeof(int32_t) * M, cudaMemcpyDeviceToDevice, st));
+    RSG_CHECK_LAUNCH();
+    ar.used = mark;
+}
+
 template <class T>
 static int32_t excl_scan(Arena &ar, const T *in, T *out, int32_t n, cudaStream_t st) {
     size_t b = 0;
@@ -1658,7 +1697,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         }
         RSG_CHECK_LAUNCH();
         phase_mark(st, "d.replay");
-        partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
+        if (exact) partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
+        else label_sort_stable(ar, W, phalo, eln, N, base, M, st);
         phase_mark(st, "d.psort");
         launch(k_run_heads, nblk(M, T), T, 0, st, eln, M, N, base, phalo, hflag);
         int32_t *heads = ar.get<int32_t>(M);
@@ -1732,13 +1772,15 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
         launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
         RSG_CHECK_LAUNCH();
-        {
+        if (exact) {
             // reassign_halo_particles: the reference's partition by halo index
             std::vector<int32_t> hs(cnt), hn(cnt);
             RSG_CUDA(cudaMemcpyAsync(hn.data(), N.n + base, 4 * cnt, cudaMemcpyDeviceToHost, st));
             RSG_CUDA(cudaMemcpyAsync(hs.data(), N.start + base, 4 * cnt, cudaMemcpyDeviceToHost, st));
             RSG_CUDA(cudaStreamSynchronize(st));
             partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
+        } else {
+            label_sort_stable(ar, W, phalo, eln, N, base, M, st);
         }
         phase_mark(st, "a.reassign");
         launch(k_halo_heads, nblk(M, T), T, 0, st, eln, M, N, base, phalo, H);
