@@ -224,6 +224,92 @@ __global__ void __launch_bounds__(256) k_norm_blk(Rec *W, HierNodes N, int32_t b
     if (threadIdx.x == 0) norm_sigmas(corr, level0, ims, sig + 2 * k);
 }
 
+// Batched form, nodes above RSG_SMALL particles: cut into chunks of
+// RSG_NCH records, one block per chunk; per-chunk partial sums are added per
+// node in chunk order (deterministic).
+#define RSG_NCH 4096
+struct NChunk {
+    int32_t node, start, n, pad;  // node: level-local index
+};
+struct NPart {
+    double d[21];
+};
+__global__ void k_nch_count(HierNodes N, int32_t base, int32_t cnt, int32_t *nch) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > cnt) return;
+    int n = (k < cnt) ? N.n[base + k] : 0;
+    nch[k] = (n > RSG_SMALL) ? (n + RSG_NCH - 1) / RSG_NCH : 0;
+}
+__global__ void k_nch_fill(HierNodes N, int32_t base, int32_t cnt, const int32_t *nch,
+                           const int32_t *c0, NChunk *C) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cnt) return;
+    int s = N.start[base + k], n = N.n[base + k];
+    for (int c = 0; c < nch[k]; c++) {
+        NChunk x;
+        x.node = k;
+        x.start = s + c * RSG_NCH;
+        x.n = min(RSG_NCH, n - c * RSG_NCH);
+        x.pad = 0;
+        C[c0[k] + c] = x;
+    }
+}
+__global__ void __launch_bounds__(256) k_nch_sum6(const Rec *W, const NChunk *C, NPart *P) {
+    __shared__ double sm[40];
+    NChunk c = C[blockIdx.x];
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < c.n; i += blockDim.x)
+        for (int d = 0; d < 6; d++) a[d] += (double)W[c.start + i].pos[d];
+    for (int d = 0; d < 6; d++) {
+        double t = block_sum_d(a[d], sm);
+        if (threadIdx.x == 0) P[blockIdx.x].d[d] = t;
+    }
+}
+__global__ void k_nch_mean(HierNodes N, int32_t base, int32_t cnt, const int32_t *nch,
+                           const int32_t *c0, const NPart *P, double *mean) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cnt || nch[k] == 0) return;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = c0[k]; c < c0[k] + nch[k]; c++)
+        for (int d = 0; d < 6; d++) a[d] += P[c].d[d];
+    for (int d = 0; d < 6; d++) mean[6 * k + d] = a[d] / (double)N.n[base + k];
+}
+__global__ void __launch_bounds__(256) k_nch_mom(Rec *W, const NChunk *C, const double *mean,
+                                                 NPart *P) {
+    __shared__ double sm[40];
+    NChunk c = C[blockIdx.x];
+    double mu[6];
+    for (int d = 0; d < 6; d++) mu[d] = mean[6 * c.node + d];
+    double cc[21];
+    for (int j = 0; j < 21; j++) cc[j] = 0;
+    for (int i = threadIdx.x; i < c.n; i += blockDim.x) {
+        float q[6];
+        for (int d = 0; d < 6; d++) {
+            q[d] = __double2float_rn((double)W[c.start + i].pos[d] - mu[d]);
+            W[c.start + i].pos[d] = q[d];
+        }
+        int j = 0;
+        for (int x = 0; x < 6; x++)
+            for (int y = x; y < 6; y++) cc[j++] += (double)fmul(q[x], q[y]);
+    }
+    for (int j = 0; j < 21; j++) {
+        double t = block_sum_d(cc[j], sm);
+        if (threadIdx.x == 0) P[blockIdx.x].d[j] = t;
+    }
+}
+__global__ void k_nch_fin(HierNodes N, int32_t base, int32_t cnt, const int32_t *nch,
+                          const int32_t *c0, const NPart *P, int level0, double ims,
+                          double *sig) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= cnt || nch[k] == 0) return;
+    double cc[21];
+    for (int j = 0; j < 21; j++) cc[j] = 0;
+    for (int c = c0[k]; c < c0[k] + nch[k]; c++)
+        for (int j = 0; j < 21; j++) cc[j] += P[c].d[j];
+    for (int j = 0; j < 21; j++) cc[j] /= (double)N.n[base + k];
+    norm_sigmas(cc, level0, ims, sig + 2 * k);
+}
+
 // Larger nodes: one block, deterministic tree reductions.
 __global__ void k_norm_par(Rec *W, HierNodes N, int32_t base, int level0, double ims,
                            double *sig, int seq_max) {
@@ -261,16 +347,17 @@ __global__ void k_norm_par(Rec *W, HierNodes N, int32_t base, int level0, double
     if (threadIdx.x == 0) norm_sigmas(corr, level0, ims, sig + 2 * k);
 }
 
-// Divide by the dispersions unless one of them is zero (src/groupies.c:825-829).
-__global__ void k_norm_div(Rec *W, HierNodes N, int32_t base, const double *sig) {
-    int k = blockIdx.x;
-    int node = base + k;
-    int s = N.start[node], n = N.n[node];
+// Divide by the dispersions unless one of them is zero (src/groupies.c:825-829),
+// one thread per record.
+__global__ void k_norm_div_el(Rec *W, int64_t M, const int32_t *eln, const double *sig) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    if (k < 0) return;
     double sx = sig[2 * k], sv = sig[2 * k + 1];
     if (!sx || !sv) return;
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-        for (int d = 0; d < 6; d++)
-            W[s + i].pos[d] = __double2float_rn((double)W[s + i].pos[d] / (d < 3 ? sx : sv));
+    for (int d = 0; d < 6; d++)
+        W[i].pos[d] = __double2float_rn((double)W[i].pos[d] / (d < 3 ? sx : sv));
 }
 
 // x advanced by m steps of rand_r's generator (x <- 1103515245 x + 12345
@@ -476,6 +563,59 @@ __global__ void k_target_smem(HierNodes N, int32_t base, const int32_t *soff, co
     for (int i = threadIdx.x; i < nt; i += blockDim.x) a_s[i] = a[i];
     __syncthreads();
     if (threadIdx.x == 0) N.target_r[node] = median_r(a_s, nt, seed_in[k], frac);
+}
+// Batched form: the sample's floor(nt * FOF_FRACTION)-th smallest distance by
+// an 8-bit-per-pass radix select on the distances' order-preserving bit
+// patterns, in shared memory, one block per node.  This is the exact order
+// statistic; the reference's quickselect returns the same value except when
+// its early exit (equal first and last elements of the range) fires on a
+// range that is not constant.
+__global__ void __launch_bounds__(256) k_target_rs(HierNodes N, int32_t base, const int32_t *soff,
+                                                   const float *prad, float frac, int exact) {
+    extern __shared__ unsigned ks[];
+    __shared__ int hist[256];
+    __shared__ unsigned pre_s;
+    __shared__ int rank_s;
+    int k = blockIdx.x;
+    int node = base + k;
+    int n = N.n[node];
+    int nt = exact ? n : (n < 10000 ? n : 10000);
+    if (nt > RSG_TARGET_SMEM || nt < 1) return;
+    const float *a = prad + soff[k];
+    if (nt < 2) {
+        if (threadIdx.x == 0) N.target_r[node] = a[0];
+        return;
+    }
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) ks[i] = f2ord(a[i]);
+    int64_t kk = (int64_t)__float2ll_rz(fmul(__ll2float_rn(nt), frac));
+    if (kk > nt - 1) kk = nt - 1;
+    if (threadIdx.x == 0) {
+        pre_s = 0;
+        rank_s = (int)kk;
+    }
+    unsigned mask = 0;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        hist[threadIdx.x] = 0;
+        __syncthreads();
+        unsigned pre = pre_s;
+        for (int i = threadIdx.x; i < nt; i += blockDim.x)
+            if ((ks[i] & mask) == pre) atomicAdd(&hist[(ks[i] >> shift) & 255u], 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int cum = 0, rank = rank_s;
+            for (int b = 0; b < 256; b++) {
+                if (cum + hist[b] > rank) {
+                    pre_s = pre | ((unsigned)b << shift);
+                    rank_s = rank - cum;
+                    break;
+                }
+                cum += hist[b];
+            }
+        }
+        mask |= 255u << shift;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) N.target_r[node] = ord2f(pre_s);
 }
 // Larger samples (EXACT_LL_CALC): in place in global memory.
 __global__ void k_target(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
@@ -1207,8 +1347,23 @@ __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, co
             dx = fsub(c0, W[ps + i].pos[0]); ds = fadd(ds, fmul(dx, dx));
             dx = fsub(c1, W[ps + i].pos[1]); ds = fadd(ds, fmul(dx, dx));
             dx = fsub(c2, W[ps + i].pos[2]); ds = fadd(ds, fmul(dx, dx));
-            int64_t b = (int64_t)(sqrt((double)ds) * (double)rsc);
-            if (b < 50) atomicAdd(&bins[b], 1);
+            // b = (int64_t)(sqrt((double)ds) * rsc) as the reference computes it.  The
+            // FP32 estimate is within 2e-5 of that product (below 50 bins), so it
+            // decides b unless it lies within 1e-4 of a bin edge; then the FP64
+            // expression is evaluated.
+            float bf = sqrtf(ds) * rsc;
+            int key = -1;  // bin, or -1 past the last one
+            if (bf < 60.f) {
+                float fr = bf - floorf(bf);
+                int64_t b = (fr < 1e-4f || fr > 1.f - 1e-4f)
+                                ? (int64_t)(sqrt((double)ds) * (double)rsc)
+                                : (int64_t)bf;
+                if (b < 50) key = (int)b;
+            }
+            // lanes with the same bin add once (shared-memory atomics on 50 bins
+            // would otherwise serialise)
+            unsigned peers = __match_any_sync(__activemask(), key);
+            if (key >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&bins[key], __popc(peers));
         }
     }
     __syncthreads();
@@ -1604,6 +1759,9 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             throw Failure();
         }
         size_t mark = ar.used;
+        // element -> node of this level
+        RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
+        launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
         {
             double *sig = ar.get<double>(2 * (int64_t)cnt);
             if (exact)
@@ -1614,9 +1772,30 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                        L == 0, cfg.initial_metric_scaling, sig);
             launch(k_norm_blk, cnt, 256, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig,
                    seq_max);
-            launch(k_norm_par, cnt, T, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig,
-                   seq_max);
-            launch(k_norm_div, cnt, T, 0, st, W, N, base, sig);
+            if (exact) {
+                launch(k_norm_par, cnt, T, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling,
+                       sig, seq_max);
+            } else {
+                int32_t *nch = ar.get<int32_t>(cnt + 1), *c0 = ar.get<int32_t>(cnt + 1);
+                launch(k_nch_count, nblk(cnt + 1, T), T, 0, st, N, base, cnt, nch);
+                int32_t nc = excl_scan(ar, (const int32_t *)nch, c0, cnt + 1, st);
+                if (nc > 0) {
+                    NChunk *C = ar.get<NChunk>(nc);
+                    NPart *P = ar.get<NPart>(nc);
+                    double *mean = ar.get<double>(6 * (int64_t)cnt);
+                    launch(k_nch_fill, nblk(cnt, T), T, 0, st, N, base, cnt, (const int32_t *)nch,
+                           (const int32_t *)c0, C);
+                    launch(k_nch_sum6, nc, 256, 0, st, (const Rec *)W, (const NChunk *)C, P);
+                    launch(k_nch_mean, nblk(cnt, T), T, 0, st, N, base, cnt, (const int32_t *)nch,
+                           (const int32_t *)c0, (const NPart *)P, mean);
+                    launch(k_nch_mom, nc, 256, 0, st, W, (const NChunk *)C, (const double *)mean, P);
+                    launch(k_nch_fin, nblk(cnt, T), T, 0, st, N, base, cnt, (const int32_t *)nch,
+                           (const int32_t *)c0, (const NPart *)P, L == 0,
+                           cfg.initial_metric_scaling, sig);
+                }
+            }
+            launch(k_norm_div_el, nblk(M, T), T, 0, st, W, M, (const int32_t *)eln,
+                   (const double *)sig);
             RSG_CHECK_LAUNCH();
         }
         phase_mark(st, "d.norm_sd");
@@ -1656,15 +1835,18 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                 int nt = cfg.exact_ll_calc ? hn[k] : (hn[k] < 10000 ? hn[k] : 10000);
                 if (nt <= RSG_TARGET_SMEM && nt > ntmax) ntmax = nt;
             }
-            launch(k_target_smem, cnt, 64, (size_t)4 * (ntmax > 0 ? ntmax : 1), st, N, base,
-                   (const int32_t *)soff, (const float *)prad, (const unsigned *)seeds,
-                   (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
+            if (exact)
+                launch(k_target_smem, cnt, 64, (size_t)4 * (ntmax > 0 ? ntmax : 1), st, N, base,
+                       (const int32_t *)soff, (const float *)prad, (const unsigned *)seeds,
+                       (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
+            else
+                launch(k_target_rs, cnt, 256, (size_t)4 * (ntmax > 0 ? ntmax : 1), st, N, base,
+                       (const int32_t *)soff, (const float *)prad, (float)cfg.fof_fraction,
+                       (int)cfg.exact_ll_calc);
             launch(k_target, nblk(cnt, 32), 32, 0, st, N, base, cnt, soff, prad, seeds,
                    (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
         }
         phase_mark(st, "d.nn_target");
-        RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
-        launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
         if (exact) {
             // later neighbours within target_r, as CSR lists
             int32_t *ncnt = par, *noff = root;
@@ -1792,11 +1974,11 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         int32_t *glv = ar.get<int32_t>(ngr + 1), *gnode = ar.get<int32_t>(ngr + 1);
         launch(k_list_growing, nblk(cnt, T), T, 0, st, N, base, cnt, goffs, glist, glv);
         launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, goffs, gnode);
-        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc, seq_max);
+        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc, exact ? seq_max : 0);
         launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 0);
         launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E);
         launch(k_fix_parents, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
-        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc, seq_max);
+        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc, exact ? seq_max : 0);
         RSG_CHECK_LAUNCH();
         phase_mark(st, "a.props_parents");
         if (L == 0) {
@@ -1806,7 +1988,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             int32_t *alist = ar.get<int32_t>(na + 1), *anode = ar.get<int32_t>(na + 1);
             launch(k_list_all, nblk(cnt, T), T, 0, st, N, base, cnt, aoff, alist);
             launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, aoff, anode);
-            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc, seq_max);
+            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc, exact ? seq_max : 0);
             launch(k_corekeys, nblk(M, T), T, 0, st, W, eln, M, phalo, H, key, val);
             sort_pairs(ar, key, key2, val, val2, M, keybits, st);
             launch(k_gather<Rec>, nblk(M, T), T, 0, st, W, val2, M, W2);
@@ -1820,7 +2002,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             // find_subs tail (src/groupies.c:697-703): child counts and basic
             // properties for every halo, then the additional properties.
             launch(k_num_child, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
-            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc, seq_max);
+            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc, exact ? seq_max : 0);
             RSG_CHECK_LAUNCH();
         }
         ar.used = mark;
