@@ -1243,16 +1243,82 @@ __global__ void k_halo_tails(const int32_t *eln, int64_t M, HierNodes N, int32_t
     if (i == s + n - 1 || phalo[i] != phalo[i + 1]) H[phalo[i]].num_p = i + 1 - H[phalo[i]].p_start;
 }
 
+// The halo fields of calc_basic_halo_props from the mean and the summed
+// squared deviations (src/properties.c:88-125); returns whether the Vmax
+// histogram is built and its scale.
+__device__ void basic_decide(rsg_halo &hh, const double *mean, const double *p2, int np,
+                             const DevCfg *C, int *do_bins, float *rsc_out) {
+    hh.r = hh.vrms = 0;
+    for (int k = 0; k < 6; k++) {
+        if (k < 3) hh.r = (float)((double)hh.r + p2[k] / (double)np);
+        else hh.vrms = (float)((double)hh.vrms + p2[k] / (double)np);
+    }
+    double pe = (double)hh.r / (double)np, ve = (double)hh.vrms / (double)np;
+    if ((!hh.min_pos_err) || ((double)hh.min_pos_err > pe)) {
+        hh.min_pos_err = (float)pe;
+        hh.n_core = hh.num_p;
+        for (int k = 0; k < 3; k++) hh.pos[k] = (float)mean[k];
+    }
+    if ((!hh.min_vel_err) || ((double)hh.min_vel_err > ve)) {
+        hh.min_vel_err = (float)ve;
+        for (int k = 3; k < 6; k++) hh.pos[k] = (float)mean[k];
+    }
+    for (int k = 3; k < 6; k++) hh.bulkvel[k - 3] = (float)mean[k];
+    hh.m = (float)hh.num_p;
+    if (!hh.num_child_particles) hh.num_child_particles = hh.num_p;
+    hh.r = (float)cbrt((double)hh.num_p / ((4.0 * M_PI / 3.0) * C->rvir_dens));
+    hh.child_r = (float)cbrt((double)hh.num_child_particles / ((4.0 * M_PI / 3.0) * C->rvir_dens));
+    hh.vmax = hh.vmax_r = 0;
+    *do_bins = (hh.child_r > 0);
+    *rsc_out = (float)(50.0 / (double)hh.child_r);
+}
+// The Vmax histogram bin of one particle at squared distance ds:
+// (int64_t)(sqrt((double)ds) * rsc) as the reference computes it, or -1 past
+// bin 49.  The FP32 estimate is within 2e-5 of that product below 60, so it
+// decides the bin unless it lies within 1e-4 of a bin edge; then the FP64
+// expression is evaluated.
+__device__ __forceinline__ int vmax_bin(float ds, float rsc) {
+    float bf = sqrtf(ds) * rsc;
+    if (!(bf < 60.f)) return -1;
+    float fr = bf - floorf(bf);
+    int64_t b = (fr < 1e-4f || fr > 1.f - 1e-4f) ? (int64_t)(sqrt((double)ds) * (double)rsc)
+                                                  : (int64_t)bf;
+    return (b < 50) ? (int)b : -1;
+}
+// Vmax and Rvmax from the 50-bin mass histogram (src/properties.c:39-69), then
+// the final radius and vrms of calc_basic_halo_props.
+__device__ void basic_vmax(rsg_halo &hh, const int *bins, int do_bins, float rsc_s,
+                           const DevCfg *C) {
+    if (do_bins) {
+        float rsc = rsc_s, vm = 0.f;
+        int64_t tp = 0;
+        for (int i = 0; i < 50; i++) {
+            float r = (float)((i + 1.0) / (double)rsc);
+            if ((double)r < C->force_res) r = (float)C->force_res;
+            tp += bins[i];
+            float vc = __fdiv_rn(__ll2float_rn(tp), r);
+            if (vc > vm) vm = vc;
+        }
+        float sn = (float)C->scale_now;
+        float v = (float)sqrt(RSG_GC * (double)vm * C->particle_mass / (double)sn);
+        hh.vmax = v;
+        hh.vmax_r = (float)(sqrt((double)sn) * (double)v * C->dyn_time);
+    }
+    if (hh.vmax_r) hh.r = hh.vmax_r;
+    hh.vrms = (float)sqrt((double)hh.vrms);
+}
+
 // calc_basic_halo_props + estimate_vmax (src/properties.c:39-125); one
 // block per listed halo.
 __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, const DevCfg *C,
-                              int seq_max) {
+                              int seq_max, int big) {
     __shared__ double sm[40];
     __shared__ double mean[6], p2[6];
     __shared__ int bins[50];
     int h = list[blockIdx.x];
     rsg_halo &hh = H[h];
     int ps = (int)hh.p_start, np = (int)hh.num_p;
+    if (np > big) return;  // chunked path (batched form)
     if (np <= seq_max) {
         // in array order (src/properties.c:76-87): the block stages values,
         // thread 0 adds them
@@ -1314,29 +1380,11 @@ __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, co
     __shared__ int do_bins;
     __syncthreads();
     if (threadIdx.x == 0) {
-        hh.r = hh.vrms = 0;
-        for (int k = 0; k < 6; k++) {
-            if (k < 3) hh.r = (float)((double)hh.r + p2[k] / (double)np);
-            else hh.vrms = (float)((double)hh.vrms + p2[k] / (double)np);
-        }
-        double pe = (double)hh.r / (double)np, ve = (double)hh.vrms / (double)np;
-        if ((!hh.min_pos_err) || ((double)hh.min_pos_err > pe)) {
-            hh.min_pos_err = (float)pe;
-            hh.n_core = hh.num_p;
-            for (int k = 0; k < 3; k++) hh.pos[k] = (float)mean[k];
-        }
-        if ((!hh.min_vel_err) || ((double)hh.min_vel_err > ve)) {
-            hh.min_vel_err = (float)ve;
-            for (int k = 3; k < 6; k++) hh.pos[k] = (float)mean[k];
-        }
-        for (int k = 3; k < 6; k++) hh.bulkvel[k - 3] = (float)mean[k];
-        hh.m = (float)hh.num_p;
-        if (!hh.num_child_particles) hh.num_child_particles = hh.num_p;
-        hh.r = (float)cbrt((double)hh.num_p / ((4.0 * M_PI / 3.0) * C->rvir_dens));
-        hh.child_r = (float)cbrt((double)hh.num_child_particles / ((4.0 * M_PI / 3.0) * C->rvir_dens));
-        hh.vmax = hh.vmax_r = 0;
-        do_bins = (hh.child_r > 0);
-        rsc_s = (float)(50.0 / (double)hh.child_r);
+        int db;
+        float rs;
+        basic_decide(hh, mean, p2, np, C, &db, &rs);
+        do_bins = db;
+        rsc_s = rs;
     }
     __syncthreads();
     if (do_bins) {
@@ -1347,19 +1395,7 @@ __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, co
             dx = fsub(c0, W[ps + i].pos[0]); ds = fadd(ds, fmul(dx, dx));
             dx = fsub(c1, W[ps + i].pos[1]); ds = fadd(ds, fmul(dx, dx));
             dx = fsub(c2, W[ps + i].pos[2]); ds = fadd(ds, fmul(dx, dx));
-            // b = (int64_t)(sqrt((double)ds) * rsc) as the reference computes it.  The
-            // FP32 estimate is within 2e-5 of that product (below 50 bins), so it
-            // decides b unless it lies within 1e-4 of a bin edge; then the FP64
-            // expression is evaluated.
-            float bf = sqrtf(ds) * rsc;
-            int key = -1;  // bin, or -1 past the last one
-            if (bf < 60.f) {
-                float fr = bf - floorf(bf);
-                int64_t b = (fr < 1e-4f || fr > 1.f - 1e-4f)
-                                ? (int64_t)(sqrt((double)ds) * (double)rsc)
-                                : (int64_t)bf;
-                if (b < 50) key = (int)b;
-            }
+            int key = vmax_bin(ds, rsc);
             // lanes with the same bin add once (shared-memory atomics on 50 bins
             // would otherwise serialise)
             unsigned peers = __match_any_sync(__activemask(), key);
@@ -1367,25 +1403,114 @@ __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, co
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        if (do_bins) {
-            float rsc = rsc_s, vm = 0.f;
-            int64_t tp = 0;
-            for (int i = 0; i < 50; i++) {
-                float r = (float)((i + 1.0) / (double)rsc);
-                if ((double)r < C->force_res) r = (float)C->force_res;
-                tp += bins[i];
-                float vc = __fdiv_rn(__ll2float_rn(tp), r);
-                if (vc > vm) vm = vc;
-            }
-            float sn = (float)C->scale_now;
-            float v = (float)sqrt(RSG_GC * (double)vm * C->particle_mass / (double)sn);
-            hh.vmax = v;
-            hh.vmax_r = (float)(sqrt((double)sn) * (double)v * C->dyn_time);
-        }
-        if (hh.vmax_r) hh.r = hh.vmax_r;
-        hh.vrms = (float)sqrt((double)hh.vrms);
+    if (threadIdx.x == 0) basic_vmax(hh, bins, do_bins, rsc_s, C);
+}
+
+// Batched form, halos above RSG_BP_BIG particles: calc_basic_halo_props over
+// chunks of RSG_BP_CH particles, one block per chunk per pass; the partial
+// sums and histograms are added per halo in chunk order (deterministic).
+#define RSG_BP_BIG 16384
+#define RSG_BP_CH 4096
+struct BPChunk {
+    int32_t t, start, n, pad;  // t: entry of the halo list
+};
+struct BPPart {
+    double d[6];
+    int bins[50];
+};
+__global__ void k_bp_nch(const rsg_halo *H, const int32_t *list, int32_t nl, int32_t *nch) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > nl) return;
+    int np = (t < nl) ? (int)H[list[t]].num_p : 0;
+    nch[t] = (np > RSG_BP_BIG) ? (np + RSG_BP_CH - 1) / RSG_BP_CH : 0;
+}
+__global__ void k_bp_fill(const rsg_halo *H, const int32_t *list, int32_t nl, const int32_t *nch,
+                          const int32_t *c0, BPChunk *C) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl) return;
+    const rsg_halo &hh = H[list[t]];
+    int ps = (int)hh.p_start, np = (int)hh.num_p;
+    for (int c = 0; c < nch[t]; c++) {
+        BPChunk x;
+        x.t = t;
+        x.start = ps + c * RSG_BP_CH;
+        x.n = min(RSG_BP_CH, np - c * RSG_BP_CH);
+        x.pad = 0;
+        C[c0[t] + c] = x;
     }
+}
+__global__ void __launch_bounds__(256) k_bp_sum6(const Rec *W, const BPChunk *C,
+                                                 const double *mean, BPPart *P) {
+    __shared__ double sm[40];
+    BPChunk c = C[blockIdx.x];
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < c.n; i += blockDim.x)
+        for (int d = 0; d < 6; d++) {
+            double x = (double)W[c.start + i].pos[d];
+            if (mean) {  // second pass: squared deviations
+                x -= mean[6 * c.t + d];
+                x *= x;
+            }
+            a[d] += x;
+        }
+    for (int d = 0; d < 6; d++) {
+        double t = block_sum_d(a[d], sm);
+        if (threadIdx.x == 0) P[blockIdx.x].d[d] = t;
+    }
+}
+__global__ void k_bp_mean(const rsg_halo *H, const int32_t *list, int32_t nl, const int32_t *nch,
+                          const int32_t *c0, const BPPart *P, double *mean) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl || nch[t] == 0) return;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = c0[t]; c < c0[t] + nch[t]; c++)
+        for (int d = 0; d < 6; d++) a[d] += P[c].d[d];
+    for (int d = 0; d < 6; d++) mean[6 * t + d] = a[d] / (double)H[list[t]].num_p;
+}
+__global__ void k_bp_decide(rsg_halo *H, const int32_t *list, int32_t nl, const int32_t *nch,
+                            const int32_t *c0, const BPPart *P, const double *mean,
+                            const DevCfg *C, int *dob, float *rsc) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl || nch[t] == 0) return;
+    double p2[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = c0[t]; c < c0[t] + nch[t]; c++)
+        for (int d = 0; d < 6; d++) p2[d] += P[c].d[d];
+    rsg_halo &hh = H[list[t]];
+    basic_decide(hh, mean + 6 * t, p2, (int)hh.num_p, C, &dob[t], &rsc[t]);
+}
+__global__ void __launch_bounds__(256) k_bp_hist(const Rec *W, const BPChunk *C,
+                                                 const rsg_halo *H, const int32_t *list,
+                                                 const int *dob, const float *rsc, BPPart *P) {
+    __shared__ int bins[50];
+    BPChunk c = C[blockIdx.x];
+    if (threadIdx.x < 50) bins[threadIdx.x] = 0;
+    __syncthreads();
+    if (dob[c.t]) {
+        const rsg_halo &hh = H[list[c.t]];
+        float r = rsc[c.t], c0 = hh.pos[0], c1 = hh.pos[1], c2 = hh.pos[2];
+        for (int i = threadIdx.x; i < c.n; i += blockDim.x) {
+            float dx, ds = 0.f;
+            dx = fsub(c0, W[c.start + i].pos[0]); ds = fadd(ds, fmul(dx, dx));
+            dx = fsub(c1, W[c.start + i].pos[1]); ds = fadd(ds, fmul(dx, dx));
+            dx = fsub(c2, W[c.start + i].pos[2]); ds = fadd(ds, fmul(dx, dx));
+            int key = vmax_bin(ds, r);
+            unsigned peers = __match_any_sync(__activemask(), key);
+            if (key >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&bins[key], __popc(peers));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 50) P[blockIdx.x].bins[threadIdx.x] = bins[threadIdx.x];
+}
+__global__ void k_bp_vmax(rsg_halo *H, const int32_t *list, int32_t nl, const int32_t *nch,
+                          const int32_t *c0, const BPPart *P, const int *dob, const float *rsc,
+                          const DevCfg *C) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nl || nch[t] == 0) return;
+    int bins[50];
+    for (int b = 0; b < 50; b++) bins[b] = 0;
+    for (int c = c0[t]; c < c0[t] + nch[t]; c++)
+        for (int b = 0; b < 50; b++) bins[b] += P[c].bins[b];
+    basic_vmax(H[list[t]], bins, dob[t], rsc[t], C);
 }
 
 // growing-halo list of a level: node glist entries concatenated
@@ -1605,6 +1730,45 @@ static void sort_pairs(Arena &ar, K *k, K *k2, V *v, V *v2, int64_t n, int bits,
     RSG_CHECK_LAUNCH();
     ar.used = m;
 }
+static int32_t excl_scan_i32(Arena &ar, const int32_t *in, int32_t *out, int32_t n,
+                             cudaStream_t st);
+
+// calc_basic_halo_props for the listed halos: one block per halo, and in the
+// batched form the chunked passes for halos above RSG_BP_BIG particles.
+static void basic_props(Arena &ar, const Rec *W, rsg_halo *H, const int32_t *list, int32_t nl,
+                        const DevCfg *d_dc, int seq_max, int exact, cudaStream_t st) {
+    const int T = 256;
+    if (nl <= 0) return;
+    launch(k_basic_props, nl, T, 0, st, W, H, list, d_dc, exact ? seq_max : 0,
+           exact ? 0x7fffffff : RSG_BP_BIG);
+    if (exact) return;
+    size_t mark = ar.used;
+    int32_t *nch = ar.get<int32_t>(nl + 1), *c0 = ar.get<int32_t>(nl + 1);
+    launch(k_bp_nch, nblk(nl + 1, T), T, 0, st, (const rsg_halo *)H, list, nl, nch);
+    int32_t nc = excl_scan_i32(ar, nch, c0, nl + 1, st);
+    if (nc > 0) {
+        BPChunk *C = ar.get<BPChunk>(nc);
+        BPPart *P = ar.get<BPPart>(nc);
+        double *mean = ar.get<double>(6 * (int64_t)nl);
+        int *dob = ar.get<int>(nl);
+        float *rsc = ar.get<float>(nl);
+        launch(k_bp_fill, nblk(nl, T), T, 0, st, (const rsg_halo *)H, list, nl,
+               (const int32_t *)nch, (const int32_t *)c0, C);
+        launch(k_bp_sum6, nc, 256, 0, st, W, (const BPChunk *)C, (const double *)nullptr, P);
+        launch(k_bp_mean, nblk(nl, T), T, 0, st, (const rsg_halo *)H, list, nl,
+               (const int32_t *)nch, (const int32_t *)c0, (const BPPart *)P, mean);
+        launch(k_bp_sum6, nc, 256, 0, st, W, (const BPChunk *)C, (const double *)mean, P);
+        launch(k_bp_decide, nblk(nl, T), T, 0, st, H, list, nl, (const int32_t *)nch,
+               (const int32_t *)c0, (const BPPart *)P, (const double *)mean, d_dc, dob, rsc);
+        launch(k_bp_hist, nc, 256, 0, st, W, (const BPChunk *)C, (const rsg_halo *)H, list,
+               (const int *)dob, (const float *)rsc, P);
+        launch(k_bp_vmax, nblk(nl, T), T, 0, st, H, list, nl, (const int32_t *)nch,
+               (const int32_t *)c0, (const BPPart *)P, (const int *)dob, (const float *)rsc, d_dc);
+    }
+    RSG_CHECK_LAUNCH();
+    ar.used = mark;
+}
+
 static void label_sort_stable(Arena &ar, Rec *W, int32_t *lab, const int32_t *eln, HierNodes N,
                               int32_t base, int64_t M, cudaStream_t st) {
     const int T = 256;
@@ -1642,6 +1806,10 @@ static int32_t excl_scan(Arena &ar, const T *in, T *out, int32_t n, cudaStream_t
     RSG_CUDA(cudaMemcpyAsync(&last, out + n - 1, sizeof(T), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     return (int32_t)last;
+}
+static int32_t excl_scan_i32(Arena &ar, const int32_t *in, int32_t *out, int32_t n,
+                             cudaStream_t st) {
+    return excl_scan(ar, in, out, n, st);
 }
 static int32_t select_flagged(Arena &ar, const int32_t *flag, int32_t *out, int64_t n,
                               int32_t first, cudaStream_t st) {
@@ -1974,11 +2142,11 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         int32_t *glv = ar.get<int32_t>(ngr + 1), *gnode = ar.get<int32_t>(ngr + 1);
         launch(k_list_growing, nblk(cnt, T), T, 0, st, N, base, cnt, goffs, glist, glv);
         launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, goffs, gnode);
-        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc, exact ? seq_max : 0);
+        basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
         launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 0);
         launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E);
         launch(k_fix_parents, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
-        if (ngr) launch(k_basic_props, ngr, T, 0, st, W, H, glv, d_dc, exact ? seq_max : 0);
+        basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
         RSG_CHECK_LAUNCH();
         phase_mark(st, "a.props_parents");
         if (L == 0) {
@@ -1988,7 +2156,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             int32_t *alist = ar.get<int32_t>(na + 1), *anode = ar.get<int32_t>(na + 1);
             launch(k_list_all, nblk(cnt, T), T, 0, st, N, base, cnt, aoff, alist);
             launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, aoff, anode);
-            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc, exact ? seq_max : 0);
+            basic_props(ar, W, H, alist, na, d_dc, seq_max, exact, st);
             launch(k_corekeys, nblk(M, T), T, 0, st, W, eln, M, phalo, H, key, val);
             sort_pairs(ar, key, key2, val, val2, M, keybits, st);
             launch(k_gather<Rec>, nblk(M, T), T, 0, st, W, val2, M, W2);
@@ -2002,7 +2170,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             // find_subs tail (src/groupies.c:697-703): child counts and basic
             // properties for every halo, then the additional properties.
             launch(k_num_child, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
-            if (na) launch(k_basic_props, na, T, 0, st, W, H, alist, d_dc, exact ? seq_max : 0);
+            basic_props(ar, W, H, alist, na, d_dc, seq_max, exact, st);
             RSG_CHECK_LAUNCH();
         }
         ar.used = mark;
