@@ -239,7 +239,7 @@ class DevicePath:
         self.n = n
         self.batched = 1 if batched else 0
         self.st = setup_config(cfg)
-        self.halo_cap = halo_cap or (n // 4 + 1024)
+        self.halo_cap = halo_cap or (n // 16 + 65536)
         self.out = torch.empty(n * PARTICLE.itemsize, dtype=torch.uint8, device="cuda")
         self.halos = torch.empty(self.halo_cap * HALO.itemsize, dtype=torch.uint8, device="cuda")
         self.extra = torch.empty(self.halo_cap * EXTRA.itemsize, dtype=torch.uint8, device="cuda")

@@ -56,6 +56,7 @@ struct KNode {
 struct Arena {
     char *base = nullptr;
     size_t cap = 0, used = 0, peak = 0;
+    bool fixed = false;  // borrowed storage: nothing beside it may be allocated
     void reserve(size_t bytes);
     void *take(size_t bytes);
     template <class T>

@@ -582,7 +582,25 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     int64_t ne = 0;
     RSG_CUDA(cudaMemcpyAsync(&ne, loff + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
-    int *llist = ar.get<int>(ne > 0 ? ne : 1);
+    // The list lives in the arena when it fits beside what the rest of the FOF
+    // takes from it (~64 B per particle); a larger one (hundreds of entries
+    // per particle in very dense snapshots) gets an allocation of its own for
+    // this call, except in a fixed arena, which fails instead.
+    struct ListBuf {
+        void *p = nullptr;
+        ~ListBuf() {
+            if (p) cudaFree(p);
+        }
+    } lbuf;
+    int *llist;
+    size_t lbytes = sizeof(int) * (size_t)(ne > 0 ? ne : 1);
+    size_t lat = (ar.used + 255) & ~(size_t)255;
+    if (ar.fixed || lat + lbytes + (size_t)64 * n + (64u << 20) <= ar.cap) {
+        llist = ar.get<int>(ne > 0 ? ne : 1);
+    } else {
+        RSG_CUDA(cudaMalloc(&lbuf.p, lbytes));
+        llist = (int *)lbuf.p;
+    }
     launch(k_llist_w, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
            (const uint8_t *)cnt, (const int64_t *)loff, lcnt, llist, skipcnt, err);
     phase_mark(st, "fof.elist");

@@ -72,6 +72,7 @@ struct BorrowedArena {
     BorrowedArena(void *p, size_t bytes) {
         a.base = (char *)p;
         a.cap = bytes;
+        a.fixed = true;
     }
     ~BorrowedArena() {
         a.base = nullptr;

@@ -1108,14 +1108,69 @@ __device__ __forceinline__ float asc_x(const AscHalo &h, const float *pos) {
     float b = __fdiv_rn(v2, fmul(h.vrms, h.vrms));
     return fadd(a, b);
 }
+// Buckets of 32 consecutive growing halos (in list order, which follows the
+// hierarchy, so neighbours in the list are neighbours in space) for nodes
+// with more than RSG_ASC_BUCKET growing halos: the box of their centres and
+// the largest radius.  For a particle, box distance^2 / rmax^2 is at most the
+// float x of every valid halo in the bucket (every rounded operation of x is
+// monotone in its inputs), so a bucket whose bound is not below the running
+// best x holds no halo that passes the strict test: skipping it leaves the
+// choice, ties included, as the halo-by-halo scan makes it.
+#define RSG_ASC_BUCKET 64
+struct AscBucket {
+    float mn[3], mx[3], rmax;
+    int32_t inv;  // holds a halo without a valid metric (never skipped)
+};
+__global__ void k_asc_buckets(HierNodes N, int32_t base, const rsg_halo *H,
+                              const int32_t *glist, AscBucket *bk) {
+    int node = base + blockIdx.x;
+    int ng = N.ng[node], h0 = N.h0[node];
+    if (ng <= RSG_ASC_BUCKET) return;
+    int nb = (ng + 31) / 32;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        AscBucket B;
+        for (int d = 0; d < 3; d++) {
+            B.mn[d] = INFINITY;
+            B.mx[d] = -INFINITY;
+        }
+        B.rmax = 0.f;
+        B.inv = 0;
+        for (int g = 32 * b; g < ng && g < 32 * b + 32; g++) {
+            const rsg_halo &hh = H[glist[h0 + g]];
+            if (hh.vrms <= 0 || hh.r <= 0 || !(hh.r == hh.r)) {
+                B.inv = 1;
+                continue;
+            }
+            for (int d = 0; d < 3; d++) {
+                B.mn[d] = fminf(B.mn[d], hh.pos[d]);
+                B.mx[d] = fmaxf(B.mx[d], hh.pos[d]);
+            }
+            B.rmax = fmaxf(B.rmax, hh.r);
+        }
+        bk[h0 + b] = B;
+    }
+}
+// lower bound of x over a bucket's valid halos (see k_asc_buckets)
+__device__ __forceinline__ float asc_bucket_lb(const AscBucket &B, const float *pos) {
+    float d2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float gap = 0.f;
+        if (pos[i] < B.mn[i]) gap = fsub(B.mn[i], pos[i]);
+        else if (pos[i] > B.mx[i]) gap = fsub(pos[i], B.mx[i]);
+        d2 = fadd(d2, fmul(gap, gap));
+    }
+    return __fdiv_rn(d2, fmul(B.rmax, B.rmax));
+}
 __global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_halo *H,
                              const rsg_extra_halo_info *E, const int32_t *glist,
-                             const int32_t *redirect, int32_t *phalo) {
+                             const int32_t *redirect, const AscBucket *bk, int32_t *phalo) {
     __shared__ AscHalo gs[RSG_ASC_SMEM];
     int node = base + blockIdx.x;
     int s = N.start[node], n = N.n[node];
     int mi = N.maxi[node], ng = N.ng[node], h0 = N.h0[node];
     const bool staged = ng <= RSG_ASC_SMEM;
+    const bool buckets = ng > RSG_ASC_BUCKET;
     if (staged)
         for (int g = threadIdx.x; g < ng; g += blockDim.x) {
             const rsg_halo &hh = H[glist[h0 + g]];
@@ -1153,6 +1208,13 @@ __global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_
         float best = bvalid ? (float)sqrt((double)bx) : 1e20f;
         int bh = mi;
         for (int g = 0; g < ng; g++) {
+            if (buckets && (g & 31) == 0) {
+                const AscBucket &B = bk[h0 + (g >> 5)];
+                if (bvalid && !B.inv && !(asc_bucket_lb(B, pos) < bx)) {
+                    g += 31;  // no halo of this bucket can pass the strict test
+                    continue;
+                }
+            }
             AscHalo c;
             if (staged) c = gs[g];
             else {
@@ -2105,6 +2167,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     rsg_extra_halo_info *E = d_extra;
     launch(k_halo_init, nblk(NH, T), T, 0, st, H, E, NH);
     int32_t *glist = ar.get<int32_t>(NH), *redirect = ar.get<int32_t>(NH);
+    AscBucket *ascb = ar.get<AscBucket>(NH);  // bucket b of a node at h0 + b
     int32_t *stk = ar.get<int32_t>(NH + 1);
     RSG_CHECK_LAUNCH();
 
@@ -2117,7 +2180,10 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         launch(k_asc_mark, cnt, T, 0, st, W, d_p, N, base, H, phalo);
         phase_mark(st, "a.mark");
         launch(k_asc_seed, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, glist, redirect, cfg.force_res);
-        launch(k_asc_assign, cnt, T, 0, st, W, N, base, H, E, glist, redirect, phalo);
+        launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H, (const int32_t *)glist,
+               ascb);
+        launch(k_asc_assign, cnt, T, 0, st, W, N, base, H, E, glist, redirect,
+               (const AscBucket *)ascb, phalo);
         phase_mark(st, "a.seed_assign");
         RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
         launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
