@@ -1084,13 +1084,11 @@ __global__ void k_asc_seed(HierNodes N, int32_t base, int32_t count, rsg_halo *H
 // (float)sqrt((double)x) of the float sum x = r^2/h.r^2 + v^2/h.vrms^2,
 // which is monotone in x: a candidate whose x is not below the best one's
 // cannot win the strict comparison, so the square root is only taken for
-// candidates that might (same choice, ties included).  The block stages the
-// growing halos' centres and scales in shared memory.
+// candidates that might (same choice, ties included).
 struct AscHalo {
     float pos[6];
     float r, vrms;
 };
-#define RSG_ASC_SMEM 1024
 __device__ __forceinline__ bool asc_valid(const AscHalo &h) { return !(h.vrms <= 0 || h.r <= 0); }
 __device__ __forceinline__ float asc_x(const AscHalo &h, const float *pos) {
     float r2 = 0.f, v2 = 0.f;
@@ -1122,7 +1120,7 @@ struct AscBucket {
     int32_t inv;  // holds a halo without a valid metric (never skipped)
 };
 __global__ void k_asc_buckets(HierNodes N, int32_t base, const rsg_halo *H,
-                              const int32_t *glist, AscBucket *bk) {
+                              const int32_t *glist, AscBucket *bk, AscBucket *bk2) {
     int node = base + blockIdx.x;
     int ng = N.ng[node], h0 = N.h0[node];
     if (ng <= RSG_ASC_BUCKET) return;
@@ -1149,6 +1147,22 @@ __global__ void k_asc_buckets(HierNodes N, int32_t base, const rsg_halo *H,
         }
         bk[h0 + b] = B;
     }
+    // super-buckets of 32 buckets (1024 halos)
+    __syncthreads();
+    int nsb = (nb + 31) / 32;
+    for (int sb = threadIdx.x; sb < nsb; sb += blockDim.x) {
+        AscBucket S = bk[h0 + 32 * sb];
+        for (int b = 32 * sb + 1; b < nb && b < 32 * sb + 32; b++) {
+            const AscBucket &B = bk[h0 + b];
+            for (int d = 0; d < 3; d++) {
+                S.mn[d] = fminf(S.mn[d], B.mn[d]);
+                S.mx[d] = fmaxf(S.mx[d], B.mx[d]);
+            }
+            S.rmax = fmaxf(S.rmax, B.rmax);
+            S.inv |= B.inv;
+        }
+        bk2[h0 + sb] = S;
+    }
 }
 // lower bound of x over a bucket's valid halos (see k_asc_buckets)
 __device__ __forceinline__ float asc_bucket_lb(const AscBucket &B, const float *pos) {
@@ -1162,26 +1176,32 @@ __device__ __forceinline__ float asc_bucket_lb(const AscBucket &B, const float *
     }
     return __fdiv_rn(d2, fmul(B.rmax, B.rmax));
 }
-__global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_halo *H,
-                             const rsg_extra_halo_info *E, const int32_t *glist,
-                             const int32_t *redirect, const AscBucket *bk, int32_t *phalo) {
-    __shared__ AscHalo gs[RSG_ASC_SMEM];
-    int node = base + blockIdx.x;
-    int s = N.start[node], n = N.n[node];
+// One thread per particle of the level (the node from eln): a node of
+// millions of particles spreads over the whole GPU.  Same choice as the
+// per-node form, with buckets and super-buckets (1024 halos) skipped when
+// their bound is not below the running best.
+__global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, HierNodes N,
+                               int32_t base, const rsg_halo *H, const rsg_extra_halo_info *E,
+                               const int32_t *glist, const int32_t *redirect,
+                               const AscBucket *bk, const AscBucket *bk2, int32_t *phalo) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    if (k < 0) return;
+    int node = base + k;
+    int ph = phalo[i];
+    if (ph >= 0) {
+        if (redirect[ph] >= 0) phalo[i] = redirect[ph];
+        return;
+    }
     int mi = N.maxi[node], ng = N.ng[node], h0 = N.h0[node];
-    const bool staged = ng <= RSG_ASC_SMEM;
-    const bool buckets = ng > RSG_ASC_BUCKET;
-    if (staged)
-        for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-            const rsg_halo &hh = H[glist[h0 + g]];
-            for (int d = 0; d < 3; d++) {
-                gs[g].pos[d] = hh.pos[d];
-                gs[g].pos[d + 3] = hh.bulkvel[d];
-            }
-            gs[g].r = hh.r;
-            gs[g].vrms = hh.vrms;
-        }
-    __syncthreads();
+    if (ng == 1) {
+        phalo[i] = mi;
+        return;
+    }
+    float pos[6];
+#pragma unroll
+    for (int d = 0; d < 6; d++) pos[d] = W[i].pos[d];
     AscHalo hm;
     for (int d = 0; d < 3; d++) {
         hm.pos[d] = H[mi].pos[d];
@@ -1189,56 +1209,48 @@ __global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_
     }
     hm.r = H[mi].r;
     hm.vrms = H[mi].vrms;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        int ph = phalo[s + i];
-        if (ph >= 0) {
-            if (redirect[ph] >= 0) phalo[s + i] = redirect[ph];
-            continue;
-        }
-        if (ng == 1) {
-            phalo[s + i] = mi;
-            continue;
-        }
-        float pos[6];
-#pragma unroll
-        for (int d = 0; d < 6; d++) pos[d] = W[s + i].pos[d];
-        // the running best: its metric and, when valid, its x
-        bool bvalid = asc_valid(hm);
-        float bx = bvalid ? asc_x(hm, pos) : 0.f;
-        float best = bvalid ? (float)sqrt((double)bx) : 1e20f;
-        int bh = mi;
-        for (int g = 0; g < ng; g++) {
-            if (buckets && (g & 31) == 0) {
-                const AscBucket &B = bk[h0 + (g >> 5)];
-                if (bvalid && !B.inv && !(asc_bucket_lb(B, pos) < bx)) {
-                    g += 31;  // no halo of this bucket can pass the strict test
+    bool bvalid = asc_valid(hm);
+    float bx = bvalid ? asc_x(hm, pos) : 0.f;
+    float best = bvalid ? (float)sqrt((double)bx) : 1e20f;
+    int bh = mi;
+    const bool buckets = ng > RSG_ASC_BUCKET;
+    for (int g = 0; g < ng;) {
+        if (buckets && bvalid) {
+            if ((g & 1023) == 0) {
+                const AscBucket &S = bk2[h0 + (g >> 10)];
+                if (!S.inv && !(asc_bucket_lb(S, pos) < bx)) {
+                    g += 1024;
                     continue;
                 }
             }
-            AscHalo c;
-            if (staged) c = gs[g];
-            else {
-                const rsg_halo &hh = H[glist[h0 + g]];
-                for (int d = 0; d < 3; d++) {
-                    c.pos[d] = hh.pos[d];
-                    c.pos[d + 3] = hh.bulkvel[d];
+            if ((g & 31) == 0) {
+                const AscBucket &B = bk[h0 + (g >> 5)];
+                if (!B.inv && !(asc_bucket_lb(B, pos) < bx)) {
+                    g += 32;
+                    continue;
                 }
-                c.r = hh.r;
-                c.vrms = hh.vrms;
             }
-            float m;
-            if (!asc_valid(c)) {
-                m = 1e20f;
-                if (m < best) {
-                    best = m;
-                    bh = glist[h0 + g];
-                    bvalid = false;
-                }
-                continue;
+        }
+        const rsg_halo &hh = H[glist[h0 + g]];
+        AscHalo c;
+        for (int d = 0; d < 3; d++) {
+            c.pos[d] = hh.pos[d];
+            c.pos[d + 3] = hh.bulkvel[d];
+        }
+        c.r = hh.r;
+        c.vrms = hh.vrms;
+        if (!asc_valid(c)) {
+            if (1e20f < best) {
+                best = 1e20f;
+                bh = glist[h0 + g];
+                bvalid = false;
             }
-            float x = asc_x(c, pos);
-            if (bvalid && !(x < bx)) continue;  // metric >= best
-            m = (float)sqrt((double)x);
+            g++;
+            continue;
+        }
+        float x = asc_x(c, pos);
+        if (!(bvalid && !(x < bx))) {
+            float m = (float)sqrt((double)x);
             if (m < best) {
                 best = m;
                 bx = x;
@@ -1246,13 +1258,14 @@ __global__ void k_asc_assign(const Rec *W, HierNodes N, int32_t base, const rsg_
                 bh = glist[h0 + g];
             }
         }
-        int h = bh;
-        for (int guard = 0; guard < 100000 && E[h].sub_of > -1; guard++) {
-            if (pdist(H[h], pos) > E[h].max_metric) h = (int)E[h].sub_of;
-            else break;
-        }
-        phalo[s + i] = h;
+        g++;
     }
+    int h = bh;
+    for (int guard = 0; guard < 100000 && E[h].sub_of > -1; guard++) {
+        if (pdist(H[h], pos) > E[h].max_metric) h = (int)E[h].sub_of;
+        else break;
+    }
+    phalo[i] = h;
 }
 
 // Batched form: the records of every node grouped by label with one stable
@@ -1642,75 +1655,67 @@ __global__ void k_list_node(int32_t count, const int32_t *loff, int32_t *hnode) 
 }
 
 // _fix_parents (src/groupies.c:425-485) and calc_num_child_particles
-// (src/properties.c:139-163) for the node's halo range; one thread per node.
-__device__ void fix_parents_dev(rsg_halo *H, rsg_extra_halo_info *E, int h0, int h1) {
-    for (int i = h0; i < h1; i++) {
+// (src/properties.c:139-163) for every node of a level in parallel.  Sequentially, each halo i (ascending) is pushed to the front of
+// its parent's child list, so a parent's list runs from its largest child
+// down: next_cochild(i) is the largest sibling below i, prev_cochild(i) the
+// smallest sibling above it, child(P) the largest child.  Sorting (parent,
+// index) pairs gives those neighbours directly.  num_child_particles is the
+// sum of num_p over the halo's subtree: every halo adds its num_p to itself
+// and each ancestor.
+__global__ void k_fp_count(HierNodes N, int32_t base, int32_t cnt, int32_t *hc) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > cnt) return;
+    hc[k] = (k < cnt) ? N.h1[base + k] - N.h0[base + k] : 0;
+}
+__global__ void k_fp_reset(HierNodes N, int32_t base, rsg_extra_halo_info *E) {
+    int node = base + blockIdx.x;
+    for (int i = N.h0[node] + threadIdx.x; i < N.h1[node]; i += blockDim.x) {
         E[i].next_cochild = E[i].prev_cochild = E[i].child = -1;
         if (E[i].sub_of == i) E[i].sub_of = -1;
     }
-    for (int i = h0; i < h1; i++) {
-        E[i].max_metric = 1e10f;
+}
+__global__ void k_fp_keys(HierNodes N, int32_t base, const int32_t *hofs, const rsg_halo *H,
+                          rsg_extra_halo_info *E, uint64_t *key, uint32_t *val) {
+    int node = base + blockIdx.x;
+    int h0 = N.h0[node];
+    for (int i = h0 + threadIdx.x; i < N.h1[node]; i += blockDim.x) {
         int64_t so = E[i].sub_of;
-        if (so < 0) continue;
-        E[i].max_metric = pdist(H[i], H[so].pos);
-        int64_t nx = E[so].child;
-        E[i].next_cochild = nx;
-        E[i].prev_cochild = -1;
-        E[so].child = i;
-        if (nx > -1) E[nx].prev_cochild = i;
+        E[i].max_metric = (so < 0) ? 1e10f : pdist(H[i], H[so].pos);
+        int64_t at = hofs[blockIdx.x] + (i - h0);
+        key[at] = (so < 0) ? ~0ull : (((uint64_t)so << 32) | (uint64_t)(uint32_t)i);
+        val[at] = (uint32_t)at;
     }
 }
-__device__ void num_child_dev(rsg_halo *H, const rsg_extra_halo_info *E, int h0, int h1,
-                              int32_t *stk) {
-    for (int i = h0; i < h1; i++) H[i].num_child_particles = 0;
-    for (int i = h0; i < h1; i++) {
-        if (H[i].num_child_particles) continue;
-        // iterative post-order walk of the child lists from i
-        int sp = 0;
-        stk[sp++] = i;
-        H[i].num_child_particles = H[i].num_p;
+__global__ void k_fp_link(const uint64_t *key, int64_t n, rsg_extra_halo_info *E) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= n || key[e] == ~0ull) return;
+    uint64_t p = key[e] >> 32;
+    int i = (int)(uint32_t)key[e];
+    bool lo = e > 0 && (key[e - 1] >> 32) == p;
+    bool hi = e + 1 < n && key[e + 1] != ~0ull && (key[e + 1] >> 32) == p;
+    E[i].next_cochild = lo ? (int64_t)(uint32_t)key[e - 1] : -1;
+    E[i].prev_cochild = hi ? (int64_t)(uint32_t)key[e + 1] : -1;
+    if (!hi) E[p].child = i;
+}
+__global__ void k_nc_sum(HierNodes N, int32_t base, rsg_halo *H, const rsg_extra_halo_info *E,
+                         int *err) {
+    int node = base + blockIdx.x;
+    int h0 = N.h0[node], h1 = N.h1[node];
+    for (int i = h0 + threadIdx.x; i < h1; i += blockDim.x) H[i].num_child_particles = 0;
+    __syncthreads();
+    for (int i = h0 + threadIdx.x; i < h1; i += blockDim.x) {
+        unsigned long long np = (unsigned long long)H[i].num_p;
+        int64_t a = i;
         int guard = 0;
-        while (sp && ++guard < 100000000) {
-            int h = stk[sp - 1];
-            // find the first child not yet accumulated: children are
-            // accumulated in list order, marked by a cursor kept in stk
-            // entries above the halo; use the sign of flags bit 30 as visited
-            int64_t c = E[h].child;
-            bool pushed = false;
-            while (c > -1) {
-                if (!(H[c].flags & (1 << 30))) {
-                    H[c].flags |= (1 << 30);
-                    if (!H[c].num_child_particles) {
-                        H[c].num_child_particles = H[c].num_p;
-                        stk[sp++] = (int)c;
-                        pushed = true;
-                        break;
-                    }
-                    H[h].num_child_particles += H[c].num_child_particles;
-                }
-                c = E[c].next_cochild;
+        while (a >= h0 && a < h1) {
+            atomicAdd((unsigned long long *)&H[a].num_child_particles, np);
+            a = E[a].sub_of;
+            if (++guard > (h1 - h0)) {  // a cycle of sub_of links
+                atomicExch(err, 1);
+                break;
             }
-            if (pushed) continue;
-            sp--;
-            if (sp) H[stk[sp - 1]].num_child_particles += H[h].num_child_particles;
         }
     }
-    for (int i = h0; i < h1; i++) H[i].flags &= ~(int64_t)(1 << 30);
-}
-__global__ void k_fix_parents(HierNodes N, int32_t base, int32_t count, rsg_halo *H,
-                              rsg_extra_halo_info *E, int32_t *stk) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    int node = base + k;
-    fix_parents_dev(H, E, N.h0[node], N.h1[node]);
-    num_child_dev(H, E, N.h0[node], N.h1[node], stk + N.h0[node]);
-}
-__global__ void k_num_child(HierNodes N, int32_t base, int32_t count, rsg_halo *H,
-                            const rsg_extra_halo_info *E, int32_t *stk) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    int node = base + k;
-    num_child_dev(H, E, N.h0[node], N.h1[node], stk + N.h0[node]);
 }
 
 // core sort keys: within each halo of the level-0 nodes, by float squared
@@ -1794,6 +1799,31 @@ static void sort_pairs(Arena &ar, K *k, K *k2, V *v, V *v2, int64_t n, int bits,
 }
 static int32_t excl_scan_i32(Arena &ar, const int32_t *in, int32_t *out, int32_t n,
                              cudaStream_t st);
+
+// _fix_parents (+ calc_num_child_particles) for the nodes [base, base + cnt)
+static void fix_parents_level(Arena &ar, HierNodes N, int32_t base, int32_t cnt, rsg_halo *H,
+                              rsg_extra_halo_info *E, int *err, bool fix, cudaStream_t st) {
+    const int T = 256;
+    if (cnt <= 0) return;
+    size_t mark = ar.used;
+    if (fix) {
+        int32_t *hofs = ar.get<int32_t>(cnt + 1);
+        launch(k_fp_count, nblk(cnt + 1, T), T, 0, st, N, base, cnt, hofs);
+        int32_t nh = excl_scan_i32(ar, hofs, hofs, cnt + 1, st);
+        launch(k_fp_reset, cnt, T, 0, st, N, base, E);
+        if (nh > 0) {
+            uint64_t *k1 = ar.get<uint64_t>(nh), *k2 = ar.get<uint64_t>(nh);
+            uint32_t *v1 = ar.get<uint32_t>(nh), *v2 = ar.get<uint32_t>(nh);
+            launch(k_fp_keys, cnt, T, 0, st, N, base, (const int32_t *)hofs, (const rsg_halo *)H, E,
+                   k1, v1);
+            sort_pairs(ar, k1, k2, v1, v2, nh, 64, st);
+            launch(k_fp_link, nblk(nh, T), T, 0, st, (const uint64_t *)k2, (int64_t)nh, E);
+        }
+    }
+    launch(k_nc_sum, cnt, T, 0, st, N, base, H, (const rsg_extra_halo_info *)E, err);
+    RSG_CHECK_LAUNCH();
+    ar.used = mark;
+}
 
 // calc_basic_halo_props for the listed halos: one block per halo, and in the
 // batched form the chunked passes for halos above RSG_BP_BIG particles.
@@ -2167,7 +2197,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     rsg_extra_halo_info *E = d_extra;
     launch(k_halo_init, nblk(NH, T), T, 0, st, H, E, NH);
     int32_t *glist = ar.get<int32_t>(NH), *redirect = ar.get<int32_t>(NH);
-    AscBucket *ascb = ar.get<AscBucket>(NH);  // bucket b of a node at h0 + b
+    // bucket b (32 halos) and super-bucket sb (1024 halos) of a node at h0 + b, h0 + sb
+    AscBucket *ascb = ar.get<AscBucket>(NH), *ascb2 = ar.get<AscBucket>(NH);
     int32_t *stk = ar.get<int32_t>(NH + 1);
     RSG_CHECK_LAUNCH();
 
@@ -2180,13 +2211,15 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         launch(k_asc_mark, cnt, T, 0, st, W, d_p, N, base, H, phalo);
         phase_mark(st, "a.mark");
         launch(k_asc_seed, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, glist, redirect, cfg.force_res);
-        launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H, (const int32_t *)glist,
-               ascb);
-        launch(k_asc_assign, cnt, T, 0, st, W, N, base, H, E, glist, redirect,
-               (const AscBucket *)ascb, phalo);
-        phase_mark(st, "a.seed_assign");
         RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
         launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
+        launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H, (const int32_t *)glist,
+               ascb, ascb2);
+        launch(k_asc_assign_p, nblk(M, 128), 128, 0, st, (const Rec *)W, M, (const int32_t *)eln,
+               N, base, (const rsg_halo *)H, (const rsg_extra_halo_info *)E,
+               (const int32_t *)glist, (const int32_t *)redirect, (const AscBucket *)ascb,
+               (const AscBucket *)ascb2, phalo);
+        phase_mark(st, "a.seed_assign");
         RSG_CHECK_LAUNCH();
         if (exact) {
             // reassign_halo_particles: the reference's partition by halo index
@@ -2211,7 +2244,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
         launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 0);
         launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E);
-        launch(k_fix_parents, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
+        fix_parents_level(ar, N, base, cnt, H, E, err, true, st);
         basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
         RSG_CHECK_LAUNCH();
         phase_mark(st, "a.props_parents");
@@ -2231,11 +2264,11 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             std::swap(phalo, phalo2);
             launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 1);
             launch(k_best_parent, nblk(na, T), T, 0, st, N, base, cnt, aoff, alist, anode, H, E);
-            launch(k_fix_parents, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
+            fix_parents_level(ar, N, base, cnt, H, E, err, true, st);
             RSG_CHECK_LAUNCH();
             // find_subs tail (src/groupies.c:697-703): child counts and basic
             // properties for every halo, then the additional properties.
-            launch(k_num_child, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, stk);
+            fix_parents_level(ar, N, base, cnt, H, E, err, false, st);
             basic_props(ar, W, H, alist, na, d_dc, seq_max, exact, st);
             RSG_CHECK_LAUNCH();
         }
