@@ -39,7 +39,6 @@ template <int D, class RecT, int ITEMS>
 __global__ void k_box_runs(const RecT *recs, int64_t nrec, const int32_t *owner,
                            unsigned *bmin, unsigned *bmax) {
     int64_t i0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * ITEMS;
-    if (i0 >= nrec) return;
     int cur = -1;
     unsigned lo[D], hi[D];
     for (int it = 0; it < ITEMS; it++) {
@@ -66,11 +65,24 @@ __global__ void k_box_runs(const RecT *recs, int64_t nrec, const int32_t *owner,
             hi[d] = max(hi[d], o);
         }
     }
-    if (cur >= 0)
+    // last run: a warp whose lanes all hold the same node (the top levels of
+    // a build) combines it first and issues one atomic per dimension
+    const unsigned FULL = 0xffffffffu;
+    if (__match_any_sync(FULL, cur) == FULL) {
+        if (cur >= 0)
+            for (int d = 0; d < D; d++) {
+                unsigned a = __reduce_min_sync(FULL, lo[d]), b = __reduce_max_sync(FULL, hi[d]);
+                if ((threadIdx.x & 31) == 0) {
+                    atomicMin(&bmin[(int64_t)cur * D + d], a);
+                    atomicMax(&bmax[(int64_t)cur * D + d], b);
+                }
+            }
+    } else if (cur >= 0) {
         for (int d = 0; d < D; d++) {
             atomicMin(&bmin[(int64_t)cur * D + d], lo[d]);
             atomicMax(&bmax[(int64_t)cur * D + d], hi[d]);
         }
+    }
 }
 
 template <int D>
