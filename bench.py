@@ -252,6 +252,21 @@ def reference_arm(args, rk):
     print(json.dumps(line), flush=True)
 
 
+def precision_study(rk, scale, forms):
+    """Potential forms against the first of `forms` (normally 3, the FP64
+    direct sum) on the isolated-groups workload (mpi-rockstar_gb300/precision.py)."""
+    from mpi_rockstar_gb300 import precision
+    rk.build()
+    p, box, mp, ng = rk.synth(3, scale, SEED)
+    cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    t0 = time.time()
+    runs = precision.run_forms(rk, p, cfg, forms)
+    res = precision.compare(runs, cfg, ref=forms[0], forms=forms[1:])
+    res.update({"workload": "isolated groups (potential/unbinding precision study)",
+                "scale": scale, "planted_groups": ng, "study_s": round(time.time() - t0, 1)})
+    print(json.dumps(res))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -264,10 +279,20 @@ def main():
     ap.add_argument("--kernel-table", default="",
                     help="write per-kernel CUDA-event times of one extra (untimed) step of "
                          "each form to this file")
+    ap.add_argument("--precision-study", action="store_true",
+                    help="instead of the bench line: the potential precision study on the "
+                         "isolated-groups workload at --scale, one JSON line")
+    ap.add_argument("--precision-forms", default="3,0,1,2",
+                    help="potential forms of the study; the first is the reference "
+                         "(3: FP64 direct sum, O(n^2) per group)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rk = load_pkg()
+    if args.precision_study:
+        if rank == 0:
+            precision_study(rk, args.scale, [int(f) for f in args.precision_forms.split(",")])
+        return
     if args.impl == "reference":
         if rank == 0:
             reference_arm(args, rk)

@@ -160,9 +160,20 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
  *           bit-identical potentials;
  *   form 1: the batched precision form (FP32 distances and 1/r, FP32
  *           Kahan-compensated sums; node sizes from parallel sums; the same
- *           tree and opening rule). */
+ *           tree and opening rule);
+ *   form 2: form 1's terms summed in plain FP32 (no compensation);
+ *   form 3: FP64 direct sum over all pairs, mp / max(r, FORCE_RES) (no
+ *           reference counterpart: the precision reference; O(n^2)).
+ * Every form permutes po the same way. */
 int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct rsg_config *cfg,
                           int32_t form);
+
+/* Selects the potential form (0-3, as for rsg_compute_potential) that the
+ * batched substructure form (rsg_find_subs_batch, rsg_path_device with
+ * batched = 1) uses from now on, process-wide; the default is 1.  The plain
+ * form always uses form 0.  Returns the previous form, or RSG_ERR_ARGS.
+ * No reference counterpart: it serves the potential precision study. */
+int32_t rsg_set_potential_form(int32_t form);
 
 /* Allocation-free 3D FOF of one chunk: rsg_rockstar_fof on device buffers,
  * with no counterpart in the reference (whose fof.c grows its buffers with

@@ -64,6 +64,11 @@ def lib():
         h.rsg_profile_table.argtypes = [C.c_char_p, i64]
         h.rsg_find_subs.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, i64, vp]
         h.rsg_rockstar_fof_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, vp, i64, vp, vp]
+        h.rsg_set_potential_form.restype = C.c_int32
+        h.rsg_set_potential_form.argtypes = [C.c_int32]
+        h.rsg_debug_keep_potentials.argtypes = [C.c_int32]
+        h.rsg_debug_potentials.restype = i64
+        h.rsg_debug_potentials.argtypes = [vp, i64]
         for name, args in _EXTRA_SIGS.items():
             if hasattr(h, name):
                 getattr(h, name).argtypes = args
@@ -128,6 +133,38 @@ def compute_potential(po, cfg, form=0):
     q = np.array(po, dtype=POTENTIAL, copy=True)
     _check(lib().rsg_compute_potential(q.ctypes.data, len(q), C.byref(st), form))
     return q
+
+
+POTENTIAL_FORMS = {0: "FP64 Barnes-Hut (reference arithmetic)",
+                   1: "FP32 Barnes-Hut, Kahan-compensated sums",
+                   2: "FP32 Barnes-Hut, plain sums",
+                   3: "FP64 direct sum"}
+
+
+def set_potential_form(form):
+    """Potential form of the batched substructure form from now on
+    (rsg_set_potential_form); returns the previous one."""
+    r = int(lib().rsg_set_potential_form(int(form)))
+    if r < 0:
+        _check(r)
+    return r
+
+
+def keep_potentials(on=True):
+    """Keep the potential records of each later find_subs / path call (test
+    hook); last_potentials() returns them."""
+    lib().rsg_debug_keep_potentials(1 if on else 0)
+
+
+def last_potentials():
+    """POTENTIAL records of the last call made after keep_potentials(True):
+    sorted by halo (index in the halo output, stored in the `_pad` field),
+    potential-only records (ke < 0) after a halo's own, then by radius."""
+    k = int(lib().rsg_debug_potentials(None, 0))
+    out = np.zeros(k, POTENTIAL)
+    if k:
+        lib().rsg_debug_potentials(out.ctypes.data, k)
+    return out
 
 
 def debug_hierarchy():

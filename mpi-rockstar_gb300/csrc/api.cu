@@ -3,6 +3,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <vector>
 
 #include "kdtree_impl.cuh"
@@ -27,7 +28,10 @@ __global__ void k_zero_pe(PotRec *PO, int64_t n) {
 
 void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const int32_t *rn,
                   int32_t ntrees, double mp, double force_res, int *err, cudaStream_t st,
-                  int exact);
+                  int form);
+int set_batched_potential_form(int f);
+extern std::atomic<bool> g_keep_po;
+extern std::vector<PotRec> g_dbg_po;
 
 // One device context per host thread: a stream and a scratch arena that is
 // reused across calls (the role the reference's threadprivate scratch
@@ -262,7 +266,7 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
 
 int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct rsg_config *cfg,
                           int32_t form) {
-    if (!cfg || num_po < 0 || (num_po > 0 && !po) || (form != 0 && form != 1)) {
+    if (!cfg || num_po < 0 || (num_po > 0 && !po) || form < 0 || form > 3) {
         set_error(RSG_ERR_ARGS, "rsg_compute_potential: bad arguments");
         return RSG_ERR_ARGS;
     }
@@ -285,7 +289,7 @@ int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct
         RSG_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), C.st));
         launch(k_zero_pe, nblk(num_po, 256), 256, 0, C.st, d, num_po);
         bh_potential(C.ar, d, num_po, seg, seg + 1, 1, cfg->particle_mass, cfg->force_res, err,
-                     C.st, form == 0 ? 1 : 0);
+                     C.st, form);
         int herr[2];
         RSG_CUDA(cudaMemcpyAsync(po, d, sizeof(PotRec) * num_po, cudaMemcpyDeviceToHost, C.st));
         RSG_CUDA(cudaMemcpyAsync(herr, err, sizeof(herr), cudaMemcpyDeviceToHost, C.st));
@@ -299,6 +303,25 @@ int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct
     } catch (Failure &) {
         return error_code();
     }
+}
+
+int32_t rsg_set_potential_form(int32_t form) {
+    if (form < 0 || form > 3) {
+        set_error(RSG_ERR_ARGS, "rsg_set_potential_form: form must be 0-3");
+        return RSG_ERR_ARGS;
+    }
+    return rsg::set_batched_potential_form(form);
+}
+
+void rsg_debug_keep_potentials(int32_t on) {
+    rsg::g_keep_po.store(on != 0);
+    if (!on) std::vector<rsg::PotRec>().swap(rsg::g_dbg_po);
+}
+
+int64_t rsg_debug_potentials(struct rsg_potential *out, int64_t cap) {
+    int64_t k = (int64_t)rsg::g_dbg_po.size();
+    if (out && cap > 0) memcpy(out, rsg::g_dbg_po.data(), sizeof(rsg_potential) * (size_t)(k < cap ? k : cap));
+    return k;
 }
 
 // Test hook: the subgroup hierarchy of the last rsg_find_subs call on this

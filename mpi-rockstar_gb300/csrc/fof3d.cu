@@ -23,6 +23,8 @@
 #include <limits.h>
 
 #include <cub/cub.cuh>
+#include <thrust/binary_search.h>
+#include <thrust/execution_policy.h>
 
 #include "kdtree_impl.cuh"
 
@@ -298,17 +300,20 @@ __global__ void __launch_bounds__(128) k_count_w(const KNode<3> *nodes, const Re
 }
 // Later dense neighbours of every dense particle k (j > k, j in S_r(k)),
 // counted then listed; skipcnt[j] counts the dense k that can skip j.
+// With llist, k's entries go to llist[loff[k] - lbase ...] (lbase: the
+// offset of the first particle of the chunk being listed).
 __global__ void __launch_bounds__(128) k_llist_w(const KNode<3> *nodes, const Rec *recs,
                                                  const int *dense, int nd, float r,
                                                  const uint8_t *cnt, const int64_t *loff,
-                                                 int *lcnt, int *llist, int *skipcnt, int *err) {
+                                                 int64_t lbase, int *lcnt, int *llist,
+                                                 int *skipcnt, int *err) {
     if (warp_idle(nd)) return;
     int k;
     bool act = warp_query(dense, nd, &k);
     float c[3] = {0, 0, 0};
     if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
     int m = 0;
-    int64_t base = (loff && act) ? loff[k] : 0;
+    int64_t base = (loff && act) ? loff[k] - lbase : 0;
     auto add = [&](int j) {
         if (j > k && cnt[j] > 16) {
             if (llist) llist[base + m] = j;
@@ -396,29 +401,47 @@ __global__ void k_link_2r(const KNode<3> *nodes, const Rec *recs, int n, float r
 // earlier neighbour of each.  A particle with none pending that was not
 // skipped is a seed (all its earlier potential skippers are decided and
 // none of them is a seed).
-__global__ void k_kahn(const int *front, int nf, const int64_t *loff, const int *llist, int *state,
-                       int *skipcnt, int *next, int *nnext) {
+// When the lists are built one chunk of particles [c0, cend) at a time
+// (lbase = loff[c0]), a particle decided beyond cend has no list yet: it
+// keeps its state and enters the first frontier of its own chunk.
+__global__ void k_kahn(const int *front, int nf, const int64_t *loff, int64_t lbase,
+                       const int *llist, int cend, int *state, int *skipcnt, int *next,
+                       int *nnext) {
     int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= nf) return;
     int k = front[w];
     int sk = state[k];
-    for (int64_t e = loff[k] + lane; e < loff[k + 1]; e += 32) {
+    for (int64_t e = loff[k] - lbase + lane; e < loff[k + 1] - lbase; e += 32) {
         int j = llist[e];
-        if (sk == 1 && atomicCAS(&state[j], 0, 2) == 0) next[atomicAdd(nnext, 1)] = j;
-        if (atomicSub(&skipcnt[j], 1) == 1 && atomicCAS(&state[j], 0, 1) == 0)
+        if (sk == 1 && atomicCAS(&state[j], 0, 2) == 0 && j < cend) next[atomicAdd(nnext, 1)] = j;
+        if (atomicSub(&skipcnt[j], 1) == 1 && atomicCAS(&state[j], 0, 1) == 0 && j < cend)
             next[atomicAdd(nnext, 1)] = j;
     }
 }
-__global__ void k_kahn_init(const int *dense, int nd, const int *skipcnt, int *state, int *front,
-                            int *nfront) {
+// Dense particles with no earlier potential skipper are seeds; those of
+// [0, cend) start the first frontier.
+__global__ void k_kahn_init(const int *dense, int nd, const int *skipcnt, int cend, int *state,
+                            int *front, int *nfront) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nd) return;
     int i = dense[t];
     if (skipcnt[i] == 0) {
         state[i] = 1;
-        front[atomicAdd(nfront, 1)] = i;
+        if (i < cend) front[atomicAdd(nfront, 1)] = i;
     }
 }
+// First frontier of a later chunk: its dense particles already decided
+// while earlier chunks were walked.
+__global__ void k_kahn_chunk(const int *dense, int nd, const int *state, int *front, int *nfront) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nd) return;
+    int i = dense[t];
+    if (state[i] != 0) front[atomicAdd(nfront, 1)] = i;
+}
+struct ChunkTarget {
+    int64_t step;
+    __host__ __device__ int64_t operator()(int64_t t) const { return (t + 1) * step; }
+};
 __global__ void k_state8(const int *s32, int n, uint8_t *s8) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) s8[i] = (uint8_t)s32[i];
@@ -573,7 +596,8 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     RSG_CUDA(cudaMemsetAsync(lcnt, 0, sizeof(int) * (n + 1), st));
     RSG_CUDA(cudaMemsetAsync(skipcnt, 0, sizeof(int) * n, st));
     launch(k_llist_w, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
-           (const uint8_t *)cnt, (const int64_t *)nullptr, lcnt, (int *)nullptr, skipcnt, err);
+           (const uint8_t *)cnt, (const int64_t *)nullptr, (int64_t)0, lcnt, (int *)nullptr,
+           skipcnt, err);
     size_t cb = 0;
     thrust::transform_iterator<ToI64, const int32_t *, int64_t> lc64((const int32_t *)lcnt, ToI64{});
     cub::DeviceScan::ExclusiveSum(nullptr, cb, lc64, loff, n + 1, st);
@@ -583,9 +607,12 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     RSG_CUDA(cudaMemcpyAsync(&ne, loff + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     // The list lives in the arena when it fits beside what the rest of the FOF
-    // takes from it (~64 B per particle); a larger one (hundreds of entries
+    // takes from it (~64 B per particle).  A larger one (hundreds of entries
     // per particle in very dense snapshots) gets an allocation of its own for
-    // this call, except in a fixed arena, which fails instead.
+    // this call, as large as free device memory allows (less 1 GiB, or
+    // RSG_FOF_LIST_ENTRIES entries when that is set); when the whole list
+    // does not fit, it is built and walked one chunk of particles at a time,
+    // chunks in particle order.  A fixed arena holds the list whole or fails.
     struct ListBuf {
         void *p = nullptr;
         ~ListBuf() {
@@ -593,44 +620,110 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
         }
     } lbuf;
     int *llist;
-    size_t lbytes = sizeof(int) * (size_t)(ne > 0 ? ne : 1);
+    int64_t lcap = ne > 0 ? ne : 1;  // entries the list buffer holds
     size_t lat = (ar.used + 255) & ~(size_t)255;
-    if (ar.fixed || lat + lbytes + (size_t)64 * n + (64u << 20) <= ar.cap) {
-        llist = ar.get<int>(ne > 0 ? ne : 1);
+    const char *lenv = getenv("RSG_FOF_LIST_ENTRIES");
+    int64_t lforce = lenv ? atoll(lenv) : 0;
+    if (ar.fixed || (!lforce && lat + sizeof(int) * (size_t)lcap + (size_t)64 * n + (64u << 20) <= ar.cap)) {
+        llist = ar.get<int>(lcap);
     } else {
-        RSG_CUDA(cudaMalloc(&lbuf.p, lbytes));
+        size_t fb = 0, tb = 0;
+        RSG_CUDA(cudaMemGetInfo(&fb, &tb));
+        int64_t avail = fb > ((size_t)1 << 30) ? (int64_t)((fb - ((size_t)1 << 30)) / sizeof(int)) : 0;
+        if (lforce > 0) avail = lforce;
+        if (avail < lcap) lcap = avail;
+        RSG_CUDA(cudaMalloc(&lbuf.p, sizeof(int) * (size_t)(lcap > 0 ? lcap : 1)));
         llist = (int *)lbuf.p;
     }
-    launch(k_llist_w, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
-           (const uint8_t *)cnt, (const int64_t *)loff, lcnt, llist, skipcnt, err);
-    phase_mark(st, "fof.elist");
+    // chunk boundaries: particles c[t] .. c[t+1], dense entries d[t] .. d[t+1]
+    std::vector<int> cb_h(2, 0), db_h(2, 0);
+    std::vector<int64_t> lb_h(1, 0);
+    cb_h[1] = n;
+    db_h[1] = nd;
+    if (lcap < ne) {
+        int maxl = 0;
+        {
+            int *dmax = ar.get<int>(1);
+            size_t mb = 0;
+            cub::DeviceReduce::Max(nullptr, mb, lcnt, dmax, n, st);
+            size_t m0 = ar.used;
+            void *mt = ar.take(mb + 256);
+            cub::DeviceReduce::Max(mt, mb, lcnt, dmax, n, st);
+            ar.used = m0;
+            RSG_CUDA(cudaMemcpyAsync(&maxl, dmax, sizeof(int), cudaMemcpyDeviceToHost, st));
+            RSG_CUDA(cudaStreamSynchronize(st));
+        }
+        int64_t step = lcap - maxl;
+        if (step < (int64_t)maxl || step < (1 << 16)) {
+            set_error(RSG_ERR_LIMIT, "later-dense lists need more device memory than is free");
+            throw Failure();
+        }
+        int64_t m = (ne + step - 1) / step;  // chunks
+        int *cbd = ar.get<int>(m + 1), *dbd = ar.get<int>(m + 1);
+        thrust::transform_iterator<ChunkTarget, thrust::counting_iterator<int64_t>, int64_t> tgt(
+            thrust::counting_iterator<int64_t>(0), ChunkTarget{step});
+        thrust::lower_bound(thrust::cuda::par_nosync.on(st), loff, loff + n + 1, tgt, tgt + (m - 1), cbd);
+        thrust::lower_bound(thrust::cuda::par_nosync.on(st), dense, dense + nd, cbd, cbd + (m - 1), dbd);
+        cb_h.assign(m + 1, 0);
+        db_h.assign(m + 1, 0);
+        RSG_CUDA(cudaMemcpyAsync(cb_h.data() + 1, cbd, sizeof(int) * (m - 1), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaMemcpyAsync(db_h.data() + 1, dbd, sizeof(int) * (m - 1), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        cb_h[m] = n;
+        db_h[m] = nd;
+        lb_h.assign(m + 1, 0);
+        for (int64_t t = 0; t <= m; t++)
+            RSG_CUDA(cudaMemcpyAsync(&lb_h[t], loff + cb_h[t], sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        for (int64_t t = 0; t < m; t++)
+            if (lb_h[t + 1] - lb_h[t] > lcap) {
+                set_error(RSG_ERR_LIMIT, "later-dense list chunk exceeds its buffer");
+                throw Failure();
+            }
+    }
+    const int nchunks = (int)cb_h.size() - 1;
     int *state32 = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(state32, 0, sizeof(int) * n, st));
     int *fa = ar.get<int>(nd + 1), *fb = ar.get<int>(nd + 1), *nf = ar.get<int>(2);
     RSG_CUDA(cudaMemsetAsync(nf, 0, sizeof(int) * 2, st));
-    launch(k_kahn_init, nblk(nd, T), T, 0, st, dense, nd, skipcnt, state32, fa, nf);
-    int hf = 0, rounds = 0;
-    RSG_CUDA(cudaMemcpyAsync(&hf, nf, sizeof(int), cudaMemcpyDeviceToHost, st));
-    RSG_CUDA(cudaStreamSynchronize(st));
-    while (hf > 0) {
-        RSG_CUDA(cudaMemsetAsync(nf + 1, 0, sizeof(int), st));
-        launch(k_kahn, nblk((int64_t)hf * 32, T), T, 0, st, fa, hf, loff, llist, state32, skipcnt, fb,
-               nf + 1);
-        RSG_CUDA(cudaMemcpyAsync(&hf, nf + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    launch(k_kahn_init, nblk(nd, T), T, 0, st, dense, nd, skipcnt, cb_h[1], state32, fa, nf);
+    int rounds = 0;
+    for (int t = 0; t < nchunks; t++) {
+        int d0 = db_h[t], d1 = db_h[t + 1];
+        if (d1 <= d0) continue;
+        int64_t lbase = lb_h.size() > 1 ? lb_h[t] : 0;
+        launch(k_llist_w, nblk(d1 - d0, TW), TW, 0, st, F.nodes, recs, (const int *)dense + d0,
+               d1 - d0, r, (const uint8_t *)cnt, (const int64_t *)loff, lbase, lcnt, llist, skipcnt,
+               err);
+        if (t > 0) {
+            RSG_CUDA(cudaMemsetAsync(nf, 0, sizeof(int), st));
+            launch(k_kahn_chunk, nblk(d1 - d0, T), T, 0, st, (const int *)dense + d0, d1 - d0,
+                   (const int *)state32, fa, nf);
+        }
+        int hf = 0;
+        RSG_CUDA(cudaMemcpyAsync(&hf, nf, sizeof(int), cudaMemcpyDeviceToHost, st));
         RSG_CUDA(cudaStreamSynchronize(st));
-        std::swap(fa, fb);
-        if (++rounds > 10000000) {
-            set_error(RSG_ERR_LIMIT, "seed selection did not converge");
-            throw Failure();
+        while (hf > 0) {
+            RSG_CUDA(cudaMemsetAsync(nf + 1, 0, sizeof(int), st));
+            launch(k_kahn, nblk((int64_t)hf * 32, T), T, 0, st, fa, hf, loff, lbase, llist,
+                   cb_h[t + 1], state32, skipcnt, fb, nf + 1);
+            RSG_CUDA(cudaMemcpyAsync(&hf, nf + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+            RSG_CUDA(cudaStreamSynchronize(st));
+            std::swap(fa, fb);
+            if (++rounds > 10000000) {
+                set_error(RSG_ERR_LIMIT, "seed selection did not converge");
+                throw Failure();
+            }
         }
     }
+    phase_mark(st, "fof.elist");
     // non-dense particles: state 2 (never seeds)
     uint8_t *state = ar.get<uint8_t>(n);
     launch(k_state8, nblk(n, T), T, 0, st, state32, n, state);
     phase_mark(st, "fof.seeds");
     if (getenv("RSG_TIMING"))
-        fprintf(stderr, "  [fof] dense %d, later-list %lld, frontier steps %d\n", nd,
-                (long long)ne, rounds);
+        fprintf(stderr, "  [fof] dense %d, later-list %lld in %d chunk(s), frontier steps %d\n",
+                nd, (long long)ne, nchunks, rounds);
     last_stats()[RSG_STAT_DENSE] = nd;
     last_stats()[RSG_STAT_LATER_LIST] = ne;
     uint8_t *skipped = ar.get<uint8_t>(n);

@@ -12,6 +12,9 @@
 //  3. potential-only particles dropped, the rest sorted by r^2;
 //  4. core velocity, kinetic energy, then the density/shape/NFW scans for
 //     all particles and for bound particles (src/properties.c:165-510).
+#include <atomic>
+#include <vector>
+
 #include <cub/cub.cuh>
 
 #include "halo_math.cuh"
@@ -296,13 +299,15 @@ __global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, 
 // receives the same terms in the same order as in the reference (the self
 // leaf's pairs in ascending partner order, opened leaves in point order,
 // monopoles as visited), so the FP64 form is bit-identical to it.
-//   F32 = false: r = max(sqrt(r2), FORCE_RES) and m / r in FP64, as the
-//                reference computes them;
-//   F32 = true:  the batched precision form: squared distance and 1/r in
-//                FP32 (rsqrtf), each particle's sum Kahan-compensated in
-//                FP32.  The opening test itself stays in FP64.
+//   MODE 0: r = max(sqrt(r2), FORCE_RES) and m / r in FP64, as the
+//           reference computes them;
+//   MODE 1: the batched precision form: squared distance and 1/r in FP32
+//           (rsqrtf), each particle's sum Kahan-compensated in FP32;
+//   MODE 2: the MODE 1 terms summed in plain FP32 (no compensation), the
+//           uncompensated baseline of the precision study.
+// The opening test itself is the same in every mode.
 #define RSG_BH_G 16
-template <bool F32>
+template <int MODE>
 __global__ void __launch_bounds__(64) k_bh_walk(const KNode<3> *nodes, const int32_t *leaves,
                                                 int32_t nl, const BHNode *B, PotRec *PO,
                                                 double mp, double force_res, int *err) {
@@ -311,6 +316,7 @@ __global__ void __launch_bounds__(64) k_bh_walk(const KNode<3> *nodes, const int
     int a = leaves[t];
     const KNode<3> &n = nodes[a];
     const BHNode bn = B[a];
+    constexpr bool F32 = MODE != 0;
     const float mpf = (float)mp, fr2f = (float)(force_res * force_res);
     for (int p0 = 0; p0 < n.n; p0 += RSG_BH_G) {
         int np_ = min(RSG_BH_G, n.n - p0);
@@ -334,11 +340,13 @@ __global__ void __launch_bounds__(64) k_bh_walk(const KNode<3> *nodes, const int
         // adds one term to particle p's sum
 #define RSG_BH_ADD(p, term64, term32)                  \
     do {                                                \
-        if (F32) {                                      \
+        if (MODE == 1) {                                \
             float y_ = (term32) - c[p];                 \
             float t_ = s[p] + y_;                       \
             c[p] = (t_ - s[p]) - y_;                    \
             s[p] = t_;                                  \
+        } else if (MODE == 2) {                         \
+            s[p] += (term32);                           \
         } else {                                        \
             acc[p] += (term64);                         \
         }                                               \
@@ -1576,14 +1584,83 @@ static int32_t select_idx(Arena &ar, const int32_t *flag, int32_t *out, int32_t 
     return h;
 }
 
-// Barnes-Hut potentials for the segments (rs[k], rn[k]) of PO.
+// FP64 direct sum over every pair of each set, the reference values of the
+// potential precision study (no counterpart in the reference, which only has
+// the Barnes-Hut walk): pe_i += mp * sum_{j != i} 1 / max(r_ij, FORCE_RES),
+// with coordinate differences, r^2 and 1/r in FP64.  One block per tile of
+// RSG_DT targets of one set (tile t of set k: tof[k] <= t < tof[k + 1]);
+// sources pass through shared memory RSG_DT at a time.
+#define RSG_DT 256
+__global__ void k_direct_tiles(const int32_t *rn, int32_t ns, int32_t *cnt) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k <= ns) cnt[k] = k < ns ? (rn[k] + RSG_DT - 1) / RSG_DT : 0;
+}
+__global__ void __launch_bounds__(RSG_DT) k_direct64(PotRec *PO, const int32_t *rs,
+                                                     const int32_t *rn, const int32_t *tof,
+                                                     int32_t ns, double mp, double force_res) {
+    __shared__ double sx[RSG_DT], sy[RSG_DT], sz[RSG_DT];
+    const int32_t t = blockIdx.x;
+    int32_t lo = 0, hi = ns;  // last k with tof[k] <= t
+    while (hi - lo > 1) {
+        int32_t mid = (lo + hi) >> 1;
+        if (tof[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    const int32_t s0 = rs[lo], n = rn[lo];
+    const int32_t i = (t - tof[lo]) * RSG_DT + (int32_t)threadIdx.x;
+    const bool act = i < n;
+    double xi = 0, yi = 0, zi = 0;
+    if (act) {
+        xi = PO[s0 + i].pos[0];
+        yi = PO[s0 + i].pos[1];
+        zi = PO[s0 + i].pos[2];
+    }
+    const double fr2 = force_res * force_res, ifr = 1.0 / force_res;
+    double acc = 0;
+    for (int32_t j0 = 0; j0 < n; j0 += RSG_DT) {
+        const int32_t jj = j0 + (int32_t)threadIdx.x;
+        __syncthreads();
+        if (jj < n) {
+            sx[threadIdx.x] = PO[s0 + jj].pos[0];
+            sy[threadIdx.x] = PO[s0 + jj].pos[1];
+            sz[threadIdx.x] = PO[s0 + jj].pos[2];
+        }
+        __syncthreads();
+        const int32_t m = min(RSG_DT, n - j0), self = i - j0;
+        for (int32_t q = 0; q < m; q++) {
+            double dx = xi - sx[q], dy = yi - sy[q], dz = zi - sz[q];
+            double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+            double inv = r2 < fr2 ? ifr : rsqrt(r2);
+            acc += q == self ? 0.0 : inv;
+        }
+    }
+    if (act) PO[s0 + i].pe += mp * acc;
+}
+
+// Potentials for the segments (rs[k], rn[k]) of PO.  Every form first builds
+// the Barnes-Hut forest, which permutes each segment into tree order, so the
+// records come out in the same order whatever the form:
+//   0  Barnes-Hut, the reference's FP64 arithmetic (node sums in order);
+//   1  Barnes-Hut, FP32 terms with Kahan-compensated FP32 sums;
+//   2  Barnes-Hut, FP32 terms with plain FP32 sums;
+//   3  FP64 direct sum over all pairs (precision reference).
 void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const int32_t *rn,
                   int32_t ntrees, double mp, double force_res, int *err, cudaStream_t st,
-                  int exact) {
+                  int form) {
     const int T = 256;
     if (ntrees == 0) return;
+    const int exact = form == 0;
     Forest<3> F = build_forest<3, PotRec>(ar, PO, npo, rs, rn, ntrees, npo, 10, st);
     phase_mark(st, "p.bh_tree");
+    if (form == 3) {
+        int32_t *cnt = ar.get<int32_t>(ntrees + 1), *tof = ar.get<int32_t>(ntrees + 1);
+        launch(k_direct_tiles, nblk(ntrees + 1, T), T, 0, st, rn, ntrees, cnt);
+        int32_t ntiles = scan_i32(ar, cnt, tof, ntrees + 1, st);
+        if (ntiles) launch(k_direct64, ntiles, RSG_DT, 0, st, PO, rs, rn, tof, ntrees, mp, force_res);
+        RSG_CHECK_LAUNCH();
+        phase_mark(st, "p.direct");
+        return;
+    }
     BHNode *B = ar.get<BHNode>(F.nnodes);
     launch(k_bh_leaf, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, PO, mp, B);
     for (int l = F.nlv - 2; l >= 0; l--) {
@@ -1601,11 +1678,14 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     int32_t *lf = ar.get<int32_t>(F.nnodes), *leaves = ar.get<int32_t>(F.nnodes);
     launch(k_leaf_list_flags, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, lf);
     int32_t nl = select_idx(ar, lf, leaves, F.nnodes, st);
-    if (exact)
-        launch(k_bh_walk<false>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
+    if (form == 0)
+        launch(k_bh_walk<0>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
+               err);
+    else if (form == 1)
+        launch(k_bh_walk<1>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
                err);
     else
-        launch(k_bh_walk<true>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
+        launch(k_bh_walk<2>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
                err);
     RSG_CHECK_LAUNCH();
     phase_mark(st, "p.bh_walk");
@@ -1687,6 +1767,18 @@ static void seg_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, PotRec *P
     ar.used = mark;
 }
 
+// Potential form of the batched path (bh_potential's forms 0-3; the plain
+// path always uses form 0), process-wide, set by rsg_set_potential_form.
+static std::atomic<int> g_pot_form{1};
+int batched_potential_form() { return g_pot_form.load(std::memory_order_relaxed); }
+int set_batched_potential_form(int f) { return g_pot_form.exchange(f); }
+
+// Test hook: when g_keep_po is set, the potential records of the last
+// additional_props call (sorted by halo, then potential-only last, then
+// radius; pe and ke final) are kept in g_dbg_po.
+std::atomic<bool> g_keep_po{false};
+std::vector<PotRec> g_dbg_po;
+
 void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec *W,
                       int64_t M, rsg_halo *H, rsg_extra_halo_info *E, int32_t NH,
                       cudaStream_t st, int exact) {
@@ -1719,7 +1811,8 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
         int32_t nr = select_idx(ar, rflag, hl, NH, st);
         int32_t *rs = ar.get<int32_t>(nr + 1), *rn = ar.get<int32_t>(nr + 1);
         if (nr) launch(k_bh_root_arrays, nblk(nr, T), T, 0, st, hl, nr, toff, tot, rs, rn);
-        bh_potential(ar, PO, npo, rs, rn, nr, dc.particle_mass, dc.force_res, err, st, exact);
+        bh_potential(ar, PO, npo, rs, rn, nr, dc.particle_mass, dc.force_res, err, st,
+                     exact ? 0 : batched_potential_form());
         ar.used = m2;
     }
     // drop potential-only records and sort every halo's records by r^2
@@ -1757,6 +1850,12 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     }
     RSG_CHECK_LAUNCH();
     phase_mark(st, "p.scans");
+    if (g_keep_po.load()) {
+        g_dbg_po.resize(npo);
+        if (npo)
+            RSG_CUDA(cudaMemcpyAsync(g_dbg_po.data(), PO2, sizeof(PotRec) * npo,
+                                     cudaMemcpyDeviceToHost, st));
+    }
     int herr[2];
     unsigned long long hwork[4];
     RSG_CUDA(cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, st));

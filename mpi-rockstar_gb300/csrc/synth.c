@@ -20,12 +20,24 @@
  *      above 5000 particles carry 0-20 NFW subhalos (1-10% of the host each,
  *      c = 12) at radii drawn from the host profile, moving with a bulk
  *      velocity drawn from the host dispersion; 35% background.
+ *   3  isolated groups for the potential/unbinding precision study:
+ *      200000 groups with counts from dN/dN ~ N^-1.9 on [20, hi], where
+ *      hi = 2e6 at scale 1 and 2e6 * scale (at least 2000) below it, so a
+ *      reduced-scale run keeps the expected number of groups near the top
+ *      of the range; m_p = 1e9 Msun/h.  Half NFW, half Hernquist (a = r200/c),
+ *      c log-uniform in [4, 15], both truncated at r200, one group per cell
+ *      of a cubic lattice (cell = 2 r200 of the largest group + 1 Mpc/h), so
+ *      no group links to another.  Velocities: bulk N(0, 300 km/s) per
+ *      component plus N(0, V200^2/3) per component, except for the first 10%
+ *      of each group's particles, which move isotropically at 1.2-3 times the
+ *      escape speed of the truncated profile at their radius.  No background.
  *   4  512^3 particles, 500 Mpc/h box; hosts on [20, 5e6] with
  *      c = 10 (N/1e4)^-0.1, subhalos as in 2, 45% background.
  *   5  one NFW host of 2e7 particles (c = 5) with 2000 subhalos (power law on
  *      [20, 2e5], c = 12); the 20 largest carry 5-30 sub-subhalos each; plus
  *      5e6 background particles in a 20 Mpc/h box.
  * Particle masses for 2, 4 and 5 follow the box: m_p = Om rho_c L^3 / N.
+ * With scale < 1 the structure counts shrink with it as described above.
  */
 #include <math.h>
 #include <stdint.h>
@@ -80,6 +92,8 @@ struct halo_spec {
     double cen[3], vel[3];
     double rs, c, sigma; /* scale radius (Mpc/h), concentration, 1D dispersion */
     double r200;
+    int prof;          /* 0 NFW, 1 Hernquist (a = r200 / c) */
+    int64_t n_fast;    /* leading particles launched above the escape speed */
 };
 
 struct synth_plan {
@@ -177,6 +191,53 @@ static void plan_hosts(struct synth_plan *pl, int cfg, double scale, uint64_t se
     (void)scale;
 }
 
+/* Hernquist radius (Mpc/h) enclosing fraction f of the mass inside R = c a */
+static double hernquist_inverse(double f, double a, double c) {
+    double sr = sqrt(f) * c / (c + 1.0);
+    return a * sr / (1.0 - sr);
+}
+
+/* escape speed (km/s) at radius r of a profile truncated at r200 */
+static double escape_speed(const struct halo_spec *s, double mp, double r) {
+    double m = (double)s->n * mp, phi;
+    if (r < 1e-6 * s->rs) r = 1e-6 * s->rs;
+    if (s->prof == 1) {
+        double a = s->rs, R = s->r200, mn = m * (R + a) * (R + a) / (R * R);
+        phi = GRAV * mn * (1.0 / (r + a) - a / ((R + a) * (R + a)));
+    } else {
+        double x = r / s->rs;
+        phi = GRAV * m / (s->rs * nfw_m(s->c)) * (log1p(x) / x - 1.0 / (1.0 + s->c));
+    }
+    return sqrt(2.0 * fmax(phi, 0.0));
+}
+
+static void plan_isolated(struct synth_plan *pl, double scale, uint64_t seed) {
+    int64_t ng = (int64_t)(200000 * scale + 0.5);
+    if (ng < 1) ng = 1;
+    double hi = scale >= 1.0 ? 2e6 : fmax(2000.0, 2e6 * scale);
+    double rmax = 0;
+    for (int64_t k = 0; k < ng; k++) {
+        struct halo_spec s;
+        memset(&s, 0, sizeof(s));
+        s.n = (int64_t)powerlaw(u01(seed, 51, k), 20, hi, 1.9);
+        double c = exp(log(4.0) + u01(seed, 52, k) * (log(15.0) - log(4.0)));
+        s.prof = u01(seed, 53, k) < 0.5 ? 1 : 0;
+        set_profile(&s, pl->mp, c);
+        s.n_fast = s.n / 10;
+        for (int d = 0; d < 3; d++) s.vel[d] = 300.0 * gauss(seed, 54, 3 * k + d);
+        if (s.r200 > rmax) rmax = s.r200;
+        plan_push(pl, s);
+    }
+    double cell = 2.0 * rmax + 1.0;
+    int64_t side = 1;
+    while (side * side * side < ng) side++;
+    pl->box = cell * (double)side;
+    for (int64_t k = 0; k < ng; k++) {
+        int64_t c[3] = {k % side, (k / side) % side, k / (side * side)};
+        for (int d = 0; d < 3; d++) pl->h[k].cen[d] = ((double)c[d] + 0.5) * cell;
+    }
+}
+
 static void plan_cluster(struct synth_plan *pl, double scale, uint64_t seed) {
     int64_t nhost = (int64_t)(2e7 * scale);
     struct halo_spec host;
@@ -241,9 +302,16 @@ static int make_plan(struct synth_plan *pl, int cfg, double scale, uint64_t seed
     switch (cfg) {
     case 1: pl->n_total = (int64_t)(262144 * scale); pl->box = 40.0 * cbrt(scale); pl->mp = 1e9; break;
     case 2: pl->n_total = (int64_t)(2097152 * scale); pl->box = 80.0 * cbrt(scale); break;
+    case 3: pl->mp = 1e9; plan_isolated(pl, scale, seed); break;
     case 4: pl->n_total = (int64_t)(134217728 * scale); pl->box = 500.0 * cbrt(scale); break;
     case 5: pl->n_total = (int64_t)(2.5e7 * scale); pl->box = 20.0 * cbrt(scale); break;
     default: return -1;
+    }
+    if (cfg == 3) {
+        int64_t s = 0;
+        for (int64_t i = 0; i < pl->nh; i++) { pl->h[i].start = s; s += pl->h[i].n; }
+        pl->n_struct = pl->n_total = s;
+        return 0;
     }
     if (pl->n_total < 1) return -1;
     if (!pl->mp) pl->mp = OMEGA_M * RHO_CRIT * pl->box * pl->box * pl->box / (double)pl->n_total;
@@ -289,7 +357,8 @@ int synth_generate(int cfg, double scale, uint64_t seed, struct particle *out,
         const struct halo_spec *s = pl.h + hi;
         uint64_t st = 1000000 + (uint64_t)hi;
         for (int64_t k = 0; k < s->n; k++) {
-            double x = nfw_inverse(u01(seed, st, 8 * k), s->c) * s->rs;
+            double x = s->prof == 1 ? hernquist_inverse(u01(seed, st, 8 * k), s->rs, s->c)
+                                    : nfw_inverse(u01(seed, st, 8 * k), s->c) * s->rs;
             double mu = 2.0 * u01(seed, st, 8 * k + 1) - 1.0;
             double ph = 2.0 * M_PI * u01(seed, st, 8 * k + 2);
             double sn = sqrt(fmax(0.0, 1.0 - mu * mu));
@@ -297,6 +366,18 @@ int synth_generate(int cfg, double scale, uint64_t seed, struct particle *out,
             q->pos[0] = wrap(s->cen[0] + x * sn * cos(ph), box);
             q->pos[1] = wrap(s->cen[1] + x * sn * sin(ph), box);
             q->pos[2] = wrap(s->cen[2] + x * mu, box);
+            if (k < s->n_fast) {
+                /* isotropic, 1.2-3x the escape speed at this radius */
+                uint64_t sf = 5000000 + (uint64_t)hi;
+                double v = (1.2 + 1.8 * u01(seed, sf, 3 * k)) * escape_speed(s, pl.mp, x);
+                double vm = 2.0 * u01(seed, sf, 3 * k + 1) - 1.0;
+                double vp = 2.0 * M_PI * u01(seed, sf, 3 * k + 2);
+                double vs = sqrt(fmax(0.0, 1.0 - vm * vm));
+                q->pos[3] = (float)(s->vel[0] + v * vs * cos(vp));
+                q->pos[4] = (float)(s->vel[1] + v * vs * sin(vp));
+                q->pos[5] = (float)(s->vel[2] + v * vm);
+                continue;
+            }
             for (int d = 0; d < 3; d++)
                 q->pos[3 + d] = (float)(s->vel[d] + s->sigma * gauss(seed, st, 4 * k + 2 + d + 4 * (int64_t)s->n));
         }

@@ -5,6 +5,8 @@ import glob
 import os
 import re
 
+import numpy as np
+
 from conftest import ROOT
 
 
@@ -51,3 +53,19 @@ def test_errors_without_gpu(rk):
         assert e.code in (-2, -3)
     else:
         raise AssertionError("expected an error without a GPU")
+
+
+def test_isolated_groups_workload(rk):
+    """The precision study's snapshot: one group per lattice cell, every
+    particle at least 0.5 Mpc/h inside its cell, so no two groups can link."""
+    p, box, mp, ng = rk.synth(3, 0.002)
+    assert ng == 400 and mp == 1e9
+    side = int(np.ceil(ng ** (1 / 3) - 1e-9))
+    cell = box / side
+    x = p["pos"][:, :3].astype(np.float64)
+    f = x - np.floor(x / cell) * cell
+    assert f.min() >= 0.5 - 1e-4 and f.max() <= cell - 0.5 + 1e-4
+    # every occupied cell is one of the first ng cells in x-fastest order
+    c = np.floor(x / cell).astype(np.int64)
+    idx = c[:, 0] + side * (c[:, 1] + side * c[:, 2])
+    assert idx.max() < ng and len(np.unique(idx)) == ng

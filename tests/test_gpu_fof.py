@@ -69,3 +69,24 @@ def test_fof_empty_and_tiny(rk):
         out, off, sz = rk.rockstar_fof(p, c)
         assert len(out) == n
         assert (len(off) == 1) == (n >= 10)
+
+
+@pytest.mark.parametrize("cfg_id,scale,parts", [(2, 0.25, 4), (3, 0.01, 7)])
+def test_fof_chunked_later_lists(rk, cfg_id, scale, parts, monkeypatch):
+    """A later-dense list larger than its buffer is built and walked in
+    chunks of particles; the groups must be the same bytes as with the whole
+    list (RSG_FOF_LIST_ENTRIES caps the buffer)."""
+    p, box, mp, _ = rk.synth(cfg_id, scale)
+    cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    whole = rk.rockstar_fof(p, cfg)
+    ne = rk.last_stats()["later_list"]
+    assert ne > 4 * (1 << 17)
+    monkeypatch.setenv("RSG_FOF_LIST_ENTRIES", str(ne // parts))
+    chunked = rk.rockstar_fof(p, cfg)
+    assert rk.last_stats()["later_list"] == ne
+    for a, b in zip(whole, chunked):
+        assert a.tobytes() == b.tobytes()
+    monkeypatch.setenv("RSG_FOF_LIST_ENTRIES", "1000")
+    with pytest.raises(rk.RockstarError) as e:
+        rk.rockstar_fof(p, cfg)
+    assert e.value.code == -4
