@@ -231,6 +231,77 @@ __global__ void k_bh_internal_warp(const KNode<3> *nodes, int32_t first, int32_t
     }
 }
 
+// Batched form, internal nodes of more than RSG_BH_HUGE points: one block
+// per chunk of RSG_BH_CH points forms the chunk's sum and maximum of squared
+// distances to the node's mass centre (part[item]); one thread per node
+// adds the chunks in order.  item = (node, chunk); the chunks of node j of
+// a level are items first[j] .. first[j + 1].
+#define RSG_BH_HUGE 65536
+#define RSG_BH_CH 16384
+__device__ __forceinline__ BHNode bh_merge(const BHNode &L, const BHNode &R) {
+    BHNode b;
+    b.m = fadd(L.m, R.m);
+    for (int j = 0; j < 3; j++)
+        b.mc[j] = b.m ? __fdiv_rn(fadd(fmul(R.mc[j], R.m), fmul(L.mc[j], L.m)), b.m) : 0.f;
+    return b;
+}
+__global__ void __launch_bounds__(256) k_bh_huge_part(const KNode<3> *nodes, const int2 *item,
+                                                      const PotRec *PO, const BHNode *B,
+                                                      double2 *part) {
+    __shared__ double s_s[8], m_s[8];
+    const int2 it = item[blockIdx.x];
+    const KNode<3> &x = nodes[it.x];
+    const BHNode b = bh_merge(B[x.left], B[x.left + 1]);
+    const int i0 = it.y * RSG_BH_CH, i1 = min(x.n, i0 + RSG_BH_CH);
+    double sx = 0, bm = 0;
+    for (int i = i0 + threadIdx.x; i < i1; i += 256) {
+        double dx = d2d(b.mc, PO[x.start + i].pos);
+        if (bm < dx) bm = dx;
+        sx += dx;
+    }
+    for (int o = 16; o; o >>= 1) {
+        sx += __shfl_down_sync(0xffffffffu, sx, o);
+        bm = fmax(bm, __shfl_down_sync(0xffffffffu, bm, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_s[threadIdx.x >> 5] = sx;
+        m_s[threadIdx.x >> 5] = bm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; w++) {
+            sx += s_s[w];
+            bm = fmax(bm, m_s[w]);
+        }
+        part[blockIdx.x] = make_double2(sx, bm);
+    }
+}
+__global__ void k_bh_huge_fin(const KNode<3> *nodes, const int32_t *node, const int32_t *first,
+                              int32_t nn, const double2 *part, BHNode *B) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nn) return;
+    int a = node[j];
+    const KNode<3> &x = nodes[a];
+    BHNode b = bh_merge(B[x.left], B[x.left + 1]);
+    double sx = 0, bm = 0;
+    for (int c = first[j]; c < first[j + 1]; c++) {
+        sx += part[c].x;
+        bm = fmax(bm, part[c].y);
+    }
+    bm = sqrt(bm) / 2.0;
+    b.dmin = (float)(bm + sqrt(bm * bm + sx / (x.n * 1.0)));
+    B[a] = b;
+}
+__global__ void k_bh_huge_flags(const KNode<3> *nodes, int32_t nn, int32_t *f) {
+    int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < nn) f[a] = nodes[a].div >= 0 && nodes[a].n > RSG_BH_HUGE;
+}
+__global__ void k_bh_huge_sizes(const KNode<3> *nodes, const int32_t *node, int32_t nn,
+                                int32_t *n) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < nn) n[j] = nodes[node[j]].n;
+}
+
 // Large internal nodes: the block computes every point's squared distance
 // to the mass centre; the maximum is a reduction and the sum is added by one
 // thread in point order, as _compute_dmin does.
@@ -243,6 +314,7 @@ __global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, 
     int a = first + blockIdx.x;
     const KNode<3> &x = nodes[a];
     if (x.div < 0 || x.n <= RSG_BH_BIG) return;
+    if (!exact && x.n > RSG_BH_HUGE) return;  // k_bh_huge_*
     if (threadIdx.x == 0) {
         const BHNode &L = B[x.left], &R = B[x.left + 1];
         bs.m = fadd(L.m, R.m);
@@ -1663,6 +1735,42 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     }
     BHNode *B = ar.get<BHNode>(F.nnodes);
     launch(k_bh_leaf, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, PO, mp, B);
+    // batched form: the nodes of more than RSG_BH_HUGE points, by level, and
+    // their chunks (node ids ascend with the level index in the forest)
+    std::vector<int32_t> hn_node, hn_first(1, 0);  // per huge node: id, first item
+    std::vector<int2> hitem;
+    int2 *d_item = nullptr;
+    int32_t *d_hnode = nullptr, *d_hfirst = nullptr;
+    double2 *d_part = nullptr;
+    if (!exact) {
+        int32_t *hf = ar.get<int32_t>(F.nnodes), *hid = ar.get<int32_t>(F.nnodes);
+        launch(k_bh_huge_flags, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, hf);
+        int32_t nh = select_idx(ar, hf, hid, F.nnodes, st);
+        if (nh) {
+            int32_t *hsz = ar.get<int32_t>(nh);
+            launch(k_bh_huge_sizes, nblk(nh, T), T, 0, st, F.nodes, hid, nh, hsz);
+            std::vector<int32_t> sz(nh);
+            hn_node.resize(nh);
+            RSG_CUDA(cudaMemcpyAsync(hn_node.data(), hid, 4 * nh, cudaMemcpyDeviceToHost, st));
+            RSG_CUDA(cudaMemcpyAsync(sz.data(), hsz, 4 * nh, cudaMemcpyDeviceToHost, st));
+            RSG_CUDA(cudaStreamSynchronize(st));
+            for (int32_t j = 0; j < nh; j++) {
+                int nc = (sz[j] + RSG_BH_CH - 1) / RSG_BH_CH;
+                for (int c = 0; c < nc; c++) hitem.push_back(make_int2(hn_node[j], c));
+                hn_first.push_back((int32_t)hitem.size());
+            }
+            d_item = ar.get<int2>(hitem.size());
+            d_part = ar.get<double2>(hitem.size());
+            d_hnode = ar.get<int32_t>(nh);
+            d_hfirst = ar.get<int32_t>(nh + 1);
+            RSG_CUDA(cudaMemcpyAsync(d_item, hitem.data(), sizeof(int2) * hitem.size(),
+                                     cudaMemcpyHostToDevice, st));
+            RSG_CUDA(cudaMemcpyAsync(d_hnode, hn_node.data(), 4 * nh, cudaMemcpyHostToDevice, st));
+            RSG_CUDA(cudaMemcpyAsync(d_hfirst, hn_first.data(), 4 * (nh + 1),
+                                     cudaMemcpyHostToDevice, st));
+        }
+    }
+    size_t hj = hn_node.size();  // huge nodes not yet done (taken from the back: deepest first)
     for (int l = F.nlv - 2; l >= 0; l--) {
         int32_t a = F.lv_first[l], b = F.lv_first[l + 1];
         if (b > a) {
@@ -1672,6 +1780,16 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
                 launch(k_bh_internal_warp, nblk((int64_t)(b - a) * 32, 256), 256, 0, st, F.nodes, a,
                        b - a, PO, B);
             launch(k_bh_internal_big, b - a, 256, 0, st, F.nodes, a, b - a, PO, B, exact);
+            size_t j1 = hj;
+            while (hj > 0 && hn_node[hj - 1] >= a) hj--;
+            if (j1 > hj) {
+                int32_t i0 = hn_first[hj], i1 = hn_first[j1];
+                launch(k_bh_huge_part, i1 - i0, 256, 0, st, F.nodes, (const int2 *)d_item + i0,
+                       PO, (const BHNode *)B, d_part + i0);
+                launch(k_bh_huge_fin, nblk((int)(j1 - hj), 64), 64, 0, st, F.nodes,
+                       (const int32_t *)d_hnode + hj, (const int32_t *)d_hfirst + hj,
+                       (int32_t)(j1 - hj), (const double2 *)d_part, B);
+            }
         }
     }
     phase_mark(st, "p.bh_mass");

@@ -1015,66 +1015,113 @@ __global__ void k_halo_init(rsg_halo *H, rsg_extra_halo_info *E, int32_t nh) {
 }
 
 // src/groupies.c:542-551: particle -> halo from the children's halos, and
-// real coordinates restored from the caller's particles.
-__global__ void k_asc_mark(Rec *W, const rsg_particle *P, HierNodes N, int32_t base,
-                           const rsg_halo *H, int32_t *phalo) {
-    int node = base + blockIdx.x;
-    int s = N.start[node], n = N.n[node];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        phalo[s + i] = -1;
-        const rsg_particle &q = P[W[s + i].ridx];
+// real coordinates restored from the caller's particles.  The restore runs
+// one thread per particle of the level; the marks one warp per halo (block
+// (k, y) takes every gridDim.y-th group of warps of node k's halos).  The
+// reference's loop over the halos in index order leaves a particle listed by
+// several halos with the largest index, which atomicMax gives in any order.
+__global__ void k_asc_restore(Rec *W, const rsg_particle *P, const int32_t *eln, int64_t M,
+                              int32_t *phalo) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M || eln[i] < 0) return;
+    phalo[i] = -1;
+    const rsg_particle &q = P[W[i].ridx];
 #pragma unroll
-        for (int d = 0; d < 6; d++) W[s + i].pos[d] = q.pos[d];
-    }
-    __syncthreads();
-    for (int h = N.h0[node]; h < N.h1[node]; h++) {
+    for (int d = 0; d < 6; d++) W[i].pos[d] = q.pos[d];
+}
+__global__ void k_asc_halo_mark(HierNodes N, int32_t base, const rsg_halo *H, int32_t *phalo) {
+    int node = base + blockIdx.x;
+    int h0 = N.h0[node], h1 = N.h1[node];
+    const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int h = h0 + blockIdx.y * wpb + w; h < h1; h += gridDim.y * wpb) {
         int ps = (int)H[h].p_start, np = (int)H[h].num_p;
-        for (int j = threadIdx.x; j < np; j += blockDim.x) phalo[ps + j] = h;
+        for (int j = lane; j < np; j += 32) atomicMax(&phalo[ps + j], h);
     }
 }
 
 // _find_biggest_parent without temporal information (src/groupies.c:362-380)
-__device__ int biggest(const rsg_halo *H, int h0, int h1, int growing_only, int first) {
-    int mi = growing_only ? first : h0;
-    for (int i = h0; i < h1; i++) {
+// is a running strict maximum of (vmax, num_p) from a start halo: the first
+// index holding the largest pair, except that a NaN vmax never replaces and
+// a NaN at the start is never replaced.  big_gt: candidate a beats b.
+__device__ __forceinline__ bool big_gt(const rsg_halo &a, const rsg_halo &b) {
+    return a.vmax > b.vmax || (a.vmax == b.vmax && a.num_p > b.num_p);
+}
+// That choice over halos h0..h1 (growing ones only, starting from `first`,
+// or all, starting from h0) as a block reduction (blockDim 256).
+__device__ int biggest_blk(const rsg_halo *H, int h0, int h1, int growing_only, int first) {
+    __shared__ int red[256];
+    int start = growing_only ? first : h0;
+    int loc = -1;
+    for (int i = h0 + threadIdx.x; i < h1; i += blockDim.x) {
         if (growing_only && !(H[i].flags & RSG_GROWING)) continue;
-        if (H[i].vmax > H[mi].vmax) mi = i;
-        if (H[i].vmax == H[mi].vmax && H[i].num_p > H[mi].num_p) mi = i;
+        if (H[i].vmax != H[i].vmax) continue;
+        if (loc < 0 || big_gt(H[i], H[loc])) loc = i;
     }
-    return mi;
+    red[threadIdx.x] = loc;
+    __syncthreads();
+    for (int o = blockDim.x >> 1; o; o >>= 1) {
+        if (threadIdx.x < o) {
+            int a = red[threadIdx.x], b = red[threadIdx.x + o];
+            if (a < 0 || (b >= 0 && (big_gt(H[b], H[a]) || (!big_gt(H[a], H[b]) && b < a))))
+                red[threadIdx.x] = b;
+        }
+        __syncthreads();
+    }
+    int best = red[0];
+    __syncthreads();
+    if (best < 0 || H[start].vmax != H[start].vmax) return start;
+    return big_gt(H[best], H[start]) ? best : (growing_only ? start : best);
 }
 
 // src/groupies.c:553-582: biggest seed, Poisson/force-resolution merges,
-// growing list.  One thread per node.
-__global__ void k_asc_seed(HierNodes N, int32_t base, int32_t count, rsg_halo *H,
-                           rsg_extra_halo_info *E, int32_t *glist, int32_t *redirect,
-                           double force_res) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    int node = base + k;
+// growing list.  One block (256 threads) per node: the merge test of every
+// halo against the biggest in parallel, the growing list compacted in index
+// order.
+__global__ void __launch_bounds__(256) k_asc_seed_blk(HierNodes N, int32_t base, rsg_halo *H,
+                                                      rsg_extra_halo_info *E, int32_t *glist,
+                                                      int32_t *redirect, double force_res) {
+    typedef cub::BlockScan<int, 256> Scan;
+    __shared__ typename Scan::TempStorage ts;
+    __shared__ int run;
+    int node = base + blockIdx.x;
     int h0 = N.h0[node], h1 = N.h1[node];
-    int mi = biggest(H, h0, h1, 0, 0);
-    H[mi].flags |= RSG_GROWING;
-    E[mi].sub_of = -1;
-    int ng = 0;
-    glist[h0 + ng++] = mi;
-    for (int i = h0; i < h1; i++) {
-        redirect[i] = -1;
-        if (i == mi || !(H[i].flags & RSG_GROWING)) continue;
-        int force;
-        if (poisson_or_force(H[i], H[mi], force_res, &force)) {
-            H[i].flags -= (H[i].flags & RSG_GROWING);
-            E[i].sub_of = mi;
-            if (!force) {
-                redirect[i] = mi;
-                H[i].num_p = 0;
-            }
-            continue;
-        }
-        glist[h0 + ng++] = i;
+    int mi = biggest_blk(H, h0, h1, 0, 0);
+    if (threadIdx.x == 0) {
+        H[mi].flags |= RSG_GROWING;
+        E[mi].sub_of = -1;
+        glist[h0] = mi;
+        run = 1;
     }
-    N.maxi[node] = mi;
-    N.ng[node] = ng;
+    __syncthreads();
+    for (int c0 = h0; c0 < h1; c0 += 256) {
+        int i = c0 + threadIdx.x, keep = 0;
+        if (i < h1) {
+            redirect[i] = -1;
+            if (i != mi && (H[i].flags & RSG_GROWING)) {
+                int force;
+                if (poisson_or_force(H[i], H[mi], force_res, &force)) {
+                    H[i].flags -= (H[i].flags & RSG_GROWING);
+                    E[i].sub_of = mi;
+                    if (!force) {
+                        redirect[i] = mi;
+                        H[i].num_p = 0;
+                    }
+                } else {
+                    keep = 1;
+                }
+            }
+        }
+        int at, tot;
+        Scan(ts).ExclusiveSum(keep, at, tot);
+        if (keep) glist[h0 + run + at] = i;
+        __syncthreads();
+        if (threadIdx.x == 0) run += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        N.maxi[node] = mi;
+        N.ng[node] = run;
+    }
 }
 
 // src/groupies.c:584-609: particles of merged seeds go to the biggest halo;
@@ -1120,9 +1167,10 @@ struct AscBucket {
     int32_t inv;  // holds a halo without a valid metric (never skipped)
 };
 __global__ void k_asc_buckets(HierNodes N, int32_t base, const rsg_halo *H,
-                              const int32_t *glist, AscBucket *bk, AscBucket *bk2) {
+                              const int32_t *glist, int all, AscBucket *bk, AscBucket *bk2) {
     int node = base + blockIdx.x;
-    int ng = N.ng[node], h0 = N.h0[node];
+    int h0 = N.h0[node];
+    int ng = all ? N.h1[node] - h0 : N.ng[node];
     if (ng <= RSG_ASC_BUCKET) return;
     int nb = (ng + 31) / 32;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -1134,7 +1182,7 @@ __global__ void k_asc_buckets(HierNodes N, int32_t base, const rsg_halo *H,
         B.rmax = 0.f;
         B.inv = 0;
         for (int g = 32 * b; g < ng && g < 32 * b + 32; g++) {
-            const rsg_halo &hh = H[glist[h0 + g]];
+            const rsg_halo &hh = H[all ? h0 + g : glist[h0 + g]];
             if (hh.vrms <= 0 || hh.r <= 0 || !(hh.r == hh.r)) {
                 B.inv = 1;
                 continue;
@@ -1589,12 +1637,15 @@ __global__ void k_bp_vmax(rsg_halo *H, const int32_t *list, int32_t nl, const in
 }
 
 // growing-halo list of a level: node glist entries concatenated
-__global__ void k_list_growing(HierNodes N, int32_t base, int32_t count, const int32_t *goff,
-                               const int32_t *glist, int32_t *list) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
+// One block per node.
+__global__ void k_list_growing(HierNodes N, int32_t base, const int32_t *goff,
+                               const int32_t *glist, int32_t *list, int32_t *lnode) {
+    int k = blockIdx.x;
     int node = base + k;
-    for (int g = 0; g < N.ng[node]; g++) list[goff[k] + g] = glist[N.h0[node] + g];
+    for (int g = threadIdx.x; g < N.ng[node]; g += blockDim.x) {
+        list[goff[k] + g] = glist[N.h0[node] + g];
+        lnode[goff[k] + g] = k;
+    }
 }
 __global__ void k_ng(HierNodes N, int32_t base, int32_t count, int32_t *out, int all) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1611,21 +1662,44 @@ __global__ void k_list_all(HierNodes N, int32_t base, int32_t count, const int32
     for (int h = N.h0[node]; h < N.h1[node]; h++) list[off[k] + h - N.h0[node]] = h;
 }
 
-// Biggest halo among growing ones (all = 0) or all halos (all = 1).
-__global__ void k_maxi(HierNodes N, int32_t base, int32_t count, const rsg_halo *H,
-                       const int32_t *glist, int all) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    int node = base + k;
+// Biggest halo among growing ones (all = 0) or all halos (all = 1); one
+// block (256 threads) per node.
+__global__ void __launch_bounds__(256) k_maxi(HierNodes N, int32_t base, const rsg_halo *H,
+                                              const int32_t *glist, int all) {
+    int node = base + blockIdx.x;
     int h0 = N.h0[node];
-    N.maxi[node] = all ? biggest(H, h0, N.h1[node], 0, 0)
-                       : biggest(H, h0, N.h1[node], 1, glist[h0]);
+    int mi = all ? biggest_blk(H, h0, N.h1[node], 0, 0)
+                 : biggest_blk(H, h0, N.h1[node], 1, glist[h0]);
+    if (threadIdx.x == 0) N.maxi[node] = mi;
 }
 
-// find_best_parent (src/subhalo_metric.c:185-191) over the node's listed halos.
+// hdist(c, h) (calc_halo_dist) and, when the value is a metric rather than
+// the 1e20 of a too-small or invalid candidate, its float sum x before the
+// square root (else x = inf).
+__device__ __forceinline__ float hdist_x(const rsg_halo &c, const rsg_halo &h, float *x) {
+    *x = INFINITY;
+    if ((double)h.r > (double)c.r * 0.99999) return 1e20f;
+    if (c.vrms <= 0 || c.r <= 0) return 1e20f;
+    AscHalo a;
+    for (int d = 0; d < 3; d++) {
+        a.pos[d] = c.pos[d];
+        a.pos[d + 3] = c.bulkvel[d];
+    }
+    a.r = c.r;
+    a.vrms = c.vrms;
+    *x = asc_x(a, h.pos);
+    return (float)sqrt((double)*x);
+}
+// find_best_parent (src/subhalo_metric.c:185-191) over the node's listed
+// halos, first strict minimum in list order.  Nodes listing more than
+// RSG_ASC_BUCKET halos skip buckets (k_asc_buckets over the same list) that
+// cannot hold a winner while the best is at most 1e20 (then the 1e20 of a
+// too-small or invalid candidate cannot win): either every valid halo of
+// the bucket is too small (r * 0.99999 < h.r for the largest r), or the
+// bucket's lower bound of x is not below the best's x.
 __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const int32_t *loff,
                               const int32_t *list, const int32_t *hnode, rsg_halo *H,
-                              rsg_extra_halo_info *E) {
+                              rsg_extra_halo_info *E, const AscBucket *bk, const AscBucket *bk2) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int tot = loff[count];
     if (t >= tot) return;
@@ -1635,15 +1709,40 @@ __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const in
     int mi = N.maxi[node];
     int res = h;
     if (h != mi) {
-        float best = hdist(H[mi], H[h]);
+        const rsg_halo &hh = H[h];
+        float bx;
+        float best = hdist_x(H[mi], hh, &bx);
         res = mi;
-        for (int g = loff[k]; g < loff[k + 1]; g++) {
-            int c = list[g];
-            float m = hdist(H[c], H[h]);
+        const int g0 = loff[k], n = loff[k + 1] - g0, h0 = N.h0[node];
+        const bool buckets = bk && n > RSG_ASC_BUCKET;
+        for (int g = 0; g < n;) {
+            if (buckets && best <= 1e20f) {
+                if ((g & 1023) == 0) {
+                    const AscBucket &S = bk2[h0 + (g >> 10)];
+                    if ((double)hh.r > (double)S.rmax * 0.99999 ||
+                        !(asc_bucket_lb(S, hh.pos) < bx)) {
+                        g += 1024;
+                        continue;
+                    }
+                }
+                if ((g & 31) == 0) {
+                    const AscBucket &B = bk[h0 + (g >> 5)];
+                    if ((double)hh.r > (double)B.rmax * 0.99999 ||
+                        !(asc_bucket_lb(B, hh.pos) < bx)) {
+                        g += 32;
+                        continue;
+                    }
+                }
+            }
+            int c = list[g0 + g];
+            float x;
+            float m = hdist_x(H[c], hh, &x);
             if (m < best) {
                 best = m;
+                bx = x;
                 res = c;
             }
+            g++;
         }
     }
     E[h].sub_of = res;
@@ -2208,13 +2307,14 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         int32_t base = lvl_base[L], cnt = lvl_cnt[L];
         if (cnt == 0) continue;
         size_t mark = ar.used;
-        launch(k_asc_mark, cnt, T, 0, st, W, d_p, N, base, H, phalo);
-        phase_mark(st, "a.mark");
-        launch(k_asc_seed, nblk(cnt, 64), 64, 0, st, N, base, cnt, H, E, glist, redirect, cfg.force_res);
         RSG_CUDA(cudaMemsetAsync(eln, 0xff, 4 * M, st));
         launch(k_fill_eln, cnt, T, 0, st, N, base, eln);
+        launch(k_asc_restore, nblk(M, T), T, 0, st, W, d_p, (const int32_t *)eln, M, phalo);
+        launch(k_asc_halo_mark, dim3(cnt, 8), T, 0, st, N, base, (const rsg_halo *)H, phalo);
+        phase_mark(st, "a.mark");
+        launch(k_asc_seed_blk, cnt, 256, 0, st, N, base, H, E, glist, redirect, cfg.force_res);
         launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H, (const int32_t *)glist,
-               ascb, ascb2);
+               0, ascb, ascb2);
         launch(k_asc_assign_p, nblk(M, 128), 128, 0, st, (const Rec *)W, M, (const int32_t *)eln,
                N, base, (const rsg_halo *)H, (const rsg_extra_halo_info *)E,
                (const int32_t *)glist, (const int32_t *)redirect, (const AscBucket *)ascb,
@@ -2239,11 +2339,13 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         launch(k_ng, nblk(cnt + 1, T), T, 0, st, N, base, cnt, goffs, 0);
         int32_t ngr = excl_scan(ar, goffs, goffs, cnt + 1, st);
         int32_t *glv = ar.get<int32_t>(ngr + 1), *gnode = ar.get<int32_t>(ngr + 1);
-        launch(k_list_growing, nblk(cnt, T), T, 0, st, N, base, cnt, goffs, glist, glv);
-        launch(k_list_node, nblk(cnt, T), T, 0, st, cnt, goffs, gnode);
+        launch(k_list_growing, cnt, T, 0, st, N, base, goffs, glist, glv, gnode);
         basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
-        launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 0);
-        launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E);
+        launch(k_maxi, cnt, 256, 0, st, N, base, (const rsg_halo *)H, glist, 0);
+        launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H, (const int32_t *)glist,
+               0, ascb, ascb2);
+        launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E,
+               (const AscBucket *)ascb, (const AscBucket *)ascb2);
         fix_parents_level(ar, N, base, cnt, H, E, err, true, st);
         basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
         RSG_CHECK_LAUNCH();
@@ -2262,8 +2364,11 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             launch(k_gather<int32_t>, nblk(M, T), T, 0, st, phalo, val2, M, phalo2);
             std::swap(W, W2);
             std::swap(phalo, phalo2);
-            launch(k_maxi, nblk(cnt, T), T, 0, st, N, base, cnt, H, glist, 1);
-            launch(k_best_parent, nblk(na, T), T, 0, st, N, base, cnt, aoff, alist, anode, H, E);
+            launch(k_maxi, cnt, 256, 0, st, N, base, (const rsg_halo *)H, glist, 1);
+            launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H,
+                   (const int32_t *)glist, 1, ascb, ascb2);
+            launch(k_best_parent, nblk(na, T), T, 0, st, N, base, cnt, aoff, alist, anode, H, E,
+                   (const AscBucket *)ascb, (const AscBucket *)ascb2);
             fix_parents_level(ar, N, base, cnt, H, E, err, true, st);
             RSG_CHECK_LAUNCH();
             // find_subs tail (src/groupies.c:697-703): child counts and basic
