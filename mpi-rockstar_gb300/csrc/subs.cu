@@ -1224,6 +1224,154 @@ __device__ __forceinline__ float asc_bucket_lb(const AscBucket &B, const float *
     }
     return __fdiv_rn(d2, fmul(B.rmax, B.rmax));
 }
+// Nodes with more than RSG_ASC_BUCKET growing halos also get their halos in
+// Morton order of position (within the node's box of halo centres), so that
+// buckets of 32 and 1024 halos are compact in space.  The scan order then
+// differs from the list order; the choice stays the list scan's because a
+// candidate is taken on (metric, list position) lexicographically: the
+// first list position among the smallest metrics, which is what the strict
+// sequential comparison keeps.
+__device__ __forceinline__ uint32_t morton10(uint32_t v) {
+    v &= 1023u;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+__global__ void k_asc_sort_keys(HierNodes N, int32_t base, const rsg_halo *H,
+                                const int32_t *glist, uint32_t *key, int32_t *val, int32_t *sb,
+                                int32_t *se) {
+    __shared__ float mn[3], mx[3];
+    int k = blockIdx.x, node = base + k;
+    int ng = N.ng[node], h0 = N.h0[node];
+    if (threadIdx.x == 0) {
+        sb[k] = h0;
+        se[k] = ng > RSG_ASC_BUCKET ? h0 + ng : h0;
+        for (int d = 0; d < 3; d++) {
+            mn[d] = INFINITY;
+            mx[d] = -INFINITY;
+        }
+    }
+    __syncthreads();
+    if (ng <= RSG_ASC_BUCKET) return;
+    float lmn[3] = {INFINITY, INFINITY, INFINITY}, lmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        const float *p = H[glist[h0 + g]].pos;
+        for (int d = 0; d < 3; d++) {
+            lmn[d] = fminf(lmn[d], p[d]);
+            lmx[d] = fmaxf(lmx[d], p[d]);
+        }
+    }
+    __shared__ float red[6][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int d = 0; d < 3; d++) {
+        float a = lmn[d], b = lmx[d];
+        for (int o = 16; o; o >>= 1) {
+            a = fminf(a, __shfl_xor_sync(0xffffffffu, a, o));
+            b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+        }
+        if (lane == 0) {
+            red[d][w] = a;
+            red[d + 3][w] = b;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int v = 0; v < (int)(blockDim.x >> 5); v++)
+            for (int d = 0; d < 3; d++) {
+                mn[d] = fminf(mn[d], red[d][v]);
+                mx[d] = fmaxf(mx[d], red[d + 3][v]);
+            }
+    __syncthreads();
+    float sc[3];
+    for (int d = 0; d < 3; d++) sc[d] = (mx[d] > mn[d]) ? 1023.99f / (mx[d] - mn[d]) : 0.f;
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        const float *p = H[glist[h0 + g]].pos;
+        uint32_t q[3];
+        for (int d = 0; d < 3; d++) {
+            float t = (p[d] - mn[d]) * sc[d];
+            q[d] = (t >= 0.f && t < 1024.f) ? (uint32_t)t : 0u;
+        }
+        key[h0 + g] = morton10(q[0]) | (morton10(q[1]) << 1) | (morton10(q[2]) << 2);
+        val[h0 + g] = g;
+    }
+}
+// Candidate records of the Morton-ordered nodes: ah[h0 + j] is the halo at
+// sorted position j, gi[h0 + j] its (list position, halo index).
+__global__ void k_asc_sorted_recs(HierNodes N, int32_t base, const rsg_halo *H,
+                                  const int32_t *glist, const int32_t *sval, AscHalo *ah,
+                                  int2 *gi) {
+    int node = base + blockIdx.x;
+    int ng = N.ng[node], h0 = N.h0[node];
+    if (ng <= RSG_ASC_BUCKET) return;
+    for (int j = threadIdx.x; j < ng; j += blockDim.x) {
+        int g = sval[h0 + j], h = glist[h0 + g];
+        const rsg_halo &hh = H[h];
+        AscHalo c;
+        for (int d = 0; d < 3; d++) {
+            c.pos[d] = hh.pos[d];
+            c.pos[d + 3] = hh.bulkvel[d];
+        }
+        c.r = hh.r;
+        c.vrms = hh.vrms;
+        ah[h0 + j] = c;
+        gi[h0 + j] = make_int2(g, h);
+    }
+}
+// Buckets of 32 (and 1024) consecutive Morton-ordered candidates.
+__global__ void k_asc_buckets_s(HierNodes N, int32_t base, const AscHalo *ah, AscBucket *bk,
+                                AscBucket *bk2) {
+    int node = base + blockIdx.x;
+    int ng = N.ng[node], h0 = N.h0[node];
+    if (ng <= RSG_ASC_BUCKET) return;
+    int nb = (ng + 31) / 32;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        AscBucket B;
+        for (int d = 0; d < 3; d++) {
+            B.mn[d] = INFINITY;
+            B.mx[d] = -INFINITY;
+        }
+        B.rmax = 0.f;
+        B.inv = 0;
+        for (int j = 32 * b; j < ng && j < 32 * b + 32; j++) {
+            const AscHalo &c = ah[h0 + j];
+            if (c.vrms <= 0 || c.r <= 0 || !(c.r == c.r)) {
+                B.inv = 1;
+                continue;
+            }
+            for (int d = 0; d < 3; d++) {
+                B.mn[d] = fminf(B.mn[d], c.pos[d]);
+                B.mx[d] = fmaxf(B.mx[d], c.pos[d]);
+            }
+            B.rmax = fmaxf(B.rmax, c.r);
+        }
+        bk[h0 + b] = B;
+    }
+    __syncthreads();
+    int nsb = (nb + 31) / 32;
+    for (int sb = threadIdx.x; sb < nsb; sb += blockDim.x) {
+        AscBucket S = bk[h0 + 32 * sb];
+        for (int b = 32 * sb + 1; b < nb && b < 32 * sb + 32; b++) {
+            const AscBucket &B = bk[h0 + b];
+            for (int d = 0; d < 3; d++) {
+                S.mn[d] = fminf(S.mn[d], B.mn[d]);
+                S.mx[d] = fmaxf(S.mx[d], B.mx[d]);
+            }
+            S.rmax = fmaxf(S.rmax, B.rmax);
+            S.inv |= B.inv;
+        }
+        bk2[h0 + sb] = S;
+    }
+}
+// Smallest x whose metric (float)sqrt((double)x) can exceed `best`: any x
+// at or above best's float successor squared (exact in FP64) gives a metric
+// of at least that successor.
+__device__ __forceinline__ double asc_xcut(float best) {
+    double nb = (double)nextafterf(best, INFINITY);
+    return nb * nb;
+}
+
 // One thread per particle of the level (the node from eln): a node of
 // millions of particles spreads over the whole GPU.  Same choice as the
 // per-node form, with buckets and super-buckets (1024 halos) skipped when
@@ -1231,7 +1379,8 @@ __device__ __forceinline__ float asc_bucket_lb(const AscBucket &B, const float *
 __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, HierNodes N,
                                int32_t base, const rsg_halo *H, const rsg_extra_halo_info *E,
                                const int32_t *glist, const int32_t *redirect,
-                               const AscBucket *bk, const AscBucket *bk2, int32_t *phalo) {
+                               const AscBucket *bk, const AscBucket *bk2, const AscHalo *ah,
+                               const int2 *gi, int32_t *phalo) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= M) return;
     int k = eln[i];
@@ -1261,52 +1410,76 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
     float bx = bvalid ? asc_x(hm, pos) : 0.f;
     float best = bvalid ? (float)sqrt((double)bx) : 1e20f;
     int bh = mi;
-    const bool buckets = ng > RSG_ASC_BUCKET;
-    for (int g = 0; g < ng;) {
-        if (buckets && bvalid) {
-            if ((g & 1023) == 0) {
-                const AscBucket &S = bk2[h0 + (g >> 10)];
-                if (!S.inv && !(asc_bucket_lb(S, pos) < bx)) {
-                    g += 1024;
+    if (ng > RSG_ASC_BUCKET) {
+        // Morton-ordered candidates, (metric, list position) lexicographic;
+        // mi holds list position 0.
+        int bpos = 0;
+        double cut = asc_xcut(best);
+        for (int j = 0; j < ng;) {
+            if ((j & 1023) == 0) {
+                const AscBucket &S = bk2[h0 + (j >> 10)];
+                if ((!S.inv || best < 1e20f) && (double)asc_bucket_lb(S, pos) >= cut) {
+                    j += 1024;
                     continue;
                 }
             }
-            if ((g & 31) == 0) {
-                const AscBucket &B = bk[h0 + (g >> 5)];
-                if (!B.inv && !(asc_bucket_lb(B, pos) < bx)) {
-                    g += 32;
+            if ((j & 31) == 0) {
+                const AscBucket &B = bk[h0 + (j >> 5)];
+                if ((!B.inv || best < 1e20f) && (double)asc_bucket_lb(B, pos) >= cut) {
+                    j += 32;
                     continue;
                 }
             }
-        }
-        const rsg_halo &hh = H[glist[h0 + g]];
-        AscHalo c;
-        for (int d = 0; d < 3; d++) {
-            c.pos[d] = hh.pos[d];
-            c.pos[d + 3] = hh.bulkvel[d];
-        }
-        c.r = hh.r;
-        c.vrms = hh.vrms;
-        if (!asc_valid(c)) {
-            if (1e20f < best) {
-                best = 1e20f;
-                bh = glist[h0 + g];
-                bvalid = false;
+            const AscHalo c = ah[h0 + j];
+            float m;
+            if (!asc_valid(c)) {
+                m = 1e20f;
+            } else {
+                float x = asc_x(c, pos);
+                if ((double)x >= cut) {
+                    j++;
+                    continue;
+                }
+                m = (float)sqrt((double)x);
             }
-            g++;
-            continue;
-        }
-        float x = asc_x(c, pos);
-        if (!(bvalid && !(x < bx))) {
-            float m = (float)sqrt((double)x);
-            if (m < best) {
+            int gp = gi[h0 + j].x;
+            if (m < best || (m == best && gp < bpos)) {
                 best = m;
-                bx = x;
-                bvalid = true;
-                bh = glist[h0 + g];
+                bpos = gp;
+                bh = gi[h0 + j].y;
+                cut = asc_xcut(best);
+            }
+            j++;
+        }
+    } else {
+        for (int g = 0; g < ng; g++) {
+            const rsg_halo &hh = H[glist[h0 + g]];
+            AscHalo c;
+            for (int d = 0; d < 3; d++) {
+                c.pos[d] = hh.pos[d];
+                c.pos[d + 3] = hh.bulkvel[d];
+            }
+            c.r = hh.r;
+            c.vrms = hh.vrms;
+            if (!asc_valid(c)) {
+                if (1e20f < best) {
+                    best = 1e20f;
+                    bh = glist[h0 + g];
+                    bvalid = false;
+                }
+                continue;
+            }
+            float x = asc_x(c, pos);
+            if (!(bvalid && !(x < bx))) {
+                float m = (float)sqrt((double)x);
+                if (m < best) {
+                    best = m;
+                    bx = x;
+                    bvalid = true;
+                    bh = glist[h0 + g];
+                }
             }
         }
-        g++;
     }
     int h = bh;
     for (int guard = 0; guard < 100000 && E[h].sub_of > -1; guard++) {
@@ -2298,6 +2471,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     int32_t *glist = ar.get<int32_t>(NH), *redirect = ar.get<int32_t>(NH);
     // bucket b (32 halos) and super-bucket sb (1024 halos) of a node at h0 + b, h0 + sb
     AscBucket *ascb = ar.get<AscBucket>(NH), *ascb2 = ar.get<AscBucket>(NH);
+    AscHalo *asch = ar.get<AscHalo>(NH);
+    int2 *ascgi = ar.get<int2>(NH);
     int32_t *stk = ar.get<int32_t>(NH + 1);
     RSG_CHECK_LAUNCH();
 
@@ -2313,12 +2488,27 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         launch(k_asc_halo_mark, dim3(cnt, 8), T, 0, st, N, base, (const rsg_halo *)H, phalo);
         phase_mark(st, "a.mark");
         launch(k_asc_seed_blk, cnt, 256, 0, st, N, base, H, E, glist, redirect, cfg.force_res);
-        launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H, (const int32_t *)glist,
-               0, ascb, ascb2);
+        {
+            size_t m2 = ar.used;
+            uint32_t *sk = ar.get<uint32_t>(NH), *sk2 = ar.get<uint32_t>(NH);
+            int32_t *sv = ar.get<int32_t>(NH), *sv2 = ar.get<int32_t>(NH);
+            int32_t *sb = ar.get<int32_t>(cnt), *se = ar.get<int32_t>(cnt);
+            launch(k_asc_sort_keys, cnt, 128, 0, st, N, base, (const rsg_halo *)H,
+                   (const int32_t *)glist, sk, sv, sb, se);
+            size_t tb = 0;
+            cub::DeviceSegmentedSort::SortPairs(nullptr, tb, sk, sk2, sv, sv2, NH, cnt, sb, se, st);
+            void *tmp = ar.take(tb + 256);
+            cub::DeviceSegmentedSort::SortPairs(tmp, tb, sk, sk2, sv, sv2, NH, cnt, sb, se, st);
+            RSG_CHECK_LAUNCH();
+            launch(k_asc_sorted_recs, cnt, 128, 0, st, N, base, (const rsg_halo *)H,
+                   (const int32_t *)glist, (const int32_t *)sv2, asch, ascgi);
+            ar.used = m2;
+        }
+        launch(k_asc_buckets_s, cnt, 64, 0, st, N, base, (const AscHalo *)asch, ascb, ascb2);
         launch(k_asc_assign_p, nblk(M, 128), 128, 0, st, (const Rec *)W, M, (const int32_t *)eln,
                N, base, (const rsg_halo *)H, (const rsg_extra_halo_info *)E,
                (const int32_t *)glist, (const int32_t *)redirect, (const AscBucket *)ascb,
-               (const AscBucket *)ascb2, phalo);
+               (const AscBucket *)ascb2, (const AscHalo *)asch, (const int2 *)ascgi, phalo);
         phase_mark(st, "a.seed_assign");
         RSG_CHECK_LAUNCH();
         if (exact) {
