@@ -1153,66 +1153,17 @@ __device__ __forceinline__ float asc_x(const AscHalo &h, const float *pos) {
     float b = __fdiv_rn(v2, fmul(h.vrms, h.vrms));
     return fadd(a, b);
 }
-// Buckets of 32 consecutive growing halos (in list order, which follows the
-// hierarchy, so neighbours in the list are neighbours in space) for nodes
-// with more than RSG_ASC_BUCKET growing halos: the box of their centres and
-// the largest radius.  For a particle, box distance^2 / rmax^2 is at most the
-// float x of every valid halo in the bucket (every rounded operation of x is
-// monotone in its inputs), so a bucket whose bound is not below the running
-// best x holds no halo that passes the strict test: skipping it leaves the
-// choice, ties included, as the halo-by-halo scan makes it.
+// Buckets of 32 consecutive candidates (k_asc_buckets_s) for nodes with more
+// than RSG_ASC_BUCKET of them: the box of their centres and the largest
+// radius over the valid ones (inv: the bucket holds an invalid halo).  For a
+// point, box distance^2 / rmax^2 is at most the float x of every valid halo
+// in the bucket (every rounded operation of x is monotone in its inputs).
 #define RSG_ASC_BUCKET 64
 struct AscBucket {
     float mn[3], mx[3], rmax;
-    int32_t inv;  // holds a halo without a valid metric (never skipped)
+    int32_t inv;  // holds a halo without a valid metric
 };
-__global__ void k_asc_buckets(HierNodes N, int32_t base, const rsg_halo *H,
-                              const int32_t *glist, int all, AscBucket *bk, AscBucket *bk2) {
-    int node = base + blockIdx.x;
-    int h0 = N.h0[node];
-    int ng = all ? N.h1[node] - h0 : N.ng[node];
-    if (ng <= RSG_ASC_BUCKET) return;
-    int nb = (ng + 31) / 32;
-    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-        AscBucket B;
-        for (int d = 0; d < 3; d++) {
-            B.mn[d] = INFINITY;
-            B.mx[d] = -INFINITY;
-        }
-        B.rmax = 0.f;
-        B.inv = 0;
-        for (int g = 32 * b; g < ng && g < 32 * b + 32; g++) {
-            const rsg_halo &hh = H[all ? h0 + g : glist[h0 + g]];
-            if (hh.vrms <= 0 || hh.r <= 0 || !(hh.r == hh.r)) {
-                B.inv = 1;
-                continue;
-            }
-            for (int d = 0; d < 3; d++) {
-                B.mn[d] = fminf(B.mn[d], hh.pos[d]);
-                B.mx[d] = fmaxf(B.mx[d], hh.pos[d]);
-            }
-            B.rmax = fmaxf(B.rmax, hh.r);
-        }
-        bk[h0 + b] = B;
-    }
-    // super-buckets of 32 buckets (1024 halos)
-    __syncthreads();
-    int nsb = (nb + 31) / 32;
-    for (int sb = threadIdx.x; sb < nsb; sb += blockDim.x) {
-        AscBucket S = bk[h0 + 32 * sb];
-        for (int b = 32 * sb + 1; b < nb && b < 32 * sb + 32; b++) {
-            const AscBucket &B = bk[h0 + b];
-            for (int d = 0; d < 3; d++) {
-                S.mn[d] = fminf(S.mn[d], B.mn[d]);
-                S.mx[d] = fmaxf(S.mx[d], B.mx[d]);
-            }
-            S.rmax = fmaxf(S.rmax, B.rmax);
-            S.inv |= B.inv;
-        }
-        bk2[h0 + sb] = S;
-    }
-}
-// lower bound of x over a bucket's valid halos (see k_asc_buckets)
+// lower bound of x over a bucket's valid halos
 __device__ __forceinline__ float asc_bucket_lb(const AscBucket &B, const float *pos) {
     float d2 = 0.f;
 #pragma unroll
@@ -1239,12 +1190,16 @@ __device__ __forceinline__ uint32_t morton10(uint32_t v) {
     v = (v | (v << 2)) & 0x09249249u;
     return v;
 }
+// all = 0: the node's growing list glist[h0 ..]; all = 1: halos h0 .. h1.
+__device__ __forceinline__ int asc_count(const HierNodes &N, int node, int all) {
+    return all ? N.h1[node] - N.h0[node] : N.ng[node];
+}
 __global__ void k_asc_sort_keys(HierNodes N, int32_t base, const rsg_halo *H,
-                                const int32_t *glist, uint32_t *key, int32_t *val, int32_t *sb,
-                                int32_t *se) {
+                                const int32_t *glist, int all, uint32_t *key, int32_t *val,
+                                int32_t *sb, int32_t *se) {
     __shared__ float mn[3], mx[3];
     int k = blockIdx.x, node = base + k;
-    int ng = N.ng[node], h0 = N.h0[node];
+    int ng = asc_count(N, node, all), h0 = N.h0[node];
     if (threadIdx.x == 0) {
         sb[k] = h0;
         se[k] = ng > RSG_ASC_BUCKET ? h0 + ng : h0;
@@ -1257,7 +1212,7 @@ __global__ void k_asc_sort_keys(HierNodes N, int32_t base, const rsg_halo *H,
     if (ng <= RSG_ASC_BUCKET) return;
     float lmn[3] = {INFINITY, INFINITY, INFINITY}, lmx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-        const float *p = H[glist[h0 + g]].pos;
+        const float *p = H[all ? h0 + g : glist[h0 + g]].pos;
         for (int d = 0; d < 3; d++) {
             lmn[d] = fminf(lmn[d], p[d]);
             lmx[d] = fmaxf(lmx[d], p[d]);
@@ -1287,7 +1242,7 @@ __global__ void k_asc_sort_keys(HierNodes N, int32_t base, const rsg_halo *H,
     float sc[3];
     for (int d = 0; d < 3; d++) sc[d] = (mx[d] > mn[d]) ? 1023.99f / (mx[d] - mn[d]) : 0.f;
     for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-        const float *p = H[glist[h0 + g]].pos;
+        const float *p = H[all ? h0 + g : glist[h0 + g]].pos;
         uint32_t q[3];
         for (int d = 0; d < 3; d++) {
             float t = (p[d] - mn[d]) * sc[d];
@@ -1300,13 +1255,13 @@ __global__ void k_asc_sort_keys(HierNodes N, int32_t base, const rsg_halo *H,
 // Candidate records of the Morton-ordered nodes: ah[h0 + j] is the halo at
 // sorted position j, gi[h0 + j] its (list position, halo index).
 __global__ void k_asc_sorted_recs(HierNodes N, int32_t base, const rsg_halo *H,
-                                  const int32_t *glist, const int32_t *sval, AscHalo *ah,
+                                  const int32_t *glist, int all, const int32_t *sval, AscHalo *ah,
                                   int2 *gi) {
     int node = base + blockIdx.x;
-    int ng = N.ng[node], h0 = N.h0[node];
+    int ng = asc_count(N, node, all), h0 = N.h0[node];
     if (ng <= RSG_ASC_BUCKET) return;
     for (int j = threadIdx.x; j < ng; j += blockDim.x) {
-        int g = sval[h0 + j], h = glist[h0 + g];
+        int g = sval[h0 + j], h = all ? h0 + g : glist[h0 + g];
         const rsg_halo &hh = H[h];
         AscHalo c;
         for (int d = 0; d < 3; d++) {
@@ -1320,10 +1275,10 @@ __global__ void k_asc_sorted_recs(HierNodes N, int32_t base, const rsg_halo *H,
     }
 }
 // Buckets of 32 (and 1024) consecutive Morton-ordered candidates.
-__global__ void k_asc_buckets_s(HierNodes N, int32_t base, const AscHalo *ah, AscBucket *bk,
-                                AscBucket *bk2) {
+__global__ void k_asc_buckets_s(HierNodes N, int32_t base, int all, const AscHalo *ah,
+                                AscBucket *bk, AscBucket *bk2) {
     int node = base + blockIdx.x;
-    int ng = N.ng[node], h0 = N.h0[node];
+    int ng = asc_count(N, node, all), h0 = N.h0[node];
     if (ng <= RSG_ASC_BUCKET) return;
     int nb = (ng + 31) / 32;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -1373,9 +1328,11 @@ __device__ __forceinline__ double asc_xcut(float best) {
 }
 
 // One thread per particle of the level (the node from eln): a node of
-// millions of particles spreads over the whole GPU.  Same choice as the
-// per-node form, with buckets and super-buckets (1024 halos) skipped when
-// their bound is not below the running best.
+// millions of particles spreads over the whole GPU.  Nodes with more than
+// RSG_ASC_BUCKET growing halos scan their Morton-ordered candidates and skip
+// a bucket (32) or super-bucket (1024 halos) whose lower bound of x reaches
+// asc_xcut of the running best (and, unless the best is below 1e20, holds
+// no invalid halo); the others scan the list in order.
 __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, HierNodes N,
                                int32_t base, const rsg_halo *H, const rsg_extra_halo_info *E,
                                const int32_t *glist, const int32_t *redirect,
@@ -1864,15 +1821,18 @@ __device__ __forceinline__ float hdist_x(const rsg_halo &c, const rsg_halo &h, f
     return (float)sqrt((double)*x);
 }
 // find_best_parent (src/subhalo_metric.c:185-191) over the node's listed
-// halos, first strict minimum in list order.  Nodes listing more than
-// RSG_ASC_BUCKET halos skip buckets (k_asc_buckets over the same list) that
-// cannot hold a winner while the best is at most 1e20 (then the 1e20 of a
-// too-small or invalid candidate cannot win): either every valid halo of
-// the bucket is too small (r * 0.99999 < h.r for the largest r), or the
-// bucket's lower bound of x is not below the best's x.
+// halos: the first strict minimum of calc_halo_dist in list order, starting
+// from the biggest halo (which therefore wins every tie).  Nodes listing
+// more than RSG_ASC_BUCKET halos scan their Morton-ordered candidates
+// (k_asc_sorted_recs over the same list) and take (metric, list position)
+// lexicographically, the biggest halo holding position -1.  While the best
+// is below 1e20 (the value of a too-small or invalid candidate), a bucket is
+// skipped when every valid halo in it is too small (r * 0.99999 < h.r for
+// its largest r) or its lower bound of x reaches the cut of the best.
 __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const int32_t *loff,
                               const int32_t *list, const int32_t *hnode, rsg_halo *H,
-                              rsg_extra_halo_info *E, const AscBucket *bk, const AscBucket *bk2) {
+                              rsg_extra_halo_info *E, const AscBucket *bk, const AscBucket *bk2,
+                              const AscHalo *ah, const int2 *gi) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int tot = loff[count];
     if (t >= tot) return;
@@ -1887,35 +1847,60 @@ __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const in
         float best = hdist_x(H[mi], hh, &bx);
         res = mi;
         const int g0 = loff[k], n = loff[k + 1] - g0, h0 = N.h0[node];
-        const bool buckets = bk && n > RSG_ASC_BUCKET;
-        for (int g = 0; g < n;) {
-            if (buckets && best <= 1e20f) {
-                if ((g & 1023) == 0) {
-                    const AscBucket &S = bk2[h0 + (g >> 10)];
-                    if ((double)hh.r > (double)S.rmax * 0.99999 ||
-                        !(asc_bucket_lb(S, hh.pos) < bx)) {
-                        g += 1024;
-                        continue;
+        if (n > RSG_ASC_BUCKET) {
+            int bpos = -1;
+            double cut = asc_xcut(best);
+            const double hr = (double)hh.r;
+            for (int j = 0; j < n;) {
+                if (best < 1e20f) {
+                    if ((j & 1023) == 0) {
+                        const AscBucket &S = bk2[h0 + (j >> 10)];
+                        if (hr > (double)S.rmax * 0.99999 ||
+                            (double)asc_bucket_lb(S, hh.pos) >= cut) {
+                            j += 1024;
+                            continue;
+                        }
+                    }
+                    if ((j & 31) == 0) {
+                        const AscBucket &B = bk[h0 + (j >> 5)];
+                        if (hr > (double)B.rmax * 0.99999 ||
+                            (double)asc_bucket_lb(B, hh.pos) >= cut) {
+                            j += 32;
+                            continue;
+                        }
                     }
                 }
-                if ((g & 31) == 0) {
-                    const AscBucket &B = bk[h0 + (g >> 5)];
-                    if ((double)hh.r > (double)B.rmax * 0.99999 ||
-                        !(asc_bucket_lb(B, hh.pos) < bx)) {
-                        g += 32;
+                const AscHalo c = ah[h0 + j];
+                float m;
+                if (hr > (double)c.r * 0.99999 || c.vrms <= 0 || c.r <= 0) {
+                    m = 1e20f;
+                } else {
+                    float x = asc_x(c, hh.pos);
+                    if ((double)x >= cut) {
+                        j++;
                         continue;
                     }
+                    m = (float)sqrt((double)x);
+                }
+                int gp = gi[h0 + j].x;
+                if (m < best || (m == best && gp < bpos)) {
+                    best = m;
+                    bpos = gp;
+                    res = gi[h0 + j].y;
+                    cut = asc_xcut(best);
+                }
+                j++;
+            }
+        } else {
+            for (int g = 0; g < n; g++) {
+                int c = list[g0 + g];
+                float x;
+                float m = hdist_x(H[c], hh, &x);
+                if (m < best) {
+                    best = m;
+                    res = c;
                 }
             }
-            int c = list[g0 + g];
-            float x;
-            float m = hdist_x(H[c], hh, &x);
-            if (m < best) {
-                best = m;
-                bx = x;
-                res = c;
-            }
-            g++;
         }
     }
     E[h].sub_of = res;
@@ -2217,6 +2202,27 @@ DevCfg make_devcfg(const rsg_config &c) {
     return d;
 }
 
+// Morton-ordered candidate records and their buckets for the level's nodes
+// with more than RSG_ASC_BUCKET listed halos (all: see asc_count).
+static void asc_sorted(Arena &ar, HierNodes N, int32_t base, int32_t cnt, const rsg_halo *H,
+                       const int32_t *glist, int all, int32_t NH, AscHalo *ah, int2 *gi,
+                       AscBucket *bk, AscBucket *bk2, cudaStream_t st) {
+    size_t m2 = ar.used;
+    uint32_t *sk = ar.get<uint32_t>(NH), *sk2 = ar.get<uint32_t>(NH);
+    int32_t *sv = ar.get<int32_t>(NH), *sv2 = ar.get<int32_t>(NH);
+    int32_t *sb = ar.get<int32_t>(cnt), *se = ar.get<int32_t>(cnt);
+    launch(k_asc_sort_keys, cnt, 128, 0, st, N, base, H, glist, all, sk, sv, sb, se);
+    size_t tb = 0;
+    cub::DeviceSegmentedSort::SortPairs(nullptr, tb, sk, sk2, sv, sv2, NH, cnt, sb, se, st);
+    void *tmp = ar.take(tb + 256);
+    cub::DeviceSegmentedSort::SortPairs(tmp, tb, sk, sk2, sv, sv2, NH, cnt, sb, se, st);
+    RSG_CHECK_LAUNCH();
+    launch(k_asc_sorted_recs, cnt, 128, 0, st, N, base, H, glist, all, (const int32_t *)sv2, ah,
+           gi);
+    launch(k_asc_buckets_s, cnt, 64, 0, st, N, base, all, (const AscHalo *)ah, bk, bk2);
+    ar.used = m2;
+}
+
 SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int64_t *goff_h,
                          const int64_t *gsz_h, int64_t ngroups, const rsg_config &cfg,
                          rsg_halo *d_halos, rsg_extra_halo_info *d_extra, int64_t max_halos,
@@ -2488,23 +2494,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         launch(k_asc_halo_mark, dim3(cnt, 8), T, 0, st, N, base, (const rsg_halo *)H, phalo);
         phase_mark(st, "a.mark");
         launch(k_asc_seed_blk, cnt, 256, 0, st, N, base, H, E, glist, redirect, cfg.force_res);
-        {
-            size_t m2 = ar.used;
-            uint32_t *sk = ar.get<uint32_t>(NH), *sk2 = ar.get<uint32_t>(NH);
-            int32_t *sv = ar.get<int32_t>(NH), *sv2 = ar.get<int32_t>(NH);
-            int32_t *sb = ar.get<int32_t>(cnt), *se = ar.get<int32_t>(cnt);
-            launch(k_asc_sort_keys, cnt, 128, 0, st, N, base, (const rsg_halo *)H,
-                   (const int32_t *)glist, sk, sv, sb, se);
-            size_t tb = 0;
-            cub::DeviceSegmentedSort::SortPairs(nullptr, tb, sk, sk2, sv, sv2, NH, cnt, sb, se, st);
-            void *tmp = ar.take(tb + 256);
-            cub::DeviceSegmentedSort::SortPairs(tmp, tb, sk, sk2, sv, sv2, NH, cnt, sb, se, st);
-            RSG_CHECK_LAUNCH();
-            launch(k_asc_sorted_recs, cnt, 128, 0, st, N, base, (const rsg_halo *)H,
-                   (const int32_t *)glist, (const int32_t *)sv2, asch, ascgi);
-            ar.used = m2;
-        }
-        launch(k_asc_buckets_s, cnt, 64, 0, st, N, base, (const AscHalo *)asch, ascb, ascb2);
+        asc_sorted(ar, N, base, cnt, H, glist, 0, NH, asch, ascgi, ascb, ascb2, st);
         launch(k_asc_assign_p, nblk(M, 128), 128, 0, st, (const Rec *)W, M, (const int32_t *)eln,
                N, base, (const rsg_halo *)H, (const rsg_extra_halo_info *)E,
                (const int32_t *)glist, (const int32_t *)redirect, (const AscBucket *)ascb,
@@ -2532,10 +2522,10 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         launch(k_list_growing, cnt, T, 0, st, N, base, goffs, glist, glv, gnode);
         basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
         launch(k_maxi, cnt, 256, 0, st, N, base, (const rsg_halo *)H, glist, 0);
-        launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H, (const int32_t *)glist,
-               0, ascb, ascb2);
+        asc_sorted(ar, N, base, cnt, H, glist, 0, NH, asch, ascgi, ascb, ascb2, st);
         launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E,
-               (const AscBucket *)ascb, (const AscBucket *)ascb2);
+               (const AscBucket *)ascb, (const AscBucket *)ascb2, (const AscHalo *)asch,
+               (const int2 *)ascgi);
         fix_parents_level(ar, N, base, cnt, H, E, err, true, st);
         basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
         RSG_CHECK_LAUNCH();
@@ -2555,10 +2545,10 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             std::swap(W, W2);
             std::swap(phalo, phalo2);
             launch(k_maxi, cnt, 256, 0, st, N, base, (const rsg_halo *)H, glist, 1);
-            launch(k_asc_buckets, cnt, 64, 0, st, N, base, (const rsg_halo *)H,
-                   (const int32_t *)glist, 1, ascb, ascb2);
+            asc_sorted(ar, N, base, cnt, H, glist, 1, NH, asch, ascgi, ascb, ascb2, st);
             launch(k_best_parent, nblk(na, T), T, 0, st, N, base, cnt, aoff, alist, anode, H, E,
-                   (const AscBucket *)ascb, (const AscBucket *)ascb2);
+                   (const AscBucket *)ascb, (const AscBucket *)ascb2, (const AscHalo *)asch,
+                   (const int2 *)ascgi);
             fix_parents_level(ar, N, base, cnt, H, E, err, true, st);
             RSG_CHECK_LAUNCH();
             // find_subs tail (src/groupies.c:697-703): child counts and basic
