@@ -79,25 +79,33 @@ __device__ bool walk_sets(const rsg_halo *H, const rsg_extra_halo_info *E, int b
     return true;
 }
 
+// Per halo: records of its potential set (tot), the records of its own
+// halos that stay after the potential-only ones are dropped (kept), and the
+// copy segments (nseg: one per set member and RSG_SEG_MAX records).
+#define RSG_SEG_MAX 8192
 __global__ void k_set_count(const rsg_halo *H, const rsg_extra_halo_info *E, int32_t NH,
-                            double ratio, int32_t *tot, int32_t *nseg, int *err) {
+                            double ratio, int32_t *tot, int32_t *nseg, int32_t *kept, int *err) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h > NH) return;
     if (h == NH) {
         tot[h] = 0;
         nseg[h] = 0;
+        kept[h] = 0;
         return;
     }
-    int t = 0, s = 0;
+    int t = 0, s = 0, kp = 0;
     if (H[h].num_p >= 1) {
         bool ok = walk_sets(H, E, h, ratio, [&](int x, int pot) {
-            t += (int)H[x].num_p;
-            s++;
+            int n = (int)H[x].num_p;
+            t += n;
+            if (!pot) kp += n;
+            s += n > 0 ? (n + RSG_SEG_MAX - 1) / RSG_SEG_MAX : 1;
         });
         if (!ok) atomicExch(err, 1);
     }
     tot[h] = t;
     nseg[h] = s;
+    kept[h] = kp;
 }
 
 __global__ void k_set_segs(const rsg_halo *H, const rsg_extra_halo_info *E, int32_t NH,
@@ -110,8 +118,11 @@ __global__ void k_set_segs(const rsg_halo *H, const rsg_extra_halo_info *E, int3
         int flag = 0;
         if (x == h) flag = 1;
         if (!pot && ((double)H[x].num_p < (double)bnp * 0.03)) flag = 2;
-        segs[k++] = Seg{(int32_t)H[x].p_start, (int32_t)H[x].num_p, dst, h, pot, flag};
-        dst += (int)H[x].num_p;
+        int n = (int)H[x].num_p, src = (int32_t)H[x].p_start;
+        if (n <= 0) segs[k++] = Seg{src, n, dst, h, pot, flag};
+        for (int o = 0; o < n; o += RSG_SEG_MAX)
+            segs[k++] = Seg{src + o, min(RSG_SEG_MAX, n - o), dst + o, h, pot, flag};
+        dst += n;
     });
 }
 
@@ -1601,17 +1612,6 @@ __global__ void k_halo_scans_list(rsg_halo *H, const rsg_extra_halo_info *E, con
     more_props(hh, q, tot, 1, C);
 }
 
-// records of every halo kept after dropping the potential-only ones; one
-// warp per halo
-__global__ void k_kept_count(const PotRec *PO, const int32_t *toff, const int32_t *tot,
-                             int32_t NH, int32_t *kept) {
-    int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (h >= NH) return;
-    int c = 0;
-    for (int i = lane; i < tot[h]; i += 32) c += PO[toff[h] + i].ke >= 0;
-    for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if (lane == 0) kept[h] = c;
-}
 __global__ void k_bh_roots(const int32_t *toff, const int32_t *tot, int32_t NH, int32_t *rflag) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h < NH) rflag[h] = tot[h] > 1;
@@ -1909,8 +1909,9 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     RSG_CUDA(cudaMemsetAsync(work, 0, 32, st));
     int32_t *tot = ar.get<int32_t>(NH + 1), *nseg = ar.get<int32_t>(NH + 1);
     int32_t *toff = ar.get<int32_t>(NH + 1), *soff = ar.get<int32_t>(NH + 1);
+    int32_t *kept = ar.get<int32_t>(NH + 1);
     launch(k_set_count, nblk(NH + 1, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio, tot,
-                                                 nseg, err);
+           nseg, kept, err);
     check_i32_total(ar, tot, NH + 1, "potential records", st);
     int32_t npo = scan_i32(ar, tot, toff, NH + 1, st);
     phase_mark(st, "p.sets");
@@ -1950,8 +1951,6 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
         ar.used = m2;
     }
     phase_mark(st, "p.sort");
-    int32_t *kept = ar.get<int32_t>(NH + 1);
-    launch(k_kept_count, nblk((int64_t)NH * 32, T), T, 0, st, PO2, toff, tot, NH, kept);
     {
         int32_t *fs = ar.get<int32_t>(NH), *fbg = ar.get<int32_t>(NH);
         int32_t *ls = ar.get<int32_t>(NH), *lb = ar.get<int32_t>(NH);

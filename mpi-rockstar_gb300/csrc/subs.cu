@@ -2017,29 +2017,37 @@ __global__ void k_halo_group(HierNodes N, const int32_t *leaves, int32_t nl, int
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nl) hgrp[i] = N.group[leaves[i]];
 }
+// Working records of every group: one thread per record, its group by a
+// binary search over the record offsets (a group of millions of particles
+// spreads over the GPU), and one thread per group for the level-0 nodes.
 __global__ void k_make_w(const rsg_particle *P, int64_t ng, const int64_t *goff,
-                         const int64_t *woff, const int64_t *gsz, Rec *W, int32_t *wgroup,
-                         HierNodes N) {
-    int g = blockIdx.x;
-    if (g >= ng) return;
-    int64_t s = woff[g], n = gsz[g], o = goff[g];
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-        Rec r;
+                         const int64_t *woff, int64_t M, Rec *W, int32_t *wgroup) {
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= M) return;
+    int64_t lo = 0, hi = ng;  // last g with woff[g] <= e
+    while (hi - lo > 1) {
+        int64_t mid = (lo + hi) >> 1;
+        if (woff[mid] <= e) lo = mid;
+        else hi = mid;
+    }
+    int64_t src = goff[lo] + (e - woff[lo]);
+    Rec r;
 #pragma unroll
-        for (int d = 0; d < 6; d++) r.pos[d] = P[o + i].pos[d];
-        r.ridx = (int32_t)(o + i);
-        r.aux = 0;
-        W[s + i] = r;
-        wgroup[s + i] = g;
-    }
-    if (threadIdx.x == 0) {
-        N.start[g] = (int32_t)s;
-        N.n[g] = (int32_t)n;
-        N.parent[g] = -1;
-        N.group[g] = g;
-        N.level[g] = 0;
-        N.nchild[g] = 0;
-    }
+    for (int d = 0; d < 6; d++) r.pos[d] = P[src].pos[d];
+    r.ridx = (int32_t)src;
+    r.aux = 0;
+    W[e] = r;
+    wgroup[e] = (int32_t)lo;
+}
+__global__ void k_make_nodes(int64_t ng, const int64_t *woff, const int64_t *gsz, HierNodes N) {
+    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    N.start[g] = (int32_t)woff[g];
+    N.n[g] = (int32_t)gsz[g];
+    N.parent[g] = -1;
+    N.group[g] = (int32_t)g;
+    N.level[g] = 0;
+    N.nchild[g] = 0;
 }
 
 // ---- host driver ------------------------------------------------------------
@@ -2281,7 +2289,9 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     int *err = ar.get<int>(4);
     RSG_CUDA(cudaMemsetAsync(err, 0, 16, st));
     phase_mark(st, "");
-    launch(k_make_w, (int)G, T, 0, st, d_p, G, d_goff, d_woff, d_gsz, W, wgroup, N);
+    launch(k_make_w, nblk(M, T), T, 0, st, (const rsg_particle *)d_p, G, (const int64_t *)d_goff,
+           (const int64_t *)d_woff, M, W, wgroup);
+    launch(k_make_nodes, nblk(G, T), T, 0, st, G, (const int64_t *)d_woff, (const int64_t *)d_gsz, N);
     RSG_CHECK_LAUNCH();
 
     // ---------------- descending ----------------
