@@ -267,6 +267,20 @@ def precision_study(rk, scale, forms):
     print(json.dumps(res))
 
 
+def run_autotune(rk, cfg_id, scale):
+    """Size-class thresholds by measurement (mpi-rockstar_gb300/autotune.py)."""
+    from mpi_rockstar_gb300 import autotune
+    rk.build()
+    p, box, mp, _ = rk.synth(cfg_id, scale, SEED)
+    cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    res = autotune.autotune(rk, p, cfg, log=lambda m: print(m, file=sys.stderr, flush=True))
+    workload = "synthetic workload %d at scale %g: %d particles" % (cfg_id, scale, len(p))
+    autotune.save(res, rk.TUNING_FILE, workload)
+    print(json.dumps({"workload": workload, "best": res["best"], "default": res["default"],
+                      "best_ms": res["best_ms"], "default_ms": res["default_ms"],
+                      "trials": len(res["trials"])}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -282,6 +296,10 @@ def main():
     ap.add_argument("--precision-study", action="store_true",
                     help="instead of the bench line: the potential precision study on the "
                          "isolated-groups workload at --scale, one JSON line")
+    ap.add_argument("--autotune", action="store_true",
+                    help="instead of the bench line: tune the batched form's size-class "
+                         "thresholds on the workload (--cfg, --scale) and write them to "
+                         "mpi-rockstar_gb300/tuning.json, which later runs apply")
     ap.add_argument("--precision-forms", default="3,0,1,2",
                     help="potential forms of the study; the first is the reference "
                          "(3: FP64 direct sum, O(n^2) per group)")
@@ -292,6 +310,10 @@ def main():
     if args.precision_study:
         if rank == 0:
             precision_study(rk, args.scale, [int(f) for f in args.precision_forms.split(",")])
+        return
+    if args.autotune:
+        if rank == 0:
+            run_autotune(rk, args.cfg, args.scale)
         return
     if args.impl == "reference":
         if rank == 0:
@@ -309,6 +331,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     rk.build()
+    tuned = rk.load_tuning()  # size-class thresholds from a committed autotune run, if any
     p, box, mp, _ = rk.synth(args.cfg, args.scale, SEED + rank)
     n = len(p)
     cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=n)
@@ -434,7 +457,9 @@ def main():
                        "l2": "flushed between steps (256 MiB write)", "form": "batched",
                        "plain_particles_per_s": n * world / (plain_ms * 1e-3),
                        "plain_ms_per_step": plain_ms, "plain_halos": plain_res[2],
-                       "plain_gpu_launches": plain_launches},
+                       "plain_gpu_launches": plain_launches,
+                       "tuning": rk.get_tuning(),
+                       "tuning_source": "mpi-rockstar_gb300/tuning.json" if tuned else "defaults"},
             "e2e": {"value": e2e_v, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,

@@ -175,6 +175,23 @@ int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct
  * No reference counterpart: it serves the potential precision study. */
 int32_t rsg_set_potential_form(int32_t form);
 
+/* Size-class thresholds and chunk sizes of the batched form, by name
+ * (process-wide; no reference counterpart):
+ *   asc_bucket_min  nodes with more growing halos scan Morton-ordered
+ *                   buckets in the particle assignment and parent search (64)
+ *   bh_huge         Barnes-Hut nodes with more points take the chunked
+ *                   node pass (65536), bh_chunk points per chunk (16384)
+ *   seg_max         records per potential-set copy segment (8192)
+ *   norm_chunk      records per chunk of the chunked norm_sd (4096)
+ *   bp_big          halos with more particles take the chunked basic
+ *                   properties (16384), bp_chunk particles per chunk (4096)
+ * They change speed only (choices stay exact, sums change at most by FP64
+ * rounding).  rsg_set_tuning returns RSG_ERR_ARGS for an unknown name or a
+ * value outside the parameter's range; mpi-rockstar_gb300/autotune.py picks
+ * them by measurement. */
+int32_t rsg_set_tuning(const char *name, int64_t value);
+int32_t rsg_get_tuning(const char *name, int64_t *value);
+
 /* Allocation-free 3D FOF of one chunk: rsg_rockstar_fof on device buffers,
  * with no counterpart in the reference (whose fof.c grows its buffers with
  * realloc).  It allocates nothing: every scratch buffer is carved from one

@@ -67,6 +67,10 @@ def lib():
         h.rsg_set_potential_form.restype = C.c_int32
         h.rsg_set_potential_form.argtypes = [C.c_int32]
         h.rsg_debug_keep_potentials.argtypes = [C.c_int32]
+        h.rsg_set_tuning.restype = C.c_int32
+        h.rsg_set_tuning.argtypes = [C.c_char_p, i64]
+        h.rsg_get_tuning.restype = C.c_int32
+        h.rsg_get_tuning.argtypes = [C.c_char_p, vp]
         h.rsg_debug_potentials.restype = i64
         h.rsg_debug_potentials.argtypes = [vp, i64]
         for name, args in _EXTRA_SIGS.items():
@@ -148,6 +152,39 @@ def set_potential_form(form):
     if r < 0:
         _check(r)
     return r
+
+
+TUNING_NAMES = ("asc_bucket_min", "bh_huge", "bh_chunk", "seg_max", "norm_chunk", "bp_big",
+                "bp_chunk")
+TUNING_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+
+
+def set_tuning(name, value):
+    """One size-class threshold or chunk size of the batched form
+    (rsg_set_tuning)."""
+    _check(lib().rsg_set_tuning(name.encode(), int(value)))
+
+
+def get_tuning(name=None):
+    """The current value of one tuning parameter, or all of them as a dict."""
+    if name is None:
+        return {k: get_tuning(k) for k in TUNING_NAMES}
+    v = np.zeros(1, np.int64)
+    _check(lib().rsg_get_tuning(name.encode(), v.ctypes.data))
+    return int(v[0])
+
+
+def load_tuning(path=TUNING_FILE):
+    """Applies the parameters of an autotune result file (the `best` dict);
+    returns them, or None when the file does not exist."""
+    import json
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        best = json.load(f)["best"]
+    for k, v in best.items():
+        set_tuning(k, v)
+    return best
 
 
 def keep_potentials(on=True):

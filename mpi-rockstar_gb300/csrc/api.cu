@@ -305,6 +305,47 @@ int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct
     }
 }
 
+// name, field, smallest and largest accepted value
+struct TuneField {
+    const char *name;
+    int32_t rsg::Tuning::*f;
+    int64_t lo, hi;
+};
+static const TuneField kTune[] = {
+    {"asc_bucket_min", &rsg::Tuning::asc_bucket_min, 32, 1 << 20},
+    {"bh_huge", &rsg::Tuning::bh_huge, 4096, 1 << 30},
+    {"bh_chunk", &rsg::Tuning::bh_chunk, 1024, 1 << 24},
+    {"seg_max", &rsg::Tuning::seg_max, 256, 1 << 24},
+    {"norm_chunk", &rsg::Tuning::norm_chunk, 256, 1 << 20},
+    {"bp_big", &rsg::Tuning::bp_big, 1024, 1 << 30},
+    {"bp_chunk", &rsg::Tuning::bp_chunk, 256, 1 << 20},
+};
+
+int32_t rsg_set_tuning(const char *name, int64_t value) {
+    for (const TuneField &t : kTune)
+        if (name && !strcmp(name, t.name)) {
+            if (value < t.lo || value > t.hi) {
+                set_error(RSG_ERR_ARGS, "rsg_set_tuning: %s must lie in [%lld, %lld]", t.name,
+                          (long long)t.lo, (long long)t.hi);
+                return RSG_ERR_ARGS;
+            }
+            rsg::tuning().*(t.f) = (int32_t)value;
+            return RSG_OK;
+        }
+    set_error(RSG_ERR_ARGS, "rsg_set_tuning: unknown parameter %s", name ? name : "(null)");
+    return RSG_ERR_ARGS;
+}
+
+int32_t rsg_get_tuning(const char *name, int64_t *value) {
+    for (const TuneField &t : kTune)
+        if (name && value && !strcmp(name, t.name)) {
+            *value = rsg::tuning().*(t.f);
+            return RSG_OK;
+        }
+    set_error(RSG_ERR_ARGS, "rsg_get_tuning: unknown parameter %s", name ? name : "(null)");
+    return RSG_ERR_ARGS;
+}
+
 int32_t rsg_set_potential_form(int32_t form) {
     if (form < 0 || form > 3) {
         set_error(RSG_ERR_ARGS, "rsg_set_potential_form: form must be 0-3");

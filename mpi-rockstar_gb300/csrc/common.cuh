@@ -94,6 +94,20 @@ void phase_report();
 // indices are the RSG_STAT_* constants of the public header.
 int64_t *last_stats();
 
+// Size-class thresholds and chunk sizes of the batched form; process-wide,
+// set through rsg_set_tuning.  They change speed only: choices stay exact
+// and sums change at most by FP64 rounding.
+struct Tuning {
+    int32_t asc_bucket_min = 64;  // nodes with more halos scan Morton buckets
+    int32_t bh_huge = 65536;      // Barnes-Hut nodes above: chunked pass
+    int32_t bh_chunk = 16384;     // points per chunk of that pass
+    int32_t seg_max = 8192;       // records per potential-set copy segment
+    int32_t norm_chunk = 4096;    // records per chunk of the chunked norm_sd
+    int32_t bp_big = 16384;       // halos above: chunked basic properties
+    int32_t bp_chunk = 4096;      // particles per chunk of those
+};
+Tuning &tuning();
+
 #define RSG_STACK 96
 #define RSG_STACK6 128
 

@@ -16,6 +16,9 @@ static thread_local int64_t g_stats[RSG_STAT_COUNT];
 
 int64_t *last_stats() { return g_stats; }
 
+static Tuning g_tuning;
+Tuning &tuning() { return g_tuning; }
+
 void set_error(int code, const char *fmt, ...) {
     g_err.code = code;
     va_list ap;

@@ -81,10 +81,10 @@ __device__ bool walk_sets(const rsg_halo *H, const rsg_extra_halo_info *E, int b
 
 // Per halo: records of its potential set (tot), the records of its own
 // halos that stay after the potential-only ones are dropped (kept), and the
-// copy segments (nseg: one per set member and RSG_SEG_MAX records).
-#define RSG_SEG_MAX 8192
+// copy segments (nseg: one per set member and segmax records).
 __global__ void k_set_count(const rsg_halo *H, const rsg_extra_halo_info *E, int32_t NH,
-                            double ratio, int32_t *tot, int32_t *nseg, int32_t *kept, int *err) {
+                            double ratio, int segmax, int32_t *tot, int32_t *nseg, int32_t *kept,
+                            int *err) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h > NH) return;
     if (h == NH) {
@@ -99,7 +99,7 @@ __global__ void k_set_count(const rsg_halo *H, const rsg_extra_halo_info *E, int
             int n = (int)H[x].num_p;
             t += n;
             if (!pot) kp += n;
-            s += n > 0 ? (n + RSG_SEG_MAX - 1) / RSG_SEG_MAX : 1;
+            s += n > 0 ? (n + segmax - 1) / segmax : 1;
         });
         if (!ok) atomicExch(err, 1);
     }
@@ -109,7 +109,8 @@ __global__ void k_set_count(const rsg_halo *H, const rsg_extra_halo_info *E, int
 }
 
 __global__ void k_set_segs(const rsg_halo *H, const rsg_extra_halo_info *E, int32_t NH,
-                           double ratio, const int32_t *toff, const int32_t *soff, Seg *segs) {
+                           double ratio, int segmax, const int32_t *toff, const int32_t *soff,
+                           Seg *segs) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= NH || H[h].num_p < 1) return;
     int dst = toff[h], k = soff[h];
@@ -120,8 +121,8 @@ __global__ void k_set_segs(const rsg_halo *H, const rsg_extra_halo_info *E, int3
         if (!pot && ((double)H[x].num_p < (double)bnp * 0.03)) flag = 2;
         int n = (int)H[x].num_p, src = (int32_t)H[x].p_start;
         if (n <= 0) segs[k++] = Seg{src, n, dst, h, pot, flag};
-        for (int o = 0; o < n; o += RSG_SEG_MAX)
-            segs[k++] = Seg{src + o, min(RSG_SEG_MAX, n - o), dst + o, h, pot, flag};
+        for (int o = 0; o < n; o += segmax)
+            segs[k++] = Seg{src + o, min(segmax, n - o), dst + o, h, pot, flag};
         dst += n;
     });
 }
@@ -242,13 +243,11 @@ __global__ void k_bh_internal_warp(const KNode<3> *nodes, int32_t first, int32_t
     }
 }
 
-// Batched form, internal nodes of more than RSG_BH_HUGE points: one block
-// per chunk of RSG_BH_CH points forms the chunk's sum and maximum of squared
-// distances to the node's mass centre (part[item]); one thread per node
-// adds the chunks in order.  item = (node, chunk); the chunks of node j of
-// a level are items first[j] .. first[j + 1].
-#define RSG_BH_HUGE 65536
-#define RSG_BH_CH 16384
+// Batched form, internal nodes of more than Tuning::bh_huge points: one
+// block per chunk of `chunk` points forms the chunk's sum and maximum of
+// squared distances to the node's mass centre (part[item]); one thread per
+// node adds the chunks in order.  item = (node, chunk); the chunks of node j
+// of a level are items first[j] .. first[j + 1].
 __device__ __forceinline__ BHNode bh_merge(const BHNode &L, const BHNode &R) {
     BHNode b;
     b.m = fadd(L.m, R.m);
@@ -257,13 +256,13 @@ __device__ __forceinline__ BHNode bh_merge(const BHNode &L, const BHNode &R) {
     return b;
 }
 __global__ void __launch_bounds__(256) k_bh_huge_part(const KNode<3> *nodes, const int2 *item,
-                                                      const PotRec *PO, const BHNode *B,
-                                                      double2 *part) {
+                                                      int chunk, const PotRec *PO,
+                                                      const BHNode *B, double2 *part) {
     __shared__ double s_s[8], m_s[8];
     const int2 it = item[blockIdx.x];
     const KNode<3> &x = nodes[it.x];
     const BHNode b = bh_merge(B[x.left], B[x.left + 1]);
-    const int i0 = it.y * RSG_BH_CH, i1 = min(x.n, i0 + RSG_BH_CH);
+    const int i0 = it.y * chunk, i1 = min(x.n, i0 + chunk);
     double sx = 0, bm = 0;
     for (int i = i0 + threadIdx.x; i < i1; i += 256) {
         double dx = d2d(b.mc, PO[x.start + i].pos);
@@ -303,9 +302,9 @@ __global__ void k_bh_huge_fin(const KNode<3> *nodes, const int32_t *node, const 
     b.dmin = (float)(bm + sqrt(bm * bm + sx / (x.n * 1.0)));
     B[a] = b;
 }
-__global__ void k_bh_huge_flags(const KNode<3> *nodes, int32_t nn, int32_t *f) {
+__global__ void k_bh_huge_flags(const KNode<3> *nodes, int32_t nn, int huge, int32_t *f) {
     int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a < nn) f[a] = nodes[a].div >= 0 && nodes[a].n > RSG_BH_HUGE;
+    if (a < nn) f[a] = nodes[a].div >= 0 && nodes[a].n > huge;
 }
 __global__ void k_bh_huge_sizes(const KNode<3> *nodes, const int32_t *node, int32_t nn,
                                 int32_t *n) {
@@ -318,14 +317,14 @@ __global__ void k_bh_huge_sizes(const KNode<3> *nodes, const int32_t *node, int3
 // thread in point order, as _compute_dmin does.
 __global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, int32_t first,
                                                          int32_t count, const PotRec *PO, BHNode *B,
-                                                         int exact) {
+                                                         int exact, int huge) {
     __shared__ double dx_s[256];
     __shared__ BHNode bs;
     __shared__ double mx_s[8];
     int a = first + blockIdx.x;
     const KNode<3> &x = nodes[a];
     if (x.div < 0 || x.n <= RSG_BH_BIG) return;
-    if (!exact && x.n > RSG_BH_HUGE) return;  // k_bh_huge_*
+    if (!exact && x.n > huge) return;  // k_bh_huge_*
     if (threadIdx.x == 0) {
         const BHNode &L = B[x.left], &R = B[x.left + 1];
         bs.m = fadd(L.m, R.m);
@@ -1735,8 +1734,9 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     }
     BHNode *B = ar.get<BHNode>(F.nnodes);
     launch(k_bh_leaf, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, PO, mp, B);
-    // batched form: the nodes of more than RSG_BH_HUGE points, by level, and
+    // batched form: the nodes of more than bh_huge points, by level, and
     // their chunks (node ids ascend with the level index in the forest)
+    const int huge = tuning().bh_huge, chunk = tuning().bh_chunk;
     std::vector<int32_t> hn_node, hn_first(1, 0);  // per huge node: id, first item
     std::vector<int2> hitem;
     int2 *d_item = nullptr;
@@ -1744,7 +1744,7 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     double2 *d_part = nullptr;
     if (!exact) {
         int32_t *hf = ar.get<int32_t>(F.nnodes), *hid = ar.get<int32_t>(F.nnodes);
-        launch(k_bh_huge_flags, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, hf);
+        launch(k_bh_huge_flags, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, huge, hf);
         int32_t nh = select_idx(ar, hf, hid, F.nnodes, st);
         if (nh) {
             int32_t *hsz = ar.get<int32_t>(nh);
@@ -1755,7 +1755,7 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
             RSG_CUDA(cudaMemcpyAsync(sz.data(), hsz, 4 * nh, cudaMemcpyDeviceToHost, st));
             RSG_CUDA(cudaStreamSynchronize(st));
             for (int32_t j = 0; j < nh; j++) {
-                int nc = (sz[j] + RSG_BH_CH - 1) / RSG_BH_CH;
+                int nc = (sz[j] + chunk - 1) / chunk;
                 for (int c = 0; c < nc; c++) hitem.push_back(make_int2(hn_node[j], c));
                 hn_first.push_back((int32_t)hitem.size());
             }
@@ -1779,13 +1779,13 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
             else
                 launch(k_bh_internal_warp, nblk((int64_t)(b - a) * 32, 256), 256, 0, st, F.nodes, a,
                        b - a, PO, B);
-            launch(k_bh_internal_big, b - a, 256, 0, st, F.nodes, a, b - a, PO, B, exact);
+            launch(k_bh_internal_big, b - a, 256, 0, st, F.nodes, a, b - a, PO, B, exact, huge);
             size_t j1 = hj;
             while (hj > 0 && hn_node[hj - 1] >= a) hj--;
             if (j1 > hj) {
                 int32_t i0 = hn_first[hj], i1 = hn_first[j1];
                 launch(k_bh_huge_part, i1 - i0, 256, 0, st, F.nodes, (const int2 *)d_item + i0,
-                       PO, (const BHNode *)B, d_part + i0);
+                       chunk, PO, (const BHNode *)B, d_part + i0);
                 launch(k_bh_huge_fin, nblk((int)(j1 - hj), 64), 64, 0, st, F.nodes,
                        (const int32_t *)d_hnode + hj, (const int32_t *)d_hfirst + hj,
                        (int32_t)(j1 - hj), (const double2 *)d_part, B);
@@ -1910,16 +1910,17 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     int32_t *tot = ar.get<int32_t>(NH + 1), *nseg = ar.get<int32_t>(NH + 1);
     int32_t *toff = ar.get<int32_t>(NH + 1), *soff = ar.get<int32_t>(NH + 1);
     int32_t *kept = ar.get<int32_t>(NH + 1);
-    launch(k_set_count, nblk(NH + 1, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio, tot,
-           nseg, kept, err);
+    const int segmax = tuning().seg_max;
+    launch(k_set_count, nblk(NH + 1, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio,
+           segmax, tot, nseg, kept, err);
     check_i32_total(ar, tot, NH + 1, "potential records", st);
     int32_t npo = scan_i32(ar, tot, toff, NH + 1, st);
     phase_mark(st, "p.sets");
     int32_t ns = scan_i32(ar, nseg, soff, NH + 1, st);
     Seg *segs = ar.get<Seg>(ns + 1);
     PotRec *PO = ar.get<PotRec>(npo + 1), *PO2 = ar.get<PotRec>(npo + 1);
-    launch(k_set_segs, nblk(NH, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio, toff, soff,
-                                            segs);
+    launch(k_set_segs, nblk(NH, 64), 64, 0, st, H, E, NH, dc.include_host_potential_ratio, segmax,
+           toff, soff, segs);
     if (ns) launch(k_set_fill, ns, 128, 0, st, segs, W, H, PO);
     RSG_CHECK_LAUNCH();
     // potentials

@@ -225,22 +225,21 @@ __global__ void __launch_bounds__(256) k_norm_blk(Rec *W, HierNodes N, int32_t b
 }
 
 // Batched form, nodes above RSG_SMALL particles: cut into chunks of
-// RSG_NCH records, one block per chunk; per-chunk partial sums are added per
-// node in chunk order (deterministic).
-#define RSG_NCH 4096
+// Tuning::norm_chunk records, one block per chunk; per-chunk partial sums
+// are added per node in chunk order (deterministic).
 struct NChunk {
     int32_t node, start, n, pad;  // node: level-local index
 };
 struct NPart {
     double d[21];
 };
-__global__ void k_nch_count(HierNodes N, int32_t base, int32_t cnt, int32_t *nch) {
+__global__ void k_nch_count(HierNodes N, int32_t base, int32_t cnt, int chunk, int32_t *nch) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > cnt) return;
     int n = (k < cnt) ? N.n[base + k] : 0;
-    nch[k] = (n > RSG_SMALL) ? (n + RSG_NCH - 1) / RSG_NCH : 0;
+    nch[k] = (n > RSG_SMALL) ? (n + chunk - 1) / chunk : 0;
 }
-__global__ void k_nch_fill(HierNodes N, int32_t base, int32_t cnt, const int32_t *nch,
+__global__ void k_nch_fill(HierNodes N, int32_t base, int32_t cnt, int chunk, const int32_t *nch,
                            const int32_t *c0, NChunk *C) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= cnt) return;
@@ -248,8 +247,8 @@ __global__ void k_nch_fill(HierNodes N, int32_t base, int32_t cnt, const int32_t
     for (int c = 0; c < nch[k]; c++) {
         NChunk x;
         x.node = k;
-        x.start = s + c * RSG_NCH;
-        x.n = min(RSG_NCH, n - c * RSG_NCH);
+        x.start = s + c * chunk;
+        x.n = min(chunk, n - c * chunk);
         x.pad = 0;
         C[c0[k] + c] = x;
     }
@@ -1154,11 +1153,10 @@ __device__ __forceinline__ float asc_x(const AscHalo &h, const float *pos) {
     return fadd(a, b);
 }
 // Buckets of 32 consecutive candidates (k_asc_buckets_s) for nodes with more
-// than RSG_ASC_BUCKET of them: the box of their centres and the largest
+// than Tuning::asc_bucket_min (bmin) of them: the box of their centres and the largest
 // radius over the valid ones (inv: the bucket holds an invalid halo).  For a
 // point, box distance^2 / rmax^2 is at most the float x of every valid halo
 // in the bucket (every rounded operation of x is monotone in its inputs).
-#define RSG_ASC_BUCKET 64
 struct AscBucket {
     float mn[3], mx[3], rmax;
     int32_t inv;  // holds a halo without a valid metric
@@ -1175,7 +1173,7 @@ __device__ __forceinline__ float asc_bucket_lb(const AscBucket &B, const float *
     }
     return __fdiv_rn(d2, fmul(B.rmax, B.rmax));
 }
-// Nodes with more than RSG_ASC_BUCKET growing halos also get their halos in
+// Nodes with more than bmin growing halos also get their halos in
 // Morton order of position (within the node's box of halo centres), so that
 // buckets of 32 and 1024 halos are compact in space.  The scan order then
 // differs from the list order; the choice stays the list scan's because a
@@ -1195,21 +1193,21 @@ __device__ __forceinline__ int asc_count(const HierNodes &N, int node, int all) 
     return all ? N.h1[node] - N.h0[node] : N.ng[node];
 }
 __global__ void k_asc_sort_keys(HierNodes N, int32_t base, const rsg_halo *H,
-                                const int32_t *glist, int all, uint32_t *key, int32_t *val,
-                                int32_t *sb, int32_t *se) {
+                                const int32_t *glist, int all, int bmin, uint32_t *key,
+                                int32_t *val, int32_t *sb, int32_t *se) {
     __shared__ float mn[3], mx[3];
     int k = blockIdx.x, node = base + k;
     int ng = asc_count(N, node, all), h0 = N.h0[node];
     if (threadIdx.x == 0) {
         sb[k] = h0;
-        se[k] = ng > RSG_ASC_BUCKET ? h0 + ng : h0;
+        se[k] = ng > bmin ? h0 + ng : h0;
         for (int d = 0; d < 3; d++) {
             mn[d] = INFINITY;
             mx[d] = -INFINITY;
         }
     }
     __syncthreads();
-    if (ng <= RSG_ASC_BUCKET) return;
+    if (ng <= bmin) return;
     float lmn[3] = {INFINITY, INFINITY, INFINITY}, lmx[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int g = threadIdx.x; g < ng; g += blockDim.x) {
         const float *p = H[all ? h0 + g : glist[h0 + g]].pos;
@@ -1255,11 +1253,11 @@ __global__ void k_asc_sort_keys(HierNodes N, int32_t base, const rsg_halo *H,
 // Candidate records of the Morton-ordered nodes: ah[h0 + j] is the halo at
 // sorted position j, gi[h0 + j] its (list position, halo index).
 __global__ void k_asc_sorted_recs(HierNodes N, int32_t base, const rsg_halo *H,
-                                  const int32_t *glist, int all, const int32_t *sval, AscHalo *ah,
-                                  int2 *gi) {
+                                  const int32_t *glist, int all, int bmin, const int32_t *sval,
+                                  AscHalo *ah, int2 *gi) {
     int node = base + blockIdx.x;
     int ng = asc_count(N, node, all), h0 = N.h0[node];
-    if (ng <= RSG_ASC_BUCKET) return;
+    if (ng <= bmin) return;
     for (int j = threadIdx.x; j < ng; j += blockDim.x) {
         int g = sval[h0 + j], h = all ? h0 + g : glist[h0 + g];
         const rsg_halo &hh = H[h];
@@ -1275,11 +1273,11 @@ __global__ void k_asc_sorted_recs(HierNodes N, int32_t base, const rsg_halo *H,
     }
 }
 // Buckets of 32 (and 1024) consecutive Morton-ordered candidates.
-__global__ void k_asc_buckets_s(HierNodes N, int32_t base, int all, const AscHalo *ah,
+__global__ void k_asc_buckets_s(HierNodes N, int32_t base, int all, int bmin, const AscHalo *ah,
                                 AscBucket *bk, AscBucket *bk2) {
     int node = base + blockIdx.x;
     int ng = asc_count(N, node, all), h0 = N.h0[node];
-    if (ng <= RSG_ASC_BUCKET) return;
+    if (ng <= bmin) return;
     int nb = (ng + 31) / 32;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
         AscBucket B;
@@ -1329,7 +1327,7 @@ __device__ __forceinline__ double asc_xcut(float best) {
 
 // One thread per particle of the level (the node from eln): a node of
 // millions of particles spreads over the whole GPU.  Nodes with more than
-// RSG_ASC_BUCKET growing halos scan their Morton-ordered candidates and skip
+// bmin growing halos scan their Morton-ordered candidates and skip
 // a bucket (32) or super-bucket (1024 halos) whose lower bound of x reaches
 // asc_xcut of the running best (and, unless the best is below 1e20, holds
 // no invalid halo); the others scan the list in order.
@@ -1337,7 +1335,7 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
                                int32_t base, const rsg_halo *H, const rsg_extra_halo_info *E,
                                const int32_t *glist, const int32_t *redirect,
                                const AscBucket *bk, const AscBucket *bk2, const AscHalo *ah,
-                               const int2 *gi, int32_t *phalo) {
+                               const int2 *gi, int bmin, int32_t *phalo) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= M) return;
     int k = eln[i];
@@ -1367,7 +1365,7 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
     float bx = bvalid ? asc_x(hm, pos) : 0.f;
     float best = bvalid ? (float)sqrt((double)bx) : 1e20f;
     int bh = mi;
-    if (ng > RSG_ASC_BUCKET) {
+    if (ng > bmin) {
         // Morton-ordered candidates, (metric, list position) lexicographic;
         // mi holds list position 0.
         int bpos = 0;
@@ -1659,11 +1657,10 @@ __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, co
     if (threadIdx.x == 0) basic_vmax(hh, bins, do_bins, rsc_s, C);
 }
 
-// Batched form, halos above RSG_BP_BIG particles: calc_basic_halo_props over
-// chunks of RSG_BP_CH particles, one block per chunk per pass; the partial
-// sums and histograms are added per halo in chunk order (deterministic).
-#define RSG_BP_BIG 16384
-#define RSG_BP_CH 4096
+// Batched form, halos above Tuning::bp_big particles: calc_basic_halo_props
+// over chunks of Tuning::bp_chunk particles, one block per chunk per pass;
+// the partial sums and histograms are added per halo in chunk order
+// (deterministic).
 struct BPChunk {
     int32_t t, start, n, pad;  // t: entry of the halo list
 };
@@ -1671,14 +1668,15 @@ struct BPPart {
     double d[6];
     int bins[50];
 };
-__global__ void k_bp_nch(const rsg_halo *H, const int32_t *list, int32_t nl, int32_t *nch) {
+__global__ void k_bp_nch(const rsg_halo *H, const int32_t *list, int32_t nl, int big, int chunk,
+                         int32_t *nch) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t > nl) return;
     int np = (t < nl) ? (int)H[list[t]].num_p : 0;
-    nch[t] = (np > RSG_BP_BIG) ? (np + RSG_BP_CH - 1) / RSG_BP_CH : 0;
+    nch[t] = (np > big) ? (np + chunk - 1) / chunk : 0;
 }
-__global__ void k_bp_fill(const rsg_halo *H, const int32_t *list, int32_t nl, const int32_t *nch,
-                          const int32_t *c0, BPChunk *C) {
+__global__ void k_bp_fill(const rsg_halo *H, const int32_t *list, int32_t nl, int chunk,
+                          const int32_t *nch, const int32_t *c0, BPChunk *C) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nl) return;
     const rsg_halo &hh = H[list[t]];
@@ -1686,8 +1684,8 @@ __global__ void k_bp_fill(const rsg_halo *H, const int32_t *list, int32_t nl, co
     for (int c = 0; c < nch[t]; c++) {
         BPChunk x;
         x.t = t;
-        x.start = ps + c * RSG_BP_CH;
-        x.n = min(RSG_BP_CH, np - c * RSG_BP_CH);
+        x.start = ps + c * chunk;
+        x.n = min(chunk, np - c * chunk);
         x.pad = 0;
         C[c0[t] + c] = x;
     }
@@ -1823,7 +1821,7 @@ __device__ __forceinline__ float hdist_x(const rsg_halo &c, const rsg_halo &h, f
 // find_best_parent (src/subhalo_metric.c:185-191) over the node's listed
 // halos: the first strict minimum of calc_halo_dist in list order, starting
 // from the biggest halo (which therefore wins every tie).  Nodes listing
-// more than RSG_ASC_BUCKET halos scan their Morton-ordered candidates
+// more than bmin halos scan their Morton-ordered candidates
 // (k_asc_sorted_recs over the same list) and take (metric, list position)
 // lexicographically, the biggest halo holding position -1.  While the best
 // is below 1e20 (the value of a too-small or invalid candidate), a bucket is
@@ -1832,7 +1830,7 @@ __device__ __forceinline__ float hdist_x(const rsg_halo &c, const rsg_halo &h, f
 __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const int32_t *loff,
                               const int32_t *list, const int32_t *hnode, rsg_halo *H,
                               rsg_extra_halo_info *E, const AscBucket *bk, const AscBucket *bk2,
-                              const AscHalo *ah, const int2 *gi) {
+                              const AscHalo *ah, const int2 *gi, int bmin) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int tot = loff[count];
     if (t >= tot) return;
@@ -1847,7 +1845,7 @@ __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const in
         float best = hdist_x(H[mi], hh, &bx);
         res = mi;
         const int g0 = loff[k], n = loff[k + 1] - g0, h0 = N.h0[node];
-        if (n > RSG_ASC_BUCKET) {
+        if (n > bmin) {
             int bpos = -1;
             double cut = asc_xcut(best);
             const double hr = (double)hh.r;
@@ -2091,17 +2089,18 @@ static void fix_parents_level(Arena &ar, HierNodes N, int32_t base, int32_t cnt,
 }
 
 // calc_basic_halo_props for the listed halos: one block per halo, and in the
-// batched form the chunked passes for halos above RSG_BP_BIG particles.
+// batched form the chunked passes for halos above Tuning::bp_big particles.
 static void basic_props(Arena &ar, const Rec *W, rsg_halo *H, const int32_t *list, int32_t nl,
                         const DevCfg *d_dc, int seq_max, int exact, cudaStream_t st) {
     const int T = 256;
     if (nl <= 0) return;
     launch(k_basic_props, nl, T, 0, st, W, H, list, d_dc, exact ? seq_max : 0,
-           exact ? 0x7fffffff : RSG_BP_BIG);
+           exact ? 0x7fffffff : tuning().bp_big);
     if (exact) return;
     size_t mark = ar.used;
     int32_t *nch = ar.get<int32_t>(nl + 1), *c0 = ar.get<int32_t>(nl + 1);
-    launch(k_bp_nch, nblk(nl + 1, T), T, 0, st, (const rsg_halo *)H, list, nl, nch);
+    const int bpbig = tuning().bp_big, bpch = tuning().bp_chunk;
+    launch(k_bp_nch, nblk(nl + 1, T), T, 0, st, (const rsg_halo *)H, list, nl, bpbig, bpch, nch);
     int32_t nc = excl_scan_i32(ar, nch, c0, nl + 1, st);
     if (nc > 0) {
         BPChunk *C = ar.get<BPChunk>(nc);
@@ -2109,7 +2108,7 @@ static void basic_props(Arena &ar, const Rec *W, rsg_halo *H, const int32_t *lis
         double *mean = ar.get<double>(6 * (int64_t)nl);
         int *dob = ar.get<int>(nl);
         float *rsc = ar.get<float>(nl);
-        launch(k_bp_fill, nblk(nl, T), T, 0, st, (const rsg_halo *)H, list, nl,
+        launch(k_bp_fill, nblk(nl, T), T, 0, st, (const rsg_halo *)H, list, nl, bpch,
                (const int32_t *)nch, (const int32_t *)c0, C);
         launch(k_bp_sum6, nc, 256, 0, st, W, (const BPChunk *)C, (const double *)nullptr, P);
         launch(k_bp_mean, nblk(nl, T), T, 0, st, (const rsg_halo *)H, list, nl,
@@ -2211,7 +2210,7 @@ DevCfg make_devcfg(const rsg_config &c) {
 }
 
 // Morton-ordered candidate records and their buckets for the level's nodes
-// with more than RSG_ASC_BUCKET listed halos (all: see asc_count).
+// with more than Tuning::asc_bucket_min listed halos (all: see asc_count).
 static void asc_sorted(Arena &ar, HierNodes N, int32_t base, int32_t cnt, const rsg_halo *H,
                        const int32_t *glist, int all, int32_t NH, AscHalo *ah, int2 *gi,
                        AscBucket *bk, AscBucket *bk2, cudaStream_t st) {
@@ -2219,15 +2218,16 @@ static void asc_sorted(Arena &ar, HierNodes N, int32_t base, int32_t cnt, const 
     uint32_t *sk = ar.get<uint32_t>(NH), *sk2 = ar.get<uint32_t>(NH);
     int32_t *sv = ar.get<int32_t>(NH), *sv2 = ar.get<int32_t>(NH);
     int32_t *sb = ar.get<int32_t>(cnt), *se = ar.get<int32_t>(cnt);
-    launch(k_asc_sort_keys, cnt, 128, 0, st, N, base, H, glist, all, sk, sv, sb, se);
+    const int bmin = tuning().asc_bucket_min;
+    launch(k_asc_sort_keys, cnt, 128, 0, st, N, base, H, glist, all, bmin, sk, sv, sb, se);
     size_t tb = 0;
     cub::DeviceSegmentedSort::SortPairs(nullptr, tb, sk, sk2, sv, sv2, NH, cnt, sb, se, st);
     void *tmp = ar.take(tb + 256);
     cub::DeviceSegmentedSort::SortPairs(tmp, tb, sk, sk2, sv, sv2, NH, cnt, sb, se, st);
     RSG_CHECK_LAUNCH();
-    launch(k_asc_sorted_recs, cnt, 128, 0, st, N, base, H, glist, all, (const int32_t *)sv2, ah,
-           gi);
-    launch(k_asc_buckets_s, cnt, 64, 0, st, N, base, all, (const AscHalo *)ah, bk, bk2);
+    launch(k_asc_sorted_recs, cnt, 128, 0, st, N, base, H, glist, all, bmin, (const int32_t *)sv2,
+           ah, gi);
+    launch(k_asc_buckets_s, cnt, 64, 0, st, N, base, all, bmin, (const AscHalo *)ah, bk, bk2);
     ar.used = m2;
 }
 
@@ -2325,14 +2325,15 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                        sig, seq_max);
             } else {
                 int32_t *nch = ar.get<int32_t>(cnt + 1), *c0 = ar.get<int32_t>(cnt + 1);
-                launch(k_nch_count, nblk(cnt + 1, T), T, 0, st, N, base, cnt, nch);
+                launch(k_nch_count, nblk(cnt + 1, T), T, 0, st, N, base, cnt, tuning().norm_chunk,
+                       nch);
                 int32_t nc = excl_scan(ar, (const int32_t *)nch, c0, cnt + 1, st);
                 if (nc > 0) {
                     NChunk *C = ar.get<NChunk>(nc);
                     NPart *P = ar.get<NPart>(nc);
                     double *mean = ar.get<double>(6 * (int64_t)cnt);
-                    launch(k_nch_fill, nblk(cnt, T), T, 0, st, N, base, cnt, (const int32_t *)nch,
-                           (const int32_t *)c0, C);
+                    launch(k_nch_fill, nblk(cnt, T), T, 0, st, N, base, cnt, tuning().norm_chunk,
+                           (const int32_t *)nch, (const int32_t *)c0, C);
                     launch(k_nch_sum6, nc, 256, 0, st, (const Rec *)W, (const NChunk *)C, P);
                     launch(k_nch_mean, nblk(cnt, T), T, 0, st, N, base, cnt, (const int32_t *)nch,
                            (const int32_t *)c0, (const NPart *)P, mean);
@@ -2508,7 +2509,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         launch(k_asc_assign_p, nblk(M, 128), 128, 0, st, (const Rec *)W, M, (const int32_t *)eln,
                N, base, (const rsg_halo *)H, (const rsg_extra_halo_info *)E,
                (const int32_t *)glist, (const int32_t *)redirect, (const AscBucket *)ascb,
-               (const AscBucket *)ascb2, (const AscHalo *)asch, (const int2 *)ascgi, phalo);
+               (const AscBucket *)ascb2, (const AscHalo *)asch, (const int2 *)ascgi,
+               tuning().asc_bucket_min, phalo);
         phase_mark(st, "a.seed_assign");
         RSG_CHECK_LAUNCH();
         if (exact) {
@@ -2535,7 +2537,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         asc_sorted(ar, N, base, cnt, H, glist, 0, NH, asch, ascgi, ascb, ascb2, st);
         launch(k_best_parent, nblk(ngr, T), T, 0, st, N, base, cnt, goffs, glv, gnode, H, E,
                (const AscBucket *)ascb, (const AscBucket *)ascb2, (const AscHalo *)asch,
-               (const int2 *)ascgi);
+               (const int2 *)ascgi, tuning().asc_bucket_min);
         fix_parents_level(ar, N, base, cnt, H, E, err, true, st);
         basic_props(ar, W, H, glv, ngr, d_dc, seq_max, exact, st);
         RSG_CHECK_LAUNCH();
@@ -2558,7 +2560,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             asc_sorted(ar, N, base, cnt, H, glist, 1, NH, asch, ascgi, ascb, ascb2, st);
             launch(k_best_parent, nblk(na, T), T, 0, st, N, base, cnt, aoff, alist, anode, H, E,
                    (const AscBucket *)ascb, (const AscBucket *)ascb2, (const AscHalo *)asch,
-                   (const int2 *)ascgi);
+                   (const int2 *)ascgi, tuning().asc_bucket_min);
             fix_parents_level(ar, N, base, cnt, H, E, err, true, st);
             RSG_CHECK_LAUNCH();
             // find_subs tail (src/groupies.c:697-703): child counts and basic

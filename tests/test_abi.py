@@ -6,6 +6,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 from conftest import ROOT
 
@@ -69,3 +70,22 @@ def test_isolated_groups_workload(rk):
     c = np.floor(x / cell).astype(np.int64)
     idx = c[:, 0] + side * (c[:, 1] + side * c[:, 2])
     assert idx.max() < ng and len(np.unique(idx)) == ng
+
+
+def test_tuning_parameters(rk):
+    """rsg_set_tuning / rsg_get_tuning: names, ranges, errors (host only)."""
+    old = rk.get_tuning()
+    assert set(old) == set(rk.TUNING_NAMES)
+    try:
+        rk.set_tuning("seg_max", 4096)
+        assert rk.get_tuning("seg_max") == 4096
+        with pytest.raises(rk.RockstarError) as e:
+            rk.set_tuning("seg_max", 10)
+        assert e.value.code == -1
+        with pytest.raises(rk.RockstarError):
+            rk.set_tuning("no_such_parameter", 1)
+        with pytest.raises(rk.RockstarError):
+            rk.set_tuning("bh_huge", 100)  # must stay above the warp kernels' node size
+    finally:
+        for k, v in old.items():
+            rk.set_tuning(k, v)

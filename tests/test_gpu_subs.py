@@ -90,3 +90,34 @@ def test_find_subs_batched_golden(rk, name):
         a, b = H[ref_sets[k]], gh[got_sets[k]]
         errs.append(max(HC.rel_err(a[f], b[f]) for f in HC.FLOAT_FIELDS))
     assert np.median(errs) <= 1e-6, np.median(errs)
+
+
+def test_tuning_does_not_change_results(rk):
+    """Size-class thresholds change speed only.  The assignment bucket
+    threshold and the copy segment size leave every byte of the batched
+    output as it is; the chunk sizes of the chunked passes reorder FP64 sums,
+    so the same halos come out with properties within rounding (1e-4 for
+    every field of at least 99% of halos, as for any change of summation
+    order in the batched form)."""
+    p, box, mp, _ = rk.synth(2, 1 / 8)
+    cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    fp, off, sz = rk.rockstar_fof(p, cfg)
+    old = rk.get_tuning()
+    try:
+        ref = rk.find_subs(fp, off, sz, cfg, batched=True)
+        rk.set_tuning("asc_bucket_min", 32)
+        rk.set_tuning("seg_max", 256)
+        got = rk.find_subs(fp, off, sz, cfg, batched=True)
+        for a, b in zip(ref, got):
+            assert a.tobytes() == b.tobytes()
+        for k, v in (("norm_chunk", 1024), ("bp_big", 4096), ("bp_chunk", 1024),
+                     ("bh_huge", 4096), ("bh_chunk", 1024)):
+            rk.set_tuning(k, v)
+        got = rk.find_subs(fp, off, sz, cfg, batched=True)
+        ua, ub, worst, bad = HC.compare(HC.halo_sets(ref[0], ref[1]), ref[1],
+                                        HC.halo_sets(got[0], got[1]), got[1], 1e-4)
+        assert ua == 0 and ub == 0
+        assert len({h for _, h, _ in bad}) <= 0.01 * len(ref[1]) + 1, bad[:10]
+    finally:
+        for k, v in old.items():
+            rk.set_tuning(k, v)
