@@ -95,11 +95,20 @@ def setup_config(cfg):
     return st
 
 
-def rockstar_fof(parts, cfg):
+def rockstar_fof(parts, cfg, inplace=False):
     """3D FOF of an id-sorted particle array.  Returns (particles, offsets,
-    sizes): the permuted/deduplicated particles and each group's range."""
+    sizes): the permuted/deduplicated particles and each group's range.
+    With inplace=True the caller's (contiguous PARTICLE) array is permuted in
+    place, as rsg_rockstar_fof does, and the returned particles are a view
+    of its first num_p records."""
     st = setup_config(cfg)
-    pa = np.array(parts, dtype=PARTICLE, copy=True)
+    if inplace:
+        if not (isinstance(parts, np.ndarray) and parts.dtype == PARTICLE
+                and parts.flags.c_contiguous and parts.flags.writeable):
+            raise ValueError("inplace needs a writeable contiguous PARTICLE array")
+        pa = parts
+    else:
+        pa = np.array(parts, dtype=PARTICLE, copy=True)
     n = np.array([len(pa)], np.int64)
     cap = len(pa) // 2 + 1
     off = np.zeros(cap, np.int64)
@@ -108,15 +117,25 @@ def rockstar_fof(parts, cfg):
     _check(lib().rsg_rockstar_fof(pa.ctypes.data, n.ctypes.data, C.byref(st), off.ctypes.data,
                                   sz.ctypes.data, cap, nf.ctypes.data))
     k = int(nf[0])
+    if inplace:
+        return pa[:n[0]], off[:k].copy(), sz[:k].copy()
     return pa[:n[0]].copy(), off[:k].copy(), sz[:k].copy()
 
 
-def find_subs(parts, offsets, sizes, cfg, batched=False):
+def find_subs(parts, offsets, sizes, cfg, batched=False, inplace=False):
     """Substructure + halo properties for every group.  batched=False is the
     plain drop-in (the reference's results bit for bit); batched=True the
-    batched form (rsg_find_subs_batch).  Returns (particles, halos, extra)."""
+    batched form (rsg_find_subs_batch).  Returns (particles, halos, extra);
+    with inplace=True the caller's particle array is permuted in place and
+    returned."""
     st = setup_config(cfg)
-    pa = np.array(parts, dtype=PARTICLE, copy=True)
+    if inplace:
+        if not (isinstance(parts, np.ndarray) and parts.dtype == PARTICLE
+                and parts.flags.c_contiguous and parts.flags.writeable):
+            raise ValueError("inplace needs a writeable contiguous PARTICLE array")
+        pa = parts
+    else:
+        pa = np.array(parts, dtype=PARTICLE, copy=True)
     off = np.ascontiguousarray(offsets, np.int64)
     sz = np.ascontiguousarray(sizes, np.int64)
     cap = int(sz.sum()) // 2 + len(sz) + 16
