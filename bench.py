@@ -267,6 +267,32 @@ def precision_study(rk, scale, forms):
     print(json.dumps(res))
 
 
+def profile_only(rk, cfg_id, scale, warmup):
+    """The batched path alone: `warmup` steps, then one step whose launches
+    are timed with CUDA events (the small case an ncu capture runs)."""
+    import torch
+    rk.build()
+    p, box, mp, _ = rk.synth(cfg_id, scale, SEED)
+    cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    d_in = torch.from_numpy(p.view(np.uint8).reshape(-1)).cuda()
+    path = rk.DevicePath(len(p), cfg, batched=True)
+    for _ in range(warmup):
+        path.run(d_in.data_ptr())
+    torch.cuda.synchronize()
+    rk.profile_select("*")
+    t0 = time.perf_counter()
+    res = path.run(d_in.data_ptr())
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3
+    rows = [l.split("\t") for l in rk.profile_table().strip().splitlines()]
+    rk.profile_select("")
+    print(json.dumps({"workload": "synthetic workload %d at scale %g: %d particles"
+                      % (cfg_id, scale, len(p)), "warmup": warmup,
+                      "step_ms_with_events": ms, "halos": res[2],
+                      "launches": {r[0]: int(r[1]) for r in rows},
+                      "kernel_ms": {r[0]: float(r[2]) for r in rows[:12]}}))
+
+
 def run_autotune(rk, cfg_id, scale):
     """Size-class thresholds by measurement (mpi-rockstar_gb300/autotune.py)."""
     from mpi_rockstar_gb300 import autotune
@@ -300,6 +326,10 @@ def main():
                     help="instead of the bench line: tune the batched form's size-class "
                          "thresholds on the workload (--cfg, --scale) and write them to "
                          "mpi-rockstar_gb300/tuning.json, which later runs apply")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="instead of the bench line: --warmup batched steps, then one step "
+                         "with CUDA events around every launch; prints the step time and "
+                         "each kernel's launches (the command the ncu captures run)")
     ap.add_argument("--precision-forms", default="3,0,1,2",
                     help="potential forms of the study; the first is the reference "
                          "(3: FP64 direct sum, O(n^2) per group)")
@@ -314,6 +344,10 @@ def main():
     if args.autotune:
         if rank == 0:
             run_autotune(rk, args.cfg, args.scale)
+        return
+    if args.profile_only:
+        if rank == 0:
+            profile_only(rk, args.cfg, args.scale, args.warmup)
         return
     if args.impl == "reference":
         if rank == 0:

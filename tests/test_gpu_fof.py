@@ -30,7 +30,8 @@ def test_tree_degenerate(rk, oracle):
                               oracle.tree_order(p, dim, leaf)["id"])
 
 
-@pytest.mark.parametrize("cfg,scale", [(1, 0.25), (1, 1.0), (2, 1 / 16)])
+@pytest.mark.parametrize("cfg,scale", [(1, 0.25), (1, 1.0), (2, 1 / 16), (3, 0.005),
+                                       (4, 1 / 2048), (5, 0.004)])
 def test_fof_partition(rk, oracle, cfg, scale):
     p, box, mp, _ = rk.synth(cfg, scale)
     c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))

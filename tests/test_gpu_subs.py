@@ -44,7 +44,8 @@ def test_find_subs_golden(rk, name):
     assert not bad, "fields beyond %g: %s" % (TOL, bad[:10])
 
 
-@pytest.mark.parametrize("cfg,scale", [(1, 1.0), (2, 1 / 16)])
+@pytest.mark.parametrize("cfg,scale", [(1, 1.0), (2, 1 / 16), (3, 0.002), (4, 1 / 2048),
+                                       (5, 0.004)])
 def test_find_subs_oracle(rk, oracle, cfg, scale):
     p, box, mp, _ = rk.synth(cfg, scale)
     c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
