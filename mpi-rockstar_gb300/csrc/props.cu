@@ -468,8 +468,28 @@ __global__ void __launch_bounds__(64) k_bh_walk(const KNode<3> *nodes, const int
                 if (n.mn[i] < n2.mn[i] || n.mx[i] > n2.mx[i]) break;
             bool open = (i == 3);
             if (!open) {
-                float r2 = (float)d2d(bn.mc, B[b].mc);
-                open = !(r2 > fmul(B[b].dmin, B[b].dmin));
+                const float dm2 = fmul(B[b].dmin, B[b].dmin);
+                int dec = -1;  // 0: keep the monopole, 1: open
+                if (MODE != 0) {
+                    // The reference's r^2 is (float) of FP64 sums of the float
+                    // differences' squares.  An FP32 sum of the same squares is
+                    // within 2.4e-7 of it (relative); outside a 2e-6 band around
+                    // dmin^2 the FP32 value decides the same way, inside it the
+                    // FP64 sum decides (GB300's FP64 pipe is narrow).
+                    float dx = fsub(bn.mc[0], B[b].mc[0]), dy = fsub(bn.mc[1], B[b].mc[1]),
+                          dz = fsub(bn.mc[2], B[b].mc[2]);
+                    float sf = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, fmul(dx, dx)));
+                    if (sf > 1e-30f && sf < 1e30f && dm2 > 1e-30f && dm2 < 1e30f) {
+                        if (sf > fmul(dm2, 1.000002f)) dec = 0;
+                        else if (sf < fmul(dm2, 0.999998f)) dec = 1;
+                    }
+                }
+                if (dec < 0) {
+                    float r2 = (float)d2d(bn.mc, B[b].mc);
+                    open = !(r2 > dm2);
+                } else {
+                    open = dec == 1;
+                }
             }
             if (open) {
                 if (n2.div < 0) {

@@ -1317,12 +1317,31 @@ __global__ void k_asc_buckets_s(HierNodes N, int32_t base, int all, int bmin, co
         bk2[h0 + sb] = S;
     }
 }
-// Smallest x whose metric (float)sqrt((double)x) can exceed `best`: any x
-// at or above best's float successor squared (exact in FP64) gives a metric
-// of at least that successor.
-__device__ __forceinline__ double asc_xcut(float best) {
-    double nb = (double)nextafterf(best, INFINITY);
-    return nb * nb;
+// Smallest float x whose metric (float)sqrt((double)x) can exceed `best`:
+// any x at or above the square of best's float successor gives a metric of
+// at least that successor, and for a float x, x >= nb^2 holds exactly when
+// x >= nb^2 rounded up to a float (__fmul_ru).  The hot loops compare floats
+// only (GB300's FP64 pipe is narrow).
+__device__ __forceinline__ float asc_xcut(float best) {
+    float nb = nextafterf(best, INFINITY);
+    return __fmul_ru(nb, nb);
+}
+// calc_halo_dist's size test (double)h.r > (double)c.r * 0.99999 as a float
+// comparison c.r < T: T is the smallest float t with (double)t * 0.99999 >=
+// h.r (the product is monotone in t); -inf when no r is filtered (h.r NaN or
+// -inf), +inf when every finite r is.  A NaN c.r is never filtered either way.
+__device__ float rfilter_threshold(float hr) {
+    if (hr != hr || hr == -INFINITY) return -INFINITY;
+    if (hr == INFINITY) return INFINITY;
+    const double h = hr;
+    float t = (float)(h / 0.99999);
+    for (int i = 0; i < 8 && !((double)t * 0.99999 >= h); i++) t = nextafterf(t, INFINITY);
+    for (int i = 0; i < 8; i++) {
+        float q = nextafterf(t, -INFINITY);
+        if ((double)q * 0.99999 >= h) t = q;
+        else break;
+    }
+    return t;
 }
 
 // One thread per particle of the level (the node from eln): a node of
@@ -1369,18 +1388,18 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
         // Morton-ordered candidates, (metric, list position) lexicographic;
         // mi holds list position 0.
         int bpos = 0;
-        double cut = asc_xcut(best);
+        float cut = asc_xcut(best);
         for (int j = 0; j < ng;) {
             if ((j & 1023) == 0) {
                 const AscBucket &S = bk2[h0 + (j >> 10)];
-                if ((!S.inv || best < 1e20f) && (double)asc_bucket_lb(S, pos) >= cut) {
+                if ((!S.inv || best < 1e20f) && asc_bucket_lb(S, pos) >= cut) {
                     j += 1024;
                     continue;
                 }
             }
             if ((j & 31) == 0) {
                 const AscBucket &B = bk[h0 + (j >> 5)];
-                if ((!B.inv || best < 1e20f) && (double)asc_bucket_lb(B, pos) >= cut) {
+                if ((!B.inv || best < 1e20f) && asc_bucket_lb(B, pos) >= cut) {
                     j += 32;
                     continue;
                 }
@@ -1391,7 +1410,7 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
                 m = 1e20f;
             } else {
                 float x = asc_x(c, pos);
-                if ((double)x >= cut) {
+                if (x >= cut) {
                     j++;
                     continue;
                 }
@@ -1847,22 +1866,20 @@ __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const in
         const int g0 = loff[k], n = loff[k + 1] - g0, h0 = N.h0[node];
         if (n > bmin) {
             int bpos = -1;
-            double cut = asc_xcut(best);
-            const double hr = (double)hh.r;
+            float cut = asc_xcut(best);
+            const float rt = rfilter_threshold(hh.r);
             for (int j = 0; j < n;) {
                 if (best < 1e20f) {
                     if ((j & 1023) == 0) {
                         const AscBucket &S = bk2[h0 + (j >> 10)];
-                        if (hr > (double)S.rmax * 0.99999 ||
-                            (double)asc_bucket_lb(S, hh.pos) >= cut) {
+                        if (S.rmax < rt || asc_bucket_lb(S, hh.pos) >= cut) {
                             j += 1024;
                             continue;
                         }
                     }
                     if ((j & 31) == 0) {
                         const AscBucket &B = bk[h0 + (j >> 5)];
-                        if (hr > (double)B.rmax * 0.99999 ||
-                            (double)asc_bucket_lb(B, hh.pos) >= cut) {
+                        if (B.rmax < rt || asc_bucket_lb(B, hh.pos) >= cut) {
                             j += 32;
                             continue;
                         }
@@ -1870,11 +1887,11 @@ __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const in
                 }
                 const AscHalo c = ah[h0 + j];
                 float m;
-                if (hr > (double)c.r * 0.99999 || c.vrms <= 0 || c.r <= 0) {
+                if (c.r < rt || c.vrms <= 0 || c.r <= 0) {
                     m = 1e20f;
                 } else {
                     float x = asc_x(c, hh.pos);
-                    if ((double)x >= cut) {
+                    if (x >= cut) {
                         j++;
                         continue;
                     }
