@@ -69,6 +69,12 @@ struct Arena {
 // evaluates `dist += dx*dx` as a rounded multiply followed by a rounded add.
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+// The reference's (float)sqrt((double)x) for a float x.  Rounding the exact
+// square root to double and then to float gives the float rounding of the
+// exact root, because 53 >= 2 * 24 + 2 makes double rounding innocuous for
+// square roots (Figueroa, "When is double rounding innocuous?", 1995), so
+// the IEEE float square root is bit-identical and keeps the FP64 pipe free.
+__device__ __forceinline__ float sqrt_fd(float x) { return __fsqrt_rn(x); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }

@@ -36,7 +36,7 @@ __device__ __forceinline__ float pdist(const rsg_halo &h, const float *pos) {
     }
     float a = __fdiv_rn(r2, fmul(h.r, h.r));
     float b = __fdiv_rn(v2, fmul(h.vrms, h.vrms));
-    return (float)sqrt((double)fadd(a, b));
+    return sqrt_fd(fadd(a, b));
 }
 // calc_halo_dist, src/subhalo_metric.c:73-77
 __device__ __forceinline__ float hdist(const rsg_halo &h1, const rsg_halo &h2) {
@@ -59,8 +59,8 @@ __device__ __forceinline__ int poisson_or_force(const rsg_halo &h1, const rsg_ha
     float mpe = h1.min_pos_err, mve = h1.min_vel_err;
     dx = (float)((double)fadd(__fdiv_rn(r, mpe), __fdiv_rn(v, mve)) / 2.0);
     if (!(dx > 100)) return 1;
-    r = (float)sqrt((double)r);
-    v = (float)sqrt((double)v);
+    r = sqrt_fd(r);
+    v = sqrt_fd(v);
     if ((fadd(h1.r, h2.r) > r) && (1.5 * (double)fadd(h1.vrms, h2.vrms)) > (double)v &&
         ((double)r < 1.5 * force_res)) {
         *force = 1;

@@ -925,7 +925,7 @@ __device__ void more_props(rsg_halo &h, const PotRec *po, int64_t tot, int bound
         }
         for (int k = 0; k < 4; k++) h.alt_m[k] = (float)(npa[k] * C.particle_mass);
         h.Xoff = (float)(sqrt((double)h.Xoff) * 1e3);
-        h.Voff = (float)sqrt((double)h.Voff);
+        h.Voff = sqrt_fd(h.Voff);
         h.vrms = (float)sqrt(vrms[0] + vrms[1] + vrms[2]);
         h.vmax = (float)(RSG_VMAX_CONST * sqrt(vmax * vconv));
         h.rvmax = (float)(rvmax * 1e3);
@@ -1407,7 +1407,7 @@ __device__ void more_props_blk(rsg_halo &h, const PotRec *po, int64_t tot, int b
             }
             for (int k = 0; k < 4; k++) h.alt_m[k] = (float)(S.npa[k] * C.particle_mass);
             h.Xoff = (float)(sqrt((double)h.Xoff) * 1e3);
-            h.Voff = (float)sqrt((double)h.Voff);
+            h.Voff = sqrt_fd(h.Voff);
             h.vrms = (float)sqrt(S.vrms[0] + S.vrms[1] + S.vrms[2]);
             h.vmax = (float)(RSG_VMAX_CONST * sqrt(S.vmax * (C.particle_mass / (double)scale)));
             h.rvmax = (float)(S.rvmax * 1e3);

@@ -594,7 +594,7 @@ __global__ void k_sg_v2_fin(int32_t NH, rsg_halo *H, const int32_t *c0, const in
     }
     for (int k = 0; k < 4; k++) hh.alt_m[k] = (float)(s.npa[k] * C.particle_mass);
     hh.Xoff = (float)(sqrt((double)hh.Xoff) * 1e3);
-    hh.Voff = (float)sqrt((double)hh.Voff);
+    hh.Voff = sqrt_fd(hh.Voff);
     hh.vrms = (float)sqrt(vr[0] + vr[1] + vr[2]);
     hh.vmax = (float)(RSG_VMAX_CONST * sqrt(s.vmax * (C.particle_mass / (double)scale)));
     hh.rvmax = (float)(s.rvmax * 1e3);

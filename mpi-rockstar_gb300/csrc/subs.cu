@@ -461,7 +461,7 @@ __device__ float next_closest(const KNode<6> *nodes, int root, const Rec *W, con
         float d = dist6(c, W[o.start + i].pos);
         if (d && d < md) md = d;
     }
-    float r = (float)sqrt((double)md);
+    float r = sqrt_fd(md);
     int stack[RSG_STACK6];
     int sp = 0;
     stack[sp++] = root;
@@ -475,7 +475,7 @@ __device__ float next_closest(const KNode<6> *nodes, int root, const Rec *W, con
                 float d = dist6(c, W[x.start + i].pos);
                 if (d < r2) r2 = d;
             }
-            r = (float)sqrt((double)r2);
+            r = sqrt_fd(r2);
             continue;
         }
         int a = x.left, b = x.left + 1;
@@ -1382,7 +1382,7 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
     hm.vrms = H[mi].vrms;
     bool bvalid = asc_valid(hm);
     float bx = bvalid ? asc_x(hm, pos) : 0.f;
-    float best = bvalid ? (float)sqrt((double)bx) : 1e20f;
+    float best = bvalid ? sqrt_fd(bx) : 1e20f;
     int bh = mi;
     if (ng > bmin) {
         // Morton-ordered candidates, (metric, list position) lexicographic;
@@ -1414,7 +1414,7 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
                     j++;
                     continue;
                 }
-                m = (float)sqrt((double)x);
+                m = sqrt_fd(x);
             }
             int gp = gi[h0 + j].x;
             if (m < best || (m == best && gp < bpos)) {
@@ -1445,7 +1445,7 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
             }
             float x = asc_x(c, pos);
             if (!(bvalid && !(x < bx))) {
-                float m = (float)sqrt((double)x);
+                float m = sqrt_fd(x);
                 if (m < best) {
                     best = m;
                     bx = x;
@@ -1575,7 +1575,7 @@ __device__ void basic_vmax(rsg_halo &hh, const int *bins, int do_bins, float rsc
         hh.vmax_r = (float)(sqrt((double)sn) * (double)v * C->dyn_time);
     }
     if (hh.vmax_r) hh.r = hh.vmax_r;
-    hh.vrms = (float)sqrt((double)hh.vrms);
+    hh.vrms = sqrt_fd(hh.vrms);
 }
 
 // calc_basic_halo_props + estimate_vmax (src/properties.c:39-125); one
@@ -1835,7 +1835,7 @@ __device__ __forceinline__ float hdist_x(const rsg_halo &c, const rsg_halo &h, f
     a.r = c.r;
     a.vrms = c.vrms;
     *x = asc_x(a, h.pos);
-    return (float)sqrt((double)*x);
+    return sqrt_fd(*x);
 }
 // find_best_parent (src/subhalo_metric.c:185-191) over the node's listed
 // halos: the first strict minimum of calc_halo_dist in list order, starting
@@ -1895,7 +1895,7 @@ __global__ void k_best_parent(HierNodes N, int32_t base, int32_t count, const in
                         j++;
                         continue;
                     }
-                    m = (float)sqrt((double)x);
+                    m = sqrt_fd(x);
                 }
                 int gp = gi[h0 + j].x;
                 if (m < best || (m == best && gp < bpos)) {
