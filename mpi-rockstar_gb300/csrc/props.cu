@@ -376,90 +376,91 @@ __global__ void __launch_bounds__(256) k_bh_internal_big(const KNode<3> *nodes, 
 }
 
 // _compute_monopole_potentials(leaf, root) (src/potential.c:133-168): one
-// thread per leaf walks the tree from the root, in groups of RSG_BH_G of the
-// leaf's particles whose sums stay in registers.  A particle's potential
-// receives the same terms in the same order as in the reference (the self
-// leaf's pairs in ascending partner order, opened leaves in point order,
-// monopoles as visited), so the FP64 form is bit-identical to it.
+// half-warp per leaf walks the tree from the root, each lane holding one of
+// the leaf's particles (leaves hold at most 10 but for duplicates; larger
+// ones repeat the walk per 16).  The opening decisions belong to the leaf,
+// so the walk is the same for every lane of the half-warp, which shares one
+// stack in shared memory; the two halves of a warp walk two leaves.  A particle's
+// potential receives the same terms in the same order as in the reference
+// (the self leaf's pairs in ascending partner order, opened leaves in point
+// order, monopoles as visited), so the FP64 form is bit-identical to it.
 //   MODE 0: r = max(sqrt(r2), FORCE_RES) and m / r in FP64, as the
 //           reference computes them;
 //   MODE 1: the batched precision form: squared distance and 1/r in FP32
 //           (rsqrtf), each particle's sum Kahan-compensated in FP32;
 //   MODE 2: the MODE 1 terms summed in plain FP32 (no compensation), the
 //           uncompensated baseline of the precision study.
-// The opening test itself is the same in every mode.
-#define RSG_BH_G 16
+// The opening decisions are the same in every mode.
+#define RSG_BH_WPB 8  // warps per block (16 leaves)
 template <int MODE>
-__global__ void __launch_bounds__(64) k_bh_walk(const KNode<3> *nodes, const int32_t *leaves,
-                                                int32_t nl, const BHNode *B, PotRec *PO,
-                                                double mp, double force_res, int *err) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nl) return;
-    int a = leaves[t];
-    const KNode<3> &n = nodes[a];
-    const BHNode bn = B[a];
+__global__ void __launch_bounds__(32 * RSG_BH_WPB) k_bh_walk(const KNode<3> *nodes,
+                                                             const int32_t *leaves, int32_t nl,
+                                                             const BHNode *B, PotRec *PO,
+                                                             double mp, double force_res,
+                                                             int *err) {
+    __shared__ int stk[2 * RSG_BH_WPB][RSG_STACK];
     constexpr bool F32 = MODE != 0;
+    const int w = threadIdx.x >> 4, lane = threadIdx.x & 15;
+    const unsigned hm = (threadIdx.x & 16) ? 0xffff0000u : 0x0000ffffu;  // this half-warp
+    const int t = blockIdx.x * 2 * RSG_BH_WPB + w;
+    if (t >= nl) return;  // whole half-warps
+    const int a = leaves[t];
+    const KNode<3> n = nodes[a];
+    const BHNode bn = B[a];
     const float mpf = (float)mp, fr2f = (float)(force_res * force_res);
-    for (int p0 = 0; p0 < n.n; p0 += RSG_BH_G) {
-        int np_ = min(RSG_BH_G, n.n - p0);
-        float px[RSG_BH_G][3];
-        double acc[RSG_BH_G];
-        float s[RSG_BH_G], c[RSG_BH_G];
-#pragma unroll
-        for (int p = 0; p < RSG_BH_G; p++) {
-            acc[p] = 0;
-            s[p] = c[p] = 0.f;
-            if (p < np_) {
-                const PotRec &r = PO[n.start + p0 + p];
-                px[p][0] = r.pos[0];
-                px[p][1] = r.pos[1];
-                px[p][2] = r.pos[2];
-                acc[p] = r.pe;
-            } else {
-                px[p][0] = px[p][1] = px[p][2] = 0.f;
-            }
+    int *st = stk[w];
+    for (int p0 = 0; p0 < n.n; p0 += 16) {
+        const int p = p0 + lane;
+        const bool act = p < n.n;
+        float px[3] = {0.f, 0.f, 0.f};
+        double acc = 0;
+        float s = 0.f, c = 0.f;
+        if (act) {
+            const PotRec &r = PO[n.start + p];
+            px[0] = r.pos[0];
+            px[1] = r.pos[1];
+            px[2] = r.pos[2];
+            acc = r.pe;
         }
-        // adds one term to particle p's sum
-#define RSG_BH_ADD(p, term64, term32)                  \
-    do {                                                \
-        if (MODE == 1) {                                \
-            float y_ = (term32) - c[p];                 \
-            float t_ = s[p] + y_;                       \
-            c[p] = (t_ - s[p]) - y_;                    \
-            s[p] = t_;                                  \
-        } else if (MODE == 2) {                         \
-            s[p] += (term32);                           \
-        } else {                                        \
-            acc[p] += (term64);                         \
-        }                                               \
-    } while (0)
+        // adds one term to this lane's sum
+        auto add = [&](double term64, float term32) {
+            if (MODE == 1) {
+                float y = term32 - c;
+                float tt = s + y;
+                c = (tt - s) - y;
+                s = tt;
+            } else if (MODE == 2) {
+                s += term32;
+            } else {
+                acc += term64;
+            }
+        };
         // direct pair with point q (softened)
-#define RSG_BH_PAIR(p, q)                                                              \
-    do {                                                                               \
-        if (F32) {                                                                     \
-            float dx = px[p][0] - q[0], dy = px[p][1] - q[1], dz = px[p][2] - q[2];    \
-            float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));                  \
-            RSG_BH_ADD(p, 0.0, mpf * rsqrtf(fmaxf(r2, fr2f)));                         \
-        } else {                                                                       \
-            double r = sqrt(d2d(px[p], q));                                            \
-            if (r < force_res) r = force_res;                                          \
-            RSG_BH_ADD(p, mp * (1.0 / r), 0.f);                                        \
-        }                                                                              \
-    } while (0)
-        int stack[RSG_STACK];
-        int sp = 0;
-        stack[sp++] = n.tree;
+        auto pair = [&](const float *q) {
+            if (F32) {
+                float dx = px[0] - q[0], dy = px[1] - q[1], dz = px[2] - q[2];
+                float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+                add(0.0, mpf * rsqrtf(fmaxf(r2, fr2f)));
+            } else {
+                double r = sqrt(d2d(px, q));
+                if (r < force_res) r = force_res;
+                add(mp * (1.0 / r), 0.f);
+            }
+        };
+        __syncwarp(hm);
+        if (lane == 0) st[0] = n.tree;
+        int sp = 1;
+        __syncwarp(hm);
         while (sp) {
-            int b = stack[--sp];
+            const int b = st[--sp];
+            __syncwarp(hm);  // every lane has read before lane 0 pushes over the slot
             const KNode<3> &n2 = nodes[b];
             if (b == a) {
                 if (n.n > 20) continue;  // degenerate leaf
                 for (int qi = 0; qi < n.n; qi++) {
                     const float *qp = PO[n.start + qi].pos;
                     float q[3] = {qp[0], qp[1], qp[2]};
-#pragma unroll
-                    for (int p = 0; p < RSG_BH_G; p++)
-                        if (p < np_ && p0 + p != qi) RSG_BH_PAIR(p, q);
+                    if (act && p != qi) pair(q);
                 }
                 continue;
             }
@@ -496,41 +497,33 @@ __global__ void __launch_bounds__(64) k_bh_walk(const KNode<3> *nodes, const int
                     for (int qi = 0; qi < n2.n; qi++) {
                         const float *qp = PO[n2.start + qi].pos;
                         float q[3] = {qp[0], qp[1], qp[2]};
-#pragma unroll
-                        for (int p = 0; p < RSG_BH_G; p++)
-                            if (p < np_) RSG_BH_PAIR(p, q);
+                        if (act) pair(q);
                     }
                 } else {
                     if (sp + 2 > RSG_STACK) {
-                        atomicExch(err, 1);
+                        if (lane == 0) atomicExch(err, 1);
                         return;
                     }
-                    stack[sp++] = n2.left + 1;
-                    stack[sp++] = n2.left;
-                }
-            } else {
-                const BHNode &m = B[b];
-#pragma unroll
-                for (int p = 0; p < RSG_BH_G; p++) {
-                    if (p >= np_) continue;
-                    if (F32) {
-                        float dx = px[p][0] - m.mc[0], dy = px[p][1] - m.mc[1],
-                              dz = px[p][2] - m.mc[2];
-                        float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
-                        RSG_BH_ADD(p, 0.0, m.m * rsqrtf(r2));
-                    } else {
-                        float r = (float)sqrt(d2d(px[p], m.mc));
-                        RSG_BH_ADD(p, (double)__fdiv_rn(m.m, r), 0.f);
+                    if (lane == 0) {
+                        st[sp] = n2.left + 1;
+                        st[sp + 1] = n2.left;
                     }
+                    sp += 2;
+                    __syncwarp(hm);
+                }
+            } else if (act) {
+                const BHNode &m = B[b];
+                if (F32) {
+                    float dx = px[0] - m.mc[0], dy = px[1] - m.mc[1], dz = px[2] - m.mc[2];
+                    float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, dx * dx));
+                    add(0.0, m.m * rsqrtf(r2));
+                } else {
+                    float r = (float)sqrt(d2d(px, m.mc));
+                    add((double)__fdiv_rn(m.m, r), 0.f);
                 }
             }
         }
-#undef RSG_BH_PAIR
-#undef RSG_BH_ADD
-#pragma unroll
-        for (int p = 0; p < RSG_BH_G; p++)
-            if (p < np_)
-                PO[n.start + p0 + p].pe = F32 ? acc[p] + ((double)s[p] - (double)c[p]) : acc[p];
+        if (act) PO[n.start + p].pe = F32 ? acc + ((double)s - (double)c) : acc;
     }
 }
 
@@ -1816,14 +1809,15 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
     int32_t *lf = ar.get<int32_t>(F.nnodes), *leaves = ar.get<int32_t>(F.nnodes);
     launch(k_leaf_list_flags, nblk(F.nnodes, T), T, 0, st, F.nodes, F.nnodes, lf);
     int32_t nl = select_idx(ar, lf, leaves, F.nnodes, st);
+    const int wb = nblk((int64_t)nl * 16, 32 * RSG_BH_WPB);
     if (form == 0)
-        launch(k_bh_walk<0>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
+        launch(k_bh_walk<0>, wb, 32 * RSG_BH_WPB, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
                err);
     else if (form == 1)
-        launch(k_bh_walk<1>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
+        launch(k_bh_walk<1>, wb, 32 * RSG_BH_WPB, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
                err);
     else
-        launch(k_bh_walk<2>, nblk(nl, 64), 64, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
+        launch(k_bh_walk<2>, wb, 32 * RSG_BH_WPB, 0, st, F.nodes, leaves, nl, B, PO, mp, force_res,
                err);
     RSG_CHECK_LAUNCH();
     phase_mark(st, "p.bh_walk");
