@@ -244,7 +244,10 @@ int64_t rsg_launch_count(void);
 int rsg_profile_select(const char *kernel_substring);
 int rsg_profile_read(int64_t *launches, double *total_ms);
 /* Per-kernel table of the timed launches ("*" selects every kernel):
- * lines "name<TAB>launches<TAB>total_ms", largest total first, written to
+ * lines "name<TAB>launches<TAB>total_ms<TAB>gap_ms", largest total first
+ * (gap_ms: device time between the end of the previous timed launch and the
+ * start of this kernel's launches -- untimed work and host round trips --
+ * when every kernel is timed), written to
  * buf (capacity cap, NUL-terminated); returns the table's length, then
  * clears the timed launches. */
 int64_t rsg_profile_table(char *buf, int64_t cap);

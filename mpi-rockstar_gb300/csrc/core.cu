@@ -59,9 +59,22 @@ Arena::~Arena() {
     if (base) cudaFree(base);
 }
 
-__global__ void k_slot_set(const int32_t *act, int32_t nact, int32_t *slot) {
+__global__ void k_slot_set(const int32_t *act, const LevelState *ls, int32_t *slot) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nact) slot[act[k]] = k;
+    if (k < ls->nact) slot[act[k]] = k;
+}
+__global__ void k_iota_i32(int32_t *a, int32_t n) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) a[k] = k;
+}
+// After k_children: the level's new nodes become [base, base + nnew).
+__global__ void k_level_advance(LevelState *ls, const int32_t *split_off, int32_t *lvl_end,
+                                int32_t level) {
+    if (threadIdx.x || blockIdx.x) return;
+    ls->base = ls->nnodes;
+    ls->nnew = ls->err ? 0 : 2 * split_off[ls->nact];
+    ls->nnodes += ls->nnew;
+    lvl_end[level] = ls->nnodes;
 }
 
 __global__ void k_root_owner(const int32_t *rstart, const int32_t *rn, int32_t ntrees, int leaf,
@@ -170,23 +183,33 @@ int rsg_profile_read(int64_t *launches, double *total_ms) {
 }
 
 int64_t rsg_profile_table(char *buf, int64_t cap) {
-    std::unordered_map<std::string, std::pair<int64_t, double>> agg;
+    struct Agg {
+        int64_t n = 0;
+        double ms = 0, gap = 0;
+    };
+    std::unordered_map<std::string, Agg> agg;
+    const rsg::ProfRec *prev = nullptr;
     for (auto &e : rsg::g_prof_ev) {
-        float ms = 0;
+        float ms = 0, gap = 0;
         if (cudaEventSynchronize(e.b) != cudaSuccess) return RSG_ERR_CUDA;
         cudaEventElapsedTime(&ms, e.a, e.b);
+        // time since the previous timed launch ended: work that is not timed
+        // (library scans and sorts, copies) and the host's round trips
+        if (prev) cudaEventElapsedTime(&gap, prev->b, e.a);
+        prev = &e;
         const char *nm = nullptr;
         std::string name = (cudaFuncGetName(&nm, e.func) == cudaSuccess && nm) ? nm : "?";
         auto &r = agg[name];
-        r.first++;
-        r.second += ms;
+        r.n++;
+        r.ms += ms;
+        r.gap += gap > 0 ? gap : 0;
     }
     std::vector<std::pair<double, std::string>> rows;
     for (auto &kv : agg) {
         char line[1024];
-        snprintf(line, sizeof(line), "%s\t%lld\t%.6f\n", kv.first.c_str(),
-                 (long long)kv.second.first, kv.second.second);
-        rows.push_back({kv.second.second, line});
+        snprintf(line, sizeof(line), "%s\t%lld\t%.6f\t%.6f\n", kv.first.c_str(),
+                 (long long)kv.second.n, kv.second.ms, kv.second.gap);
+        rows.push_back({kv.second.ms, line});
     }
     std::sort(rows.begin(), rows.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
     std::string out;

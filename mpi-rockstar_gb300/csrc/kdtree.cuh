@@ -63,6 +63,18 @@ struct PosOf<MetricRec, D> {
 
 #define RSG_FOREST_LEVELS 4096  // deepest build accepted (checked by build_forest)
 
+// Device-side state of a forest build: the level's active count and the
+// node bookkeeping, so that levels run back to back without a host round
+// trip; the host reads it every few levels.
+struct LevelState {
+    int32_t nact;    // active nodes of the level being split
+    int32_t nnodes;  // nodes created so far
+    int32_t base;    // first node created by the last level
+    int32_t nnew;    // nodes created by the last level
+    int32_t err;     // node capacity exceeded
+    int32_t pad[3];
+};
+
 template <int D>
 struct Forest {
     KNode<D> *nodes = nullptr;  // nodes[t] is the root of tree t
@@ -125,9 +137,9 @@ __global__ void k_box_final(KNode<D> *nodes, const int32_t *list, int32_t nlist,
 
 // Choose the split dimension and limit (src/fast3tree.c:736-757).
 template <int D>
-__global__ void k_prep(KNode<D> *nodes, const int32_t *act, int32_t nact, float *lim) {
+__global__ void k_prep(KNode<D> *nodes, const int32_t *act, const LevelState *ls, float *lim) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nact) return;
+    if (k >= ls->nact) return;
     KNode<D> &nd = nodes[act[k]];
     int dim = D - 1;
     float dmax = fsub(nd.mx[D - 1], nd.mn[D - 1]);
@@ -163,10 +175,10 @@ __global__ void k_flags(const RecT *recs, int64_t nrec, const int32_t *owner,
 
 // m (= #small) and q (= #big before m) per active node.
 template <int D>
-__global__ void k_counts(const KNode<D> *nodes, const int32_t *act, int32_t nact,
+__global__ void k_counts(const KNode<D> *nodes, const int32_t *act, const LevelState *ls,
                          const int32_t *rank, int32_t *m_out, int32_t *q_out) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nact) return;
+    if (k >= ls->nact) return;
     const KNode<D> &nd = nodes[act[k]];
     int s = nd.start, n = nd.n;
     int B = rank[s + n] - rank[s];
@@ -236,12 +248,19 @@ __global__ void k_copy_owned(const RecT *src, RecT *dst, int64_t nrec, const int
 }
 
 // Split bookkeeping (src/fast3tree.c:798-846): create children for nodes
-// with 0 < m < n, turn the rest into leaves.
+// with 0 < m < n, turn the rest into leaves.  The children of the level go
+// to nodes[ls->nnodes ..]; a level that would pass `cap` nodes sets ls->err
+// and changes nothing.
 template <int D>
-__global__ void k_children(KNode<D> *nodes, const int32_t *act, int32_t nact,
-                           const int32_t *m_arr, const int32_t *split_off, int32_t base,
+__global__ void k_children(KNode<D> *nodes, const int32_t *act, LevelState *ls,
+                           const int32_t *m_arr, const int32_t *split_off, int32_t cap,
                            unsigned *bmin, unsigned *bmax) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nact = ls->nact, base = ls->nnodes;
+    if ((int64_t)base + 2 * (int64_t)split_off[nact] > cap) {
+        if (k == 0) ls->err = 1;
+        return;
+    }
     if (k >= nact) return;
     int a = act[k];
     KNode<D> &nd = nodes[a];
@@ -291,12 +310,14 @@ __global__ void k_owner_update(const KNode<D> *nodes, int64_t nrec, int32_t *own
     owner[i] = (nodes[c].n > leaf) ? c : -1;
 }
 
+// sflag[0 .. ub]: 1 for the active nodes that split, 0 beyond the level's
+// active count (ub bounds it from above).
 template <int D>
 __global__ void k_split_flags(const int32_t *m_arr, const KNode<D> *nodes, const int32_t *act,
-                              int32_t nact, int32_t *sflag) {
+                              const LevelState *ls, int32_t ub, int32_t *sflag) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k > nact) return;
-    if (k == nact) {
+    if (k > ub) return;
+    if (k >= ls->nact) {
         sflag[k] = 0;
         return;
     }
@@ -304,15 +325,21 @@ __global__ void k_split_flags(const int32_t *m_arr, const KNode<D> *nodes, const
     sflag[k] = (m > 0 && m < nodes[act[k]].n) ? 1 : 0;
 }
 
+// Flags and ids of the last level's new nodes that split further, over
+// 0 .. ub (0 beyond the new nodes).
 template <int D>
-__global__ void k_next_active(const KNode<D> *nodes, int32_t base, int32_t nnew, int leaf,
-                              int32_t *flag) {
+__global__ void k_next_active(const KNode<D> *nodes, const LevelState *ls, int32_t ub, int leaf,
+                              int32_t *flag, int32_t *ids) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nnew) return;
-    flag[k] = nodes[base + k].n > leaf ? 1 : 0;
+    if (k >= ub) return;
+    const int base = ls->base;
+    flag[k] = (k < ls->nnew && nodes[base + k].n > leaf) ? 1 : 0;
+    ids[k] = base + k;
 }
 
-__global__ void k_slot_set(const int32_t *act, int32_t nact, int32_t *slot);
+__global__ void k_slot_set(const int32_t *act, const LevelState *ls, int32_t *slot);
+__global__ void k_level_advance(LevelState *ls, const int32_t *split_off, int32_t *lvl_end,
+                                int32_t level);
 
 // Builds a kd-forest over recs[0..nrec) whose trees are the segments
 // (rstart[t], rn[t]) (device arrays).  Elements outside every segment are

@@ -97,6 +97,21 @@ __global__ void k_box_final_range(KNode<D> *nodes, int32_t first, int32_t count,
     }
 }
 
+// The same for the last level's new nodes [ls->base, + ls->nnew), grid over ub.
+template <int D>
+__global__ void k_box_final_lvl(KNode<D> *nodes, const LevelState *ls, int32_t ub,
+                                const unsigned *bmin, const unsigned *bmax) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ub || k >= ls->nnew) return;
+    int a = ls->base + k;
+    for (int d = 0; d < D; d++) {
+        nodes[a].mn[d] = ord2f(bmin[(int64_t)a * D + d]);
+        nodes[a].mx[d] = ord2f(bmax[(int64_t)a * D + d]);
+    }
+}
+__global__ void k_iota_i32(int32_t *a, int32_t n);
+#define RSG_FOREST_BATCH 4  // levels between reads of the build state
+
 __global__ void k_root_owner(const int32_t *rstart, const int32_t *rn, int32_t ntrees,
                              int leaf, int32_t *owner, int32_t *box_owner);
 
@@ -128,14 +143,14 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
     float *lim = ar.get<float>(cap);
     int32_t *m_arr = ar.get<int32_t>(cap), *q_arr = ar.get<int32_t>(cap);
     int32_t *sflag = ar.get<int32_t>(cap + 1), *soff = ar.get<int32_t>(cap + 1);
-    int32_t *nflag = ar.get<int32_t>(cap);
-    int32_t *cnt = ar.get<int32_t>(2);
+    int32_t *nflag = ar.get<int32_t>(cap), *ids = ar.get<int32_t>(cap);
+    LevelState *ls = ar.get<LevelState>(1);
+    int32_t *lvl_end = ar.get<int32_t>(RSG_FOREST_LEVELS + 2);
     size_t cub_bytes = 0, b2 = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, cub_bytes, flag, rank, (int)(nrec + 1), st);
     cub::DeviceScan::ExclusiveSum(nullptr, b2, sflag, soff, (int)(cap + 1), st);
     cub_bytes = cub_bytes > b2 ? cub_bytes : b2;
-    cub::DeviceSelect::Flagged(nullptr, b2, thrust::counting_iterator<int32_t>(0), nflag, act,
-                               cnt, (int)cap, st);
+    cub::DeviceSelect::Flagged(nullptr, b2, ids, nflag, act, &ls->nact, (int)cap, st);
     cub_bytes = cub_bytes > b2 ? cub_bytes : b2;
     void *cub_tmp = ar.take(cub_bytes + 256);
 
@@ -149,63 +164,82 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
                                                                          bmin, bmax);
     launch(k_box_final_range<D>, nblk(ntrees, T), T, 0, st, nodes, 0, ntrees, bmin, bmax);
     launch(k_root_active<D>, nblk(ntrees, T), T, 0, st, nodes, ntrees, leaf, nflag);
-    cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, thrust::counting_iterator<int32_t>(0), nflag,
-                               act, cnt, ntrees, st);
+    launch(k_iota_i32, nblk(ntrees, T), T, 0, st, ids, ntrees);
+    {
+        LevelState h0 = {};
+        h0.nnodes = ntrees;
+        RSG_CUDA(cudaMemcpyAsync(ls, &h0, sizeof(h0), cudaMemcpyHostToDevice, st));
+    }
+    cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, ids, nflag, act, &ls->nact, ntrees, st);
     RSG_CHECK_LAUNCH();
-    int32_t nact = 0;
-    RSG_CUDA(cudaMemcpyAsync(&nact, cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    LevelState hs;
+    RSG_CUDA(cudaMemcpyAsync(&hs, ls, sizeof(hs), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
-    int32_t nnodes = ntrees;
     F.level_end(0);
     F.level_end(ntrees);
+    // Levels run back to back with their counts on the device; the host reads
+    // the state every RSG_FOREST_BATCH levels.  Grids are sized by an upper
+    // bound of the active count (ub): at most twice the previous level's,
+    // and at most one active node per leaf + 1 records plus the roots.
+    const int64_t amax = n_in_trees / (leaf + 1) + ntrees;
+    int64_t ub = hs.nact;
     int level = 0;
-    while (nact > 0) {
-        if (++level > RSG_FOREST_LEVELS) {
-            set_error(RSG_ERR_LIMIT, "kd-forest build exceeded %d levels", RSG_FOREST_LEVELS);
-            throw Failure();
+    while (hs.nact > 0) {
+        for (int b = 0; b < RSG_FOREST_BATCH && ub > 0; b++) {
+            if (++level > RSG_FOREST_LEVELS) {
+                set_error(RSG_ERR_LIMIT, "kd-forest build exceeded %d levels", RSG_FOREST_LEVELS);
+                throw Failure();
+            }
+            const int32_t u = (int32_t)ub;
+            launch(k_slot_set, nblk(u, T), T, 0, st, (const int32_t *)act, (const LevelState *)ls,
+                   slot);
+            launch(k_prep<D>, nblk(u, T), T, 0, st, nodes, (const int32_t *)act,
+                   (const LevelState *)ls, lim);
+            launch(k_flags<D, RecT>, nblk(nrec + 1, T), T, 0, st, recs, nrec, owner, slot, nodes,
+                   lim, flag);
+            cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, flag, rank, (int)(nrec + 1), st);
+            launch(k_counts<D>, nblk(u, T), T, 0, st, nodes, (const int32_t *)act,
+                   (const LevelState *)ls, rank, m_arr, q_arr);
+            launch(k_tables<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, slot, flag, rank,
+                   m_arr, fb, bs);
+            launch(k_scatter<D, RecT>, nblk(nrec, T), T, 0, st, nodes, recs, tmp, nrec, owner, slot,
+                   flag, rank, m_arr, q_arr, fb, bs);
+            launch(k_copy_owned<RecT>, nblk(nrec, T), T, 0, st, tmp, recs, nrec, owner);
+            launch(k_split_flags<D>, nblk(u + 1, T), T, 0, st, m_arr, nodes, (const int32_t *)act,
+                   (const LevelState *)ls, u, sflag);
+            cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, sflag, soff, u + 1, st);
+            RSG_CHECK_LAUNCH();
+            launch(k_children<D>, nblk(u, T), T, 0, st, nodes, (const int32_t *)act, ls, m_arr,
+                   (const int32_t *)soff, (int32_t)cap, bmin, bmax);
+            launch(k_level_advance, 1, 32, 0, st, ls, (const int32_t *)soff, lvl_end, level - 1);
+            launch(k_owner_update<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, box_owner, leaf);
+            launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st, recs, nrec,
+                   box_owner, bmin, bmax);
+            const int64_t u2 = std::min<int64_t>(2 * ub, cap);
+            launch(k_box_final_lvl<D>, nblk(u2, T), T, 0, st, nodes, (const LevelState *)ls,
+                   (int32_t)u2, bmin, bmax);
+            launch(k_next_active<D>, nblk(u2, T), T, 0, st, nodes, (const LevelState *)ls,
+                   (int32_t)u2, leaf, nflag, ids);
+            cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, ids, nflag, act, &ls->nact, (int)u2, st);
+            RSG_CHECK_LAUNCH();
+            ub = std::min<int64_t>(u2, amax);
         }
-        launch(k_slot_set, nblk(nact, T), T, 0, st, act, nact, slot);
-        launch(k_prep<D>, nblk(nact, T), T, 0, st, nodes, act, nact, lim);
-        launch(k_flags<D, RecT>, nblk(nrec + 1, T), T, 0, st, recs, nrec, owner, slot, nodes, lim,
-                                                          flag);
-        cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, flag, rank, (int)(nrec + 1), st);
-        launch(k_counts<D>, nblk(nact, T), T, 0, st, nodes, act, nact, rank, m_arr, q_arr);
-        launch(k_tables<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, slot, flag, rank, m_arr,
-                                                 fb, bs);
-        launch(k_scatter<D, RecT>, nblk(nrec, T), T, 0, st, nodes, recs, tmp, nrec, owner, slot,
-                                                        flag, rank, m_arr, q_arr, fb, bs);
-        launch(k_copy_owned<RecT>, nblk(nrec, T), T, 0, st, tmp, recs, nrec, owner);
-        launch(k_split_flags<D>, nblk(nact + 1, T), T, 0, st, m_arr, nodes, act, nact, sflag);
-        cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, sflag, soff, nact + 1, st);
-        RSG_CHECK_LAUNCH();
-        int32_t nsplit = 0;
-        RSG_CUDA(cudaMemcpyAsync(&nsplit, soff + nact, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaMemcpyAsync(&hs, ls, sizeof(hs), cudaMemcpyDeviceToHost, st));
         RSG_CUDA(cudaStreamSynchronize(st));
-        if (nnodes + 2 * (int64_t)nsplit > cap) {
+        if (hs.err) {
             set_error(RSG_ERR_LIMIT, "kd-forest node capacity %lld exceeded", (long long)cap);
             throw Failure();
         }
-        int32_t base = nnodes;
-        launch(k_children<D>, nblk(nact, T), T, 0, st, nodes, act, nact, m_arr, soff, base, bmin, bmax);
-        nnodes += 2 * nsplit;
-        F.level_end(nnodes);
-        launch(k_owner_update<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, box_owner, leaf);
-        if (nsplit > 0) {
-            launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st, 
-                recs, nrec, box_owner, bmin, bmax);
-            launch(k_box_final_range<D>, nblk(2 * nsplit, T), T, 0, st, nodes, base, 2 * nsplit, bmin,
-                                                                    bmax);
-            launch(k_next_active<D>, nblk(2 * nsplit, T), T, 0, st, nodes, base, 2 * nsplit, leaf,
-                                                                nflag);
-            cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, thrust::counting_iterator<int32_t>(base),
-                                       nflag, act, cnt, 2 * nsplit, st);
-            RSG_CHECK_LAUNCH();
-            RSG_CUDA(cudaMemcpyAsync(&nact, cnt, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-            RSG_CUDA(cudaStreamSynchronize(st));
-        } else {
-            nact = 0;
-        }
+        ub = hs.nact;
     }
+    if (level > 0) {
+        std::vector<int32_t> le(level);
+        RSG_CUDA(cudaMemcpyAsync(le.data(), lvl_end, sizeof(int32_t) * level,
+                                 cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        for (int l = 0; l < level; l++) F.level_end(le[l]);
+    }
+    const int32_t nnodes = hs.nnodes;
     F.nodes = nodes;
     F.nnodes = nnodes;
     ar.used = mark;
