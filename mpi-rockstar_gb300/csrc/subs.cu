@@ -1468,14 +1468,19 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
 // keep their places.  (The plain form reproduces the reference's recursive
 // midpoint partition instead, whose record order the reference's later
 // sampling depends on.)
-__global__ void k_lsort_keys(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
-                             const int32_t *lab, uint64_t *key, uint32_t *val) {
+// Keys of label_sort_stable: the label inside each node of the level; val
+// and val_out start as the identity, so elements outside the level's nodes
+// (which the segmented sort leaves alone) keep their place.
+__global__ void k_lsort_keys(const int32_t *eln, int64_t M, const int32_t *lab, uint32_t *key,
+                             uint32_t *val, uint32_t *val_out) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= M) return;
-    int k = eln[i];
-    uint64_t hi = (k >= 0) ? (uint64_t)N.start[base + k] : (uint64_t)i;
-    key[i] = (hi << 32) | (uint64_t)(uint32_t)(k >= 0 ? lab[i] + 1 : 0);
-    val[i] = (uint32_t)i;
+    key[i] = eln[i] >= 0 ? (uint32_t)(lab[i] + 1) : 0u;
+    val[i] = val_out[i] = (uint32_t)i;
+}
+__global__ void k_node_ends(HierNodes N, int32_t base, int32_t cnt, int32_t *end) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < cnt) end[k] = N.start[base + k] + N.n[base + k];
 }
 
 // Regroup keys for reassign_halo_particles (src/groupies.c:316-331) and the
@@ -2142,21 +2147,26 @@ static void basic_props(Arena &ar, const Rec *W, rsg_halo *H, const int32_t *lis
     ar.used = mark;
 }
 
+// Batched regroup: every node's elements in label order, stable (the order
+// the reference's sequential partition gives up to ties), as a segmented
+// sort over the level's nodes.
 static void label_sort_stable(Arena &ar, Rec *W, int32_t *lab, const int32_t *eln, HierNodes N,
-                              int32_t base, int64_t M, cudaStream_t st) {
+                              int32_t base, int32_t cnt, int64_t M, cudaStream_t st) {
     const int T = 256;
     size_t mark = ar.used;
-    uint64_t *k1 = ar.get<uint64_t>(M), *k2 = ar.get<uint64_t>(M);
+    uint32_t *k1 = ar.get<uint32_t>(M), *k2 = ar.get<uint32_t>(M);
     uint32_t *v1 = ar.get<uint32_t>(M), *v2 = ar.get<uint32_t>(M);
+    int32_t *se = ar.get<int32_t>(cnt);
     Rec *wt = ar.get<Rec>(M);
     int32_t *lt = ar.get<int32_t>(M);
-    launch(k_lsort_keys, nblk(M, T), T, 0, st, eln, M, N, base, (const int32_t *)lab, k1, v1);
-    int bits = 33;
-    while (bits < 64 && (1ll << (bits - 32)) <= M) bits++;
+    launch(k_lsort_keys, nblk(M, T), T, 0, st, eln, M, (const int32_t *)lab, k1, v1, v2);
+    launch(k_node_ends, nblk(cnt, T), T, 0, st, N, base, cnt, se);
     size_t b = 0;
-    RSG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, b, k1, k2, v1, v2, (int)M, 0, bits, st));
+    RSG_CUDA(cub::DeviceSegmentedSort::StableSortPairs(nullptr, b, k1, k2, v1, v2, (int)M, cnt,
+                                                       N.start + base, se, st));
     void *t = ar.take(b + 256);
-    RSG_CUDA(cub::DeviceRadixSort::SortPairs(t, b, k1, k2, v1, v2, (int)M, 0, bits, st));
+    RSG_CUDA(cub::DeviceSegmentedSort::StableSortPairs(t, b, k1, k2, v1, v2, (int)M, cnt,
+                                                       N.start + base, se, st));
     launch(k_gather<Rec>, nblk(M, T), T, 0, st, (const Rec *)W, (const uint32_t *)v2, M, wt);
     launch(k_gather<int32_t>, nblk(M, T), T, 0, st, (const int32_t *)lab, (const uint32_t *)v2, M,
            lt);
@@ -2446,7 +2456,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
         RSG_CHECK_LAUNCH();
         phase_mark(st, "d.replay");
         if (exact) partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
-        else label_sort_stable(ar, W, phalo, eln, N, base, M, st);
+        else label_sort_stable(ar, W, phalo, eln, N, base, cnt, M, st);
         phase_mark(st, "d.psort");
         launch(k_run_heads, nblk(M, T), T, 0, st, eln, M, N, base, phalo, hflag);
         int32_t *heads = ar.get<int32_t>(M);
@@ -2538,7 +2548,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             RSG_CUDA(cudaStreamSynchronize(st));
             partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
         } else {
-            label_sort_stable(ar, W, phalo, eln, N, base, M, st);
+            label_sort_stable(ar, W, phalo, eln, N, base, cnt, M, st);
         }
         phase_mark(st, "a.reassign");
         launch(k_halo_heads, nblk(M, T), T, 0, st, eln, M, N, base, phalo, H);
