@@ -67,13 +67,16 @@ __global__ void k_iota_i32(int32_t *a, int32_t n) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) a[k] = k;
 }
-// After k_children: the level's new nodes become [base, base + nnew).
-__global__ void k_level_advance(LevelState *ls, const int32_t *split_off, int32_t *lvl_end,
+// After k_children: the level's new nodes become [base, base + nnew), and
+// those that split again are the next level's active nodes.
+__global__ void k_level_advance(LevelState *ls, const int64_t *off, int32_t *lvl_end,
                                 int32_t level) {
     if (threadIdx.x || blockIdx.x) return;
+    const int64_t t = off[ls->nact];
     ls->base = ls->nnodes;
-    ls->nnew = ls->err ? 0 : 2 * split_off[ls->nact];
+    ls->nnew = ls->err ? 0 : 2 * (int32_t)(t >> 32);
     ls->nnodes += ls->nnew;
+    ls->nact = ls->err ? 0 : (int32_t)(t & 0xffffffffu);
     lvl_end[level] = ls->nnodes;
 }
 

@@ -248,16 +248,19 @@ __global__ void k_copy_owned(const RecT *src, RecT *dst, int64_t nrec, const int
 }
 
 // Split bookkeeping (src/fast3tree.c:798-846): create children for nodes
-// with 0 < m < n, turn the rest into leaves.  The children of the level go
-// to nodes[ls->nnodes ..]; a level that would pass `cap` nodes sets ls->err
-// and changes nothing.
+// with 0 < m < n, turn the rest into leaves.  off[k] packs, over the active
+// nodes before k, the splits (high 32 bits) and the children that split
+// again (low 32 bits): node k's children go to nodes[ls->nnodes + 2 * splits]
+// and those holding more than `leaf` records to next[children], which is the
+// order a selection over the new nodes gives.  A level that would pass `cap`
+// nodes sets ls->err and changes nothing.
 template <int D>
 __global__ void k_children(KNode<D> *nodes, const int32_t *act, LevelState *ls,
-                           const int32_t *m_arr, const int32_t *split_off, int32_t cap,
-                           unsigned *bmin, unsigned *bmax) {
+                           const int32_t *m_arr, const int64_t *off, int32_t cap, int leaf,
+                           int32_t *next, unsigned *bmin, unsigned *bmax) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     const int nact = ls->nact, base = ls->nnodes;
-    if ((int64_t)base + 2 * (int64_t)split_off[nact] > cap) {
+    if ((int64_t)base + 2 * (off[nact] >> 32) > cap) {
         if (k == 0) ls->err = 1;
         return;
     }
@@ -270,8 +273,11 @@ __global__ void k_children(KNode<D> *nodes, const int32_t *act, LevelState *ls,
         nd.left = -1;
         return;
     }
-    int l = base + 2 * split_off[k];
+    int l = base + 2 * (int)(off[k] >> 32);
+    int na = (int)(off[k] & 0xffffffffu);
     nd.left = l;
+    if (m > leaf) next[na++] = l;
+    if (nd.n - m > leaf) next[na] = l + 1;
     for (int c = 0; c < 2; c++) {
         KNode<D> &ch = nodes[l + c];
         ch.start = nd.start + (c ? m : 0);
@@ -310,35 +316,26 @@ __global__ void k_owner_update(const KNode<D> *nodes, int64_t nrec, int32_t *own
     owner[i] = (nodes[c].n > leaf) ? c : -1;
 }
 
-// sflag[0 .. ub]: 1 for the active nodes that split, 0 beyond the level's
-// active count (ub bounds it from above).
+// sflag[0 .. ub]: per active node, split (high 32 bits) and children that
+// split again (low 32 bits); 0 beyond the level's active count (ub bounds it
+// from above).
 template <int D>
 __global__ void k_split_flags(const int32_t *m_arr, const KNode<D> *nodes, const int32_t *act,
-                              const LevelState *ls, int32_t ub, int32_t *sflag) {
+                              const LevelState *ls, int32_t ub, int leaf, int64_t *sflag) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > ub) return;
     if (k >= ls->nact) {
         sflag[k] = 0;
         return;
     }
-    int m = m_arr[k];
-    sflag[k] = (m > 0 && m < nodes[act[k]].n) ? 1 : 0;
-}
-
-// Flags and ids of the last level's new nodes that split further, over
-// 0 .. ub (0 beyond the new nodes).
-template <int D>
-__global__ void k_next_active(const KNode<D> *nodes, const LevelState *ls, int32_t ub, int leaf,
-                              int32_t *flag, int32_t *ids) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= ub) return;
-    const int base = ls->base;
-    flag[k] = (k < ls->nnew && nodes[base + k].n > leaf) ? 1 : 0;
-    ids[k] = base + k;
+    int m = m_arr[k], n = nodes[act[k]].n;
+    int64_t v = 0;
+    if (m > 0 && m < n) v = ((int64_t)1 << 32) | (int64_t)((m > leaf) + (n - m > leaf));
+    sflag[k] = v;
 }
 
 __global__ void k_slot_set(const int32_t *act, const LevelState *ls, int32_t *slot);
-__global__ void k_level_advance(LevelState *ls, const int32_t *split_off, int32_t *lvl_end,
+__global__ void k_level_advance(LevelState *ls, const int64_t *off, int32_t *lvl_end,
                                 int32_t level);
 
 // Builds a kd-forest over recs[0..nrec) whose trees are the segments

@@ -139,10 +139,10 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
     RecT *tmp = ar.get<RecT>(nrec);
     int32_t *flag = ar.get<int32_t>(nrec + 1), *rank = ar.get<int32_t>(nrec + 1);
     int32_t *fb = ar.get<int32_t>(nrec), *bs = ar.get<int32_t>(nrec);
-    int32_t *act = ar.get<int32_t>(cap), *slot = ar.get<int32_t>(cap);
+    int32_t *act = ar.get<int32_t>(cap), *act2 = ar.get<int32_t>(cap), *slot = ar.get<int32_t>(cap);
     float *lim = ar.get<float>(cap);
     int32_t *m_arr = ar.get<int32_t>(cap), *q_arr = ar.get<int32_t>(cap);
-    int32_t *sflag = ar.get<int32_t>(cap + 1), *soff = ar.get<int32_t>(cap + 1);
+    int64_t *sflag = ar.get<int64_t>(cap + 1), *soff = ar.get<int64_t>(cap + 1);
     int32_t *nflag = ar.get<int32_t>(cap), *ids = ar.get<int32_t>(cap);
     LevelState *ls = ar.get<LevelState>(1);
     int32_t *lvl_end = ar.get<int32_t>(RSG_FOREST_LEVELS + 2);
@@ -206,21 +206,19 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
                    flag, rank, m_arr, q_arr, fb, bs);
             launch(k_copy_owned<RecT>, nblk(nrec, T), T, 0, st, tmp, recs, nrec, owner);
             launch(k_split_flags<D>, nblk(u + 1, T), T, 0, st, m_arr, nodes, (const int32_t *)act,
-                   (const LevelState *)ls, u, sflag);
+                   (const LevelState *)ls, u, leaf, sflag);
             cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, sflag, soff, u + 1, st);
             RSG_CHECK_LAUNCH();
             launch(k_children<D>, nblk(u, T), T, 0, st, nodes, (const int32_t *)act, ls, m_arr,
-                   (const int32_t *)soff, (int32_t)cap, bmin, bmax);
-            launch(k_level_advance, 1, 32, 0, st, ls, (const int32_t *)soff, lvl_end, level - 1);
+                   (const int64_t *)soff, (int32_t)cap, leaf, act2, bmin, bmax);
+            launch(k_level_advance, 1, 32, 0, st, ls, (const int64_t *)soff, lvl_end, level - 1);
+            std::swap(act, act2);  // the next level's active nodes
             launch(k_owner_update<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, box_owner, leaf);
             launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st, recs, nrec,
                    box_owner, bmin, bmax);
             const int64_t u2 = std::min<int64_t>(2 * ub, cap);
             launch(k_box_final_lvl<D>, nblk(u2, T), T, 0, st, nodes, (const LevelState *)ls,
                    (int32_t)u2, bmin, bmax);
-            launch(k_next_active<D>, nblk(u2, T), T, 0, st, nodes, (const LevelState *)ls,
-                   (int32_t)u2, leaf, nflag, ids);
-            cub::DeviceSelect::Flagged(cub_tmp, cub_bytes, ids, nflag, act, &ls->nact, (int)u2, st);
             RSG_CHECK_LAUNCH();
             ub = std::min<int64_t>(u2, amax);
         }
