@@ -75,6 +75,16 @@ __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b)
 // square roots (Figueroa, "When is double rounding innocuous?", 1995), so
 // the IEEE float square root is bit-identical and keeps the FP64 pipe free.
 __device__ __forceinline__ float sqrt_fd(float x) { return __fsqrt_rn(x); }
+// hi + lo += y with Knuth's two-sum: hi takes the rounded sum, lo gathers the
+// exact rounding errors (explicit round-to-nearest operations, so nothing is
+// contracted or reordered).
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float y) {
+    float s = __fadd_rn(hi, y);
+    float bp = __fsub_rn(s, hi);
+    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(y, bp));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }

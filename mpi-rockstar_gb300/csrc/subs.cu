@@ -154,8 +154,11 @@ __global__ void k_norm_warp(Rec *W, HierNodes N, int32_t base, int32_t count, in
         for (int o = 16; o; o >>= 1) mean[d] += __shfl_xor_sync(0xffffffffu, mean[d], o);
         mean[d] /= (double)n;
     }
-    double c[21];
-    for (int j = 0; j < 21; j++) c[j] = 0;
+    // The 21 second moments of the float products, each kept as an unevaluated
+    // float pair (hi + lo, Knuth's two-sum): about 48 bits, enough for at most
+    // RSG_SMALL terms, on the FP32 pipe (GB300's FP64 pipe is narrow).
+    float ch[21], cl[21];
+    for (int j = 0; j < 21; j++) ch[j] = cl[j] = 0.f;
     for (int i = lane; i < n; i += 32) {
         float q[6];
         for (int d = 0; d < 6; d++) {
@@ -164,11 +167,17 @@ __global__ void k_norm_warp(Rec *W, HierNodes N, int32_t base, int32_t count, in
         }
         int j = 0;
         for (int x = 0; x < 6; x++)
-            for (int y = x; y < 6; y++) c[j++] += (double)fmul(q[x], q[y]);
+            for (int y = x; y < 6; y++, j++) two_sum_acc(ch[j], cl[j], fmul(q[x], q[y]));
     }
+    double c[21];
     for (int j = 0; j < 21; j++) {
-        for (int o = 16; o; o >>= 1) c[j] += __shfl_xor_sync(0xffffffffu, c[j], o);
-        c[j] /= (double)n;
+        for (int o = 16; o; o >>= 1) {
+            float h2 = __shfl_xor_sync(0xffffffffu, ch[j], o);
+            float l2 = __shfl_xor_sync(0xffffffffu, cl[j], o);
+            two_sum_acc(ch[j], cl[j], h2);
+            cl[j] = fadd(cl[j], l2);
+        }
+        c[j] = ((double)ch[j] + (double)cl[j]) / (double)n;
     }
     if (lane == 0) norm_sigmas(c, level0, ims, sig + 2 * k);
 }
