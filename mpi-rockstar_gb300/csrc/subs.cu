@@ -1487,6 +1487,16 @@ __global__ void k_lsort_keys(const int32_t *eln, int64_t M, const int32_t *lab, 
     key[i] = eln[i] >= 0 ? (uint32_t)(lab[i] + 1) : 0u;
     val[i] = val_out[i] = (uint32_t)i;
 }
+// Keys of the whole-array form: (node start or own index, label + 1).
+__global__ void k_lsort_keys64(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
+                               const int32_t *lab, uint64_t *key, uint32_t *val) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    uint64_t hi = (k >= 0) ? (uint64_t)N.start[base + k] : (uint64_t)i;
+    key[i] = (hi << 32) | (uint64_t)(uint32_t)(k >= 0 ? lab[i] + 1 : 0);
+    val[i] = (uint32_t)i;
+}
 __global__ void k_node_ends(HierNodes N, int32_t base, int32_t cnt, int32_t *end) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < cnt) end[k] = N.start[base + k] + N.n[base + k];
@@ -2157,25 +2167,51 @@ static void basic_props(Arena &ar, const Rec *W, rsg_halo *H, const int32_t *lis
 }
 
 // Batched regroup: every node's elements in label order, stable (the order
-// the reference's sequential partition gives up to ties), as a segmented
-// sort over the level's nodes.
+// the reference's sequential partition gives up to ties).  Levels whose
+// nodes all hold at most RSG_SEGSORT_MAX elements use a segmented sort over
+// the nodes on the labels alone; a level with a larger node (where the
+// segmented sort's per-segment path is slow) sorts the whole array on
+// (node start, label) keys.
+#define RSG_SEGSORT_MAX (1 << 18)
 static void label_sort_stable(Arena &ar, Rec *W, int32_t *lab, const int32_t *eln, HierNodes N,
                               int32_t base, int32_t cnt, int64_t M, cudaStream_t st) {
     const int T = 256;
     size_t mark = ar.used;
-    uint32_t *k1 = ar.get<uint32_t>(M), *k2 = ar.get<uint32_t>(M);
-    uint32_t *v1 = ar.get<uint32_t>(M), *v2 = ar.get<uint32_t>(M);
-    int32_t *se = ar.get<int32_t>(cnt);
+    int nmax = 0;
+    {
+        int *d = ar.get<int>(1);
+        size_t mb = 0;
+        cub::DeviceReduce::Max(nullptr, mb, N.n + base, d, cnt, st);
+        void *mt = ar.take(mb + 256);
+        cub::DeviceReduce::Max(mt, mb, N.n + base, d, cnt, st);
+        RSG_CUDA(cudaMemcpyAsync(&nmax, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        ar.used = mark;
+    }
     Rec *wt = ar.get<Rec>(M);
     int32_t *lt = ar.get<int32_t>(M);
-    launch(k_lsort_keys, nblk(M, T), T, 0, st, eln, M, (const int32_t *)lab, k1, v1, v2);
-    launch(k_node_ends, nblk(cnt, T), T, 0, st, N, base, cnt, se);
-    size_t b = 0;
-    RSG_CUDA(cub::DeviceSegmentedSort::StableSortPairs(nullptr, b, k1, k2, v1, v2, (int)M, cnt,
-                                                       N.start + base, se, st));
-    void *t = ar.take(b + 256);
-    RSG_CUDA(cub::DeviceSegmentedSort::StableSortPairs(t, b, k1, k2, v1, v2, (int)M, cnt,
-                                                       N.start + base, se, st));
+    uint32_t *v1 = ar.get<uint32_t>(M), *v2 = ar.get<uint32_t>(M);
+    if (nmax <= RSG_SEGSORT_MAX) {
+        uint32_t *k1 = ar.get<uint32_t>(M), *k2 = ar.get<uint32_t>(M);
+        int32_t *se = ar.get<int32_t>(cnt);
+        launch(k_lsort_keys, nblk(M, T), T, 0, st, eln, M, (const int32_t *)lab, k1, v1, v2);
+        launch(k_node_ends, nblk(cnt, T), T, 0, st, N, base, cnt, se);
+        size_t b = 0;
+        RSG_CUDA(cub::DeviceSegmentedSort::StableSortPairs(nullptr, b, k1, k2, v1, v2, (int)M, cnt,
+                                                           N.start + base, se, st));
+        void *t = ar.take(b + 256);
+        RSG_CUDA(cub::DeviceSegmentedSort::StableSortPairs(t, b, k1, k2, v1, v2, (int)M, cnt,
+                                                           N.start + base, se, st));
+    } else {
+        uint64_t *k1 = ar.get<uint64_t>(M), *k2 = ar.get<uint64_t>(M);
+        launch(k_lsort_keys64, nblk(M, T), T, 0, st, eln, M, N, base, (const int32_t *)lab, k1, v1);
+        int bits = 33;
+        while (bits < 64 && (1ll << (bits - 32)) <= M) bits++;
+        size_t b = 0;
+        RSG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, b, k1, k2, v1, v2, (int)M, 0, bits, st));
+        void *t = ar.take(b + 256);
+        RSG_CUDA(cub::DeviceRadixSort::SortPairs(t, b, k1, k2, v1, v2, (int)M, 0, bits, st));
+    }
     launch(k_gather<Rec>, nblk(M, T), T, 0, st, (const Rec *)W, (const uint32_t *)v2, M, wt);
     launch(k_gather<int32_t>, nblk(M, T), T, 0, st, (const int32_t *)lab, (const uint32_t *)v2, M,
            lt);
