@@ -87,8 +87,8 @@ def short_name(mangled):
 def parse_table(txt):
     rows = []
     for line in txt.splitlines():
-        parts = line.split("\t")
-        if len(parts) == 3:
+        parts = line.split("\t")  # name, launches, total ms[, gap before ms]
+        if len(parts) >= 3:
             rows.append((short_name(parts[0]), int(parts[1]), float(parts[2])))
     return rows
 

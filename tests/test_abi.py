@@ -89,3 +89,11 @@ def test_tuning_parameters(rk):
     finally:
         for k, v in old.items():
             rk.set_tuning(k, v)
+
+
+def test_bench_parses_profile_table():
+    """bench.py reads rsg_profile_table's lines (name, launches, total ms,
+    gap ms) to pick the kernel whose roofline it reports."""
+    import bench
+    rows = bench.parse_table("_ZN3rsg4k_nnEPKv\t10\t12.5\t0.02\n_ZN3rsg6k_kahnEv\t3\t1.0\t0.5\n")
+    assert rows == [("k_nn", 10, 12.5), ("k_kahn", 3, 1.0)]
