@@ -42,7 +42,7 @@ ALGO_BYTES = {
     # union-find parent written (4 B)
     "k_fof6_w": lambda st, L: 28.0 * st["items_6d"] / max(L, 1),
     # assignment: position read, label read and written
-    "k_asc_assign": lambda st, L: 32.0 * st["items_6d"] / max(L, 1),
+    "k_asc_assign_p": lambda st, L: 32.0 * st["items_6d"] / max(L, 1),
     # basic halo properties: two passes over the halo's positions
     "k_basic_props": lambda st, L: 48.0 * st["items_6d"] / max(L, 1),
     # norm_sd: positions read and written back
@@ -52,6 +52,7 @@ ALGO_BYTES = {
     "k_nn": lambda st, L: 28.0 * st["samples_6d"] / max(L, 1),
     # median selection: every sample distance read once
     "k_target_smem": lambda st, L: 4.0 * st["samples_6d"] / max(L, 1),
+    "k_target_rs": lambda st, L: 4.0 * st["samples_6d"] / max(L, 1),
     # later-dense lists: positions of the dense particles in both launches,
     # every entry written once
     "k_llist_w": lambda st, L: (32.0 * st["dense"] + 4.0 * st["later_list"]) / max(L, 1),

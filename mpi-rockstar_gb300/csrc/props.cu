@@ -6,7 +6,7 @@
 //     (calc_particle_radii, src/groupies.c:212-270);
 //  2. potentials: the reference's Barnes-Hut code reproduced on the GPU -- a
 //     forest of kd-trees (10 points per leaf, exact fast3tree permutation),
-//     mass centres and opening radii bottom-up, and one thread per leaf
+//     mass centres and opening radii bottom-up, and one half-warp per leaf
 //     walking the tree in the reference's order so every FP64 sum matches
 //     (src/potential.c:22-192);
 //  3. potential-only particles dropped, the rest sorted by r^2;
