@@ -17,7 +17,8 @@ def _cfg(rk, p, box, mp):
     return rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
 
 
-@pytest.mark.parametrize("cfg,scale", [(1, 0.05), (1, 0.25), (2, 1 / 32)])
+@pytest.mark.parametrize("cfg,scale", [(1, 0.05), (1, 0.25), (2, 1 / 32), (3, 0.001),
+                                       (4, 1 / 4096), (5, 0.002)])
 def test_restatement_equals_reference(rk, oracle, cfg, scale):
     from oracle import refcall
     p, box, mp, _ = rk.synth(cfg, scale)
