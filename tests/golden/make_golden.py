@@ -23,7 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-CASES = [("c1_q", 1, 0.25), ("c2_s", 2, 1 / 32), ("c1_tiny", 1, 0.02)]
+CASES = [("c1_q", 1, 0.25), ("c2_s", 2, 1 / 32), ("c1_tiny", 1, 0.02),
+         ("c3_t", 3, 0.001), ("c5_t", 5, 0.002)]
 SEED = 20261203
 
 
@@ -57,12 +58,15 @@ def canon(parts, off, sz, n):
     return lab
 
 
-def main():
+def main(names=None):
+    """Writes every case, or only those named on the command line."""
     rk = load_pkg()
     rk.build()
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")])
     from oracle import refcall
     for name, cfg, scale in CASES:
+        if names and name not in names:
+            continue
         p, box, mp, _ = rk.synth(cfg, scale, SEED)
         c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
         refcall.setup(c)
@@ -80,4 +84,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

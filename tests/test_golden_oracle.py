@@ -15,7 +15,7 @@ GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 SHAPE = {"b_to_a", "c_to_a", "A", "b_to_a2", "c_to_a2", "A2", "inertia_tensor", "inertia_tensor2"}
 
 
-@pytest.mark.parametrize("name", ["c1_tiny", "c1_q", "c2_s"])
+@pytest.mark.parametrize("name", ["c1_tiny", "c1_q", "c2_s", "c3_t", "c5_t"])
 def test_oracle_matches_golden(rk, oracle, name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     p, box, mp, _ = rk.synth(int(z["cfg"]), float(z["scale"]), int(z["seed"]))

@@ -32,7 +32,7 @@ def load_case(rk, name):
     return z, p, fp, c, H, E
 
 
-@pytest.mark.parametrize("name", ["c1_tiny", "c1_q", "c2_s"])
+@pytest.mark.parametrize("name", ["c1_tiny", "c1_q", "c2_s", "c3_t", "c5_t"])
 def test_find_subs_golden(rk, name):
     z, p, fp, c, H, E = load_case(rk, name)
     parts, gh, ge = rk.find_subs(fp, z["fof_off"], z["fof_sz"], c)
@@ -66,7 +66,7 @@ def test_find_subs_oracle(rk, oracle, cfg, scale):
     assert not bad, bad[:10]
 
 
-@pytest.mark.parametrize("name", ["c1_tiny", "c1_q"])
+@pytest.mark.parametrize("name", ["c1_tiny", "c1_q", "c3_t"])
 def test_find_subs_batched_golden(rk, name):
     """The batched form on inputs whose subgroups never exceed the 10000
     particles at which the reference samples its linking length: membership
