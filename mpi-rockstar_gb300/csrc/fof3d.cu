@@ -30,11 +30,6 @@
 
 namespace rsg {
 
-
-struct TravStatus {
-    int *flag;  // set to 1 when a traversal stack overflows
-};
-
 // Sphere search (src/fast3tree.c:377-414) on tree `root` of a 3D forest.
 // on_range(start, n) receives nodes that lie entirely inside the sphere
 // (shortcut of :386-392), on_point(j) leaf points with dist < r^2.  Either

@@ -38,12 +38,6 @@ __device__ __forceinline__ float pdist(const rsg_halo &h, const float *pos) {
     float b = __fdiv_rn(v2, fmul(h.vrms, h.vrms));
     return sqrt_fd(fadd(a, b));
 }
-// calc_halo_dist, src/subhalo_metric.c:73-77
-__device__ __forceinline__ float hdist(const rsg_halo &h1, const rsg_halo &h2) {
-    if ((double)h2.r > (double)h1.r * 0.99999) return 1e20f;
-    return pdist(h1, h2.pos);
-}
-
 // could_be_poisson_or_force_res, src/groupies.c:333-360
 __device__ __forceinline__ int poisson_or_force(const rsg_halo &h1, const rsg_halo &h2,
                                                 double force_res, int *force) {

@@ -107,33 +107,6 @@ __global__ void k_root_init(const int32_t *rstart, const int32_t *rn, int32_t nt
     }
 }
 
-// Box of every node listed in `owner` (per element), via ordered atomics.
-template <int D, class RecT>
-__global__ void k_box_accum(const RecT *recs, int64_t nrec, const int32_t *owner,
-                            unsigned *bmin, unsigned *bmax) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= nrec) return;
-    int a = owner[i];
-    if (a < 0) return;
-    const RecT r = recs[i];
-    for (int d = 0; d < D; d++) {
-        unsigned o = f2ord(PosOf<RecT, D>::get(r, d));
-        atomicMin(&bmin[(int64_t)a * D + d], o);
-        atomicMax(&bmax[(int64_t)a * D + d], o);
-    }
-}
-
-template <int D>
-__global__ void k_box_final(KNode<D> *nodes, const int32_t *list, int32_t nlist,
-                            const unsigned *bmin, const unsigned *bmax) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nlist) return;
-    int a = list[k];
-    for (int d = 0; d < D; d++) {
-        nodes[a].mn[d] = ord2f(bmin[(int64_t)a * D + d]);
-        nodes[a].mx[d] = ord2f(bmax[(int64_t)a * D + d]);
-    }
-}
 
 // Choose the split dimension and limit (src/fast3tree.c:736-757).
 template <int D>

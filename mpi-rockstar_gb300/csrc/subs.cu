@@ -1844,9 +1844,9 @@ __global__ void __launch_bounds__(256) k_maxi(HierNodes N, int32_t base, const r
     if (threadIdx.x == 0) N.maxi[node] = mi;
 }
 
-// hdist(c, h) (calc_halo_dist) and, when the value is a metric rather than
-// the 1e20 of a too-small or invalid candidate, its float sum x before the
-// square root (else x = inf).
+// calc_halo_dist(c, h) (src/subhalo_metric.c:73-77) and, when the value is
+// a metric rather than the 1e20 of a too-small or invalid candidate, its
+// float sum x before the square root (else x = inf).
 __device__ __forceinline__ float hdist_x(const rsg_halo &c, const rsg_halo &h, float *x) {
     *x = INFINITY;
     if ((double)h.r > (double)c.r * 0.99999) return 1e20f;
