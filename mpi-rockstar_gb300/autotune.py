@@ -33,17 +33,15 @@ def _median(v):
     return v[len(v) // 2]
 
 
-def autotune(rk, parts, cfg, reps=5, passes=2, min_gain=0.01, names=None, log=None):
-    """Tunes on one workload (`parts`, a PARTICLE array, and its Config).
-    Leaves the best values set and returns {"best", "default", "best_ms",
-    "default_ms", "trials"}."""
+def device_step(rk, parts, cfg, reps):
+    """A function timing the median of `reps` batched steps on device-resident
+    particles (one warm-up step first)."""
     import numpy as np
     import torch
 
-    names = list(names or CANDIDATES)
     d_in = torch.from_numpy(np.ascontiguousarray(parts).view(np.uint8).reshape(-1)).cuda()
     path = rk.DevicePath(len(parts), cfg, batched=True)
-    trials = []
+    path.run(d_in.data_ptr())  # warm-up: arena growth, module load
 
     def step_ms():
         ts = []
@@ -54,7 +52,18 @@ def autotune(rk, parts, cfg, reps=5, passes=2, min_gain=0.01, names=None, log=No
             ts.append((time.perf_counter() - t0) * 1e3)
         return _median(ts)
 
-    path.run(d_in.data_ptr())  # warm-up: arena growth, module load
+    return step_ms
+
+
+def autotune(rk, parts, cfg, reps=5, passes=2, min_gain=0.01, names=None, log=None,
+             step_ms=None):
+    """Tunes on one workload (`parts`, a PARTICLE array, and its Config), or
+    with any `step_ms()` timer.  Leaves the best values set and returns
+    {"best", "default", "best_ms", "default_ms", "trials"}."""
+    names = list(names or CANDIDATES)
+    trials = []
+    if step_ms is None:
+        step_ms = device_step(rk, parts, cfg, reps)
     default = rk.get_tuning()
     cur = dict(default)
     cur_ms = step_ms()
@@ -80,7 +89,6 @@ def autotune(rk, parts, cfg, reps=5, passes=2, min_gain=0.01, names=None, log=No
                 cur_ms = step_ms()  # re-measure with the new value in place
         if not changed:
             break
-    del path, d_in
     return {"best": cur, "default": default, "best_ms": cur_ms, "default_ms": default_ms,
             "trials": trials}
 
