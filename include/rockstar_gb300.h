@@ -192,6 +192,20 @@ int32_t rsg_set_potential_form(int32_t form);
 int32_t rsg_set_tuning(const char *name, int64_t value);
 int32_t rsg_get_tuning(const char *name, int64_t *value);
 
+/* The per-halo potential records the reference hands to its
+ * analyze_halo_generic callback (src/properties.c:554-555, declared in
+ * src/io/io_generic.h:12-18): after the potentials and kinetic energies,
+ * with the potential-only records dropped, sorted by r^2.  When
+ * rsg_keep_halo_records(1) is set (process-wide), rsg_find_subs,
+ * rsg_find_subs_batch and rsg_path_device keep them.  rsg_halo_records then
+ * copies those of the last call to out, and count[i] records of halo i
+ * (its index in that call's halo output, nh halos) start at out[first[i]].
+ * Call it with out = NULL for the sizes.  Returns the number of records, or
+ * RSG_ERR_ARGS when cap is too small. */
+int32_t rsg_keep_halo_records(int32_t on);
+int64_t rsg_halo_records(struct rsg_potential *out, int64_t cap, int64_t *first, int64_t *count,
+                         int64_t nh);
+
 /* Allocation-free 3D FOF of one chunk: rsg_rockstar_fof on device buffers,
  * with no counterpart in the reference (whose fof.c grows its buffers with
  * realloc).  It allocates nothing: every scratch buffer is carved from one

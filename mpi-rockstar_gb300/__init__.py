@@ -67,6 +67,10 @@ def lib():
         h.rsg_set_potential_form.restype = C.c_int32
         h.rsg_set_potential_form.argtypes = [C.c_int32]
         h.rsg_debug_keep_potentials.argtypes = [C.c_int32]
+        h.rsg_keep_halo_records.restype = C.c_int32
+        h.rsg_keep_halo_records.argtypes = [C.c_int32]
+        h.rsg_halo_records.restype = i64
+        h.rsg_halo_records.argtypes = [vp, i64, vp, vp, i64]
         h.rsg_set_tuning.restype = C.c_int32
         h.rsg_set_tuning.argtypes = [C.c_char_p, i64]
         h.rsg_get_tuning.restype = C.c_int32
@@ -204,6 +208,28 @@ def load_tuning(path=TUNING_FILE):
     for k, v in best.items():
         set_tuning(k, v)
     return best
+
+
+def keep_halo_records(on=True):
+    """Keep, from the next calls, every halo's potential records as the
+    reference's analyze_halo_generic receives them (rsg_keep_halo_records)."""
+    _check(lib().rsg_keep_halo_records(1 if on else 0))
+
+
+def halo_records(nh):
+    """Records of the last call's nh halos: (records, first, count), halo i's
+    records being records[first[i]:first[i] + count[i]] (sorted by r^2)."""
+    first = np.zeros(max(nh, 1), np.int64)
+    count = np.zeros(max(nh, 1), np.int64)
+    k = int(lib().rsg_halo_records(None, 0, first.ctypes.data, count.ctypes.data, nh))
+    if k < 0:
+        _check(k)
+    out = np.zeros(k, POTENTIAL)
+    r = int(lib().rsg_halo_records(out.ctypes.data if k else None, k, first.ctypes.data,
+                                   count.ctypes.data, nh))
+    if r < 0:
+        _check(r)
+    return out, first[:nh].copy(), count[:nh].copy()
 
 
 def keep_potentials(on=True):

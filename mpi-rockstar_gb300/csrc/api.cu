@@ -365,6 +365,57 @@ int64_t rsg_debug_potentials(struct rsg_potential *out, int64_t cap) {
     return k;
 }
 
+int32_t rsg_keep_halo_records(int32_t on) {
+    rsg_debug_keep_potentials(on);
+    return RSG_OK;
+}
+
+int64_t rsg_halo_records(struct rsg_potential *out, int64_t cap, int64_t *first, int64_t *count,
+                         int64_t nh) {
+    const std::vector<rsg::PotRec> &R = rsg::g_dbg_po;
+    if (nh < 0 || (nh > 0 && (!first || !count))) {
+        set_error(RSG_ERR_ARGS, "rsg_halo_records: bad arguments");
+        return RSG_ERR_ARGS;
+    }
+    // a record's halo is its index in the call's halo output (kept in the
+    // record's padding); potential-only records carry ke < 0
+    auto halo_of = [](const rsg::PotRec &r) {
+        int32_t h;
+        memcpy(&h, &r.pad, sizeof h);
+        return (int64_t)h;
+    };
+    std::vector<int64_t> c((size_t)(nh > 0 ? nh : 0), 0);
+    int64_t total = 0;
+    for (const rsg::PotRec &r : R) {
+        int64_t h = halo_of(r);
+        if (r.ke < 0 || h < 0 || h >= nh) continue;
+        c[(size_t)h]++;
+        total++;
+    }
+    if (nh > 0) {
+        int64_t at = 0;
+        for (int64_t h = 0; h < nh; h++) {
+            first[h] = at;
+            count[h] = c[(size_t)h];
+            at += c[(size_t)h];
+        }
+    }
+    if (out) {
+        if (cap < total) {
+            set_error(RSG_ERR_ARGS, "rsg_halo_records: %lld records, capacity %lld",
+                      (long long)total, (long long)cap);
+            return RSG_ERR_ARGS;
+        }
+        std::vector<int64_t> at(first, first + nh);
+        for (const rsg::PotRec &r : R) {
+            int64_t h = halo_of(r);
+            if (r.ke < 0 || h < 0 || h >= nh) continue;
+            memcpy(out + at[(size_t)h]++, &r, sizeof(rsg_potential));
+        }
+    }
+    return total;
+}
+
 // Test hook: the subgroup hierarchy of the last rsg_find_subs call on this
 // thread: per node its level, size and 6D linking length (normalised units).
 int64_t rsg_debug_hierarchy(int32_t *level, int32_t *n, float *target_r, int64_t cap) {

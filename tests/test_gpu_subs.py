@@ -122,3 +122,26 @@ def test_tuning_does_not_change_results(rk):
     finally:
         for k, v in old.items():
             rk.set_tuning(k, v)
+
+
+@pytest.mark.parametrize("batched", [False, True])
+def test_halo_records_for_analyze_callback(rk, batched):
+    """rsg_halo_records: every halo's records as the reference hands them to
+    analyze_halo_generic (its own and its children's particles, potential-only
+    records dropped, sorted by r^2, kinetic energies set)."""
+    p, box, mp, _ = rk.synth(2, 1 / 32)
+    cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    fp, off, sz = rk.rockstar_fof(p, cfg)
+    rk.keep_halo_records(True)
+    try:
+        parts, h, e = rk.find_subs(fp, off, sz, cfg, batched=batched)
+        rec, first, cnt = rk.halo_records(len(h))
+    finally:
+        rk.keep_halo_records(False)
+    assert cnt.sum() == len(rec) > 0
+    live = h["num_p"] >= 1
+    assert np.array_equal(cnt[live], h["num_child_particles"][live])
+    assert (cnt[~live] == 0).all()
+    for i in np.flatnonzero(live):
+        r = rec[first[i]:first[i] + cnt[i]]
+        assert (np.diff(r["r2"]) >= 0).all() and (r["ke"] >= 0).all()
