@@ -100,10 +100,11 @@ def test_bench_parses_profile_table():
 
 
 def test_integration_shim_compiles(tmp_path):
-    """The reference-side shim of INTEGRATION.md, compiled as C against the
-    reference's own headers (its struct layouts asserted equal to the C
-    ABI's under the reference build flags) and include/rockstar_gb300.h.
-    Needs the reference checkout; skipped where it is absent."""
+    """The reference-side shim (the C code blocks of the integration guide at
+    the repository root), compiled as C against the reference's own headers
+    (its struct layouts asserted equal to the C ABI's under the reference
+    build flags) and include/rockstar_gb300.h.  Needs the reference
+    checkout; skipped where it is absent."""
     import subprocess
     import __graft_entry__ as ge
     if not os.path.isdir(ge.REF_SRC):
