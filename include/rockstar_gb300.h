@@ -198,7 +198,7 @@ int32_t rsg_get_tuning(const char *name, int64_t *value);
  * with the potential-only records dropped, sorted by r^2.  When
  * rsg_keep_halo_records(1) is set (process-wide), rsg_find_subs,
  * rsg_find_subs_batch and rsg_path_device keep them.  rsg_halo_records then
- * copies those of the last call to out, and count[i] records of halo i
+ * copies those of the calling thread's last call to out, and count[i] records of halo i
  * (its index in that call's halo output, nh halos) start at out[first[i]].
  * Call it with out = NULL for the sizes.  Returns the number of records, or
  * RSG_ERR_ARGS when cap is too small. */

@@ -31,7 +31,7 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
                   int form);
 int set_batched_potential_form(int f);
 extern std::atomic<bool> g_keep_po;
-extern std::vector<PotRec> g_dbg_po;
+extern thread_local std::vector<PotRec> g_dbg_po;
 
 // One device context per host thread: a stream and a scratch arena that is
 // reused across calls (the role the reference's threadprivate scratch

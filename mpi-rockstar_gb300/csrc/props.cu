@@ -1905,11 +1905,11 @@ static std::atomic<int> g_pot_form{1};
 int batched_potential_form() { return g_pot_form.load(std::memory_order_relaxed); }
 int set_batched_potential_form(int f) { return g_pot_form.exchange(f); }
 
-// Test hook: when g_keep_po is set, the potential records of the last
-// additional_props call (sorted by halo, then potential-only last, then
-// radius; pe and ke final) are kept in g_dbg_po.
+// When g_keep_po is set (rsg_keep_halo_records), the potential records of
+// this host thread's last additional_props call (sorted by halo, then
+// potential-only last, then radius; pe and ke final) are kept in g_dbg_po.
 std::atomic<bool> g_keep_po{false};
-std::vector<PotRec> g_dbg_po;
+thread_local std::vector<PotRec> g_dbg_po;
 
 void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec *W,
                       int64_t M, rsg_halo *H, rsg_extra_halo_info *E, int32_t NH,
