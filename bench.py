@@ -4,20 +4,24 @@ hierarchy -> particle assignment -> potentials / unbinding -> properties.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 One step is the whole path over one synthetic snapshot.  The default
-workload is the 128^3 substructure snapshot (2,097,152 particles, 80 Mpc/h,
-NFW hosts with subhalos, 35% background; csrc/synth.c workload 2).  Under
-torchrun every rank processes its own snapshot (seed + rank): the path
-shards by snapshot region / group with no exchange, so scaling is weak.
+workload is the 512^3 snapshot (134,217,728 particles, 500 Mpc/h, 200,000
+NFW hosts with subhalos, 45% background; csrc/synth.c workload 4), the
+configuration the metric is quoted on.  Under torchrun every rank processes
+its own snapshot (seed + rank): replicas, no exchange, so scaling is weak.
 
-value   : particles/s with the particles already in HBM (rsg_path_device),
-          timed per step with CUDA events; L2 is flushed between steps.
+value   : particles/s of the batched form with the particles already in HBM
+          (rsg_path_device), timed per step with CUDA events; L2 is flushed
+          between steps.  The plain drop-in is timed beside it.
 e2e     : the same metric through the C ABI with host buffers
-          (rsg_rockstar_fof + rsg_find_subs from pinned memory), copies
+          (rsg_rockstar_fof + rsg_find_subs_batch on a pinned array), copies
           included.
+parity  : on a bounded sample of the workload, the plain form against the
+          oracle (bit for bit) and the batched form's membership; on the full
+          workload the batched form against the plain one (config.tolerance).
 roofline: the dominant kernel (by device time in the launch list), timed
           with CUDA events on its stream during the timed steps.
 cpu_baseline: the C restatement of the reference (oracle/) on one host core
-          over a bounded sample of the same workload.
+          over the same bounded sample.
 """
 import argparse
 import json
@@ -33,6 +37,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 METRIC = "particles/s through FOF+6D+unbind+props, batched vs plain on GB300 @ stated tol"
 SEED = 20261203
+# bounded samples of each workload (same density and structure, smaller box):
+# the CPU baseline and the oracle parity check run on SAMPLE_SCALE, the
+# reference arm times REF_SCALE per step
+SAMPLE_SCALE = {1: 0.25, 2: 0.125, 3: 0.005, 4: 1 / 64, 5: 0.02}
+REF_SCALE = {1: 1.0, 2: 1.0, 3: 0.05, 4: 1 / 32, 5: 0.1}
 # Algorithmic (compulsory) bytes of ONE launch of a kernel, from the work
 # counters the library reports for the step (rsg_last_stats): every input
 # record read once, every output written once; node data held in L2 is not
@@ -157,7 +166,9 @@ class Clocks:
 
 def cpu_baseline_port(rk, cfg_id, scale):
     """The oracle restatement on one core over a bounded sample: workload
-    `cfg_id` at `scale` (same density and structure), the whole path."""
+    `cfg_id` at `scale` (same density and structure), the whole path.
+    Returns the baseline entry and the sample with the oracle's output, which
+    the parity check compares the GPU with."""
     from oracle import restatement as O
     O.build()
     p, box, mp, _ = rk.synth(cfg_id, scale, SEED)
@@ -165,11 +176,98 @@ def cpu_baseline_port(rk, cfg_id, scale):
     O.setup(c)
     t0 = time.perf_counter()
     fp, off, sz = O.fof(p)
-    O.find_subs(fp, off, sz)
-    dt = time.perf_counter() - t0
-    return {"value": len(p) / dt, "unit": "particles/s", "cores": 1, "kind": "port",
-            "sample": "workload %d at scale %g (%d particles), full path, one step, 1 thread"
-                      % (cfg_id, scale, len(p))}
+    t1 = time.perf_counter()
+    ro = O.find_subs(fp, off, sz)
+    t2 = time.perf_counter()
+    entry = {"value": len(p) / (t2 - t0), "unit": "particles/s", "cores": 1, "kind": "port",
+             "sample": "workload %d at scale %g (%d particles), full path, one step, 1 thread"
+                       % (cfg_id, scale, len(p)),
+             "fof_s": round(t1 - t0, 3), "find_subs_s": round(t2 - t1, 3)}
+    return entry, (p, c, fp, off, sz, ro)
+
+
+HALO_INT = ("num_p", "num_child_particles", "n_core", "flags")
+
+
+def _halo_labels(parts, halos, nid):
+    """Halo index of every particle id (-1: in no halo)."""
+    lab = np.full(nid, -1, np.int64)
+    n = np.clip(halos["num_p"], 0, None).astype(np.int64)
+    keep = np.flatnonzero(n > 0)
+    cnt = n[keep]
+    if not len(cnt):
+        return lab
+    first = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+    pos = np.repeat(halos["p_start"][keep].astype(np.int64) - first, cnt) + np.arange(cnt.sum())
+    lab[parts["id"][pos]] = np.repeat(keep, cnt)
+    return lab
+
+
+def catalogue_compare(pa, ha, pb, hb, tol=1e-4):
+    """Two halo catalogues of the same particles: particles outside halos
+    with identical members on both sides, and matched halos with a float
+    field beyond `tol` (relative) or a different integer field."""
+    nid = int(max(pa["id"].max(initial=0), pb["id"].max(initial=0))) + 1
+    la, lb = _halo_labels(pa, ha, nid), _halo_labels(pb, hb, nid)
+    inside = (la >= 0) | (lb >= 0)
+    w = len(hb) + 1
+    uk, cnt = np.unique((la[inside] + 1) * w + (lb[inside] + 1), return_counts=True)
+    A, B = uk // w - 1, uk % w - 1
+    sa = np.bincount(la[la >= 0], minlength=len(ha))
+    sb = np.bincount(lb[lb >= 0], minlength=len(hb))
+    ok = (A >= 0) & (B >= 0)
+    ok[ok] &= (cnt[ok] == sa[A[ok]]) & (cnt[ok] == sb[B[ok]])
+    mA, mB = A[ok], B[ok]
+    over = np.zeros(len(mA), bool)
+    for f in ha.dtype.names:
+        if ha.dtype[f].base.kind != "f":
+            continue
+        x = ha[f][mA].astype(np.float64).reshape(len(mA), -1)
+        y = hb[f][mB].astype(np.float64).reshape(len(mB), -1)
+        same = (x == y) | (np.isnan(x) & np.isnan(y))
+        den = np.maximum(np.abs(x), np.abs(y))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            e = np.where(same, 0.0, np.abs(x - y) / np.where(den > 0, den, 1.0))
+        over |= (e > tol).any(axis=1)
+    for f in HALO_INT:
+        over |= ha[f][mA] != hb[f][mB]
+    return {"membership_diff_particles": int(cnt[~ok].sum()),
+            "halos_with_particles": [int((sa > 0).sum()), int((sb > 0).sum())],
+            "halos_matched": int(len(mA)), "halos_over_1e-4": int(over.sum())}
+
+
+def canon_nan(a):
+    b = a.copy()
+    for f in b.dtype.names:
+        if b.dtype[f].base.kind == "f":
+            v = b[f]
+            v[np.isnan(v)] = np.nan
+    return b
+
+
+def sample_parity(rk, sample):
+    """The GPU path (rsg_path_device, both forms) on the CPU baseline's
+    sample against the oracle's output for it."""
+    import torch
+    p, c, fp, off, sz, ro = sample
+    d_in = torch.from_numpy(p.view(np.uint8).reshape(-1)).cuda()
+    out = {"sample_particles": len(p)}
+    for form, batched in (("plain", False), ("batched", True)):
+        path = rk.DevicePath(len(p), c, batched=batched)
+        path.run(d_in.data_ptr())
+        parts, h, e = path.results()
+        cmp = catalogue_compare(ro[0], ro[1], parts, h)
+        if not batched:
+            exact = (parts.tobytes() == ro[0].tobytes()
+                     and canon_nan(h).tobytes() == canon_nan(ro[1]).tobytes()
+                     and e.tobytes() == ro[2].tobytes())
+            out["plain_vs_oracle"] = "bit-identical" if exact else "differs"
+            cmp["bit_identical"] = exact
+        out[form] = cmp
+        cmp["near_threshold_pairs"] = rk.last_stats()["near_6d"]
+        del path
+    torch.cuda.empty_cache()
+    return out
 
 
 # ---- reference arm: the oracle port over all host cores -------------------
@@ -204,7 +302,9 @@ def reference_arm(args, rk):
     from oracle import layouts as OL
     from oracle import restatement as O
     O.build()
-    p, box, mp, _ = rk.synth(args.cfg, args.scale, SEED)
+    rscale = args.ref_scale if args.ref_scale else REF_SCALE.get(args.cfg, 1.0) * args.scale
+    p, box, mp, _ = rk.synth(args.cfg, rscale, SEED)
+    n_full = rk.synth_count(args.cfg, args.scale, SEED)
     fields = {f.name: getattr(rk.Config(particle_mass=mp, box_size=box, total_particles=len(p)),
                               f.name) for f in dataclasses.fields(OL.Config)}
     O.setup(OL.Config(**fields))
@@ -243,11 +343,14 @@ def reference_arm(args, rk):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": "synthetic workload %d (%d particles)" % (args.cfg, len(p)),
-                       "particles": len(p), "host_cores": ncores},
+            "config": {"workload": "synthetic workload %d at scale %g: %d particles"
+                                   % (args.cfg, args.scale, n_full),
+                       "particles": n_full, "sample_particles": len(p), "host_cores": ncores},
             "cpu_baseline": {"value": v, "unit": "particles/s", "cores": ncores, "kind": "port",
-                             "sample": "full workload, FOF serial, find_subs over groups on "
-                                       "%d processes" % ncores},
+                             "sample": "workload %d at scale %g (%d particles, same density and "
+                                       "structure) per step; FOF serial, find_subs over the "
+                                       "groups on %d processes" % (args.cfg, rscale, len(p),
+                                                                   ncores)},
             "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -314,8 +417,17 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cfg", type=int, default=2)
+    ap.add_argument("--cfg", type=int, default=4,
+                    help="synthetic workload (csrc/synth.c); 4 is the 512^3 snapshot")
     ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--plain-steps", type=int, default=1,
+                    help="timed steps of the plain form (after one untimed step) on workloads "
+                         "above 2^23 particles; smaller ones use --steps/--warmup")
+    ap.add_argument("--sample-scale", type=float, default=None,
+                    help="scale of the bounded sample the CPU baseline and the oracle parity "
+                         "check run on (default: per workload, about 10-20 s of CPU work)")
+    ap.add_argument("--ref-scale", type=float, default=None,
+                    help="scale of the sample each reference-arm step runs on")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-table", default="",
                     help="write per-kernel CUDA-event times of one extra (untimed) step of "
@@ -355,9 +467,10 @@ def main():
             reference_arm(args, rk)
         return
     # CPU baseline first: no GPU context exists yet
-    cpu = None
+    cpu, sample = None, None
     if rank == 0 and world >= 1 and not args.no_cpu_baseline and args.gpus == 1:
-        cpu = cpu_baseline_port(rk, args.cfg, args.scale)
+        sscale = args.sample_scale or SAMPLE_SCALE.get(args.cfg, 0.1) * args.scale
+        cpu, sample = cpu_baseline_port(rk, args.cfg, min(sscale, args.scale))
     import torch
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
@@ -388,8 +501,8 @@ def main():
         rk.profile_select("")
         return e0.elapsed_time(e1), tab
 
-    def timed(path, steps, prof):
-        for _ in range(args.warmup):
+    def timed(path, steps, prof, warmup=None):
+        for _ in range(args.warmup if warmup is None else warmup):
             path.run(d_in.data_ptr())
         torch.cuda.synchronize()
         if dist:
@@ -413,9 +526,14 @@ def main():
         rk.profile_select("")
         return float(np.mean(times)), res, launches, kl, kms
 
-    # plain drop-in (the reference's results bit for bit), then the batched form
+    # plain drop-in (the reference's results bit for bit), then the batched form;
+    # on the large workloads the plain form gets one untimed and --plain-steps
+    # timed steps (it is reported beside the headline, not as it)
+    big = n > (1 << 23)
+    plain_steps = args.plain_steps if big else args.steps
     plain_path = rk.DevicePath(n, cfg, batched=False)
-    plain_ms, plain_res, plain_launches, _, _ = timed(plain_path, args.steps, None)
+    plain_ms, plain_res, plain_launches, _, _ = timed(plain_path, plain_steps, None,
+                                                      1 if big else None)
     batched_path = rk.DevicePath(n, cfg, batched=True)
     batched_path.run(d_in.data_ptr())
     # the dominant kernel of the batched step, by device time
@@ -426,6 +544,17 @@ def main():
     step_ms, res, launches, kl, kms = timed(batched_path, args.steps, top)
     clk = clocks.stop()
     stats = rk.last_stats()
+    # the batched form's output against the plain form's on the full workload
+    # (the plain form is pinned bit for bit to the oracle by the tests and by
+    # the sample check below)
+    tol = None
+    if rank == 0:
+        pa, ha, _ = plain_path.results()
+        pb, hb, _ = batched_path.results()
+        tol = catalogue_compare(pa, ha, pb, hb)
+        tol["near_threshold_pairs"] = stats["near_6d"]
+        tol["against"] = "plain form on the same snapshot"
+        del pa, ha, pb, hb
     if dist:
         t = torch.tensor([step_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -462,6 +591,13 @@ def main():
         d2h = len(fp) * 32 + 16 * len(off) + len(fp) * 32 + len(halos) * (312 + 48)
     e2e_v = n * world / min(e2e_t)
 
+    parity = None
+    if sample is not None:
+        del plain_path
+        torch.cuda.empty_cache()
+        parity = sample_parity(rk, sample)
+        parity["oracle"] = "C restatement of the reference (oracle/), same sample"
+
     pk, pk_kind = peaks()
     roof = None
     if kl:
@@ -495,12 +631,15 @@ def main():
                        "l2": "flushed between steps (256 MiB write)", "form": "batched",
                        "plain_particles_per_s": n * world / (plain_ms * 1e-3),
                        "plain_ms_per_step": plain_ms, "plain_halos": plain_res[2],
+                       "plain_steps": plain_steps,
+                       "batched_over_plain": plain_ms / step_ms,
+                       "tolerance": tol,
                        "plain_gpu_launches": plain_launches,
                        "tuning": rk.get_tuning(),
                        "tuning_source": "mpi-rockstar_gb300/tuning.json" if tuned else "defaults"},
             "e2e": {"value": e2e_v, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+            "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "parity": parity,
             "work": stats,
             "clocks": clk, "peak_source": pk_kind}
     if rank == 0:

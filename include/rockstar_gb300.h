@@ -103,11 +103,13 @@ int rsg_config_setup(struct rsg_config *cfg);
  * previous particle in kd-tree order, src/rockstar.c:368-397) are removed
  * and *num_p shrinks accordingly.  Group i occupies
  * p[fof_offsets[i] .. fof_offsets[i] + fof_sizes[i]); groups of fewer than
- * MIN_HALO_PARTICLES are dropped as in src/fof.c:226-255.  Membership is
- * identical to the reference; the order of groups and of particles inside
- * a group is this library's (groups by first kd-tree position, particles in
- * kd-tree order), as the reference's is an artefact of its union-find.
- * Particles in no group follow the last group. */
+ * MIN_HALO_PARTICLES are dropped as in src/fof.c:226-255.  The result is
+ * the reference's byte for byte: the permutation of p (particles in no group
+ * first, then one run per union-find label in ascending label order, groups
+ * too small to keep included, as partition_sort_particles leaves them,
+ * src/fof.c:184-224) and the groups in build_fullfofs order.  The union-find
+ * labels are derived from the link lists in parallel and equal the ones the
+ * reference's sequential linking produces. */
 int rsg_rockstar_fof(struct rsg_particle *p, int64_t *num_p, const struct rsg_config *cfg,
                      int64_t *fof_offsets, int64_t *fof_sizes, int64_t max_fofs,
                      int64_t *num_fofs);
@@ -168,6 +170,17 @@ int rsg_path_device(const struct rsg_particle *d_in, int64_t n, const struct rsg
 int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct rsg_config *cfg,
                           int32_t form);
 
+/* Kinetic energies of one particle set about a centre: replaces
+ * compute_kinetic_energy(po, num_po, vel_cen, pos_cen, scale_now)
+ * (src/potential.h:25, src/potential.c:194-211), with the cosmology (Om, Ol,
+ * W0, WA) taken from cfg.  Every record with ke >= 0 gets
+ * ke = a/(2G) sum_k (v_k - vel_cen_k + H(a) a (x_k - pos_cen_k))^2 with the
+ * reference's float/double conversions; records with ke < 0 (potential-only)
+ * are left alone.  po is not reordered. */
+int rsg_compute_kinetic_energy(struct rsg_potential *po, int64_t num_po, const float *vel_cen,
+                               const float *pos_cen, float scale_now,
+                               const struct rsg_config *cfg);
+
 /* Selects the potential form (0-3, as for rsg_compute_potential) that the
  * batched substructure form (rsg_find_subs_batch, rsg_path_device with
  * batched = 1) uses from now on, process-wide; the default is 1.  The plain
@@ -201,18 +214,23 @@ int32_t rsg_get_tuning(const char *name, int64_t *value);
  * copies those of the calling thread's last call to out, and count[i] records of halo i
  * (its index in that call's halo output, nh halos) start at out[first[i]].
  * Call it with out = NULL for the sizes.  Returns the number of records, or
- * RSG_ERR_ARGS when cap is too small. */
+ * RSG_ERR_ARGS when cap is too small.  Records are kept per host thread;
+ * rsg_keep_halo_records(0) frees the calling thread's at once and every
+ * other thread's at that thread's next call, and while the switch is off
+ * rsg_halo_records reports none. */
 int32_t rsg_keep_halo_records(int32_t on);
 int64_t rsg_halo_records(struct rsg_potential *out, int64_t cap, int64_t *first, int64_t *count,
                          int64_t nh);
 
 /* Allocation-free 3D FOF of one chunk: rsg_rockstar_fof on device buffers,
  * with no counterpart in the reference (whose fof.c grows its buffers with
- * realloc).  It allocates nothing: every scratch buffer is carved from one
- * fixed device array of RSG_NOALLOC_SCRATCH_BYTES per device, reserved when
- * the library's module for it loads at the first call on a device (make
- * that call before any stream capture).  For callers that cannot let a
- * library allocate or free device memory while their own kernels run.
+ * realloc).  It allocates no device memory: every scratch buffer is carved
+ * from one fixed device array of RSG_NOALLOC_SCRATCH_BYTES per device.  The
+ * first call in a process (and the first after a device reset) loads the
+ * library's kernels and that array, which takes device memory once: make
+ * it at setup, before any stream capture.  Later calls take none.  For
+ * callers that cannot let a library allocate or free device memory while
+ * their own kernels run.
  *   d_in  : num_p particles on the device (num_p <= RSG_NOALLOC_MAX_PARTICLES,
  *           else RSG_ERR_LIMIT); not modified.
  *   d_out : device, capacity num_p, must not overlap d_in; receives the
@@ -247,7 +265,9 @@ int rsg_rockstar_fof_noalloc(const struct rsg_particle *d_in, int64_t num_p,
 #define RSG_STAT_LATER_LIST 9    /* 3D FOF later-dense-neighbour entries */
 #define RSG_STAT_6D_ITEMS 10     /* particles summed over the 6D hierarchy levels */
 #define RSG_STAT_6D_SAMPLES 11   /* linking-length samples summed over the levels */
-#define RSG_STAT_COUNT 12
+#define RSG_STAT_NEAR_6D 12      /* 6D particle pairs whose distance is within 1e-6
+                                    (relative) of their subgroup's linking length */
+#define RSG_STAT_COUNT 13
 int rsg_last_stats(int64_t *vals, int32_t n);
 
 /* Instrumentation: kernels launched by this library so far (process-wide),

@@ -10,6 +10,7 @@ Function names follow the reference calls they replace:
   find_subs         <- find_subs() over all groups  src/groupies.c:669-708
                        as the loop of src/mpi_main.cpp:1363-1389 runs it
   compute_potential <- compute_potential()          src/potential.c:183-192
+  compute_kinetic_energy <- compute_kinetic_energy() src/potential.c:194-211
 """
 import ctypes as C
 import os
@@ -60,6 +61,7 @@ def lib():
         h.rsg_profile_read.argtypes = [vp, vp]
         h.rsg_last_stats.argtypes = [vp, C.c_int32]
         h.rsg_compute_potential.argtypes = [vp, i64, vp, C.c_int32]
+        h.rsg_compute_kinetic_energy.argtypes = [vp, i64, vp, vp, C.c_float, vp]
         h.rsg_profile_table.restype = i64
         h.rsg_profile_table.argtypes = [C.c_char_p, i64]
         h.rsg_find_subs.argtypes = [vp, i64, vp, vp, i64, vp, vp, vp, i64, vp]
@@ -159,6 +161,18 @@ def compute_potential(po, cfg, form=0):
     st = setup_config(cfg)
     q = np.array(po, dtype=POTENTIAL, copy=True)
     _check(lib().rsg_compute_potential(q.ctypes.data, len(q), C.byref(st), form))
+    return q
+
+
+def compute_kinetic_energy(po, vel_cen, pos_cen, scale_now, cfg):
+    """compute_kinetic_energy (src/potential.c:194-211) on the GPU: a copy of
+    the POTENTIAL records with ke set for every record whose ke >= 0."""
+    st = setup_config(cfg)
+    q = np.array(po, dtype=POTENTIAL, copy=True)
+    vc = np.ascontiguousarray(vel_cen, np.float32)
+    pc = np.ascontiguousarray(pos_cen, np.float32)
+    _check(lib().rsg_compute_kinetic_energy(q.ctypes.data, len(q), vc.ctypes.data,
+                                            pc.ctypes.data, float(scale_now), C.byref(st)))
     return q
 
 
@@ -270,9 +284,7 @@ def tree_order(parts, dim, leaf):
 _synth = None
 
 
-def synth(cfg_id, scale=1.0, seed=20261203):
-    """Seeded synthetic snapshot (see csrc/synth.c).  Returns
-    (particles, box_size, particle_mass, n_structures)."""
+def _synth_lib():
     global _synth
     if _synth is None:
         h = C.CDLL(SYNTH)
@@ -281,6 +293,21 @@ def synth(cfg_id, scale=1.0, seed=20261203):
         h.synth_generate.argtypes = [C.c_int, C.c_double, C.c_uint64, C.c_void_p, C.c_int64,
                                      C.c_void_p, C.c_void_p, C.c_void_p]
         _synth = h
+    return _synth
+
+
+def synth_count(cfg_id, scale=1.0, seed=20261203):
+    """Particles in synth(cfg_id, scale, seed), without generating them."""
+    n = _synth_lib().synth_count(cfg_id, scale, seed)
+    if n < 0:
+        raise ValueError("bad synthetic workload %r scale %r" % (cfg_id, scale))
+    return int(n)
+
+
+def synth(cfg_id, scale=1.0, seed=20261203):
+    """Seeded synthetic snapshot (see csrc/synth.c).  Returns
+    (particles, box_size, particle_mass, n_structures)."""
+    _synth_lib()
     n = _synth.synth_count(cfg_id, scale, seed)
     if n < 0:
         raise ValueError("bad synthetic workload %r scale %r" % (cfg_id, scale))
@@ -314,7 +341,8 @@ def profile_read():
 
 
 STAT_NAMES = ("particles", "groups", "halos", "pot_records", "kept_big", "kept_small",
-              "halos_big", "halos_small", "dense", "later_list", "items_6d", "samples_6d")
+              "halos_big", "halos_small", "dense", "later_list", "items_6d", "samples_6d",
+              "near_6d")
 
 
 def last_stats():
@@ -372,3 +400,11 @@ class DevicePath:
                                      self.halos.data_ptr(), self.extra.data_ptr(),
                                      self.halo_cap, self._nh.ctypes.data, self.batched))
         return int(self._np[0]), int(self._nf[0]), int(self._nh[0])
+
+    def results(self):
+        """(particles, halos, extra) of the last run, copied to the host."""
+        n, nh = int(self._np[0]), int(self._nh[0])
+        parts = self.out[: n * PARTICLE.itemsize].cpu().numpy().view(PARTICLE).copy()
+        h = self.halos[: nh * HALO.itemsize].cpu().numpy().view(HALO).copy()
+        e = self.extra[: nh * EXTRA.itemsize].cpu().numpy().view(EXTRA).copy()
+        return parts, h, e

@@ -30,6 +30,9 @@ void bh_potential(Arena &ar, PotRec *PO, int64_t npo, const int32_t *rs, const i
                   int32_t ntrees, double mp, double force_res, int *err, cudaStream_t st,
                   int form);
 int set_batched_potential_form(int f);
+void kinetic_energy_device(PotRec *d, int64_t n, const float *vc, const float *pc, float scale,
+                           double hub, cudaStream_t st);
+double hubble100(const rsg_config &c, float scale);
 extern std::atomic<bool> g_keep_po;
 extern thread_local std::vector<PotRec> g_dbg_po;
 
@@ -305,6 +308,30 @@ int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct
     }
 }
 
+int rsg_compute_kinetic_energy(struct rsg_potential *po, int64_t num_po, const float *vel_cen,
+                               const float *pos_cen, float scale_now,
+                               const struct rsg_config *cfg) {
+    if (!cfg || !vel_cen || !pos_cen || num_po < 0 || (num_po > 0 && !po) || !(scale_now > 0)) {
+        set_error(RSG_ERR_ARGS, "rsg_compute_kinetic_energy: bad arguments");
+        return RSG_ERR_ARGS;
+    }
+    try {
+        Ctx &C = ctx();
+        if (num_po == 0) return RSG_OK;
+        C.ar.reserve((size_t)num_po * sizeof(PotRec) + (16u << 20));
+        C.ar.reset();
+        PotRec *d = C.ar.get<PotRec>(num_po);
+        RSG_CUDA(cudaMemcpyAsync(d, po, sizeof(PotRec) * num_po, cudaMemcpyHostToDevice, C.st));
+        kinetic_energy_device(d, num_po, vel_cen, pos_cen, scale_now, hubble100(*cfg, scale_now),
+                              C.st);
+        RSG_CUDA(cudaMemcpyAsync(po, d, sizeof(PotRec) * num_po, cudaMemcpyDeviceToHost, C.st));
+        RSG_CUDA(cudaStreamSynchronize(C.st));
+        return RSG_OK;
+    } catch (Failure &) {
+        return error_code();
+    }
+}
+
 // name, field, smallest and largest accepted value
 struct TuneField {
     const char *name;
@@ -372,7 +399,9 @@ int32_t rsg_keep_halo_records(int32_t on) {
 
 int64_t rsg_halo_records(struct rsg_potential *out, int64_t cap, int64_t *first, int64_t *count,
                          int64_t nh) {
-    const std::vector<rsg::PotRec> &R = rsg::g_dbg_po;
+    static const std::vector<rsg::PotRec> none;
+    // with the switch off, no thread's records are handed out any more
+    const std::vector<rsg::PotRec> &R = rsg::g_keep_po.load() ? rsg::g_dbg_po : none;
     if (nh < 0 || (nh > 0 && (!first || !count))) {
         set_error(RSG_ERR_ARGS, "rsg_halo_records: bad arguments");
         return RSG_ERR_ARGS;

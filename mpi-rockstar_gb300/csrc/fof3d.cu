@@ -27,6 +27,8 @@
 #include <thrust/execution_policy.h>
 
 #include "kdtree_impl.cuh"
+#include "lsort.cuh"
+#include "uflabels.cuh"
 
 namespace rsg {
 
@@ -197,27 +199,6 @@ __device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float
     }
 }
 
-// ---- union-find (lock-free, root = smallest index) ----------------------
-__device__ __forceinline__ int uf_find(int *par, int x) {
-    int p = par[x];
-    while (p != x) {
-        int gp = par[p];
-        if (gp != p) par[x] = gp;  // path halving (benign race)
-        x = p;
-        p = par[x];
-    }
-    return x;
-}
-__device__ __forceinline__ void uf_unite(int *par, int a, int b) {
-    while (true) {
-        a = uf_find(par, a);
-        b = uf_find(par, b);
-        if (a == b) return;
-        if (a < b) { int t = a; a = b; b = t; }
-        if (atomicCAS(&par[a], a, b) == a) return;
-    }
-}
-
 // ---- kernels --------------------------------------------------------------
 __global__ void k_make_recs(const rsg_particle *p, int64_t n, Rec *recs, int *bad) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -350,42 +331,124 @@ __global__ void k_seed_mark(const KNode<3> *nodes, const Rec *recs, int n, float
         s);
 }
 
-__global__ void k_link_r(const KNode<3> *nodes, const Rec *recs, int n, float r,
-                         const uint8_t *cnt, const uint8_t *skipped, int *gtime, int *par,
-                         int *err) {
+// g(j): the first processed particle k with |S_r(k)| >= 2 (in tree order)
+// whose r-sphere holds j -- the moment link_particle_to_fof gives j its
+// label (src/fof.c:112-140).
+__global__ void k_gtime_r(const KNode<3> *nodes, const Rec *recs, int n, float r,
+                          const uint8_t *cnt, const uint8_t *skipped, int *gtime, int *err) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || skipped[k] || cnt[k] < 2) return;
     float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
     sphere3(
         nodes, 0, recs, c, r, err,
         [&](int a, int m) {
-            for (int j = a; j < a + m; j++) {
-                atomicMin(&gtime[j], k);
-                uf_unite(par, k, j);
-            }
+            for (int j = a; j < a + m; j++) atomicMin(&gtime[j], k);
             return true;
         },
         [&](int j) {
             atomicMin(&gtime[j], k);
-            uf_unite(par, k, j);
             return true;
         });
 }
 
-__global__ void k_link_2r(const KNode<3> *nodes, const Rec *recs, int n, float r2x,
-                          const uint8_t *state, const int *gtime, int *par, int *err) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || state[s] != 1) return;
-    float c[3] = {recs[s].pos[0], recs[s].pos[1], recs[s].pos[2]};
+// f(k), the set event k works on (src/fof.c:116-131): k's own label when an
+// earlier event gave it one, else the label of the first particle of S_r(k)
+// (walk order) labelled before k, else a new set (ptr = k).  -1: no event.
+__global__ void k_fptr3(const KNode<3> *nodes, const Rec *recs, int n, float r,
+                        const uint8_t *cnt, const uint8_t *skipped, const int *gtime, int *ptr,
+                        int *err) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (skipped[k] || cnt[k] < 2) {
+        ptr[k] = -1;
+        return;
+    }
+    int gk = gtime[k];
+    if (gk < k) {
+        ptr[k] = gk;
+        return;
+    }
+    int p = k;
+    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
     sphere3(
-        nodes, 0, recs, c, r2x, err,
+        nodes, 0, recs, c, r, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++)
-                if (gtime[j] <= s) uf_unite(par, s, j);
+                if (gtime[j] < k) {
+                    p = gtime[j];
+                    return false;
+                }
             return true;
         },
         [&](int j) {
-            if (gtime[j] <= s) uf_unite(par, s, j);
+            if (gtime[j] < k) {
+                p = gtime[j];
+                return false;
+            }
+            return true;
+        });
+    ptr[k] = p;
+}
+
+// Candidate merges of event k in walk order: for every particle of S_r(k)
+// labelled before k, link_particle_to_fof joins f(k)'s set to that
+// particle's set (src/fof.c:133-139); a seed then does the same for every
+// particle of S_2r(k) labelled by then (link_fof_to_fof, src/fof.c:142-158).  A label equal to f(k), or one this
+// event already emitted, changes nothing and is skipped.  Keys order the
+// candidates in time: (k, sphere, position in the result list).
+#define RSG_CAND_SEEN 8
+__global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r, float r2x,
+                        const uint8_t *cnt, const uint8_t *skipped, const uint8_t *state,
+                        const int *gtime, const int32_t *lab0, const int32_t *sfid, int64_t cap,
+                        unsigned long long *count, uint64_t *ckey, int32_t *cF, int32_t *cW,
+                        int *err) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || skipped[k] || cnt[k] < 2) return;
+    const int F = sfid[k];
+    int seen[RSG_CAND_SEEN];
+    int ns = 0;
+    uint32_t pos = 0;
+    int phase = 0;
+    auto visit = [&](int j) {
+        int gj = gtime[j];
+        if (phase == 0 ? gj < k : gj <= k) {
+            int W = lab0[j];
+            bool dup = (W == F);
+            for (int q = 0; q < ns; q++) dup |= (seen[q] == W);
+            if (!dup) {
+                if (ns < RSG_CAND_SEEN) seen[ns++] = W;
+                unsigned long long t = atomicAdd(count, 1ull);
+                if ((int64_t)t < cap) {
+                    ckey[t] = ((uint64_t)(uint32_t)k << 32) | ((uint64_t)phase << 31) | pos;
+                    cF[t] = F;
+                    cW[t] = W;
+                }
+            }
+        }
+        pos++;
+    };
+    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+    sphere3(
+        nodes, 0, recs, c, r, err,
+        [&](int a, int m) {
+            for (int j = a; j < a + m; j++) visit(j);
+            return true;
+        },
+        [&](int j) {
+            visit(j);
+            return true;
+        });
+    if (state[k] != 1) return;
+    phase = 1;
+    pos = 0;
+    sphere3(
+        nodes, 0, recs, c, r2x, err,
+        [&](int a, int m) {
+            for (int j = a; j < a + m; j++) visit(j);
+            return true;
+        },
+        [&](int j) {
+            visit(j);
             return true;
         });
 }
@@ -442,59 +505,48 @@ __global__ void k_state8(const int *s32, int n, uint8_t *s8) {
     if (i < n) s8[i] = (uint8_t)s32[i];
 }
 
-__global__ void k_roots(int *par, int n, int *root, int *size) {
+// Label of every particle: the smallfof of the set it joined (root null),
+// or the final root of that set.
+__global__ void k_lab3(const int *gtime, int n, const int32_t *sfid, const int32_t *root,
+                       int32_t *lab) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int gj = gtime[j];
+    lab[j] = (gj == 0x7f7f7f7f) ? -1 : (root ? root[sfid[gj]] : sfid[gj]);
+}
+__global__ void k_gather_out(const Rec *recs, const rsg_particle *in, int n, rsg_particle *out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = in[recs[k].ridx];
+}
+// After the partition sort: particles without a label first, then one run
+// per label in ascending order (src/fof.c:226-255 walks them in this order).
+__global__ void k_run_heads3(const int32_t *lab, int n, int *head) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int rt = uf_find(par, i);
-    root[i] = rt;
-    atomicAdd(&size[rt], 1);
+    head[i] = lab[i] >= 0 && (i == 0 || lab[i - 1] != lab[i]);
 }
-
-__global__ void k_keys(const int *root, const int *size, int n, int64_t minsz, uint32_t *key,
-                       uint32_t *val) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int rt = root[i];
-    bool kept = size[rt] >= 2 && size[rt] >= minsz;
-    key[i] = kept ? (uint32_t)rt : (uint32_t)n + (uint32_t)i;
-    val[i] = (uint32_t)i;
-}
-
-__global__ void k_gather_out(const uint32_t *val, const Rec *recs, const rsg_particle *in, int n,
-                             rsg_particle *out) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    out[k] = in[recs[val[k]].ridx];
-}
-
-__global__ void k_heads(const uint32_t *key, int n, int *head) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    head[k] = (key[k] < (uint32_t)n) && (k == 0 || key[k - 1] != key[k]);
-}
-
-__global__ void k_group_sizes(const int *hpos, const int *nh, const uint32_t *key, int n,
-                              int64_t *off, int64_t *sz) {
+// Runs of at least MIN_HALO_PARTICLES become groups, in run order.
+__global__ void k_runs3(const int *hpos, const int *nh, int n, int64_t minsz, int64_t *roff,
+                        int64_t *rsz, int32_t *keep) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= *nh) return;
     int s = hpos[g];
     int e = (g + 1 < *nh) ? hpos[g + 1] : n;
-    // the last group ends where the ungrouped tail (keys >= n) starts
-    if (g + 1 == *nh) {
-        int lo = s, hi = n;
-        while (lo < hi) {
-            int mid = (lo + hi) / 2;
-            if (key[mid] == key[s]) lo = mid + 1; else hi = mid;
-        }
-        e = lo;
-    }
-    off[g] = s;
-    sz[g] = e - s;
+    roff[g] = s;
+    rsz[g] = e - s;
+    keep[g] = (e - s) >= minsz;
 }
 
 __global__ void k_mark_undecided(const int *dense, int nd, uint8_t *state) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < nd) state[dense[t]] = 0;
+}
+__global__ void k_take2(const int32_t *idx, int m, const int32_t *a, const int32_t *b,
+                        int32_t *a2, int32_t *b2) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    a2[t] = a[idx[t]];
+    b2[t] = b[idx[t]];
 }
 __global__ void k_iota(int *a, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -602,7 +654,8 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     RSG_CUDA(cudaMemcpyAsync(&ne, loff + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     // The list lives in the arena when it fits beside what the rest of the FOF
-    // takes from it (~64 B per particle).  A larger one (hundreds of entries
+    // takes from it (< 256 B per particle: the label derivation and the
+    // partition sort).  A larger one (hundreds of entries
     // per particle in very dense snapshots) gets an allocation of its own for
     // this call, as large as free device memory allows (less 1 GiB, or
     // RSG_FOF_LIST_ENTRIES entries when that is set); when the whole list
@@ -619,7 +672,7 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     size_t lat = (ar.used + 255) & ~(size_t)255;
     const char *lenv = getenv("RSG_FOF_LIST_ENTRIES");
     int64_t lforce = lenv ? atoll(lenv) : 0;
-    if (ar.fixed || (!lforce && lat + sizeof(int) * (size_t)lcap + (size_t)64 * n + (64u << 20) <= ar.cap)) {
+    if (ar.fixed || (!lforce && lat + sizeof(int) * (size_t)lcap + (size_t)256 * n + (64u << 20) <= ar.cap)) {
         llist = ar.get<int>(lcap);
     } else {
         size_t fb = 0, tb = 0;
@@ -725,36 +778,99 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     RSG_CUDA(cudaMemsetAsync(skipped, 0, n, st));
     launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)state, skipped,
            err);
-    int *gtime = ar.get<int>(n), *par = ar.get<int>(n);
-    RSG_CUDA(cudaMemsetAsync(gtime, 0x7f, sizeof(int) * n, st));
-    launch(k_iota, nblk(n, T), T, 0, st, par, n);
-    launch(k_link_r, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
-           (const uint8_t *)skipped, gtime, par, err);
-    launch(k_link_2r, nblk(n, T), T, 0, st, F.nodes, recs, n, r2x, (const uint8_t *)state,
-           (const int *)gtime, par, err);
-    phase_mark(st, "fof.links");
-    int *root = ar.get<int>(n), *size = ar.get<int>(n);
-    RSG_CUDA(cudaMemsetAsync(size, 0, sizeof(int) * n, st));
-    launch(k_roots, nblk(n, T), T, 0, st, par, n, root, size);
-    uint32_t *key = ar.get<uint32_t>(n), *val = ar.get<uint32_t>(n);
-    uint32_t *key2 = ar.get<uint32_t>(n), *val2 = ar.get<uint32_t>(n);
-    launch(k_keys, nblk(n, T), T, 0, st, root, size, n, cfg.min_halo_particles, key, val);
-    size_t sb = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, sb, key, key2, val, val2, n, 0, 32, st);
-    void *stmp = ar.take(sb + 256);
-    cub::DeviceRadixSort::SortPairs(stmp, sb, key, key2, val, val2, n, 0, 32, st);
-    launch(k_gather_out, nblk(n, T), T, 0, st, val2, recs, d_in, n, d_out);
+    // labels exactly as the reference's union-find leaves them (uflabels.cuh)
+    int *gtime = ar.get<int>(n);
+    RSG_CUDA(cudaMemsetAsync(gtime, 0x7f, sizeof(int) * n, st));  // 0x7f7f7f7f: never
+    launch(k_gtime_r, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
+           (const uint8_t *)skipped, gtime, err);
+    int32_t *ptr = ar.get<int32_t>(n), *sfid = ar.get<int32_t>(n), *nsc = ar.get<int32_t>(n + 1);
+    launch(k_fptr3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
+           (const uint8_t *)skipped, (const int *)gtime, ptr, err);
+    RSG_CHECK_LAUNCH();
+    int64_t S = uf_resolve(ar, ptr, n, sfid, nsc, st);
+    phase_mark(st, "fof.first_links");
+    // candidate merges, in time order
+    unsigned long long *ccount = ar.get<unsigned long long>(1);
+    int64_t ccap = (int64_t)n / 2 + 1024;
+    size_t cmark = ar.used;
+    uint64_t *ckey = nullptr;
+    int32_t *cF = nullptr, *cW = nullptr;
+    unsigned long long hc = 0;
+    int32_t *lab0 = ar.get<int32_t>(n);
+    {
+        // lab0[j] = f(g(j)): the set j joined when it was labelled
+        launch(k_lab3, nblk(n, T), T, 0, st, (const int *)gtime, n, (const int32_t *)sfid,
+               (const int32_t *)nullptr, lab0);
+    }
+    cmark = ar.used;
+    for (int pass = 0; pass < 2; pass++) {
+        ar.used = cmark;
+        ckey = ar.get<uint64_t>(ccap);
+        cF = ar.get<int32_t>(ccap);
+        cW = ar.get<int32_t>(ccap);
+        RSG_CUDA(cudaMemsetAsync(ccount, 0, sizeof(unsigned long long), st));
+        launch(k_cand3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, r2x, (const uint8_t *)cnt,
+               (const uint8_t *)skipped, (const uint8_t *)state, (const int *)gtime,
+               (const int32_t *)lab0, (const int32_t *)sfid, ccap, ccount, ckey, cF, cW, err);
+        RSG_CHECK_LAUNCH();
+        RSG_CUDA(cudaMemcpyAsync(&hc, ccount, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        RSG_CUDA(cudaStreamSynchronize(st));
+        if ((int64_t)hc <= ccap) break;
+        ccap = (int64_t)hc;  // exact size, second pass
+    }
+    int64_t nc = (int64_t)hc;
+    if (nc >= 0x7f7f7f7f) {
+        set_error(RSG_ERR_LIMIT, "3D FOF: too many label merges (%lld)", (long long)nc);
+        throw Failure();
+    }
+    int32_t *cF2 = ar.get<int32_t>(nc + 1), *cW2 = ar.get<int32_t>(nc + 1);
+    if (nc > 0) {
+        uint64_t *ckey2 = ar.get<uint64_t>(nc);
+        int32_t *cidx = ar.get<int32_t>(nc), *cidx2 = ar.get<int32_t>(nc);
+        launch(k_iota, nblk(nc, T), T, 0, st, cidx, (int)nc);
+        size_t sb = 0;
+        cub::DeviceRadixSort::SortPairs(nullptr, sb, ckey, ckey2, cidx, cidx2, (int)nc, 0, 64, st);
+        void *stmp = ar.take(sb + 256);
+        cub::DeviceRadixSort::SortPairs(stmp, sb, ckey, ckey2, cidx, cidx2, (int)nc, 0, 64, st);
+        launch(k_take2, nblk(nc, T), T, 0, st, (const int32_t *)cidx2, (int)nc,
+               (const int32_t *)cF, (const int32_t *)cW, cF2, cW2);
+    }
+    int32_t *sroot = ar.get<int32_t>(S + 1);
+    uf_roots(ar, cF2, cW2, nc, S, sroot, st);
+    int32_t *lab = ar.get<int32_t>(n);
+    launch(k_lab3, nblk(n, T), T, 0, st, (const int *)gtime, n, (const int32_t *)sfid,
+           (const int32_t *)sroot, lab);
+    RSG_CHECK_LAUNCH();
+    phase_mark(st, "fof.labels");
+    // the reference's partition sort by label (src/fof.c:184-224), then the
+    // groups of build_fullfofs (src/fof.c:226-255)
+    {
+        std::vector<int32_t> s0(1, 0), n0(1, n);
+        partition_sort_labels<Rec>(ar, recs, lab, n, s0, n0, st);
+    }
+    launch(k_gather_out, nblk(n, T), T, 0, st, (const Rec *)recs, d_in, n, d_out);
     int *head = ar.get<int>(n), *hpos = ar.get<int>(n), *nh = ar.get<int>(1);
-    launch(k_heads, nblk(n, T), T, 0, st, key2, n, head);
+    launch(k_run_heads3, nblk(n, T), T, 0, st, (const int32_t *)lab, n, head);
     size_t hb = 0;
     cub::DeviceSelect::Flagged(nullptr, hb, thrust::counting_iterator<int>(0), head, hpos, nh, n,
                                st);
     void *htmp = ar.take(hb + 256);
     cub::DeviceSelect::Flagged(htmp, hb, thrust::counting_iterator<int>(0), head, hpos, nh, n, st);
-    launch(k_group_sizes, nblk(n / 2 + 1, T), T, 0, st, hpos, nh, key2, n, d_off, d_sz);
-    RSG_CHECK_LAUNCH();
+    int64_t *roff = ar.get<int64_t>(n / 2 + 1), *rsz = ar.get<int64_t>(n / 2 + 1);
+    int32_t *keep = ar.get<int32_t>(n / 2 + 1);
+    launch(k_runs3, nblk(n / 2 + 1, T), T, 0, st, (const int *)hpos, (const int *)nh, n,
+           (int64_t)cfg.min_halo_particles, roff, rsz, keep);
     int hnh = 0;
     RSG_CUDA(cudaMemcpyAsync(&hnh, nh, sizeof(int), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    int *nk = ar.get<int>(1);
+    size_t kb = 0;
+    cub::DeviceSelect::Flagged(nullptr, kb, roff, keep, d_off, nk, hnh, st);
+    void *ktmp = ar.take(kb + 256);
+    cub::DeviceSelect::Flagged(ktmp, kb, roff, keep, d_off, nk, hnh, st);
+    cub::DeviceSelect::Flagged(ktmp, kb, rsz, keep, d_sz, nk, hnh, st);
+    RSG_CHECK_LAUNCH();
+    RSG_CUDA(cudaMemcpyAsync(&hnh, nk, sizeof(int), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     if (hflags[2]) {

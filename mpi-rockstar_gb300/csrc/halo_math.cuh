@@ -6,6 +6,29 @@
 
 namespace rsg {
 
+// Loops that the reference runs until convergence carry an iteration limit
+// here; one that reaches it sets this flag (one copy per translation unit),
+// which the host reads at the end of the call and turns into RSG_ERR_LIMIT.
+static __device__ int g_loop_limit_hit;
+__device__ __forceinline__ void loop_limit_hit() { atomicExch(&g_loop_limit_hit, 1); }
+static inline void loop_limit_reset(cudaStream_t st) {
+    const int z = 0;
+    RSG_CUDA(cudaMemcpyToSymbolAsync(g_loop_limit_hit, &z, sizeof(int), 0, cudaMemcpyHostToDevice,
+                                     st));
+}
+// After the stream has been synchronised: fails the call if a limit was hit.
+static inline void loop_limit_check(cudaStream_t st, const char *where) {
+    int h = 0;
+    RSG_CUDA(cudaMemcpyFromSymbolAsync(&h, g_loop_limit_hit, sizeof(int), 0,
+                                       cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    if (h) {
+        set_error(RSG_ERR_LIMIT, "%s: an iterative step (quickselect, Jacobi, parent walk or "
+                  "NFW concentration) hit its iteration limit", where);
+        throw Failure();
+    }
+}
+
 #define RSG_GROWING 1
 #define RSG_GC 4.30117902e-9          // src/universal_constants.h:4
 #define RSG_VMAX_CONST 6.55833746e-5  // src/universal_constants.h:6
@@ -17,6 +40,10 @@ struct DevCfg {
     double particle_mass, force_res, scale_now, initial_metric_scaling;
     double include_host_potential_ratio, fof_fraction;
     double thresh_dens[5], rvir_dens, rvir_dens_z0, dyn_time, om, ol, w0, wa;
+    // 100 * hubble_scaling(1/SCALE_NOW - 1) with SCALE_NOW rounded to float, as
+    // compute_kinetic_energy receives it (src/potential.c:194-199); evaluated on
+    // the host with the C library's pow/log/sqrt, as the reference does
+    double hub;
     int64_t min_halo_particles, bound_props, shape_iterations, weighted_shapes, exact_ll_calc;
 };
 
@@ -107,7 +134,11 @@ __device__ inline void jacobi3(double a[3][3], double eig[3], double v[3][3]) {
     }
     state += n;
     int guard = 0;
-    while (state && ++guard < 10000) {
+    while (state) {
+        if (++guard > 10000) {  // the reference's loop ends after a few sweeps
+            loop_limit_hit();
+            break;
+        }
         mx = fabs(a[0][maxc[0]]);
         int mr = 0;
         for (int i = 1; i < n - 1; i++)

@@ -13,19 +13,19 @@ struct LSeg {
     int32_t *pivot, *m, *q;
 };
 
-__global__ void k_ls_owner(const int32_t *start, const int32_t *n, int32_t *owner) {
+static __global__ void k_ls_owner(const int32_t *start, const int32_t *n, int32_t *owner) {
     int k = blockIdx.x;
     int s = start[k], c = n[k];
     for (int i = threadIdx.x; i < c; i += blockDim.x) owner[s + i] = k;
 }
-__global__ void k_ls_init(LSeg S, int32_t ns) {
+static __global__ void k_ls_init(LSeg S, int32_t ns) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ns) return;
     S.mn[k] = 0x7fffffff;
     S.mx[k] = (int32_t)0x80000000;
 }
 template <int ITEMS>
-__global__ void k_ls_minmax(const int32_t *lab, int64_t M, const int32_t *owner, LSeg S) {
+static __global__ void k_ls_minmax(const int32_t *lab, int64_t M, const int32_t *owner, LSeg S) {
     int64_t i0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * ITEMS;
     if (i0 >= M) return;
     int cur = -1, lo = 0x7fffffff, hi = (int)0x80000000;
@@ -54,13 +54,13 @@ __global__ void k_ls_minmax(const int32_t *lab, int64_t M, const int32_t *owner,
 }
 // pivot = min + (max - min) / 2 (src/fof.c:201); segments whose labels are
 // all equal are finished (no element is "big").
-__global__ void k_ls_pivot(LSeg S, int32_t ns) {
+static __global__ void k_ls_pivot(LSeg S, int32_t ns) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ns) return;
     int64_t lo = S.mn[k], hi = S.mx[k];
     S.pivot[k] = (lo == hi) ? 0x7fffffff : (int32_t)(lo + (hi - lo) / 2);
 }
-__global__ void k_ls_flags(const int32_t *lab, int64_t M, const int32_t *owner, LSeg S,
+static __global__ void k_ls_flags(const int32_t *lab, int64_t M, const int32_t *owner, LSeg S,
                            int32_t *flag) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i > M) return;
@@ -71,7 +71,7 @@ __global__ void k_ls_flags(const int32_t *lab, int64_t M, const int32_t *owner, 
     }
     flag[i] = f;
 }
-__global__ void k_ls_counts(LSeg S, int32_t ns, const int32_t *rank) {
+static __global__ void k_ls_counts(LSeg S, int32_t ns, const int32_t *rank) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ns) return;
     int s = S.start[k], n = S.n[k];
@@ -80,7 +80,7 @@ __global__ void k_ls_counts(LSeg S, int32_t ns, const int32_t *rank) {
     S.m[k] = m;
     S.q[k] = rank[s + m] - rank[s];
 }
-__global__ void k_ls_tables(int64_t M, const int32_t *owner, LSeg S, const int32_t *flag,
+static __global__ void k_ls_tables(int64_t M, const int32_t *owner, LSeg S, const int32_t *flag,
                             const int32_t *rank, int32_t *fb, int32_t *bs) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= M) return;
@@ -130,7 +130,7 @@ __global__ void k_ls_copy(int64_t M, const int32_t *owner, const T *src, T *dst,
     ldst[i] = lsrc[i];
 }
 // next round: both halves of every split segment with >= 2 elements
-__global__ void k_ls_next(LSeg S, int32_t ns, int32_t *ns_start, int32_t *ns_n, int32_t *flag) {
+static __global__ void k_ls_next(LSeg S, int32_t ns, int32_t *ns_start, int32_t *ns_n, int32_t *flag) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ns) return;
     int s = S.start[k], n = S.n[k], m = S.m[k];

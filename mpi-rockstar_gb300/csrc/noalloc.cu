@@ -1,7 +1,8 @@
-// 3D FOF of one bounded chunk that allocates nothing: every scratch buffer
-// of the device pipeline is carved from one fixed device array declared in
-// this file, the caller passes device buffers and a stream, and the host
-// side uses only the stack.
+// 3D FOF of one bounded chunk that allocates no device memory: every
+// scratch buffer of the device pipeline is carved from one fixed device
+// array declared in this file, and the caller passes device buffers and a
+// stream.  (The host side keeps a few small std::vector tables on the host
+// heap; no call here allocates or frees device memory.)
 //
 // Who needs it: an in-situ caller -- halo finding run inside an N-body
 // code's time step on the GPU that also holds the simulation -- owns the
@@ -11,16 +12,20 @@
 // streams at every call.  Such a caller cannot let the halo finder allocate
 // or free; it can afford a fixed, known amount of memory taken once.
 //
-// Setup: the first call on each device looks up the scratch array's device
-// address with cudaGetSymbolAddress (which also loads this file's module
-// and so reserves the array) and remembers it.  Make that first call before
-// any stream capture begins.  The call synchronises its stream before it
-// returns (it reads the group count back), so it is not meant to be
-// captured into a CUDA graph.
+// Setup: every call looks up the scratch array's device address for the
+// current device with cudaGetSymbolAddress, checks the return code and
+// passes that address on; nothing is cached, so the address stays right
+// when the caller resets the device or recreates its primary context.  The
+// first call in a process (and again after such a reset) loads the
+// library's kernels and the array itself, which takes device memory once;
+// make that call at setup, before any stream capture begins.  Later calls
+// take no device memory.  The call synchronises its stream before it
+// returns (it reads the group count back).
 //
 // Zero state: no part of the scratch has to start at zero.  Every buffer
 // carved from it is written, or cleared with cudaMemsetAsync on the
-// caller's stream, before it is read.
+// caller's stream, before it is read; the array keeps the last call's
+// contents.
 //
 // Overlap: the scratch is one array per device, shared by every caller in
 // the process.  Two calls that overlapped in time on one device would
@@ -44,24 +49,19 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n, const rsg_co
 static __device__ __align__(256) char g_fof_scratch[RSG_NOALLOC_SCRATCH_BYTES];
 
 #define RSG_NOALLOC_DEVICES 64
-static void *g_scratch_addr[RSG_NOALLOC_DEVICES];
-static std::mutex g_setup_mu;
 static std::mutex g_busy[RSG_NOALLOC_DEVICES];
 
-// Once per device: the scratch array's device address.
-static int scratch_for_device(int dev, void **out) {
-    std::lock_guard<std::mutex> g(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_fof_scratch);
-        if (e != cudaSuccess || !p) {
-            set_error(RSG_ERR_CUDA, "rsg_rockstar_fof_noalloc: cudaGetSymbolAddress: %s",
-                      cudaGetErrorString(e));
-            return RSG_ERR_CUDA;
-        }
-        g_scratch_addr[dev] = p;
+// The scratch array's device address on the current device, looked up at
+// every call (cheap once the module is loaded; never stale).
+static int scratch_for_device(void **out) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_fof_scratch);
+    if (e != cudaSuccess || !p) {
+        set_error(RSG_ERR_CUDA, "rsg_rockstar_fof_noalloc: cudaGetSymbolAddress: %s",
+                  cudaGetErrorString(e));
+        return RSG_ERR_CUDA;
     }
-    *out = g_scratch_addr[dev];
+    *out = p;
     return RSG_OK;
 }
 
@@ -120,15 +120,15 @@ extern "C" int rsg_rockstar_fof_noalloc(const struct rsg_particle *d_in, int64_t
                   RSG_NOALLOC_DEVICES);
         return RSG_ERR_ARGS;
     }
-    void *scratch = nullptr;
-    int rc = scratch_for_device(dev, &scratch);
-    if (rc) return rc;
     std::unique_lock<std::mutex> busy(g_busy[dev], std::try_to_lock);
     if (!busy.owns_lock()) {
         set_error(RSG_ERR_BUSY, "rsg_rockstar_fof_noalloc: another call is using device %d's scratch",
                   dev);
         return RSG_ERR_BUSY;
     }
+    void *scratch = nullptr;
+    int rc = scratch_for_device(&scratch);
+    if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     try {
         BorrowedArena B(scratch, RSG_NOALLOC_SCRATCH_BYTES);

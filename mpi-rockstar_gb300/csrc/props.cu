@@ -543,12 +543,6 @@ __global__ void k_po_gather(const PotRec *src, const uint32_t *perm, int64_t n, 
 }
 
 // ---- per-halo scans (src/properties.c:165-510) ---------------------------
-__device__ double hubble_scaling_d(const DevCfg &c, double z) {
-    double z1 = 1.0 + z, a = 1.0 / z1;
-    double we = (a != 1.0) ? c.w0 + c.wa - c.wa * (a - 1.0) / log(a) : c.w0;
-    return sqrt(c.om * (z1 * z1 * z1) + c.ol * pow(a, -3.0 * (1.0 + we)));
-}
-
 // calculate_corevel
 __device__ void corevel(rsg_halo &h, const PotRec *q, int64_t tot, const DevCfg &C) {
     double vel[3] = {0, 0, 0}, var[3] = {0, 0, 0}, tv, bv = 0;
@@ -589,8 +583,8 @@ __device__ void corevel(rsg_halo &h, const PotRec *q, int64_t tot, const DevCfg 
 // compute_kinetic_energy (src/potential.c:194-211)
 __device__ void kinetic(PotRec *q, int64_t n, const float *vc, const float *pc, float scale,
                         const DevCfg &C) {
-    double conv = 0.5 * (double)scale / RSG_GC, z1 = 1.0 / (double)scale;
-    double hub = 100.0 * hubble_scaling_d(C, z1 - 1.0);
+    double conv = 0.5 * (double)scale / RSG_GC;
+    double hub = C.hub;
     for (int64_t i = 0; i < n; i++) {
         if (q[i].ke < 0) continue;
         q[i].ke = 0;
@@ -601,6 +595,29 @@ __device__ void kinetic(PotRec *q, int64_t n, const float *vc, const float *pc, 
         }
         q[i].ke = (float)((double)q[i].ke * conv);
     }
+}
+
+// compute_kinetic_energy on its own (rsg_compute_kinetic_energy): records
+// are independent, one thread each, same arithmetic as kinetic().
+__global__ void k_kinetic_el(PotRec *q, int64_t n, float vc0, float vc1, float vc2, float pc0,
+                             float pc1, float pc2, float scale, double hub) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n || q[i].ke < 0) return;
+    const float vc[3] = {vc0, vc1, vc2}, pc[3] = {pc0, pc1, pc2};
+    double conv = 0.5 * (double)scale / RSG_GC;
+    float ke = 0;
+    for (int j = 0; j < 3; j++) {
+        double dv = (double)fsub(q[i].pos[j + 3], vc[j]) +
+                    hub * (double)scale * (double)fsub(q[i].pos[j], pc[j]);
+        ke = (float)((double)ke + dv * dv);
+    }
+    q[i].ke = (float)((double)ke * conv);
+}
+void kinetic_energy_device(PotRec *d, int64_t n, const float *vc, const float *pc, float scale,
+                           double hub, cudaStream_t st) {
+    launch(k_kinetic_el, nblk(n, 256), 256, 0, st, d, n, vc[0], vc[1], vc[2], pc[0], pc[1], pc[2],
+           scale, hub);
+    RSG_CHECK_LAUNCH();
 }
 
 __device__ inline bool unbound(const PotRec &r) { return r.pe < (double)r.ke; }
@@ -741,7 +758,11 @@ __device__ double c_to_f(double c) {
 }
 __device__ double f_to_c(double f) {
     double c = f, tc = c_to_f(c), nc;
-    for (int guard = 0; fabs((f - tc) / f) > 1e-7 && guard < 100000; guard++) {
+    for (int guard = 0; fabs((f - tc) / f) > 1e-7; guard++) {
+        if (guard >= 100000) {  // Newton steps converge in a handful of iterations
+            loop_limit_hit();
+            break;
+        }
         double tc2 = c_to_f(c + 0.1), slope = (tc2 - tc) / 0.1;
         nc = c + (f - tc) / slope;
         if (nc < 0) c /= 2;
@@ -1573,8 +1594,8 @@ __global__ void __launch_bounds__(RSG_SB) k_halo_scans_blk(rsg_halo *H, const rs
     float sn = (float)C.scale_now;
     const float *vc = (E[h].sub_of > -1) ? hh.corevel : hh.bulkvel;
     {
-        double conv = 0.5 * (double)sn / RSG_GC, z1 = 1.0 / (double)sn;
-        double hub = 100.0 * hubble_scaling_d(C, z1 - 1.0);
+        double conv = 0.5 * (double)sn / RSG_GC;
+        double hub = C.hub;
         float vv[3] = {vc[0], vc[1], vc[2]}, pp[3] = {hh.pos[0], hh.pos[1], hh.pos[2]};
         for (int64_t i = threadIdx.x; i < tot; i += blockDim.x) {
             if (q[i].ke < 0) continue;
@@ -1919,6 +1940,7 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
     size_t mark = ar.used;
     int *err = ar.get<int>(2);
     RSG_CUDA(cudaMemsetAsync(err, 0, 8, st));
+    loop_limit_reset(st);
     unsigned long long *work = ar.get<unsigned long long>(4);
     RSG_CUDA(cudaMemsetAsync(work, 0, 32, st));
     int32_t *tot = ar.get<int32_t>(NH + 1), *nseg = ar.get<int32_t>(NH + 1);
@@ -1987,12 +2009,16 @@ void additional_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, const Rec
         if (npo)
             RSG_CUDA(cudaMemcpyAsync(g_dbg_po.data(), PO2, sizeof(PotRec) * npo,
                                      cudaMemcpyDeviceToHost, st));
+    } else if (!g_dbg_po.empty()) {
+        // the switch went off since this thread's last kept call
+        std::vector<PotRec>().swap(g_dbg_po);
     }
     int herr[2];
     unsigned long long hwork[4];
     RSG_CUDA(cudaMemcpyAsync(herr, err, 8, cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaMemcpyAsync(hwork, work, 32, cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
+    loop_limit_check(st, "halo properties");
     int64_t *S = last_stats();
     S[RSG_STAT_POT_RECORDS] = npo;
     S[RSG_STAT_KEPT_BIG] = (int64_t)hwork[0];

@@ -344,8 +344,8 @@ __global__ void __launch_bounds__(RSG_CT) k_sg_kinetic(const Chunk *CH, PotRec *
     const rsg_halo &hh = H[c.halo];
     float sn = (float)C.scale_now;
     const float *vc = (E[c.halo].sub_of > -1) ? hh.corevel : hh.bulkvel;
-    double conv = 0.5 * (double)sn / RSG_GC, z1 = 1.0 / (double)sn;
-    double hub = 100.0 * hubble_scaling_d(C, z1 - 1.0);
+    double conv = 0.5 * (double)sn / RSG_GC;
+    double hub = C.hub;
     float vv[3] = {vc[0], vc[1], vc[2]}, pp[3] = {hh.pos[0], hh.pos[1], hh.pos[2]};
     for (int k = threadIdx.x; k < c.n; k += RSG_CT) {
         PotRec &q = PO[c.start + k];

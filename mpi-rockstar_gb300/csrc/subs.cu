@@ -25,14 +25,16 @@
 #include "kdtree_impl.cuh"
 #include "lsort.cuh"
 #include "subs.cuh"
+#include "uflabels.cuh"
 
 // Ranges up to this size are summed by one thread in array order, so FP64
 // sums round exactly as the reference's sequential loops do.
 #define RSG_SEQ_MAX 65536
 // Below this size one thread does all of a node's or halo's work.
 #define RSG_SMALL 2048
-// Nodes up to this size replay their union-find in shared memory.
-#define RSG_REPLAY_SMEM 24576
+// MAX_PARTICLES_TO_SAMPLE (src/groupies.c:286): larger subgroups draw their
+// linking-length sample by array position.
+#define RSG_SAMPLE_MAX 10000
 
 namespace rsg {
 
@@ -185,14 +187,14 @@ __global__ void k_norm_warp(Rec *W, HierNodes N, int32_t base, int32_t count, in
 // Mid-size nodes: the block stages particles in shared memory and computes
 // the per-particle products; thread 0 adds them in array order.
 __global__ void __launch_bounds__(256) k_norm_blk(Rec *W, HierNodes N, int32_t base, int level0,
-                                                  double ims, double *sig, int seq_max) {
+                                                  double ims, double *sig, int lo, int hi) {
     __shared__ float q[256][6];
     __shared__ float pr[256][21];
     __shared__ double mean[6], corr[21];
     int k = blockIdx.x;
     int node = base + k;
     int s = N.start[node], n = N.n[node];
-    if (n <= RSG_SMALL || n > seq_max) return;
+    if (n <= lo || n > hi) return;
     // lane d of warp 0 owns the running sum of coordinate d
     double a = 0;
     for (int b0 = 0; b0 < n; b0 += 256) {
@@ -242,11 +244,13 @@ struct NChunk {
 struct NPart {
     double d[21];
 };
-__global__ void k_nch_count(HierNodes N, int32_t base, int32_t cnt, int chunk, int32_t *nch) {
+__global__ void k_nch_count(HierNodes N, int32_t base, int32_t cnt, int chunk, int seq_lo,
+                            int seq_hi, int32_t *nch) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > cnt) return;
     int n = (k < cnt) ? N.n[base + k] : 0;
-    nch[k] = (n > RSG_SMALL) ? (n + chunk - 1) / chunk : 0;
+    bool seq = n > seq_lo && n <= seq_hi;  // summed in order by k_norm_blk instead
+    nch[k] = (n > RSG_SMALL && !seq) ? (n + chunk - 1) / chunk : 0;
 }
 __global__ void k_nch_fill(HierNodes N, int32_t base, int32_t cnt, int chunk, const int32_t *nch,
                            const int32_t *c0, NChunk *C) {
@@ -553,7 +557,10 @@ __device__ float median_r(float *a, int nt, unsigned seed, float frac) {
         if (kk == p || (a[left] == a[right - 1])) return a[kk];
         if (kk < p) right = p;
         else left = p + 1;
-        if (++guard > 100000000) return a[kk];
+        if (++guard > 100000000) {  // cannot happen for finite input: report it
+            loop_limit_hit();
+            return a[kk];
+        }
     }
 }
 // Nodes whose sample fits in shared memory (RSG_TARGET_SMEM distances): one
@@ -572,59 +579,6 @@ __global__ void k_target_smem(HierNodes N, int32_t base, const int32_t *soff, co
     __syncthreads();
     if (threadIdx.x == 0) N.target_r[node] = median_r(a_s, nt, seed_in[k], frac);
 }
-// Batched form: the sample's floor(nt * FOF_FRACTION)-th smallest distance by
-// an 8-bit-per-pass radix select on the distances' order-preserving bit
-// patterns, in shared memory, one block per node.  This is the exact order
-// statistic; the reference's quickselect returns the same value except when
-// its early exit (equal first and last elements of the range) fires on a
-// range that is not constant.
-__global__ void __launch_bounds__(256) k_target_rs(HierNodes N, int32_t base, const int32_t *soff,
-                                                   const float *prad, float frac, int exact) {
-    extern __shared__ unsigned ks[];
-    __shared__ int hist[256];
-    __shared__ unsigned pre_s;
-    __shared__ int rank_s;
-    int k = blockIdx.x;
-    int node = base + k;
-    int n = N.n[node];
-    int nt = exact ? n : (n < 10000 ? n : 10000);
-    if (nt > RSG_TARGET_SMEM || nt < 1) return;
-    const float *a = prad + soff[k];
-    if (nt < 2) {
-        if (threadIdx.x == 0) N.target_r[node] = a[0];
-        return;
-    }
-    for (int i = threadIdx.x; i < nt; i += blockDim.x) ks[i] = f2ord(a[i]);
-    int64_t kk = (int64_t)__float2ll_rz(fmul(__ll2float_rn(nt), frac));
-    if (kk > nt - 1) kk = nt - 1;
-    if (threadIdx.x == 0) {
-        pre_s = 0;
-        rank_s = (int)kk;
-    }
-    unsigned mask = 0;
-    for (int shift = 24; shift >= 0; shift -= 8) {
-        hist[threadIdx.x] = 0;
-        __syncthreads();
-        unsigned pre = pre_s;
-        for (int i = threadIdx.x; i < nt; i += blockDim.x)
-            if ((ks[i] & mask) == pre) atomicAdd(&hist[(ks[i] >> shift) & 255u], 1);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int cum = 0, rank = rank_s;
-            for (int b = 0; b < 256; b++) {
-                if (cum + hist[b] > rank) {
-                    pre_s = pre | ((unsigned)b << shift);
-                    rank_s = rank - cum;
-                    break;
-                }
-                cum += hist[b];
-            }
-        }
-        mask |= 255u << shift;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) N.target_r[node] = ord2f(pre_s);
-}
 // Larger samples (EXACT_LL_CALC): in place in global memory.
 __global__ void k_target(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
                          float *prad, const unsigned *seed_in, float frac, int exact) {
@@ -642,6 +596,18 @@ __global__ void k_fill_eln(HierNodes N, int32_t base, int32_t *eln) {
     int k = blockIdx.x;
     int s = N.start[base + k], n = N.n[base + k];
     for (int i = threadIdx.x; i < n; i += blockDim.x) eln[s + i] = k;
+}
+
+// The level's element map split by node size: nodes above thr into ex,
+// the others into eu (-1 elsewhere).
+__global__ void k_split_eln(const int32_t *eln, int64_t M, HierNodes N, int32_t base, int thr,
+                            int32_t *ex, int32_t *eu) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int k = eln[i];
+    bool big = k >= 0 && N.n[base + k] > thr;
+    ex[i] = big ? k : -1;
+    eu[i] = (k >= 0 && !big) ? k : -1;
 }
 
 __device__ __forceinline__ int uf_find2(int *par, int x) {
@@ -677,7 +643,7 @@ template <int MODE>
 __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec *W, int64_t M,
                                                 HierNodes N, int32_t base, const int32_t *eln,
                                                 const int32_t *noff, int32_t *ncnt, int32_t *nbr,
-                                                int *par, int *err) {
+                                                int *par, int *err, unsigned long long *near) {
     const unsigned FULL = 0xffffffffu;
     int64_t w0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * 32;
     int lane = threadIdx.x & 31;
@@ -713,11 +679,17 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
                     float q[6];
 #pragma unroll
                     for (int d = 0; d < 6; d++) q[d] = W[j].pos[d];
-                    if (need && j > i && dist6(c, q) < r2) {
+                    float d = dist6(c, q);
+                    if (need && j > i && d < r2) {
                         if (MODE == 1) nbr[o + cnt] = j;
                         if (MODE == 2) uf_unite2(par, i, j);
                         cnt++;
                     }
+                    // pairs within 1e-6 of the linking length (relative, in
+                    // distance): where a last-bit change of a coordinate
+                    // could decide the link
+                    if (MODE != 0 && need && j > i && fabsf(d - r2) <= 2e-6f * r2)
+                        atomicAdd(near, 1ull);
                 }
                 continue;
             }
@@ -732,117 +704,11 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
     if (MODE == 0 && valid && k >= 0) ncnt[i] = cnt;
 }
 
-// Union-find labels exactly as link_particle_to_fof / merge_smallfofs build
-// them (src/fof.c:46-170): particles in array order, a new set takes the
-// next integer, and when a link's set meets the current set the link's root
-// survives.  Sequential per node (one thread), so the labels -- and thus the
-// partition order and the subgroup order -- are the reference's.
-__device__ __forceinline__ int sf_find(int32_t *R, int a) {
-    int r = a;
-    while (R[r] != r) r = R[r];
-    while (R[a] != r) {
-        int nx = R[a];
-        R[a] = r;
-        a = nx;
-    }
-    return r;
-}
-__global__ void k_replay6(HierNodes N, int32_t base, int32_t count, const int32_t *noff,
-                          const int32_t *nbr, int32_t *lab, int32_t *R) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    int node = base + k;
-    int s = N.start[node], n = N.n[node];
-    if (n > RSG_SMALL && n <= RSG_REPLAY_SMEM) return;
-    int32_t *RR = R + s;
-    int nsf = 0;
-    for (int i = s; i < s + n; i++) lab[i] = -1;
-    for (int i = s; i < s + n; i++) {
-        int e0 = noff[i], e1 = noff[i + 1];
-        if (e0 == e1) continue;
-        int f = lab[i];
-        if (f < 0) {
-            for (int e = e0; e < e1; e++)
-                if (lab[nbr[e]] != -1) {
-                    f = lab[nbr[e]];
-                    break;
-                }
-            if (f < 0) {
-                f = nsf++;
-                RR[f] = f;
-            }
-        }
-        for (int e = e0 - 1; e < e1; e++) {
-            int j = (e < e0) ? i : nbr[e];
-            if (lab[j] == -1) {
-                lab[j] = f;
-            } else {
-                int rl = sf_find(RR, lab[j]), rc = sf_find(RR, f);
-                if (rl != rc) RR[rc] = rl;
-            }
-        }
-    }
-    for (int i = s; i < s + n; i++)
-        if (lab[i] >= 0) lab[i] = sf_find(RR, lab[i]);
-}
-
-// The same replay for mid-size nodes with the label and root arrays in
-// shared memory (one block per node, thread 0 replays, the block loads and
-// stores).
-__global__ void k_replay6_smem(HierNodes N, int32_t base, const int32_t *noff,
-                               const int32_t *nbr, int32_t *lab_out) {
-    extern __shared__ int32_t sm_i[];
-    int k = blockIdx.x;
-    int node = base + k;
-    int s = N.start[node], n = N.n[node];
-    if (n <= RSG_SMALL || n > RSG_REPLAY_SMEM) return;
-    int32_t *lab = sm_i, *RR = sm_i + n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) lab[i] = -1;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int nsf = 0;
-        for (int i = 0; i < n; i++) {
-            int e0 = noff[s + i], e1 = noff[s + i + 1];
-            if (e0 == e1) continue;
-            int f = lab[i];
-            if (f < 0) {
-                for (int e = e0; e < e1; e++)
-                    if (lab[nbr[e] - s] != -1) {
-                        f = lab[nbr[e] - s];
-                        break;
-                    }
-                if (f < 0) {
-                    f = nsf++;
-                    RR[f] = f;
-                }
-            }
-            for (int e = e0 - 1; e < e1; e++) {
-                int j = (e < e0) ? i : nbr[e] - s;
-                if (lab[j] == -1) {
-                    lab[j] = f;
-                } else {
-                    int rl = sf_find(RR, lab[j]), rc = sf_find(RR, f);
-                    if (rl != rc) RR[rc] = rl;
-                }
-            }
-        }
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        int l = lab[i];
-        if (l >= 0) {
-            int r = l;
-            while (RR[r] != r) r = RR[r];
-            l = r;
-        }
-        lab_out[s + i] = l;
-    }
-}
-
-// Batched mode: subgroup labels from the parallel union-find of k_fof6_w<2>
-// (components are the same sets; the label is the component's first
-// position, -1 for particles without links), so the partition order is
-// deterministic but not the reference's.
+// Batched form, nodes up to the sample size: subgroup labels from the
+// parallel union-find of k_fof6_w<2> (components are the same sets; the
+// label is the component's first position, -1 for particles without links).
+// The order this gives is deterministic but not the reference's, which only
+// matters where a child subgroup samples its linking length by position.
 __global__ void k_uf6_size(const int32_t *eln, int64_t M, int *par, int *root, int *size) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= M || eln[i] < 0) return;
@@ -1465,7 +1331,11 @@ __global__ void k_asc_assign_p(const Rec *W, int64_t M, const int32_t *eln, Hier
         }
     }
     int h = bh;
-    for (int guard = 0; guard < 100000 && E[h].sub_of > -1; guard++) {
+    for (int guard = 0; E[h].sub_of > -1; guard++) {
+        if (guard >= 100000) {  // sub_of links form a forest: deeper means a cycle
+            loop_limit_hit();
+            break;
+        }
         if (pdist(H[h], pos) > E[h].max_metric) h = (int)E[h].sub_of;
         else break;
     }
@@ -2257,6 +2127,15 @@ static int32_t select_flagged(Arena &ar, const int32_t *flag, int32_t *out, int6
     return h;
 }
 
+// 100 hubble_scaling(1/a - 1) for a float scale factor (src/hubble.c:8-19
+// with src/potential.c:197-199), in host double arithmetic.
+double hubble100(const rsg_config &c, float scale) {
+    double z1 = 1.0 / (double)scale, z = z1 - 1.0;
+    double zz1 = 1.0 + z, a = 1.0 / zz1;
+    double we = (a != 1.0) ? c.w0 + c.wa - c.wa * (a - 1.0) / log(a) : c.w0;
+    return 100.0 * sqrt(c.om * (zz1 * zz1 * zz1) + c.ol * pow(a, -3.0 * (1.0 + we)));
+}
+
 DevCfg make_devcfg(const rsg_config &c) {
     DevCfg d;
     d.particle_mass = c.particle_mass;
@@ -2273,6 +2152,7 @@ DevCfg make_devcfg(const rsg_config &c) {
     d.ol = c.ol;
     d.w0 = c.w0;
     d.wa = c.wa;
+    d.hub = hubble100(c, (float)c.scale_now);
     d.min_halo_particles = c.min_halo_particles;
     d.bound_props = c.bound_props;
     d.shape_iterations = c.shape_iterations;
@@ -2310,8 +2190,16 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     SubsOut out{0};
     last_stats()[RSG_STAT_6D_ITEMS] = 0;
     last_stats()[RSG_STAT_6D_SAMPLES] = 0;
-    // ordered (bit-exact) FP64 sums up to this size; tree reductions above
-    const int seq_max = exact ? RSG_SEQ_MAX : RSG_SMALL;
+    last_stats()[RSG_STAT_NEAR_6D] = 0;
+    // Nodes whose subgroups must come out in the reference's order: all of
+    // them in the plain form; in the batched form those larger than the
+    // linking-length sample, whose children can be sampled by position
+    // (src/groupies.c:295-308), unless EXACT_LL_CALC takes every particle.
+    const int xthr = exact ? 0 : (cfg.exact_ll_calc ? INT_MAX : RSG_SAMPLE_MAX);
+    // norm_sd sums in array order (bit-exact) for nodes in (seq_lo,
+    // RSG_SEQ_MAX]; the batched form keeps its parallel sums below xthr
+    const int seq_lo = exact ? RSG_SMALL : RSG_SAMPLE_MAX;
+    const int seq_max = RSG_SEQ_MAX;
     const int T = 256;
     // groups with particles, their working offsets
     std::vector<int64_t> goff, gsz, woff;
@@ -2360,6 +2248,9 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     int32_t *hflag = ar.get<int32_t>(M + 1);
     int *err = ar.get<int>(4);
     RSG_CUDA(cudaMemsetAsync(err, 0, 16, st));
+    loop_limit_reset(st);
+    unsigned long long *near = ar.get<unsigned long long>(1);
+    RSG_CUDA(cudaMemsetAsync(near, 0, sizeof(unsigned long long), st));
     phase_mark(st, "");
     launch(k_make_w, nblk(M, T), T, 0, st, (const rsg_particle *)d_p, G, (const int64_t *)d_goff,
            (const int64_t *)d_woff, M, W, wgroup);
@@ -2391,14 +2282,14 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                 launch(k_norm_warp, nblk((int64_t)cnt * 32, 256), 256, 0, st, W, N, base, cnt,
                        L == 0, cfg.initial_metric_scaling, sig);
             launch(k_norm_blk, cnt, 256, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig,
-                   seq_max);
+                   seq_lo, RSG_SEQ_MAX);
             if (exact) {
                 launch(k_norm_par, cnt, T, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling,
                        sig, seq_max);
             } else {
                 int32_t *nch = ar.get<int32_t>(cnt + 1), *c0 = ar.get<int32_t>(cnt + 1);
                 launch(k_nch_count, nblk(cnt + 1, T), T, 0, st, N, base, cnt, tuning().norm_chunk,
-                       nch);
+                       seq_lo, RSG_SEQ_MAX, nch);
                 int32_t nc = excl_scan(ar, (const int32_t *)nch, c0, cnt + 1, st);
                 if (nc > 0) {
                     NChunk *C = ar.get<NChunk>(nc);
@@ -2456,52 +2347,64 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                 int nt = cfg.exact_ll_calc ? hn[k] : (hn[k] < 10000 ? hn[k] : 10000);
                 if (nt <= RSG_TARGET_SMEM && nt > ntmax) ntmax = nt;
             }
-            if (exact)
-                launch(k_target_smem, cnt, 64, (size_t)4 * (ntmax > 0 ? ntmax : 1), st, N, base,
-                       (const int32_t *)soff, (const float *)prad, (const unsigned *)seeds,
-                       (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
-            else
-                launch(k_target_rs, cnt, 256, (size_t)4 * (ntmax > 0 ? ntmax : 1), st, N, base,
-                       (const int32_t *)soff, (const float *)prad, (float)cfg.fof_fraction,
-                       (int)cfg.exact_ll_calc);
+            // both forms: the reference's quickselect with its early exit, whose
+            // value can differ from the exact order statistic when the sample
+            // holds equal distances (mutual nearest neighbours)
+            launch(k_target_smem, cnt, 64, (size_t)4 * (ntmax > 0 ? ntmax : 1), st, N, base,
+                   (const int32_t *)soff, (const float *)prad, (const unsigned *)seeds,
+                   (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
             launch(k_target, nblk(cnt, 32), 32, 0, st, N, base, cnt, soff, prad, seeds,
                    (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
         }
         phase_mark(st, "d.nn_target");
-        if (exact) {
+        // subgroup labels: the reference's union-find labels (uflabels.cuh) for
+        // the nodes above xthr, then its partition sort by label; a parallel
+        // union-find for the others, regrouped by a stable sort on the labels
+        std::vector<int32_t> xs, xn;
+        int nsmall = 0;
+        for (int k = 0; k < cnt; k++) {
+            if (hn[k] > xthr) {
+                xs.push_back(hs[k]);
+                xn.push_back(hn[k]);
+            } else {
+                nsmall++;
+            }
+        }
+        const int32_t *elnx = eln, *elnu = eln;
+        if (!xs.empty() && nsmall) {
+            int32_t *ex = ar.get<int32_t>(M), *eu = ar.get<int32_t>(M);
+            launch(k_split_eln, nblk(M, T), T, 0, st, (const int32_t *)eln, M, N, base, xthr, ex, eu);
+            elnx = ex;
+            elnu = eu;
+        }
+        if (!xs.empty()) {
             // later neighbours within target_r, as CSR lists
             int32_t *ncnt = par, *noff = root;
             RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
-            launch(k_fof6_w<0>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
-                   (const int32_t *)nullptr, ncnt, (int32_t *)nullptr, (int *)nullptr, err);
+            launch(k_fof6_w<0>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, elnx,
+                   (const int32_t *)nullptr, ncnt, (int32_t *)nullptr, (int *)nullptr, err, near);
             check_i32_total(ar, ncnt, M + 1, "6D neighbour lists", st);
             int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
             int32_t *nbr = ar.get<int32_t>(ne + 1);
-            launch(k_fof6_w<1>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
-                   (const int32_t *)noff, ncnt, nbr, (int *)nullptr, err);
+            launch(k_fof6_w<1>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, elnx,
+                   (const int32_t *)noff, ncnt, nbr, (int *)nullptr, err, near);
             phase_mark(st, "d.fof6d");
-            // reference labels, then the reference's partition sort by label
-            launch(k_replay6, nblk(cnt, 32), 32, 0, st, N, base, cnt, noff, nbr, phalo, csize);
-            static bool attr = false;
-            if (!attr) {
-                RSG_CUDA(cudaFuncSetAttribute(k_replay6_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              8 * RSG_REPLAY_SMEM));
-                attr = true;
-            }
-            launch(k_replay6_smem, cnt, 128, (size_t)8 * RSG_REPLAY_SMEM, st, N, base, noff, nbr, phalo);
-        } else {
-            int *ufp = csize, *ufr = key2 ? (int *)key2 : nullptr, *ufs = (int *)val2;
+            exact_labels_csr(ar, M, elnx, N.start + base, noff, nbr, phalo, st);
+        }
+        if (nsmall) {
+            int *ufp = csize, *ufr = (int *)key2, *ufs = (int *)val2;
             launch(k_init_par, nblk(M, T), T, 0, st, eln, M, ufp, ufs);
-            launch(k_fof6_w<2>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
-                   (const int32_t *)nullptr, (int32_t *)nullptr, (int32_t *)nullptr, ufp, err);
+            launch(k_fof6_w<2>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, elnu,
+                   (const int32_t *)nullptr, (int32_t *)nullptr, (int32_t *)nullptr, ufp, err, near);
             phase_mark(st, "d.fof6d");
-            launch(k_uf6_size, nblk(M, T), T, 0, st, eln, M, ufp, ufr, ufs);
-            launch(k_uf6_label, nblk(M, T), T, 0, st, eln, M, ufr, ufs, phalo);
+            launch(k_uf6_size, nblk(M, T), T, 0, st, elnu, M, ufp, ufr, ufs);
+            launch(k_uf6_label, nblk(M, T), T, 0, st, elnu, M, ufr, ufs, phalo);
         }
         RSG_CHECK_LAUNCH();
-        phase_mark(st, "d.replay");
-        if (exact) partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
-        else label_sort_stable(ar, W, phalo, eln, N, base, cnt, M, st);
+        phase_mark(st, "d.labels");
+        if (!xs.empty()) partition_sort_labels<Rec>(ar, W, phalo, M, xs, xn, st);
+        // leaves the partition-sorted nodes as they are (they are in label order)
+        if (nsmall) label_sort_stable(ar, W, phalo, eln, N, base, cnt, M, st);
         phase_mark(st, "d.psort");
         launch(k_run_heads, nblk(M, T), T, 0, st, eln, M, N, base, phalo, hflag);
         int32_t *heads = ar.get<int32_t>(M);
@@ -2655,12 +2558,16 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     launch(k_write_back, nblk(M, T), T, 0, st, W, M, wgroup, d_goff, d_woff, Pcopy, d_p);
     RSG_CHECK_LAUNCH();
     int herr[4];
+    unsigned long long hnear = 0;
     RSG_CUDA(cudaMemcpyAsync(herr, err, 16, cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaMemcpyAsync(&hnear, near, sizeof(hnear), cudaMemcpyDeviceToHost, st));
     RSG_CUDA(cudaStreamSynchronize(st));
     if (herr[0]) {
         set_error(RSG_ERR_LIMIT, "6D kd-tree traversal stack overflow");
         throw Failure();
     }
+    loop_limit_check(st, "find_subs");
+    last_stats()[RSG_STAT_NEAR_6D] = (int64_t)hnear;
     out.nhalos = NH;
     return out;
 }

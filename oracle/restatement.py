@@ -23,7 +23,7 @@ def build(force=False):
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-std=c99", "-D_DEFAULT_SOURCE", "-ffp-contract=off",
+    subprocess.check_call(["gcc", "-O3", "-std=c99", "-D_DEFAULT_SOURCE", "-ffp-contract=off",
                            "-fno-math-errno", "-fPIC", "-shared", "-o", tmp, SRC, "-lm"])
     os.replace(tmp, LIB)
     return LIB
@@ -130,3 +130,13 @@ def hierarchy():
     tr = np.zeros(cap, np.float32)
     k = min(lib().oracle_hierarchy(lv.ctypes.data, n.ctypes.data, tr.ctypes.data, cap), cap)
     return lv[:k].copy(), n[:k].copy(), tr[:k].copy()
+
+
+def kinetic_energy(po, vel_cen, pos_cen, scale_now):
+    """compute_kinetic_energy on a copy of the records (cosmology from setup)."""
+    po = np.array(po, dtype=L.POTENTIAL, copy=True)
+    vc = np.ascontiguousarray(vel_cen, np.float32)
+    pc = np.ascontiguousarray(pos_cen, np.float32)
+    lib().oracle_kinetic_energy(po.ctypes.data, len(po), vc.ctypes.data, pc.ctypes.data,
+                                C.c_float(scale_now))
+    return po

@@ -1,6 +1,8 @@
 """3D FOF on the GPU against the C restatement of the reference (which is
 itself pinned bit-exact to the reference sources): kd-tree permutations
-element for element, FOF partitions identical as sets."""
+element for element, and rockstar()'s whole output -- the permuted particle
+array (its union-find labels decide the order through the partition sort)
+and the group offsets and sizes -- byte for byte."""
 import numpy as np
 import pytest
 
@@ -41,8 +43,9 @@ def test_fof_partition(rk, oracle, cfg, scale):
     assert len(rg[0]) == len(ro[0])
     assert len(rg[1]) == len(ro[1])
     assert np.array_equal(canon_partition(*rg), canon_partition(*ro))
-    # every particle is present exactly once
-    assert np.array_equal(np.sort(rg[0]["id"]), np.sort(ro[0]["id"]))
+    # the reference's permutation and group table, byte for byte
+    assert rg[0].tobytes() == ro[0].tobytes()
+    assert np.array_equal(rg[1], ro[1]) and np.array_equal(rg[2], ro[2])
 
 
 def test_fof_duplicates(rk, oracle):
@@ -57,12 +60,13 @@ def test_fof_duplicates(rk, oracle):
     ro = oracle.fof(p)
     rg = rk.rockstar_fof(p, c)
     assert len(rg[0]) == len(ro[0]) < len(p)
-    assert np.array_equal(np.sort(rg[0]["id"]), np.sort(ro[0]["id"]))
-    assert np.array_equal(canon_partition(*rg), canon_partition(*ro))
+    assert rg[0].tobytes() == ro[0].tobytes()
+    assert np.array_equal(rg[1], ro[1]) and np.array_equal(rg[2], ro[2])
 
 
-def test_fof_empty_and_tiny(rk):
+def test_fof_empty_and_tiny(rk, oracle):
     c = rk.Config()
+    oracle.setup(c)
     for n in (0, 1, 2, 15):
         p = np.zeros(n, rk.PARTICLE)
         p["id"] = np.arange(n)
@@ -70,6 +74,31 @@ def test_fof_empty_and_tiny(rk):
         out, off, sz = rk.rockstar_fof(p, c)
         assert len(out) == n
         assert (len(off) == 1) == (n >= 10)
+        ro = oracle.fof(p)
+        assert out.tobytes() == ro[0].tobytes() and np.array_equal(off, ro[1])
+
+
+@pytest.mark.parametrize("n_groups", [1, 40])
+def test_fof_small_groups_interleaved(rk, oracle, n_groups):
+    """Clumps of 2 to 30 particles: groups below MIN_HALO_PARTICLES stay in
+    the permuted array between the kept ones, as the partition sort leaves
+    them, and only the kept ones are listed."""
+    rng = np.random.default_rng(11 + n_groups)
+    sizes = rng.integers(2, 31, size=n_groups)
+    centres = rng.uniform(1, 39, size=(n_groups, 3))
+    pos = np.concatenate([cen + rng.normal(0, 0.004, size=(k, 3)) for cen, k in zip(centres, sizes)]
+                         + [rng.uniform(0, 40, size=(3000, 3))])
+    p = np.zeros(len(pos), rk.PARTICLE)
+    p["id"] = np.arange(len(pos))
+    p["pos"][:, :3] = pos.astype(np.float32)
+    p["pos"][:, 3:] = rng.normal(0, 100, size=(len(pos), 3)).astype(np.float32)
+    c = rk.Config(particle_mass=1e9, box_size=40.0, total_particles=len(p))
+    oracle.setup(c)
+    ro = oracle.fof(p)
+    rg = rk.rockstar_fof(p, c)
+    assert rg[0].tobytes() == ro[0].tobytes()
+    assert np.array_equal(rg[1], ro[1]) and np.array_equal(rg[2], ro[2])
+    assert (rg[2] >= c.min_halo_particles).all()
 
 
 @pytest.mark.parametrize("cfg_id,scale,parts", [(2, 0.25, 4), (3, 0.01, 7)])

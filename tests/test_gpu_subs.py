@@ -1,12 +1,22 @@
 """find_subs on the GPU against the reference.
 
 Golden fixtures (tests/golden/*.npz, made by tests/golden/make_golden.py
-from the reference sources compiled as-is) hold the reference's FOF groups
-and the halos find_subs makes from them.  The GPU runs find_subs on the
-same groups in the same particle order; halos are matched by particle
-membership and their fields compared with a relative tolerance of 1e-4.
-Larger cases compare with the C restatement (pinned to the reference by
-tests/test_golden_oracle.py)."""
+from the reference sources compiled as-is, on x86) hold the reference's FOF
+groups and the halos find_subs makes from them.  The GPU runs find_subs on
+the same groups in the same particle order; halos are matched by particle
+membership, every integer field and every extra_halo_info link is compared
+exactly, and float fields with a relative tolerance of 1e-4 (the x86 long
+double of the reference's Jacobi step moves the shape fields in their last
+bits).  Against the C restatement built on the same machine (pinned to the
+reference by tests/test_golden_oracle.py) the plain form is compared byte
+for byte: permuted particles, halos (NaN payloads aside: halos without
+particles carry 0/0 values whose sign bit is the platform's) and links.
+
+The batched form must give the same halo membership; its FP64 sums run in
+another order, so a few of the reference's discrete choices that compare
+nearly equal running values (the core-velocity minimum, the 1% shape
+convergence rule) can go the other way.  Those halos are counted and the
+count is bounded."""
 import hashlib
 import os
 
@@ -18,6 +28,19 @@ import halo_compare as HC
 pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 TOL = 1e-4
+# batched form: halos whose fields may leave 1e-4 through a flipped
+# near-tie (see the module docstring), as a fraction of the matched halos
+BATCHED_FLIP_FRAC = 0.05
+
+
+def canon_nan(a):
+    """Copy of a structured array with every float NaN set to one bit pattern."""
+    b = a.copy()
+    for f in b.dtype.names:
+        if b.dtype[f].base.kind == "f":
+            v = b[f]
+            v[np.isnan(v)] = np.nan
+    return b
 
 
 def load_case(rk, name):
@@ -39,9 +62,12 @@ def test_find_subs_golden(rk, name):
     assert len(gh) == len(H)
     ref_sets = HC.sets_from_labels(z["halo_of"].astype(np.int64))
     got_sets = HC.halo_sets(parts, gh)
-    ua, ub, worst, bad = HC.compare(ref_sets, H, got_sets, gh, TOL)
+    ua, ub, worst, bad = HC.compare(ref_sets, H, got_sets, gh, TOL, ref_E=E, got_E=ge)
     assert ua == 0 and ub == 0, "halo membership differs (%d ref / %d gpu unmatched)" % (ua, ub)
     assert not bad, "fields beyond %g: %s" % (TOL, bad[:10])
+    # same halo order as the reference: the links compare as stored
+    for f in HC.LINK_FIELDS:
+        assert np.array_equal(ge[f], E[f]), f
 
 
 @pytest.mark.parametrize("cfg,scale", [(1, 1.0), (2, 1 / 16), (3, 0.002), (4, 1 / 2048),
@@ -61,36 +87,81 @@ def test_find_subs_oracle(rk, oracle, cfg, scale):
     assert a == b
     assert len(go[1]) == len(ro[1])
     ua, ub, worst, bad = HC.compare(HC.halo_sets(ro[0], ro[1]), ro[1],
-                                    HC.halo_sets(go[0], go[1]), go[1], TOL)
+                                    HC.halo_sets(go[0], go[1]), go[1], TOL, ref_E=ro[2],
+                                    got_E=go[2])
     assert ua == 0 and ub == 0
     assert not bad, bad[:10]
+    # bit for bit: permuted particles, halos, links
+    assert go[0].tobytes() == ro[0].tobytes()
+    assert canon_nan(go[1]).tobytes() == canon_nan(ro[1]).tobytes()
+    assert go[2].tobytes() == ro[2].tobytes()
 
 
-@pytest.mark.parametrize("name", ["c1_tiny", "c1_q", "c3_t"])
+def check_batched(ref_sets, ref_H, ref_E, parts, gh, ge):
+    """Identical halo membership; halos over the tolerance (any field, int,
+    link) at most BATCHED_FLIP_FRAC of the matched ones."""
+    got_sets = HC.halo_sets(parts, gh)
+    ua, ub, worst, bad = HC.compare(ref_sets, ref_H, got_sets, gh, TOL, ref_E=ref_E, got_E=ge)
+    assert ua == 0 and ub == 0, "membership differs: %d particles" % HC.membership_diff(
+        ref_sets, got_sets)
+    flipped = {h for _, h, _ in bad}
+    assert len(flipped) <= BATCHED_FLIP_FRAC * len(ref_sets) + 1, (len(flipped), len(ref_sets),
+                                                                   bad[:10])
+    return len(flipped)
+
+
+@pytest.mark.parametrize("name", ["c1_tiny", "c1_q", "c2_s", "c3_t", "c5_t"])
 def test_find_subs_batched_golden(rk, name):
-    """The batched form on inputs whose subgroups never exceed the 10000
-    particles at which the reference samples its linking length: membership
-    must equal the reference's.  Its sums run in a different order, and the
-    reference's core-velocity cut and float-rounded error minima turn
-    last-bit differences into discrete choices for a few halos, so the
-    property bound is statistical: at least 90% of halos have every field
-    within 1e-4 and the median halo's worst field is within 1e-6."""
+    """The batched form on every fixture, including c2_s and c5_t, whose
+    subgroups above 10000 particles sample their linking length by position
+    (the batched form derives those subgroups' order exactly)."""
     z, p, fp, c, H, E = load_case(rk, name)
     parts, gh, ge = rk.find_subs(fp, z["fof_off"], z["fof_sz"], c, batched=True)
     ref_sets = HC.sets_from_labels(z["halo_of"].astype(np.int64))
-    got_sets = HC.halo_sets(parts, gh)
-    ua, ub, worst, bad = HC.compare(ref_sets, H, got_sets, gh, TOL)
-    assert ua == 0 and ub == 0
-    per_halo = {}
-    for f, h, e in bad:
-        per_halo[h] = max(per_halo.get(h, 0), e)
-    n = len(ref_sets)
-    assert len(per_halo) <= 0.1 * n + 1, (len(per_halo), n)
-    errs = []
-    for k in ref_sets:
-        a, b = H[ref_sets[k]], gh[got_sets[k]]
-        errs.append(max(HC.rel_err(a[f], b[f]) for f in HC.FLOAT_FIELDS))
-    assert np.median(errs) <= 1e-6, np.median(errs)
+    check_batched(ref_sets, H, E, parts, gh, ge)
+
+
+@pytest.mark.parametrize("cfg,scale", [(2, 1 / 16), (2, 1 / 4), (4, 1 / 2048), (5, 0.004)])
+def test_find_subs_batched_oracle(rk, oracle, cfg, scale):
+    """Batched against the oracle on the benchmarked workloads, scaled down:
+    the same 6D hierarchy (level, size and linking length of every
+    subgroup), the same halo membership."""
+    p, box, mp, _ = rk.synth(cfg, scale)
+    c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    oracle.setup(c)
+    fp, off, sz = oracle.fof(p)
+    ro = oracle.find_subs(fp, off, sz)
+    ol, on, otr = oracle.hierarchy()
+    bo = rk.find_subs(fp, off, sz, c, batched=True)
+    gl, gn, gtr = rk.debug_hierarchy()
+    assert sorted(zip(ol.tolist(), on.tolist(), otr.tolist())) == \
+        sorted(zip(gl.tolist(), gn.tolist(), gtr.tolist()))
+    check_batched(HC.halo_sets(ro[0], ro[1]), ro[1], ro[2], *bo)
+
+
+@pytest.mark.parametrize("cfg,scale", [(1, 1.0), (2, 1 / 16), (4, 1 / 2048), (5, 0.004)])
+def test_path_device_against_oracle(rk, oracle, cfg, scale):
+    """rsg_path_device -- the entry the benchmark times -- on device-resident
+    particles, both forms, against the oracle's rockstar() + find_subs over
+    every group: plain bit for bit, batched with the same membership."""
+    import torch
+    p, box, mp, _ = rk.synth(cfg, scale)
+    c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    oracle.setup(c)
+    fp, off, sz = oracle.fof(p)
+    ro = oracle.find_subs(fp, off, sz)
+    d_in = torch.from_numpy(p.view(np.uint8).reshape(-1)).cuda()
+    for batched in (False, True):
+        path = rk.DevicePath(len(p), c, batched=batched)
+        num_p, nf, nh = path.run(d_in.data_ptr())
+        assert num_p == len(fp) and nf == len(off)
+        parts, gh, ge = path.results()
+        if not batched:
+            assert parts.tobytes() == ro[0].tobytes()
+            assert canon_nan(gh).tobytes() == canon_nan(ro[1]).tobytes()
+            assert ge.tobytes() == ro[2].tobytes()
+        else:
+            check_batched(HC.halo_sets(ro[0], ro[1]), ro[1], ro[2], parts, gh, ge)
 
 
 def test_tuning_does_not_change_results(rk):
