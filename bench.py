@@ -60,8 +60,7 @@ ALGO_BYTES = {
     # next-closest search: sample position read, distance written
     "k_nn": lambda st, L: 28.0 * st["samples_6d"] / max(L, 1),
     # median selection: every sample distance read once
-    "k_target_smem": lambda st, L: 4.0 * st["samples_6d"] / max(L, 1),
-    "k_target_rs": lambda st, L: 4.0 * st["samples_6d"] / max(L, 1),
+    "k_target_par": lambda st, L: 4.0 * st["samples_6d"] / max(L, 1),
     # later-dense lists: positions of the dense particles in both launches,
     # every entry written once
     "k_llist_w": lambda st, L: (32.0 * st["dense"] + 4.0 * st["later_list"]) / max(L, 1),
@@ -80,7 +79,7 @@ ALGO_BYTES = {
 # scaled to the timed launches by their units
 NCU_TRAFFIC = {
     "k_fof6_w": (62.18e6 / 1364736.0, "items_6d",
-                 "profiles/k_fof6_w_workload2_level0.md (level-0 launch, scaled by particles)"),
+                 "one ncu capture of the level-0 launch on workload 2, scaled by particles"),
 }
 
 
@@ -260,7 +259,8 @@ def sample_parity(rk, sample):
         if not batched:
             exact = (parts.tobytes() == ro[0].tobytes()
                      and canon_nan(h).tobytes() == canon_nan(ro[1]).tobytes()
-                     and e.tobytes() == ro[2].tobytes())
+                     and all(np.array_equal(e[f], ro[2][f]) for f in e.dtype.names
+                             if f != "_pad"))
             out["plain_vs_oracle"] = "bit-identical" if exact else "differs"
             cmp["bit_identical"] = exact
         out[form] = cmp
@@ -291,6 +291,28 @@ def _ref_worker(args):
     return len(h)
 
 
+def pool_find_subs(pool, ncores, fp, off, sz):
+    """find_subs over the groups on the pool's processes, groups dealt
+    largest first to the least loaded process (as the reference's dynamic
+    OpenMP loop hands them out); returns the number of halos."""
+    order = np.argsort(-sz, kind="stable")
+    chunks = [[] for _ in range(ncores)]
+    load = np.zeros(ncores)
+    for g in order:
+        k = int(np.argmin(load))
+        chunks[k].append(g)
+        load[k] += float(sz[g]) * np.log2(float(sz[g]) + 2)
+    jobs = []
+    for ch in chunks:
+        if not ch:
+            continue
+        ch = np.array(sorted(ch))
+        parts = np.concatenate([fp[off[g]:off[g] + sz[g]] for g in ch])
+        o = np.concatenate([[0], np.cumsum(sz[ch])[:-1]])
+        jobs.append((parts, o, sz[ch]))
+    return sum(pool.map(_ref_worker, jobs))
+
+
 def reference_arm(args, rk):
     """The reference's algorithm on the host cores: the C restatement (pinned
     bit-exact to the reference's sources) with the FOF serial, as rockstar()
@@ -314,22 +336,7 @@ def reference_arm(args, rk):
 
     def step():
         fp, off, sz = O.fof(p)  # serial, as rockstar() is in the reference
-        order = np.argsort(-sz, kind="stable")
-        chunks = [[] for _ in range(ncores)]
-        load = np.zeros(ncores)
-        for g in order:
-            k = int(np.argmin(load))
-            chunks[k].append(g)
-            load[k] += float(sz[g]) * np.log2(float(sz[g]) + 2)
-        jobs = []
-        for ch in chunks:
-            if not ch:
-                continue
-            ch = np.array(sorted(ch))
-            parts = np.concatenate([fp[off[g]:off[g] + sz[g]] for g in ch])
-            o = np.concatenate([[0], np.cumsum(sz[ch])[:-1]])
-            jobs.append((parts, o, sz[ch]))
-        return sum(pool.map(_ref_worker, jobs))
+        return pool_find_subs(pool, ncores, fp, off, sz)
 
     for _ in range(args.warmup):
         step()
@@ -354,6 +361,43 @@ def reference_arm(args, rk):
             "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def cpu_table(rk, specs, repeats):
+    """The reference's CPU path per workload, as the reference arm runs it:
+    the C restatement with the FOF serial and find_subs over the groups on
+    one process per host core (largest first); best of `repeats`.  One JSON
+    line per workload (the table of the benchmark spec)."""
+    import multiprocessing as mp_
+    from concurrent.futures import ProcessPoolExecutor
+    import dataclasses
+    from oracle import layouts as OL
+    from oracle import restatement as O
+    O.build()
+    ncores = os.cpu_count() or 1
+    for cfg_id, scale in specs:
+        p, box, mp, _ = rk.synth(cfg_id, scale, SEED)
+        fields = {f.name: getattr(rk.Config(particle_mass=mp, box_size=box,
+                                            total_particles=len(p)), f.name)
+                  for f in dataclasses.fields(OL.Config)}
+        O.setup(OL.Config(**fields))
+        pool = ProcessPoolExecutor(ncores, mp_context=mp_.get_context("spawn"),
+                                   initializer=_ref_init, initargs=(fields,))
+        best_f = best_s = None
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            fp, off, sz = O.fof(p)
+            t1 = time.perf_counter()
+            pool_find_subs(pool, ncores, fp, off, sz)
+            t2 = time.perf_counter()
+            best_f = min(best_f or 1e30, t1 - t0)
+            best_s = min(best_s or 1e30, t2 - t1)
+        pool.shutdown()
+        print(json.dumps({"workload": cfg_id, "scale": scale, "particles": len(p),
+                          "groups": len(sz), "host_cores": ncores, "fof_s": round(best_f, 3),
+                          "find_subs_s": round(best_s, 3),
+                          "particles_per_s": len(p) / (best_f + best_s),
+                          "repeats": repeats}), flush=True)
 
 
 def precision_study(rk, scale, forms):
@@ -443,6 +487,10 @@ def main():
                     help="instead of the bench line: --warmup batched steps, then one step "
                          "with CUDA events around every launch; prints the step time and "
                          "each kernel's launches (the command the ncu captures run)")
+    ap.add_argument("--cpu-table", default="",
+                    help="instead of the bench line: the reference's CPU path (FOF serial, "
+                         "find_subs on every host core) per workload, best of 3, for "
+                         "'cfg:scale,cfg:scale,...'; one JSON line each")
     ap.add_argument("--precision-forms", default="3,0,1,2",
                     help="potential forms of the study; the first is the reference "
                          "(3: FP64 direct sum, O(n^2) per group)")
@@ -461,6 +509,12 @@ def main():
     if args.profile_only:
         if rank == 0:
             profile_only(rk, args.cfg, args.scale, args.warmup)
+        return
+    if args.cpu_table:
+        if rank == 0:
+            specs = [(int(a), float(b)) for a, b in
+                     (x.split(":") for x in args.cpu_table.split(","))]
+            cpu_table(rk, specs, 3)
         return
     if args.impl == "reference":
         if rank == 0:

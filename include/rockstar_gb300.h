@@ -131,12 +131,16 @@ int rsg_find_subs(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offs
                   int64_t *num_halos);
 
 /* Batched form of rsg_find_subs (same arguments), replacing the same OpenMP
- * loop (src/mpi_main.cpp:1363-1389): subgroup labels come from a parallel
- * union-find and large sums from tree reductions, so halo membership and
- * properties are the reference's up to FP64 rounding except where a
- * subgroup of more than 10000 particles samples its linking length (the
- * sample depends on the reference's particle order, which this form does
- * not reproduce); halo order within a group may differ. */
+ * loop (src/mpi_main.cpp:1363-1389).  The 6D hierarchy is built as in the
+ * plain form (the reference's union-find labels, particle order, samples and
+ * quickselect); norm_sd, the Barnes-Hut node sums and the property scans of
+ * halos above a few thousand records use parallel reductions, and the
+ * potentials use the FP32 Kahan form (rsg_set_potential_form).  Halo
+ * membership equals the reference's except where a one-ulp change of a
+ * normalised coordinate or potential decides a link or a bound flag (the
+ * pairs within 1e-6 of a linking length are counted, RSG_STAT_NEAR_6D);
+ * properties agree to FP64 rounding except where a near-tie in one of the
+ * reference's discrete choices goes the other way. */
 int rsg_find_subs_batch(struct rsg_particle *p, int64_t num_p, const int64_t *fof_offsets,
                         const int64_t *fof_sizes, int64_t num_fofs, const struct rsg_config *cfg,
                         struct rsg_halo *halos, struct rsg_extra_halo_info *extra,

@@ -731,6 +731,136 @@ __device__ float total_energy(const PotRec *po, int64_t tot, float *ratio, const
 }
 
 // _calc_pseudo_evolution_masses (src/properties.c:351-382)
+// calc_shape for one halo on one warp, with the reference's summation order:
+// the lanes compute the terms of 32 records at a time (ellipsoid radius,
+// weight, products), lane c < 7 then adds accumulator c over them in record
+// order, and lane 0 takes the iteration's decisions (Jacobi, 1% rule) as
+// shape() does.  `sv` is this warp's staging area in shared memory.
+struct ShapeWarpBuf {
+    double v[32][7];
+    double orth[3][3], eig[3];
+    uint32_t skip;
+    int done;
+};
+__device__ void shape_warp(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
+                           const DevCfg &C, ShapeWarpBuf &sv) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int cl = 0;
+    for (int64_t j = lane; j < tot; j += 32) cl += !(bound && unbound(po[j]));
+    for (int o = 16; o; o >>= 1) cl += __shfl_xor_sync(FULL, cl, o);
+    const int64_t an = cl;
+    int64_t it = C.shape_iterations;
+    float minr = fmul((float)C.force_res, (float)C.force_res);
+    if (lane == 0) {
+        h.b_to_a = h.c_to_a = 0;
+        h.A[0] = h.A[1] = h.A[2] = 0;
+    }
+    if (!(h.r > 0)) return;
+    minr = (float)((double)minr * (1e6 / (double)fmul(h.r, h.r)));
+    if (an < 3) return;
+    if (an < it) it = an;
+    if (lane == 0) {
+        for (int i = 0; i < 3; i++) {
+            for (int k = 0; k < 3; k++) sv.orth[i][k] = 0;
+            sv.orth[i][i] = 1;
+            sv.eig[i] = (double)fmul(h.r, h.r) * 1e-6;
+        }
+        sv.done = 0;
+    }
+    __syncwarp();
+    const float hp0 = h.pos[0], hp1 = h.pos[1], hp2 = h.pos[2];
+    for (int64_t i = 0; i < it; i++) {
+        double a = 0;  // lane c < 7 owns accumulator c (w, m00, m11, m22, m10, m20, m21)
+        for (int64_t b0 = 0; b0 < tot; b0 += 32) {
+            const int64_t j = b0 + lane;
+            bool sk = true;
+            double vv[7];
+            if (j < tot && !(bound && unbound(po[j]))) {
+                const float *p = po[j].pos;
+                double dd[3] = {(double)fsub(p[0], hp0), (double)fsub(p[1], hp1),
+                                (double)fsub(p[2], hp2)};
+                double r = 0, dr;
+                for (int k = 0; k < 3; k++) {
+                    dr = 0;
+                    for (int l = 0; l < 3; l++) dr += sv.orth[k][l] * dd[l];
+                    r += dr * dr / sv.eig[k];
+                }
+                if (r < (double)minr) r = minr;
+                if (r > 0 && r <= 1) {
+                    double tw = (C.weighted_shapes) ? 1.0 / r : 1.0;
+                    vv[0] = tw;
+                    vv[1] = dd[0] * dd[0] * tw;
+                    vv[2] = dd[1] * dd[1] * tw;
+                    vv[3] = dd[2] * dd[2] * tw;
+                    vv[4] = dd[0] * dd[1] * tw;
+                    vv[5] = dd[0] * dd[2] * tw;
+                    vv[6] = dd[1] * dd[2] * tw;
+                    sk = false;
+                    for (int c = 0; c < 7; c++) sv.v[lane][c] = vv[c];
+                }
+            }
+            const uint32_t skip = __ballot_sync(FULL, sk);
+            __syncwarp();
+            if (lane < 7) {
+                const int m = (tot - b0) < 32 ? (int)(tot - b0) : 32;
+                for (int t = 0; t < m; t++)
+                    if (!((skip >> t) & 1u)) a += sv.v[t][lane];
+            }
+            __syncwarp();
+        }
+        double acc[7];
+        for (int c = 0; c < 7; c++) acc[c] = __shfl_sync(FULL, a, c);
+        if (lane == 0) {
+            double w = acc[0];
+            if (!w) sv.done = 1;
+            else {
+                double m[3][3] = {{acc[1], acc[4], acc[5]}, {acc[4], acc[2], acc[6]},
+                                  {acc[5], acc[6], acc[3]}};
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) m[k][l] /= (double)w;
+                double mt2[3][3], o2[3][3], e2[3];
+                for (int k = 0; k < 3; k++)
+                    for (int l = 0; l < 3; l++) mt2[k][l] = m[k][l];
+                jacobi3(m, e2, o2);
+                int a2 = 0, b = 1, c = 2;
+                if (e2[1] > e2[0]) { b = 0; a2 = 1; }
+                if (e2[2] > e2[b]) { c = b; b = 2; }
+                if (e2[b] > e2[a2]) { int t = a2; a2 = b; b = t; }
+                for (int k = 0; k < 3; k++) {
+                    sv.eig[k] = e2[k];
+                    for (int l = 0; l < 3; l++) sv.orth[k][l] = o2[k][l];
+                }
+                if (!e2[a2] || !e2[b] || !e2[c]) sv.done = 1;
+                else {
+                    float ba = (float)sqrt(e2[b] / e2[a2]);
+                    float ca = (float)sqrt(e2[c] / e2[a2]);
+                    if ((fabs((double)fsub(ba, h.b_to_a)) < 0.01 * (double)h.b_to_a) &&
+                        (fabs((double)fsub(ca, h.c_to_a)) < 0.01 * (double)h.c_to_a))
+                        sv.done = 1;
+                    else {
+                        h.b_to_a = (ba > 0) ? ba : 0;
+                        h.c_to_a = (ca > 0) ? ca : 0;
+                        double rr = sqrt(e2[a2]);
+                        for (int k = 0; k < 3; k++) {
+                            h.A[k] = (float)(1e3 * rr * o2[a2][k]);
+                            sv.eig[k] *= ((double)fmul(h.r, h.r) * 1e-6) / (rr * rr);
+                        }
+                        h.inertia_tensor[0] = (float)mt2[0][0];
+                        h.inertia_tensor[1] = (float)mt2[1][1];
+                        h.inertia_tensor[2] = (float)mt2[2][2];
+                        h.inertia_tensor[3] = (float)mt2[0][1];
+                        h.inertia_tensor[4] = (float)mt2[1][2];
+                        h.inertia_tensor[5] = (float)mt2[2][0];
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (sv.done) return;
+    }
+}
+
 __device__ void pseudo_masses(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
                               const DevCfg &C) {
     int64_t np_ = 0, npd = 0;
@@ -1899,6 +2029,8 @@ static void seg_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, PotRec *P
         phase_mark(st, "p.passes");
         for (int which = 0; which < 2; which++) {
             launch(k_sh_init, HB, HT, 0, st, NH, H, cnt, toff, d_dc, which, S);
+            launch(k_sh_small, nblk((int64_t)NH * 32, 128), 128, 0, st, NH, H, toff,
+                   (const PotRec *)PO, d_dc, (const HS *)S, bound);
             for (int64_t i = 0; i < dc.shape_iterations; i++) {
                 launch(k_sh_sum, nc, RSG_CT, 0, st, CH, PO, H, flag, S, d_dc, cp);
                 launch(k_sh_fin, HB, HT, 0, st, NH, H, c0, nch, cp, S);

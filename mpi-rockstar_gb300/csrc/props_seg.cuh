@@ -605,6 +605,12 @@ __global__ void k_sg_v2_fin(int32_t NH, rsg_halo *H, const int32_t *c0, const in
 // ---- calc_shape (src/properties.c:216-326) ---------------------------------
 // which = 0: the R_500c set [0, npa[2]); which = 1: the R_Delta set
 // [0, dtot), after the first set's results move to the *2 fields
+// Sets of at most this many records run the reference's loop itself, one
+// thread per halo (shape(), in the records' order): with a handful of
+// particles the inertia tensor is close to singular and its smallest
+// eigenvalue is rounding noise, so only the reference's own summation order
+// reproduces its axis ratios.
+#define RSG_SHAPE_SEQ 1024
 __global__ void k_sh_init(int32_t NH, rsg_halo *H, const int32_t *cnt, const int32_t *toff,
                           const DevCfg *Cp, int which, HS *S) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
@@ -622,6 +628,10 @@ __global__ void k_sh_init(int32_t NH, rsg_halo *H, const int32_t *cnt, const int
         set = s.dtot;
     }
     s.set = (int32_t)set;
+    if (set <= RSG_SHAPE_SEQ) {  // k_sh_small's
+        s.done = 1;
+        return;
+    }
     int64_t an = (set > 0) ? cnt[toff[h] + set - 1] : 0, it = C.shape_iterations;
     s.iter = 0;
     s.done = 0;
@@ -643,6 +653,15 @@ __global__ void k_sh_init(int32_t NH, rsg_halo *H, const int32_t *cnt, const int
     s.minr = minr;
     s.it = (int32_t)it;
     if (it <= 0) s.done = 1;
+}
+// The small sets of k_sh_init: shape_warp, one warp per halo.
+__global__ void __launch_bounds__(128) k_sh_small(int32_t NH, rsg_halo *H, const int32_t *toff,
+                                                  const PotRec *PO, const DevCfg *Cp,
+                                                  const HS *S, int bound) {
+    __shared__ ShapeWarpBuf buf[4];
+    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (h >= NH || H[h].num_p < 1 || S[h].set > RSG_SHAPE_SEQ) return;
+    shape_warp(H[h], PO + toff[h], S[h].set, bound, *Cp, buf[threadIdx.x >> 5]);
 }
 __global__ void __launch_bounds__(RSG_CT) k_sh_sum(const Chunk *CH, const PotRec *PO,
                                                    const rsg_halo *H, const uint8_t *flag,

@@ -32,9 +32,6 @@
 #define RSG_SEQ_MAX 65536
 // Below this size one thread does all of a node's or halo's work.
 #define RSG_SMALL 2048
-// MAX_PARTICLES_TO_SAMPLE (src/groupies.c:286): larger subgroups draw their
-// linking-length sample by array position.
-#define RSG_SAMPLE_MAX 10000
 
 namespace rsg {
 
@@ -564,20 +561,138 @@ __device__ float median_r(float *a, int nt, unsigned seed, float frac) {
     }
 }
 // Nodes whose sample fits in shared memory (RSG_TARGET_SMEM distances): one
-// block per node stages the distances, one thread selects.
+// block per node runs find_median_r with every rad_partition done by the
+// whole block.  rad_partition's loop over [left, right - 1) is the same
+// two-pointer swap as the kd-tree split (kdtree.cuh), so each element's
+// destination follows in closed form from prefix counts of the elements
+// above the pivot; thread 0 draws the pivots from the rand_r stream in the
+// reference's order.  The result is the sequential one element for element.
 #define RSG_TARGET_SMEM 10000
-__global__ void k_target_smem(HierNodes N, int32_t base, const int32_t *soff, const float *prad,
-                              const unsigned *seed_in, float frac, int exact) {
-    extern __shared__ float a_s[];
-    int k = blockIdx.x;
-    int node = base + k;
-    int n = N.n[node];
-    int nt = exact ? n : (n < 10000 ? n : 10000);
-    if (nt > RSG_TARGET_SMEM) return;
-    const float *a = prad + soff[k];
-    for (int i = threadIdx.x; i < nt; i += blockDim.x) a_s[i] = a[i];
+#define RSG_TGT_T 256
+__global__ void __launch_bounds__(RSG_TGT_T) k_target_par(HierNodes N, int32_t base,
+                                                          const int32_t *soff, const float *prad,
+                                                          const unsigned *seed_in, float frac,
+                                                          int exact) {
+    extern __shared__ float sm_f[];
+    typedef cub::BlockScan<int, RSG_TGT_T> Scan;
+    typedef cub::BlockReduce<int, RSG_TGT_T> Red;
+    __shared__ union {
+        typename Scan::TempStorage s;
+        typename Red::TempStorage r;
+    } tmp;
+    __shared__ int sh_pi, sh_done, sh_q;
+    __shared__ float sh_res;
+    const int k = blockIdx.x, node = base + k, tid = threadIdx.x;
+    const int n = N.n[node];
+    const int nt = exact ? n : (n < 10000 ? n : 10000);
+    if (nt > RSG_TARGET_SMEM || nt < 1) return;
+    float *a = sm_f, *b = sm_f + nt;
+    int *fb = (int *)(sm_f + 2 * nt), *bs = fb + nt;
+    const float *src = prad + soff[k];
+    for (int i = tid; i < nt; i += RSG_TGT_T) a[i] = src[i];
+    const int kk = (int)__float2ll_rz(fmul(__ll2float_rn(nt), frac));
+    if (nt < 2) {
+        if (tid == 0) N.target_r[node] = a[0];
+        return;
+    }
+    unsigned seed = seed_in[k];
+    int left = 0, right = nt;
     __syncthreads();
-    if (threadIdx.x == 0) N.target_r[node] = median_r(a_s, nt, seed_in[k], frac);
+    for (int guard = 0;; guard++) {
+        if (tid == 0) {
+            float u = __fdiv_rn(__int2float_rn(rand_r_glibc(&seed) % 2147483647), 2147483648.0f);
+            float pf = fadd(__int2float_rn(left), fmul(u, __int2float_rn(right - left)));
+            int pi = (int)__float2ll_rz(pf);
+            if (pi >= right) pi = right - 1;
+            float t = a[pi];
+            a[pi] = a[right - 1];
+            a[right - 1] = t;
+            sh_pi = pi;
+        }
+        __syncthreads();
+        const float piv = a[right - 1];
+        const int L = right - 1 - left;  // the swap loop runs over [left, right - 1)
+        int m;
+        if (L == 0) {
+            // one element: the reference compares a[left - 1] (left >= 1 here,
+            // since kk >= 1) and may swap it in; done as written
+            m = 0;
+            if (tid == 0) {
+                int si = left - 1;
+                if (a[si] <= piv) si++;
+                float t = a[right - 1];
+                a[right - 1] = a[si];
+                a[si] = t;
+                sh_q = si;
+            }
+            __syncthreads();
+        } else {
+            const int per = (L + RSG_TGT_T - 1) / RSG_TGT_T;
+            const int c0 = min(L, tid * per), c1 = min(L, c0 + per);
+            int cnt = 0;
+            for (int l = c0; l < c1; l++) cnt += a[left + l] > piv;
+            int before, B;
+            Scan(tmp.s).ExclusiveSum(cnt, before, B);
+            __syncthreads();
+            m = L - B;  // elements <= pivot
+            int br = before, qb = 0;
+            for (int l = c0; l < c1; l++) {
+                bool big = a[left + l] > piv;
+                int sr = l - br;
+                if (big && l < m) fb[br] = l;
+                if (!big && l >= m) bs[m - 1 - sr] = l;
+                if (big && l < m) qb++;
+                br += big;
+            }
+            int q = Red(tmp.r).Sum(qb);
+            if (tid == 0) sh_q = q;
+            __syncthreads();
+            q = sh_q;
+            br = before;
+            for (int l = c0; l < c1; l++) {
+                float v = a[left + l];
+                bool big = v > piv;
+                int sr = l - br, d;
+                if (!big && l < m) d = l;
+                else if (big && l < m) d = (br == 0) ? L - 1 : bs[br - 1] - 1;
+                else if (!big) d = fb[m - 1 - sr];
+                else {
+                    int pos_last = (q > 0) ? bs[q - 1] : L;
+                    if (l > pos_last) d = l - 1;
+                    else if (pos_last - m >= 2) d = (l == m) ? pos_last - 1 : l - 1;
+                    else d = l;
+                }
+                b[d] = v;
+                br += big;
+            }
+            __syncthreads();
+            for (int l = tid; l < L; l += RSG_TGT_T) a[left + l] = b[l];
+            __syncthreads();
+            if (tid == 0) {
+                int si = left + m;
+                float t = a[right - 1];
+                a[right - 1] = a[si];
+                a[si] = t;
+                sh_q = si;
+            }
+            __syncthreads();
+        }
+        const int p = sh_q;
+        if (tid == 0) {
+            sh_done = (kk == p || a[left] == a[right - 1]);
+            if (sh_done) sh_res = a[kk];
+            if (guard > 100000000) {  // cannot happen for finite input: report it
+                loop_limit_hit();
+                sh_done = 1;
+                sh_res = a[kk];
+            }
+        }
+        __syncthreads();
+        if (sh_done) break;
+        if (kk < p) right = p;
+        else left = p + 1;
+    }
+    if (tid == 0) N.target_r[node] = sh_res;
 }
 // Larger samples (EXACT_LL_CALC): in place in global memory.
 __global__ void k_target(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
@@ -598,38 +713,6 @@ __global__ void k_fill_eln(HierNodes N, int32_t base, int32_t *eln) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) eln[s + i] = k;
 }
 
-// The level's element map split by node size: nodes above thr into ex,
-// the others into eu (-1 elsewhere).
-__global__ void k_split_eln(const int32_t *eln, int64_t M, HierNodes N, int32_t base, int thr,
-                            int32_t *ex, int32_t *eu) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M) return;
-    int k = eln[i];
-    bool big = k >= 0 && N.n[base + k] > thr;
-    ex[i] = big ? k : -1;
-    eu[i] = (k >= 0 && !big) ? k : -1;
-}
-
-__device__ __forceinline__ int uf_find2(int *par, int x) {
-    int p = par[x];
-    while (p != x) {
-        int gp = par[p];
-        if (gp != p) par[x] = gp;
-        x = p;
-        p = par[x];
-    }
-    return x;
-}
-__device__ __forceinline__ void uf_unite2(int *par, int a, int b) {
-    while (true) {
-        a = uf_find2(par, a);
-        b = uf_find2(par, b);
-        if (a == b) return;
-        if (a < b) { int t = a; a = b; b = t; }
-        if (atomicCAS(&par[a], a, b) == a) return;
-    }
-}
-
 // _find_subfofs_at_r (src/groupies.c:274-284): every particle links to
 // itself and to the later particles within target_r (6D, strict <), which
 // the skip search returns in ascending order.
@@ -638,12 +721,12 @@ __device__ __forceinline__ void uf_unite2(int *par, int a, int b) {
 // lane's own box test admits it; at a leaf every lane tests
 // every point with its own distance test.  A lane meets exactly the points
 // of its own search, in ascending order.  MODE 0 counts, 1 fills the CSR
-// lists (exact form), 2 unites at once (batched form).
+// lists.
 template <int MODE>
 __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec *W, int64_t M,
                                                 HierNodes N, int32_t base, const int32_t *eln,
                                                 const int32_t *noff, int32_t *ncnt, int32_t *nbr,
-                                                int *par, int *err, unsigned long long *near) {
+                                                int *err, unsigned long long *near) {
     const unsigned FULL = 0xffffffffu;
     int64_t w0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * 32;
     int lane = threadIdx.x & 31;
@@ -682,7 +765,6 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
                     float d = dist6(c, q);
                     if (need && j > i && d < r2) {
                         if (MODE == 1) nbr[o + cnt] = j;
-                        if (MODE == 2) uf_unite2(par, i, j);
                         cnt++;
                     }
                     // pairs within 1e-6 of the linking length (relative, in
@@ -704,23 +786,10 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
     if (MODE == 0 && valid && k >= 0) ncnt[i] = cnt;
 }
 
-// Batched form, nodes up to the sample size: subgroup labels from the
-// parallel union-find of k_fof6_w<2> (components are the same sets; the
-// label is the component's first position, -1 for particles without links).
-// The order this gives is deterministic but not the reference's, which only
-// matters where a child subgroup samples its linking length by position.
-__global__ void k_uf6_size(const int32_t *eln, int64_t M, int *par, int *root, int *size) {
+template <class T>
+__global__ void k_gather(const T *src, const uint32_t *perm, int64_t M, T *dst) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M || eln[i] < 0) return;
-    int r = uf_find2(par, (int)i);
-    root[i] = r;
-    atomicAdd(&size[r], 1);
-}
-__global__ void k_uf6_label(const int32_t *eln, int64_t M, const int *root, const int *size,
-                            int32_t *lab) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M || eln[i] < 0) return;
-    lab[i] = size[root[i]] > 1 ? root[i] : -1;
+    if (i < M) dst[i] = src[perm[i]];
 }
 
 // Runs of equal labels after the partition sort: the kept ones (>= 0 and at
@@ -763,87 +832,6 @@ __global__ void k_make_children2(const int32_t *cidx, int32_t nc, const int32_t 
     int c = nbase + t;
     N.start[c] = p;
     N.n[c] = clen[h];
-    N.parent[c] = par;
-    N.group[c] = N.group[par];
-    N.level[c] = N.level[par] + 1;
-    N.nchild[c] = 0;
-    atomicAdd(&N.nchild[par], 1);
-}
-
-__global__ void k_init_par(const int32_t *eln, int64_t M, int *par, int *size) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M) return;
-    par[i] = (int)i;
-    size[i] = 0;
-}
-
-__global__ void k_comp_size(const int32_t *eln, int64_t M, int *par, int *root, int *size) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M || eln[i] < 0) return;
-    int rt = uf_find2(par, (int)i);
-    root[i] = rt;
-    atomicAdd(&size[rt], 1);
-}
-
-// Sort keys that regroup each level node's range: particles outside kept
-// subgroups first, then subgroups by first position (stable inside).
-__global__ void k_subkeys(const int32_t *eln, int64_t M, HierNodes N, int32_t base,
-                          const int *root, const int *size, int64_t minsz, uint64_t *key,
-                          uint32_t *val) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M) return;
-    int k = eln[i];
-    uint64_t kk;
-    if (k < 0) {
-        kk = (uint64_t)i << 32;
-    } else {
-        int s = N.start[base + k];
-        int rt = root[i];
-        bool kept = size[rt] >= minsz && size[rt] >= 2;
-        kk = ((uint64_t)s << 32) | (uint64_t)(kept ? (rt - s + 1) : 0);
-    }
-    key[i] = kk;
-    val[i] = (uint32_t)i;
-}
-
-template <class T>
-__global__ void k_gather(const T *src, const uint32_t *perm, int64_t M, T *dst) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < M) dst[i] = src[perm[i]];
-}
-
-// Heads of kept subgroups after regrouping: candidates for level L+1.
-__global__ void k_child_heads(const int32_t *eln_sorted, const uint64_t *key, int64_t M,
-                              HierNodes N, int32_t base, const int *size, int64_t minsz,
-                              int32_t *flag) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M) return;
-    int f = 0;
-    uint64_t kk = key[i];
-    uint32_t lo = (uint32_t)(kk & 0xffffffffu);
-    int k = eln_sorted[i];
-    if (k >= 0 && lo != 0 && (i == 0 || key[i - 1] != kk)) {
-        int s = N.start[base + k], pn = N.n[base + k];
-        int rt = (int)lo - 1 + s;
-        int sz = size[rt];
-        if (sz > minsz && sz < pn) f = 1;
-    }
-    flag[i] = f;
-}
-
-__global__ void k_make_children(const int32_t *heads, const int *nheads, const int32_t *eln,
-                                const uint64_t *key, HierNodes N, int32_t base, int32_t nbase,
-                                const int *size) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= *nheads) return;
-    int i = heads[t];
-    int k = eln[i];
-    int par = base + k;
-    int s = N.start[par];
-    int rt = (int)(key[i] & 0xffffffffu) - 1 + s;
-    int c = nbase + t;
-    N.start[c] = i;
-    N.n[c] = size[rt];
     N.parent[c] = par;
     N.group[c] = N.group[par];
     N.level[c] = N.level[par] + 1;
@@ -2191,14 +2179,17 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     last_stats()[RSG_STAT_6D_ITEMS] = 0;
     last_stats()[RSG_STAT_6D_SAMPLES] = 0;
     last_stats()[RSG_STAT_NEAR_6D] = 0;
-    // Nodes whose subgroups must come out in the reference's order: all of
-    // them in the plain form; in the batched form those larger than the
-    // linking-length sample, whose children can be sampled by position
-    // (src/groupies.c:295-308), unless EXACT_LL_CALC takes every particle.
-    const int xthr = exact ? 0 : (cfg.exact_ll_calc ? INT_MAX : RSG_SAMPLE_MAX);
+    // Subgroups come out in the reference's order in both forms: the order
+    // decides the linking-length sample of a child above 10000 particles
+    // (src/groupies.c:295-308), and for every child the array the
+    // reference's quickselect runs on, whose early exit on equal end values
+    // (mutual nearest neighbours) returns a value that depends on that
+    // array's order (src/groupies.c:768-786).
     // norm_sd sums in array order (bit-exact) for nodes in (seq_lo,
-    // RSG_SEQ_MAX]; the batched form keeps its parallel sums below xthr
-    const int seq_lo = exact ? RSG_SMALL : RSG_SAMPLE_MAX;
+    // RSG_SEQ_MAX] in the plain form; the batched form sums in parallel
+    // (rounding can move a normalised coordinate by one float ulp, rarely:
+    // the near-threshold count bounds what that can change)
+    const int seq_lo = exact ? RSG_SMALL : RSG_SEQ_MAX;
     const int seq_max = RSG_SEQ_MAX;
     const int T = 256;
     // groups with particles, their working offsets
@@ -2244,7 +2235,7 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
     int32_t *phalo = ar.get<int32_t>(M), *phalo2 = ar.get<int32_t>(M);
     uint64_t *key = ar.get<uint64_t>(M), *key2 = ar.get<uint64_t>(M);
     uint32_t *val = ar.get<uint32_t>(M), *val2 = ar.get<uint32_t>(M);
-    int *par = ar.get<int>(M + 1), *root = ar.get<int>(M + 1), *csize = ar.get<int>(M + 1);
+    int *par = ar.get<int>(M + 1), *root = ar.get<int>(M + 1);
     int32_t *hflag = ar.get<int32_t>(M + 1);
     int *err = ar.get<int>(4);
     RSG_CUDA(cudaMemsetAsync(err, 0, 16, st));
@@ -2350,61 +2341,39 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             // both forms: the reference's quickselect with its early exit, whose
             // value can differ from the exact order statistic when the sample
             // holds equal distances (mutual nearest neighbours)
-            launch(k_target_smem, cnt, 64, (size_t)4 * (ntmax > 0 ? ntmax : 1), st, N, base,
-                   (const int32_t *)soff, (const float *)prad, (const unsigned *)seeds,
+            static bool tgt_attr = false;
+            if (!tgt_attr) {
+                RSG_CUDA(cudaFuncSetAttribute(k_target_par,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              16 * RSG_TARGET_SMEM));
+                tgt_attr = true;
+            }
+            launch(k_target_par, cnt, RSG_TGT_T, (size_t)16 * (ntmax > 0 ? ntmax : 1), st, N,
+                   base, (const int32_t *)soff, (const float *)prad, (const unsigned *)seeds,
                    (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
             launch(k_target, nblk(cnt, 32), 32, 0, st, N, base, cnt, soff, prad, seeds,
                    (float)cfg.fof_fraction, (int)cfg.exact_ll_calc);
         }
         phase_mark(st, "d.nn_target");
-        // subgroup labels: the reference's union-find labels (uflabels.cuh) for
-        // the nodes above xthr, then its partition sort by label; a parallel
-        // union-find for the others, regrouped by a stable sort on the labels
-        std::vector<int32_t> xs, xn;
-        int nsmall = 0;
-        for (int k = 0; k < cnt; k++) {
-            if (hn[k] > xthr) {
-                xs.push_back(hs[k]);
-                xn.push_back(hn[k]);
-            } else {
-                nsmall++;
-            }
-        }
-        const int32_t *elnx = eln, *elnu = eln;
-        if (!xs.empty() && nsmall) {
-            int32_t *ex = ar.get<int32_t>(M), *eu = ar.get<int32_t>(M);
-            launch(k_split_eln, nblk(M, T), T, 0, st, (const int32_t *)eln, M, N, base, xthr, ex, eu);
-            elnx = ex;
-            elnu = eu;
-        }
-        if (!xs.empty()) {
+        // subgroup labels: the reference's union-find labels (uflabels.cuh),
+        // then its partition sort by label (lsort.cuh)
+        {
             // later neighbours within target_r, as CSR lists
             int32_t *ncnt = par, *noff = root;
             RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
-            launch(k_fof6_w<0>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, elnx,
-                   (const int32_t *)nullptr, ncnt, (int32_t *)nullptr, (int *)nullptr, err, near);
+            launch(k_fof6_w<0>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
+                   (const int32_t *)nullptr, ncnt, (int32_t *)nullptr, err, near);
             check_i32_total(ar, ncnt, M + 1, "6D neighbour lists", st);
             int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
             int32_t *nbr = ar.get<int32_t>(ne + 1);
-            launch(k_fof6_w<1>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, elnx,
-                   (const int32_t *)noff, ncnt, nbr, (int *)nullptr, err, near);
+            launch(k_fof6_w<1>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
+                   (const int32_t *)noff, ncnt, nbr, err, near);
             phase_mark(st, "d.fof6d");
-            exact_labels_csr(ar, M, elnx, N.start + base, noff, nbr, phalo, st);
-        }
-        if (nsmall) {
-            int *ufp = csize, *ufr = (int *)key2, *ufs = (int *)val2;
-            launch(k_init_par, nblk(M, T), T, 0, st, eln, M, ufp, ufs);
-            launch(k_fof6_w<2>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, elnu,
-                   (const int32_t *)nullptr, (int32_t *)nullptr, (int32_t *)nullptr, ufp, err, near);
-            phase_mark(st, "d.fof6d");
-            launch(k_uf6_size, nblk(M, T), T, 0, st, elnu, M, ufp, ufr, ufs);
-            launch(k_uf6_label, nblk(M, T), T, 0, st, elnu, M, ufr, ufs, phalo);
+            exact_labels_csr(ar, M, eln, N.start + base, noff, nbr, phalo, st);
         }
         RSG_CHECK_LAUNCH();
         phase_mark(st, "d.labels");
-        if (!xs.empty()) partition_sort_labels<Rec>(ar, W, phalo, M, xs, xn, st);
-        // leaves the partition-sorted nodes as they are (they are in label order)
-        if (nsmall) label_sort_stable(ar, W, phalo, eln, N, base, cnt, M, st);
+        partition_sort_labels<Rec>(ar, W, phalo, M, hs, hn, st);
         phase_mark(st, "d.psort");
         launch(k_run_heads, nblk(M, T), T, 0, st, eln, M, N, base, phalo, hflag);
         int32_t *heads = ar.get<int32_t>(M);
