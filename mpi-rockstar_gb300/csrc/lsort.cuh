@@ -13,10 +13,23 @@ struct LSeg {
     int32_t *pivot, *m, *q;
 };
 
-static __global__ void k_ls_owner(const int32_t *start, const int32_t *n, int32_t *owner) {
-    int k = blockIdx.x;
-    int s = start[k], c = n[k];
-    for (int i = threadIdx.x; i < c; i += blockDim.x) owner[s + i] = k;
+// owner[i]: the active segment holding element i (segments are disjoint and
+// listed by ascending start), -1 outside every segment.
+static __global__ void k_ls_owner(const int32_t *start, const int32_t *n, int32_t ns, int64_t M,
+                                  int32_t *owner) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    int lo = 0, hi = ns - 1, k = -1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        if (start[mid] <= i) {
+            k = mid;
+            lo = mid + 1;
+        } else {
+            hi = mid - 1;
+        }
+    }
+    owner[i] = (k >= 0 && i < (int64_t)start[k] + n[k]) ? k : -1;
 }
 static __global__ void k_ls_init(LSeg S, int32_t ns) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -24,17 +37,23 @@ static __global__ void k_ls_init(LSeg S, int32_t ns) {
     S.mn[k] = 0x7fffffff;
     S.mx[k] = (int32_t)0x80000000;
 }
+// Label range of every segment.  A thread reads ITEMS consecutive elements;
+// threads whose elements all belong to one segment combine their ranges
+// with the other lanes of that segment before the atomics (a large segment
+// gets one atomic pair per warp instead of one per thread).
 template <int ITEMS>
 static __global__ void k_ls_minmax(const int32_t *lab, int64_t M, const int32_t *owner, LSeg S) {
+    const unsigned FULL = 0xffffffffu;
     int64_t i0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * ITEMS;
-    if (i0 >= M) return;
+    int first = -2;  // owner shared by all of this thread's elements, -1 mixed/none
     int cur = -1, lo = 0x7fffffff, hi = (int)0x80000000;
     for (int it = 0; it < ITEMS; it++) {
         int64_t i = i0 + it;
-        if (i >= M) break;
-        int a = owner[i];
+        int a = (i < M) ? owner[i] : -1;
+        if (first == -2) first = a;
+        else if (a != first) first = -1;
         if (a != cur) {
-            if (cur >= 0) {
+            if (cur >= 0 && first == -1) {  // mixed: this run goes out on its own
                 atomicMin(&S.mn[cur], lo);
                 atomicMax(&S.mx[cur], hi);
             }
@@ -47,7 +66,15 @@ static __global__ void k_ls_minmax(const int32_t *lab, int64_t M, const int32_t 
         lo = min(lo, v);
         hi = max(hi, v);
     }
-    if (cur >= 0) {
+    bool uni = first >= 0;  // every element in one segment: combine across the warp
+    unsigned grp = __match_any_sync(FULL, uni ? first : -1);
+    if (uni) {
+        int glo = __reduce_min_sync(grp, lo), ghi = __reduce_max_sync(grp, hi);
+        if ((threadIdx.x & 31) == __ffs(grp) - 1) {
+            atomicMin(&S.mn[first], glo);
+            atomicMax(&S.mx[first], ghi);
+        }
+    } else if (cur >= 0) {
         atomicMin(&S.mn[cur], lo);
         atomicMax(&S.mx[cur], hi);
     }
@@ -192,8 +219,8 @@ void partition_sort_labels(Arena &ar, T *W, int32_t *lab, int64_t M,
             set_error(RSG_ERR_LIMIT, "label partition sort did not terminate");
             throw Failure();
         }
-        RSG_CUDA(cudaMemsetAsync(owner, 0xff, 4 * M, st));
-        launch(k_ls_owner, ns, T_, 0, st, S.start, S.n, owner);
+        launch(k_ls_owner, nblk(M, T_), T_, 0, st, (const int32_t *)S.start, (const int32_t *)S.n,
+               ns, M, owner);
         launch(k_ls_init, nblk(ns, T_), T_, 0, st, S, ns);
         launch(k_ls_minmax<8>, nblk((M + 7) / 8, T_), T_, 0, st, lab, M, owner, S);
         launch(k_ls_pivot, nblk(ns, T_), T_, 0, st, S, ns);

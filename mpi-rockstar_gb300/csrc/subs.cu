@@ -503,11 +503,35 @@ __device__ float next_closest(const KNode<6> *nodes, int root, const Rec *W, con
     return r;
 }
 
-__global__ void k_nn(const KNode<6> *nodes, const Rec *W, HierNodes N, int32_t base,
-                     int32_t count, const int32_t *soff, const int32_t *sidx, float *prad,
-                     int64_t total, int exact, int *err) {
+// Sample queries in tree order: key (node, position in the node) of every
+// sample (random positions for nodes above 10000 particles), so neighbouring
+// threads search from neighbouring particles.
+__global__ void k_nn_keys(HierNodes N, int32_t base, int32_t count, const int32_t *soff,
+                          const int32_t *sidx, int64_t total, int exact, uint64_t *key,
+                          uint32_t *val) {
     int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (g >= total) return;
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (soff[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    int n = N.n[base + lo];
+    int nt = exact ? n : (n < 10000 ? n : 10000);
+    int t = (int)(g - soff[lo]);
+    int j = (nt == n) ? t : sidx[g];
+    key[g] = ((uint64_t)(uint32_t)lo << 32) | (uint32_t)j;
+    val[g] = (uint32_t)g;
+}
+// The next-closest distance of every sample, queries taken in `order`
+// (sample indices; null: as stored), results stored by sample index.
+__global__ void k_nn(const KNode<6> *nodes, const Rec *W, HierNodes N, int32_t base,
+                     int32_t count, const int32_t *soff, const int32_t *sidx, float *prad,
+                     int64_t total, int exact, int *err, const uint32_t *order) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= total) return;
+    int64_t g = order ? (int64_t)order[q] : q;
     // node of sample g: last k with soff[k] <= g
     int lo = 0, hi = count - 1;
     while (lo < hi) {
@@ -720,8 +744,11 @@ __global__ void k_fill_eln(HierNodes N, int32_t base, int32_t *eln) {
 // each node's tree once with a shared stack, entering a node when any
 // lane's own box test admits it; at a leaf every lane tests
 // every point with its own distance test.  A lane meets exactly the points
-// of its own search, in ascending order.  MODE 0 counts, 1 fills the CSR
-// lists.
+// of its own search, in ascending order.  MODE 2 counts every list and keeps
+// its first RSG_SLOT6 entries in a fixed slot per particle (one pass for
+// almost every particle); MODE 1 fills the CSR lists of the particles whose
+// list is longer than that.
+#define RSG_SLOT6 16
 template <int MODE>
 __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec *W, int64_t M,
                                                 HierNodes N, int32_t base, const int32_t *eln,
@@ -738,13 +765,15 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
 #pragma unroll
     for (int d = 0; d < 6; d++) c[d] = (valid && k >= 0) ? W[i].pos[d] : 0.f;
     int cnt = 0;
-    int o = (MODE == 1 && valid && k >= 0) ? noff[i] : 0;
-    unsigned pending = __ballot_sync(FULL, valid && k >= 0);
+    bool part = valid && k >= 0 && (MODE != 1 || ncnt[i] > RSG_SLOT6);
+    int o = (MODE == 1 && part) ? noff[i] : 0;
+    int32_t *slot = (MODE == 2) ? nbr + (int64_t)i * RSG_SLOT6 : nullptr;
+    unsigned pending = __ballot_sync(FULL, part);
     int stack[RSG_STACK6];
     while (pending) {
         int leader = __ffs(pending) - 1;
         int kk = __shfl_sync(FULL, k, leader);
-        bool mine = valid && k == kk;
+        bool mine = part && k == kk;
         pending &= ~__ballot_sync(FULL, mine);
         int imin = (int)w0 + leader;  // the segment's first particle
         float r = N.target_r[base + kk];
@@ -759,18 +788,21 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
             if (x.div < 0) {
                 int j0 = x.start > imin + 1 ? x.start : imin + 1;
                 for (int j = j0; j < x.start + x.n; j++) {
-                    float q[6];
-#pragma unroll
-                    for (int d = 0; d < 6; d++) q[d] = W[j].pos[d];
+                    // the record as two 16-byte loads (the same address in
+                    // every lane: one broadcast transaction each)
+                    const float4 qa = reinterpret_cast<const float4 *>(W + j)[0];
+                    const float4 qb = reinterpret_cast<const float4 *>(W + j)[1];
+                    const float q[6] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y};
                     float d = dist6(c, q);
                     if (need && j > i && d < r2) {
                         if (MODE == 1) nbr[o + cnt] = j;
+                        if (MODE == 2 && cnt < RSG_SLOT6) slot[cnt] = j;
                         cnt++;
                     }
                     // pairs within 1e-6 of the linking length (relative, in
                     // distance): where a last-bit change of a coordinate
                     // could decide the link
-                    if (MODE != 0 && need && j > i && fabsf(d - r2) <= 2e-6f * r2)
+                    if (MODE == 2 && need && j > i && fabsf(d - r2) <= 2e-6f * r2)
                         atomicAdd(near, 1ull);
                 }
                 continue;
@@ -783,7 +815,18 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
             stack[sp++] = x.left;
         }
     }
-    if (MODE == 0 && valid && k >= 0) ncnt[i] = cnt;
+    if (MODE == 2 && part) ncnt[i] = cnt;
+}
+// CSR lists from the fixed slots of the lists that fit in them.
+__global__ void k_slots_csr(const int32_t *eln, int64_t M, const int32_t *ncnt,
+                            const int32_t *noff, const int32_t *slots, int32_t *nbr) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= M || eln[i] < 0) return;
+    int n = ncnt[i];
+    if (n > RSG_SLOT6) return;
+    const int32_t *sl = slots + i * RSG_SLOT6;
+    int32_t *dst = nbr + noff[i];
+    for (int t = 0; t < n; t++) dst[t] = sl[t];
 }
 
 template <class T>
@@ -2330,8 +2373,27 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                (int)cfg.exact_ll_calc);
         launch(k_sample_idx, nblk(tot, 256), 256, 0, st, N, base, cnt, (const int32_t *)soff, sidx,
                (int64_t)tot, (int)cfg.exact_ll_calc);
-        launch(k_nn, nblk(tot, 128), 128, 0, st, F.nodes, W, N, base, cnt, soff, sidx, prad,
-               (int64_t)tot, (int)cfg.exact_ll_calc, err);
+        {
+            // sampled nodes draw positions at random: search them in tree order
+            bool sampled = false;
+            for (int k = 0; k < cnt && !sampled; k++)
+                sampled = !cfg.exact_ll_calc && hn[k] > 10000;
+            uint32_t *order = nullptr;
+            size_t m0 = ar.used;
+            if (sampled) {
+                uint64_t *k1 = ar.get<uint64_t>(tot), *k2 = ar.get<uint64_t>(tot);
+                uint32_t *v1 = ar.get<uint32_t>(tot);
+                order = ar.get<uint32_t>(tot);
+                launch(k_nn_keys, nblk(tot, 256), 256, 0, st, N, base, cnt, (const int32_t *)soff,
+                       (const int32_t *)sidx, (int64_t)tot, (int)cfg.exact_ll_calc, k1, v1);
+                int bits = 33;
+                while (bits < 64 && ((int64_t)1 << (bits - 32)) < cnt) bits++;
+                sort_pairs(ar, k1, k2, v1, order, tot, bits, st);
+            }
+            launch(k_nn, nblk(tot, 128), 128, 0, st, F.nodes, W, N, base, cnt, soff, sidx, prad,
+                   (int64_t)tot, (int)cfg.exact_ll_calc, err, (const uint32_t *)order);
+            ar.used = m0;
+        }
         {
             int ntmax = 0;
             for (int32_t k = 0; k < cnt; k++) {
@@ -2361,11 +2423,14 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             // later neighbours within target_r, as CSR lists
             int32_t *ncnt = par, *noff = root;
             RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
-            launch(k_fof6_w<0>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
-                   (const int32_t *)nullptr, ncnt, (int32_t *)nullptr, err, near);
+            int32_t *slots = ar.get<int32_t>((size_t)M * RSG_SLOT6);
+            launch(k_fof6_w<2>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
+                   (const int32_t *)nullptr, ncnt, slots, err, near);
             check_i32_total(ar, ncnt, M + 1, "6D neighbour lists", st);
             int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
             int32_t *nbr = ar.get<int32_t>(ne + 1);
+            launch(k_slots_csr, nblk(M, 256), 256, 0, st, eln, M, (const int32_t *)ncnt,
+                   (const int32_t *)noff, (const int32_t *)slots, nbr);
             launch(k_fof6_w<1>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
                    (const int32_t *)noff, ncnt, nbr, err, near);
             phase_mark(st, "d.fof6d");
