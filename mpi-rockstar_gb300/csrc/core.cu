@@ -82,11 +82,11 @@ __global__ void k_level_advance(LevelState *ls, const int64_t *off, int32_t *lvl
 
 __global__ void k_root_owner(const int32_t *rstart, const int32_t *rn, int32_t ntrees, int leaf,
                              int32_t *owner, int32_t *box_owner) {
-    int t = blockIdx.x;
+    int t = blockIdx.x;  // tree; blockIdx.y strides through its elements
     if (t >= ntrees) return;
     int s = rstart[t], n = rn[t];
     int o = n > leaf ? t : -1;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = blockIdx.y * blockDim.x + threadIdx.x; i < n; i += gridDim.y * blockDim.x) {
         box_owner[s + i] = t;
         owner[s + i] = o;
     }

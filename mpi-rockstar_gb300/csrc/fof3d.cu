@@ -331,16 +331,23 @@ __global__ void k_seed_mark(const KNode<3> *nodes, const Rec *recs, int n, float
         s);
 }
 
-// g(j): the first processed particle k with |S_r(k)| >= 2 (in tree order)
-// whose r-sphere holds j -- the moment link_particle_to_fof gives j its
-// label (src/fof.c:112-140).
-__global__ void k_gtime_r(const KNode<3> *nodes, const Rec *recs, int n, float r,
-                          const uint8_t *cnt, const uint8_t *skipped, int *gtime, int *err) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n || skipped[k] || cnt[k] < 2) return;
-    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
-    sphere3(
-        nodes, 0, recs, c, r, err,
+// The label events of the 3D FOF: processed particles (not skipped) with at
+// least two particles in their r-sphere, in tree order.  The three searches
+// below take them 32 at a time with the warp-cooperative walk, so every lane
+// meets the points of its own search in the reference's order.
+
+// g(j): the first event whose r-sphere holds j -- the moment
+// link_particle_to_fof gives j its label (src/fof.c:112-140).
+__global__ void __launch_bounds__(128) k_gtime_w(const KNode<3> *nodes, const Rec *recs,
+                                                 const int *ev, int nev, float r, int *gtime,
+                                                 int *err) {
+    if (warp_idle(nev)) return;
+    int k;
+    bool act = warp_query(ev, nev, &k);
+    float c[3] = {0, 0, 0};
+    if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
+    sphere3_warp(
+        nodes, recs, c, act, r, -1, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++) atomicMin(&gtime[j], k);
             return true;
@@ -353,25 +360,26 @@ __global__ void k_gtime_r(const KNode<3> *nodes, const Rec *recs, int n, float r
 
 // f(k), the set event k works on (src/fof.c:116-131): k's own label when an
 // earlier event gave it one, else the label of the first particle of S_r(k)
-// (walk order) labelled before k, else a new set (ptr = k).  -1: no event.
-__global__ void k_fptr3(const KNode<3> *nodes, const Rec *recs, int n, float r,
-                        const uint8_t *cnt, const uint8_t *skipped, const int *gtime, int *ptr,
-                        int *err) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    if (skipped[k] || cnt[k] < 2) {
-        ptr[k] = -1;
-        return;
-    }
-    int gk = gtime[k];
-    if (gk < k) {
-        ptr[k] = gk;
-        return;
-    }
+// (walk order) labelled before k, else a new set (ptr = k).  ptr of a
+// particle that is no event stays -1.
+__global__ void __launch_bounds__(128) k_fptr_w(const KNode<3> *nodes, const Rec *recs,
+                                                const int *ev, int nev, float r, const int *gtime,
+                                                int *ptr, int *err) {
+    if (warp_idle(nev)) return;
+    int k;
+    bool act = warp_query(ev, nev, &k);
     int p = k;
-    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
-    sphere3(
-        nodes, 0, recs, c, r, err,
+    if (act) {
+        int gk = gtime[k];
+        if (gk < k) {
+            p = gk;
+            act = false;  // no search needed
+        }
+    }
+    float c[3] = {0, 0, 0};
+    if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
+    sphere3_warp(
+        nodes, recs, c, act, r, -1, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++)
                 if (gtime[j] < k) {
@@ -387,24 +395,28 @@ __global__ void k_fptr3(const KNode<3> *nodes, const Rec *recs, int n, float r,
             }
             return true;
         });
-    ptr[k] = p;
+    if (k >= 0) ptr[k] = p;
 }
 
 // Candidate merges of event k in walk order: for every particle of S_r(k)
 // labelled before k, link_particle_to_fof joins f(k)'s set to that
 // particle's set (src/fof.c:133-139); a seed then does the same for every
-// particle of S_2r(k) labelled by then (link_fof_to_fof, src/fof.c:142-158).  A label equal to f(k), or one this
-// event already emitted, changes nothing and is skipped.  Keys order the
-// candidates in time: (k, sphere, position in the result list).
+// particle of S_2r(k) labelled by then (link_fof_to_fof, src/fof.c:142-158).
+// A label equal to f(k), or one this event already emitted, changes nothing
+// and is skipped.  Keys order the candidates in time: (k, sphere, position
+// in the result list).
 #define RSG_CAND_SEEN 8
-__global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r, float r2x,
-                        const uint8_t *cnt, const uint8_t *skipped, const uint8_t *state,
-                        const int *gtime, const int32_t *lab0, const int32_t *sfid, int64_t cap,
-                        unsigned long long *count, uint64_t *ckey, int32_t *cF, int32_t *cW,
-                        int *err) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n || skipped[k] || cnt[k] < 2) return;
-    const int F = sfid[k];
+__global__ void __launch_bounds__(128) k_cand_w(const KNode<3> *nodes, const Rec *recs,
+                                                const int *ev, int nev, float r, float r2x,
+                                                const uint8_t *state, const int *gtime,
+                                                const int32_t *lab0, const int32_t *sfid,
+                                                int64_t cap, unsigned long long *count,
+                                                uint64_t *ckey, int32_t *cF, int32_t *cW,
+                                                int *err) {
+    if (warp_idle(nev)) return;
+    int k;
+    bool act = warp_query(ev, nev, &k);
+    const int F = act ? sfid[k] : -1;
     int seen[RSG_CAND_SEEN];
     int ns = 0;
     uint32_t pos = 0;
@@ -427,9 +439,10 @@ __global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r, 
         }
         pos++;
     };
-    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
-    sphere3(
-        nodes, 0, recs, c, r, err,
+    float c[3] = {0, 0, 0};
+    if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
+    sphere3_warp(
+        nodes, recs, c, act, r, -1, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++) visit(j);
             return true;
@@ -438,11 +451,10 @@ __global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r, 
             visit(j);
             return true;
         });
-    if (state[k] != 1) return;
     phase = 1;
     pos = 0;
-    sphere3(
-        nodes, 0, recs, c, r2x, err,
+    sphere3_warp(
+        nodes, recs, c, act && state[k] == 1, r2x, -1, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++) visit(j);
             return true;
@@ -553,6 +565,10 @@ __global__ void k_iota(int *a, int n) {
     if (i < n) a[i] = i;
 }
 
+struct EvFlag {
+    const uint8_t *cnt, *skipped;
+    __device__ uint8_t operator()(int i) const { return !skipped[i] && cnt[i] >= 2; }
+};
 struct DFlag {
     const uint8_t *c;
     __device__ uint8_t operator()(int i) const { return c[i] > 16; }
@@ -779,13 +795,16 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)state, skipped,
            err);
     // labels exactly as the reference's union-find leaves them (uflabels.cuh)
+    int *ev = ar.get<int>(n);
+    int nev = select_where(ar, n, EvFlag{cnt, skipped}, ev, st);
     int *gtime = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(gtime, 0x7f, sizeof(int) * n, st));  // 0x7f7f7f7f: never
-    launch(k_gtime_r, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
-           (const uint8_t *)skipped, gtime, err);
+    launch(k_gtime_w, nblk(nev, TW), TW, 0, st, F.nodes, recs, (const int *)ev, nev, r, gtime,
+           err);
     int32_t *ptr = ar.get<int32_t>(n), *sfid = ar.get<int32_t>(n), *nsc = ar.get<int32_t>(n + 1);
-    launch(k_fptr3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
-           (const uint8_t *)skipped, (const int *)gtime, ptr, err);
+    RSG_CUDA(cudaMemsetAsync(ptr, 0xff, sizeof(int32_t) * n, st));
+    launch(k_fptr_w, nblk(nev, TW), TW, 0, st, F.nodes, recs, (const int *)ev, nev, r,
+           (const int *)gtime, ptr, err);
     RSG_CHECK_LAUNCH();
     int64_t S = uf_resolve(ar, ptr, n, sfid, nsc, st);
     phase_mark(st, "fof.first_links");
@@ -809,9 +828,9 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
         cF = ar.get<int32_t>(ccap);
         cW = ar.get<int32_t>(ccap);
         RSG_CUDA(cudaMemsetAsync(ccount, 0, sizeof(unsigned long long), st));
-        launch(k_cand3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, r2x, (const uint8_t *)cnt,
-               (const uint8_t *)skipped, (const uint8_t *)state, (const int *)gtime,
-               (const int32_t *)lab0, (const int32_t *)sfid, ccap, ccount, ckey, cF, cW, err);
+        launch(k_cand_w, nblk(nev, TW), TW, 0, st, F.nodes, recs, (const int *)ev, nev, r, r2x,
+               (const uint8_t *)state, (const int *)gtime, (const int32_t *)lab0,
+               (const int32_t *)sfid, ccap, ccount, ckey, cF, cW, err);
         RSG_CHECK_LAUNCH();
         RSG_CUDA(cudaMemcpyAsync(&hc, ccount, sizeof(hc), cudaMemcpyDeviceToHost, st));
         RSG_CUDA(cudaStreamSynchronize(st));

@@ -213,12 +213,6 @@ __global__ void k_scatter(const KNode<D> *nodes, const RecT *src, RecT *dst, int
     dst[s + d] = src[i];
 }
 
-template <class RecT>
-__global__ void k_copy_owned(const RecT *src, RecT *dst, int64_t nrec, const int32_t *owner) {
-    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= nrec) return;
-    if (owner[i] >= 0) dst[i] = src[i];
-}
 
 // Split bookkeeping (src/fast3tree.c:798-846): create children for nodes
 // with 0 < m < n, turn the rest into leaves.  off[k] packs, over the active
@@ -266,10 +260,13 @@ __global__ void k_children(KNode<D> *nodes, const int32_t *act, LevelState *ls,
     }
 }
 
-// Element owner update: elements of split nodes move to their child.
-template <int D>
+// Element owner update: elements of split nodes move to their child.  The
+// levels scatter between two buffers; an element whose node stops splitting
+// is final now, and is copied from the buffer the level wrote (cur) to the
+// output array (out) when they differ -- once per element, not once per level.
+template <int D, class RecT>
 __global__ void k_owner_update(const KNode<D> *nodes, int64_t nrec, int32_t *owner,
-                               int32_t *box_owner, int leaf) {
+                               int32_t *box_owner, int leaf, const RecT *cur, RecT *out) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= nrec) return;
     int a = owner[i];
@@ -281,12 +278,15 @@ __global__ void k_owner_update(const KNode<D> *nodes, int64_t nrec, int32_t *own
     if (nd.left < 0) {
         owner[i] = -1;
         box_owner[i] = -1;
+        if (cur != out) out[i] = cur[i];
         return;
     }
     int l = nd.left;
     int c = (i - nd.start) < nodes[l].n ? l : l + 1;
     box_owner[i] = c;
-    owner[i] = (nodes[c].n > leaf) ? c : -1;
+    bool fin = nodes[c].n <= leaf;
+    owner[i] = fin ? -1 : c;
+    if (fin && cur != out) out[i] = cur[i];
 }
 
 // sflag[0 .. ub]: per active node, split (high 32 bits) and children that

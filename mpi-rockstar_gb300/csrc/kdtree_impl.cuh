@@ -157,7 +157,11 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
     launch(k_root_init<D, RecT>, nblk(ntrees, T), T, 0, st, rstart, rn, ntrees, nodes, bmin, bmax);
     RSG_CUDA(cudaMemsetAsync(owner, 0xff, sizeof(int32_t) * nrec, st));
     RSG_CUDA(cudaMemsetAsync(box_owner, 0xff, sizeof(int32_t) * nrec, st));
-    launch(k_root_owner, ntrees, 256, 0, st, rstart, rn, ntrees, leaf, owner, box_owner);
+    {
+        int64_t avg = n_in_trees / ntrees, y = avg / 2048;
+        dim3 g((unsigned)ntrees, (unsigned)(y < 1 ? 1 : (y > 4096 ? 4096 : y)));
+        launch(k_root_owner, g, 256, 0, st, rstart, rn, ntrees, leaf, owner, box_owner);
+    }
     RSG_CHECK_LAUNCH();
     const int IT = 8;
     launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st, recs, nrec, box_owner,
@@ -184,6 +188,8 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
     const int64_t amax = n_in_trees / (leaf + 1) + ntrees;
     int64_t ub = hs.nact;
     int level = 0;
+    RecT *buf[2] = {recs, tmp};  // levels scatter back and forth between these
+    int cur = 0;
     while (hs.nact > 0) {
         for (int b = 0; b < RSG_FOREST_BATCH && ub > 0; b++) {
             if (++level > RSG_FOREST_LEVELS) {
@@ -195,16 +201,16 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
                    slot);
             launch(k_prep<D>, nblk(u, T), T, 0, st, nodes, (const int32_t *)act,
                    (const LevelState *)ls, lim);
-            launch(k_flags<D, RecT>, nblk(nrec + 1, T), T, 0, st, recs, nrec, owner, slot, nodes,
-                   lim, flag);
+            launch(k_flags<D, RecT>, nblk(nrec + 1, T), T, 0, st, (const RecT *)buf[cur], nrec,
+                   owner, slot, nodes, lim, flag);
             cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, flag, rank, (int)(nrec + 1), st);
             launch(k_counts<D>, nblk(u, T), T, 0, st, nodes, (const int32_t *)act,
                    (const LevelState *)ls, rank, m_arr, q_arr);
             launch(k_tables<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, slot, flag, rank,
                    m_arr, fb, bs);
-            launch(k_scatter<D, RecT>, nblk(nrec, T), T, 0, st, nodes, recs, tmp, nrec, owner, slot,
-                   flag, rank, m_arr, q_arr, fb, bs);
-            launch(k_copy_owned<RecT>, nblk(nrec, T), T, 0, st, tmp, recs, nrec, owner);
+            launch(k_scatter<D, RecT>, nblk(nrec, T), T, 0, st, nodes, (const RecT *)buf[cur],
+                   buf[1 - cur], nrec, owner, slot, flag, rank, m_arr, q_arr, fb, bs);
+            cur ^= 1;
             launch(k_split_flags<D>, nblk(u + 1, T), T, 0, st, m_arr, nodes, (const int32_t *)act,
                    (const LevelState *)ls, u, leaf, sflag);
             cub::DeviceScan::ExclusiveSum(cub_tmp, cub_bytes, sflag, soff, u + 1, st);
@@ -213,9 +219,10 @@ Forest<D> build_forest(Arena &ar, RecT *recs, int64_t nrec, const int32_t *rstar
                    (const int64_t *)soff, (int32_t)cap, leaf, act2, bmin, bmax);
             launch(k_level_advance, 1, 32, 0, st, ls, (const int64_t *)soff, lvl_end, level - 1);
             std::swap(act, act2);  // the next level's active nodes
-            launch(k_owner_update<D>, nblk(nrec, T), T, 0, st, nodes, nrec, owner, box_owner, leaf);
-            launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st, recs, nrec,
-                   box_owner, bmin, bmax);
+            launch(k_owner_update<D, RecT>, nblk(nrec, T), T, 0, st, nodes, nrec, owner,
+                   box_owner, leaf, (const RecT *)buf[cur], recs);
+            launch(k_box_runs<D, RecT, IT>, nblk((nrec + IT - 1) / IT, T), T, 0, st,
+                   (const RecT *)buf[cur], nrec, box_owner, bmin, bmax);
             const int64_t u2 = std::min<int64_t>(2 * ub, cap);
             launch(k_box_final_lvl<D>, nblk(u2, T), T, 0, st, nodes, (const LevelState *)ls,
                    (int32_t)u2, bmin, bmax);

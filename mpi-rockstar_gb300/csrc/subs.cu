@@ -748,7 +748,7 @@ __global__ void k_fill_eln(HierNodes N, int32_t base, int32_t *eln) {
 // its first RSG_SLOT6 entries in a fixed slot per particle (one pass for
 // almost every particle); MODE 1 fills the CSR lists of the particles whose
 // list is longer than that.
-#define RSG_SLOT6 16
+#define RSG_SLOT6 32
 template <int MODE>
 __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec *W, int64_t M,
                                                 HierNodes N, int32_t base, const int32_t *eln,
