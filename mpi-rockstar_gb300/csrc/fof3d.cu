@@ -114,9 +114,17 @@ __device__ bool sphere3(const KNode<3> *nodes, int root, const Rec *recs, const 
 // returning false ends that lane's walk; nodes holding no index after the
 // lane's `after` are dropped for that lane (the points it finds after
 // `after` are unchanged).
-template <class FR, class FP>
+// on_leaf(j, hit), when given (LEAF = true), replaces on_point for leaf
+// points: every lane calls it for every point of a leaf any lane tests, in
+// converged code, with hit telling whether the point is in this lane's
+// sphere (warp-level ballots inside it are safe).  It cannot end a walk.
+struct NoLeaf {
+    __device__ void operator()(int, bool) const {}
+};
+template <class FR, class FP, bool LEAF = false, class FL = NoLeaf>
 __device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float *c, bool active,
-                             float r, int after, int *errflag, FR on_range, FP on_point) {
+                             float r, int after, int *errflag, FR on_range, FP on_point,
+                             FL on_leaf = FL()) {
     const unsigned FULL = 0xffffffffu;
     const unsigned bit = 1u << (threadIdx.x & 31);
     const float r2 = fmul(r, r);
@@ -175,13 +183,16 @@ __device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float
             for (int k = 0; k < nd.n; k++) {
                 int j = nd.start + k;
                 float q0 = recs[j].pos[0], q1 = recs[j].pos[1], q2 = recs[j].pos[2];
+                bool hit = false;
                 if (kind == 3 && !stop) {
                     float dist = 0.f, dx;
                     dx = fsub(c[0], q0); dist = fadd(dist, fmul(dx, dx));
                     dx = fsub(c[1], q1); dist = fadd(dist, fmul(dx, dx));
                     dx = fsub(c[2], q2); dist = fadd(dist, fmul(dx, dx));
-                    if (dist < r2) stop = !on_point(j);
+                    hit = dist < r2;
                 }
+                if (LEAF) on_leaf(j, hit);
+                else if (hit) stop = !on_point(j);
             }
         }
         live &= ~__ballot_sync(FULL, stop);
@@ -297,16 +308,29 @@ __global__ void __launch_bounds__(128) k_llist_w(const KNode<3> *nodes, const Re
             m++;
         }
     };
-    sphere3_warp(
-        nodes, recs, c, act, r, act ? k : INT_MAX - 1, err,
-        [&](int s, int q) {
-            for (int j = s; j < s + q; j++) add(j);
-            return true;
-        },
-        [&](int j) {
-            add(j);
-            return true;
-        });
+    // leaf points: the warp's lanes that count the same point j add their
+    // counts to skipcnt[j] with one atomic
+    const unsigned lane = threadIdx.x & 31;
+    auto leaf = [&](int j, bool hit) {
+        bool inc = hit && j > k && cnt[j] > 16;
+        if (llist) {
+            if (inc) llist[base + m] = j;
+        } else {
+            unsigned b = __ballot_sync(0xffffffffu, inc);
+            if (b && lane == (unsigned)(__ffs(b) - 1)) atomicAdd(&skipcnt[j], __popc(b));
+        }
+        m += inc;
+    };
+    auto range = [&](int s, int q) {
+        for (int j = s; j < s + q; j++) add(j);
+        return true;
+    };
+    auto point = [&](int j) {
+        add(j);
+        return true;
+    };
+    sphere3_warp<decltype(range), decltype(point), true, decltype(leaf)>(
+        nodes, recs, c, act, r, act ? k : INT_MAX - 1, err, range, point, leaf);
     if (act && !llist) lcnt[k] = m;
 }
 // Searches with atomic updates on the points found keep one thread per
@@ -331,23 +355,16 @@ __global__ void k_seed_mark(const KNode<3> *nodes, const Rec *recs, int n, float
         s);
 }
 
-// The label events of the 3D FOF: processed particles (not skipped) with at
-// least two particles in their r-sphere, in tree order.  The three searches
-// below take them 32 at a time with the warp-cooperative walk, so every lane
-// meets the points of its own search in the reference's order.
-
-// g(j): the first event whose r-sphere holds j -- the moment
-// link_particle_to_fof gives j its label (src/fof.c:112-140).
-__global__ void __launch_bounds__(128) k_gtime_w(const KNode<3> *nodes, const Rec *recs,
-                                                 const int *ev, int nev, float r, int *gtime,
-                                                 int *err) {
-    if (warp_idle(nev)) return;
-    int k;
-    bool act = warp_query(ev, nev, &k);
-    float c[3] = {0, 0, 0};
-    if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
-    sphere3_warp(
-        nodes, recs, c, act, r, -1, err,
+// g(j): the first processed particle k with |S_r(k)| >= 2 (in tree order)
+// whose r-sphere holds j -- the moment link_particle_to_fof gives j its
+// label (src/fof.c:112-140).
+__global__ void k_gtime_r(const KNode<3> *nodes, const Rec *recs, int n, float r,
+                          const uint8_t *cnt, const uint8_t *skipped, int *gtime, int *err) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || skipped[k] || cnt[k] < 2) return;
+    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+    sphere3(
+        nodes, 0, recs, c, r, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++) atomicMin(&gtime[j], k);
             return true;
@@ -360,26 +377,25 @@ __global__ void __launch_bounds__(128) k_gtime_w(const KNode<3> *nodes, const Re
 
 // f(k), the set event k works on (src/fof.c:116-131): k's own label when an
 // earlier event gave it one, else the label of the first particle of S_r(k)
-// (walk order) labelled before k, else a new set (ptr = k).  ptr of a
-// particle that is no event stays -1.
-__global__ void __launch_bounds__(128) k_fptr_w(const KNode<3> *nodes, const Rec *recs,
-                                                const int *ev, int nev, float r, const int *gtime,
-                                                int *ptr, int *err) {
-    if (warp_idle(nev)) return;
-    int k;
-    bool act = warp_query(ev, nev, &k);
-    int p = k;
-    if (act) {
-        int gk = gtime[k];
-        if (gk < k) {
-            p = gk;
-            act = false;  // no search needed
-        }
+// (walk order) labelled before k, else a new set (ptr = k).  -1: no event.
+__global__ void k_fptr3(const KNode<3> *nodes, const Rec *recs, int n, float r,
+                        const uint8_t *cnt, const uint8_t *skipped, const int *gtime, int *ptr,
+                        int *err) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (skipped[k] || cnt[k] < 2) {
+        ptr[k] = -1;
+        return;
     }
-    float c[3] = {0, 0, 0};
-    if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
-    sphere3_warp(
-        nodes, recs, c, act, r, -1, err,
+    int gk = gtime[k];
+    if (gk < k) {
+        ptr[k] = gk;
+        return;
+    }
+    int p = k;
+    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+    sphere3(
+        nodes, 0, recs, c, r, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++)
                 if (gtime[j] < k) {
@@ -395,28 +411,24 @@ __global__ void __launch_bounds__(128) k_fptr_w(const KNode<3> *nodes, const Rec
             }
             return true;
         });
-    if (k >= 0) ptr[k] = p;
+    ptr[k] = p;
 }
 
 // Candidate merges of event k in walk order: for every particle of S_r(k)
 // labelled before k, link_particle_to_fof joins f(k)'s set to that
 // particle's set (src/fof.c:133-139); a seed then does the same for every
-// particle of S_2r(k) labelled by then (link_fof_to_fof, src/fof.c:142-158).
-// A label equal to f(k), or one this event already emitted, changes nothing
-// and is skipped.  Keys order the candidates in time: (k, sphere, position
-// in the result list).
+// particle of S_2r(k) labelled by then (link_fof_to_fof, src/fof.c:142-158).  A label equal to f(k), or one this
+// event already emitted, changes nothing and is skipped.  Keys order the
+// candidates in time: (k, sphere, position in the result list).
 #define RSG_CAND_SEEN 8
-__global__ void __launch_bounds__(128) k_cand_w(const KNode<3> *nodes, const Rec *recs,
-                                                const int *ev, int nev, float r, float r2x,
-                                                const uint8_t *state, const int *gtime,
-                                                const int32_t *lab0, const int32_t *sfid,
-                                                int64_t cap, unsigned long long *count,
-                                                uint64_t *ckey, int32_t *cF, int32_t *cW,
-                                                int *err) {
-    if (warp_idle(nev)) return;
-    int k;
-    bool act = warp_query(ev, nev, &k);
-    const int F = act ? sfid[k] : -1;
+__global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r, float r2x,
+                        const uint8_t *cnt, const uint8_t *skipped, const uint8_t *state,
+                        const int *gtime, const int32_t *lab0, const int32_t *sfid, int64_t cap,
+                        unsigned long long *count, uint64_t *ckey, int32_t *cF, int32_t *cW,
+                        int *err) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || skipped[k] || cnt[k] < 2) return;
+    const int F = sfid[k];
     int seen[RSG_CAND_SEEN];
     int ns = 0;
     uint32_t pos = 0;
@@ -439,10 +451,9 @@ __global__ void __launch_bounds__(128) k_cand_w(const KNode<3> *nodes, const Rec
         }
         pos++;
     };
-    float c[3] = {0, 0, 0};
-    if (act) { c[0] = recs[k].pos[0]; c[1] = recs[k].pos[1]; c[2] = recs[k].pos[2]; }
-    sphere3_warp(
-        nodes, recs, c, act, r, -1, err,
+    float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+    sphere3(
+        nodes, 0, recs, c, r, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++) visit(j);
             return true;
@@ -451,10 +462,11 @@ __global__ void __launch_bounds__(128) k_cand_w(const KNode<3> *nodes, const Rec
             visit(j);
             return true;
         });
+    if (state[k] != 1) return;
     phase = 1;
     pos = 0;
-    sphere3_warp(
-        nodes, recs, c, act && state[k] == 1, r2x, -1, err,
+    sphere3(
+        nodes, 0, recs, c, r2x, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++) visit(j);
             return true;
@@ -565,10 +577,6 @@ __global__ void k_iota(int *a, int n) {
     if (i < n) a[i] = i;
 }
 
-struct EvFlag {
-    const uint8_t *cnt, *skipped;
-    __device__ uint8_t operator()(int i) const { return !skipped[i] && cnt[i] >= 2; }
-};
 struct DFlag {
     const uint8_t *c;
     __device__ uint8_t operator()(int i) const { return c[i] > 16; }
@@ -795,16 +803,13 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)state, skipped,
            err);
     // labels exactly as the reference's union-find leaves them (uflabels.cuh)
-    int *ev = ar.get<int>(n);
-    int nev = select_where(ar, n, EvFlag{cnt, skipped}, ev, st);
     int *gtime = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(gtime, 0x7f, sizeof(int) * n, st));  // 0x7f7f7f7f: never
-    launch(k_gtime_w, nblk(nev, TW), TW, 0, st, F.nodes, recs, (const int *)ev, nev, r, gtime,
-           err);
+    launch(k_gtime_r, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
+           (const uint8_t *)skipped, gtime, err);
     int32_t *ptr = ar.get<int32_t>(n), *sfid = ar.get<int32_t>(n), *nsc = ar.get<int32_t>(n + 1);
-    RSG_CUDA(cudaMemsetAsync(ptr, 0xff, sizeof(int32_t) * n, st));
-    launch(k_fptr_w, nblk(nev, TW), TW, 0, st, F.nodes, recs, (const int *)ev, nev, r,
-           (const int *)gtime, ptr, err);
+    launch(k_fptr3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
+           (const uint8_t *)skipped, (const int *)gtime, ptr, err);
     RSG_CHECK_LAUNCH();
     int64_t S = uf_resolve(ar, ptr, n, sfid, nsc, st);
     phase_mark(st, "fof.first_links");
@@ -828,9 +833,9 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
         cF = ar.get<int32_t>(ccap);
         cW = ar.get<int32_t>(ccap);
         RSG_CUDA(cudaMemsetAsync(ccount, 0, sizeof(unsigned long long), st));
-        launch(k_cand_w, nblk(nev, TW), TW, 0, st, F.nodes, recs, (const int *)ev, nev, r, r2x,
-               (const uint8_t *)state, (const int *)gtime, (const int32_t *)lab0,
-               (const int32_t *)sfid, ccap, ccount, ckey, cF, cW, err);
+        launch(k_cand3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, r2x, (const uint8_t *)cnt,
+               (const uint8_t *)skipped, (const uint8_t *)state, (const int *)gtime,
+               (const int32_t *)lab0, (const int32_t *)sfid, ccap, ccount, ckey, cF, cW, err);
         RSG_CHECK_LAUNCH();
         RSG_CUDA(cudaMemcpyAsync(&hc, ccount, sizeof(hc), cudaMemcpyDeviceToHost, st));
         RSG_CUDA(cudaStreamSynchronize(st));

@@ -148,17 +148,33 @@ __global__ void k_ls_scatter(int64_t M, const int32_t *owner, LSeg S, const int3
     dst[s + d] = src[i];
     ldst[s + d] = lsrc[i];
 }
+// After a round: every element moves to the half of its segment it now
+// lies in; a half that goes on (flag) gets its compacted index (nidx), and
+// the elements of a half that is finished are final and are copied from the
+// buffer the round wrote (src) to the output arrays when they differ.
 template <class T>
-__global__ void k_ls_copy(int64_t M, const int32_t *owner, const T *src, T *dst,
-                          const int32_t *lsrc, int32_t *ldst) {
+__global__ void k_ls_owner_next(int64_t M, int32_t *owner, LSeg S, const int32_t *nflag,
+                                const int32_t *nidx, const T *src, T *dst, const int32_t *lsrc,
+                                int32_t *ldst) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M || owner[i] < 0) return;
-    dst[i] = src[i];
-    ldst[i] = lsrc[i];
+    if (i >= M) return;
+    int a = owner[i];
+    if (a < 0) return;
+    int h = 2 * a + ((i - S.start[a]) < S.m[a] ? 0 : 1);
+    if (nflag[h]) {
+        owner[i] = nidx[h];
+        return;
+    }
+    owner[i] = -1;
+    if (src != dst) {
+        dst[i] = src[i];
+        ldst[i] = lsrc[i];
+    }
 }
 // next round: both halves of every split segment with >= 2 elements
 static __global__ void k_ls_next(LSeg S, int32_t ns, int32_t *ns_start, int32_t *ns_n, int32_t *flag) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == ns) flag[2 * ns] = 0;  // the scan's last entry
     if (k >= ns) return;
     int s = S.start[k], n = S.n[k], m = S.m[k];
     bool split = S.mn[k] != S.mx[k];
@@ -201,36 +217,50 @@ void partition_sort_labels(Arena &ar, T *W, int32_t *lab, int64_t M,
     S.mn = ar.get<int32_t>(cap); S.mx = ar.get<int32_t>(cap);
     S.pivot = ar.get<int32_t>(cap); S.m = ar.get<int32_t>(cap); S.q = ar.get<int32_t>(cap);
     int32_t *nst = ar.get<int32_t>(2 * cap), *nn = ar.get<int32_t>(2 * cap);
-    int32_t *nflag = ar.get<int32_t>(2 * cap);
+    int32_t *nflag = ar.get<int32_t>(2 * cap + 1), *nidx = ar.get<int32_t>(2 * cap + 1);
     int32_t *owner = ar.get<int32_t>(M), *flag = ar.get<int32_t>(M + 1), *rank = ar.get<int32_t>(M + 1);
     int32_t *fb = ar.get<int32_t>(M), *bs = ar.get<int32_t>(M);
     T *tw = ar.get<T>(M);
     int32_t *tl = ar.get<int32_t>(M);
     int *cnt = ar.get<int>(1);
-    size_t b1 = 0, b2 = 0;
+    size_t b1 = 0, b2 = 0, b3 = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, b1, flag, rank, (int)(M + 1), st);
     cub::DeviceSelect::Flagged(nullptr, b2, nst, nflag, S.start, cnt, (int)(2 * cap), st);
-    void *tmp = ar.take((b1 > b2 ? b1 : b2) + 256);
-    size_t tb = (b1 > b2 ? b1 : b2) + 256;
+    cub::DeviceScan::ExclusiveSum(nullptr, b3, nflag, nidx, (int)(2 * cap + 1), st);
+    if (b2 > b1) b1 = b2;
+    if (b3 > b1) b1 = b3;
+    void *tmp = ar.take(b1 + 256);
+    size_t tb = b1 + 256;
     RSG_CUDA(cudaMemcpyAsync(S.start, s0.data(), 4 * ns, cudaMemcpyHostToDevice, st));
     RSG_CUDA(cudaMemcpyAsync(S.n, n0.data(), 4 * ns, cudaMemcpyHostToDevice, st));
+    // rounds scatter back and forth between (W, lab) and (tw, tl); an
+    // element is copied to (W, lab) once, when its segment is finished
+    T *wb[2] = {W, tw};
+    int32_t *lb[2] = {lab, tl};
+    int cur = 0;
+    launch(k_ls_owner, nblk(M, T_), T_, 0, st, (const int32_t *)S.start, (const int32_t *)S.n, ns,
+           M, owner);
     for (int round = 0; ns > 0; round++) {
         if (round > 200) {
             set_error(RSG_ERR_LIMIT, "label partition sort did not terminate");
             throw Failure();
         }
-        launch(k_ls_owner, nblk(M, T_), T_, 0, st, (const int32_t *)S.start, (const int32_t *)S.n,
-               ns, M, owner);
         launch(k_ls_init, nblk(ns, T_), T_, 0, st, S, ns);
-        launch(k_ls_minmax<8>, nblk((M + 7) / 8, T_), T_, 0, st, lab, M, owner, S);
+        launch(k_ls_minmax<8>, nblk((M + 7) / 8, T_), T_, 0, st, (const int32_t *)lb[cur], M,
+               (const int32_t *)owner, S);
         launch(k_ls_pivot, nblk(ns, T_), T_, 0, st, S, ns);
-        launch(k_ls_flags, nblk(M + 1, T_), T_, 0, st, lab, M, owner, S, flag);
+        launch(k_ls_flags, nblk(M + 1, T_), T_, 0, st, (const int32_t *)lb[cur], M,
+               (const int32_t *)owner, S, flag);
         cub::DeviceScan::ExclusiveSum(tmp, tb, flag, rank, (int)(M + 1), st);
         launch(k_ls_counts, nblk(ns, T_), T_, 0, st, S, ns, rank);
         launch(k_ls_tables, nblk(M, T_), T_, 0, st, M, owner, S, flag, rank, fb, bs);
-        launch(k_ls_scatter<T>, nblk(M, T_), T_, 0, st, M, owner, S, flag, rank, fb, bs, W, tw, lab, tl);
-        launch(k_ls_copy<T>, nblk(M, T_), T_, 0, st, M, owner, tw, W, tl, lab);
-        launch(k_ls_next, nblk(ns, T_), T_, 0, st, S, ns, nst, nn, nflag);
+        launch(k_ls_scatter<T>, nblk(M, T_), T_, 0, st, M, owner, S, flag, rank, fb, bs,
+               (const T *)wb[cur], wb[1 - cur], (const int32_t *)lb[cur], lb[1 - cur]);
+        cur ^= 1;
+        launch(k_ls_next, nblk(ns + 1, T_), T_, 0, st, S, ns, nst, nn, nflag);
+        cub::DeviceScan::ExclusiveSum(tmp, tb, nflag, nidx, 2 * ns + 1, st);
+        launch(k_ls_owner_next<T>, nblk(M, T_), T_, 0, st, M, owner, S, (const int32_t *)nflag,
+               (const int32_t *)nidx, (const T *)wb[cur], W, (const int32_t *)lb[cur], lab);
         cub::DeviceSelect::Flagged(tmp, tb, nst, nflag, S.start, cnt, 2 * ns, st);
         cub::DeviceSelect::Flagged(tmp, tb, nn, nflag, S.n, cnt, 2 * ns, st);
         RSG_CHECK_LAUNCH();

@@ -610,7 +610,7 @@ __global__ void k_sg_v2_fin(int32_t NH, rsg_halo *H, const int32_t *c0, const in
 // particles the inertia tensor is close to singular and its smallest
 // eigenvalue is rounding noise, so only the reference's own summation order
 // reproduces its axis ratios.
-#define RSG_SHAPE_SEQ 64
+#define RSG_SHAPE_SEQ 256
 __global__ void k_sh_init(int32_t NH, rsg_halo *H, const int32_t *cnt, const int32_t *toff,
                           const DevCfg *Cp, int which, HS *S) {
     int h = blockIdx.x * blockDim.x + threadIdx.x;
