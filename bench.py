@@ -62,10 +62,10 @@ ALGO_BYTES = {
     # median selection: every sample distance read once
     "k_target_par": lambda st, L: 4.0 * st["samples_6d"] / max(L, 1),
     # later-dense lists: positions of the dense particles in both launches,
-    # every entry written once
-    "k_llist_w": lambda st, L: (32.0 * st["dense"] + 4.0 * st["later_list"]) / max(L, 1),
-    # seed selection: every list entry read, its pending count updated
-    "k_kahn": lambda st, L: 12.0 * st["later_list"] / max(L, 1),
+    # every entry (one per dense pair) written once
+    "k_llist_w": lambda st, L: (32.0 * st["dense"] + 4.0 * st["dense_pairs"]) / max(L, 1),
+    # seed frontiers: every list entry read, its pending count updated
+    "k_kahn": lambda st, L: 12.0 * st["dense_pairs"] / max(L, 1),
     # potentials: record read (48 B), potential written (8 B)
     "k_bh_walk": lambda st, L: 56.0 * st["pot_records"] / max(L, 1),
     # property scans: record read, kinetic energy written

@@ -266,12 +266,14 @@ int rsg_rockstar_fof_noalloc(const struct rsg_particle *d_in, int64_t num_p,
 #define RSG_STAT_HALOS_BIG 6
 #define RSG_STAT_HALOS_SMALL 7
 #define RSG_STAT_DENSE 8         /* 3D FOF particles with > 16 neighbours */
-#define RSG_STAT_LATER_LIST 9    /* 3D FOF later-dense-neighbour entries */
+#define RSG_STAT_DENSE_PAIRS 9   /* 3D FOF pairs of dense particles k < j with j in
+                                    k's r-sphere */
 #define RSG_STAT_6D_ITEMS 10     /* particles summed over the 6D hierarchy levels */
 #define RSG_STAT_6D_SAMPLES 11   /* linking-length samples summed over the levels */
 #define RSG_STAT_NEAR_6D 12      /* 6D particle pairs whose distance is within 1e-6
                                     (relative) of their subgroup's linking length */
-#define RSG_STAT_COUNT 13
+#define RSG_STAT_SEED_STEPS 13   /* 3D FOF seed frontiers (device-side loop steps) */
+#define RSG_STAT_COUNT 14
 int rsg_last_stats(int64_t *vals, int32_t n);
 
 /* Instrumentation: kernels launched by this library so far (process-wide),

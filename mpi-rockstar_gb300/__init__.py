@@ -341,8 +341,8 @@ def profile_read():
 
 
 STAT_NAMES = ("particles", "groups", "halos", "pot_records", "kept_big", "kept_small",
-              "halos_big", "halos_small", "dense", "later_list", "items_6d", "samples_6d",
-              "near_6d")
+              "halos_big", "halos_small", "dense", "dense_pairs", "items_6d", "samples_6d",
+              "near_6d", "seed_steps")
 
 
 def last_stats():

@@ -22,6 +22,7 @@
 // included.
 #include <limits.h>
 
+#include <cooperative_groups.h>
 #include <cub/cub.cuh>
 #include <thrust/binary_search.h>
 #include <thrust/execution_policy.h>
@@ -31,6 +32,42 @@
 #include "uflabels.cuh"
 
 namespace rsg {
+
+namespace cg = cooperative_groups;
+
+// The reference's two box tests, in its operation order:
+// _fast3tree_box_not_intersect_sphere and _fast3tree_box_inside_sphere
+// (src/fast3tree.c:293-330).
+__device__ __forceinline__ bool box_out3(const KNode<3> &nd, const float *c, float r2) {
+    float d = 0.f, e;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        if ((e = fsub(c[i], nd.mn[i])) < 0) {
+            d = fadd(d, fmul(e, e));
+            if (d >= r2) return true;
+        } else if ((e = fsub(c[i], nd.mx[i])) > 0) {
+            d = fadd(d, fmul(e, e));
+            if (d >= r2) return true;
+        }
+    }
+    return false;
+}
+__device__ __forceinline__ bool box_inside3(const KNode<3> &nd, const float *c, float r,
+                                            float r2) {
+    if (fabsf(fsub(c[0], nd.mn[0])) > r) return false;
+    float dist = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float dx = fsub(nd.mn[i], c[i]);
+        dx = fmul(dx, dx);
+        float dx2 = fsub(c[i], nd.mx[i]);
+        dx2 = fmul(dx2, dx2);
+        if (dx2 > dx) dx = dx2;
+        dist = fadd(dist, dx);
+        if (dist > r2) return false;
+    }
+    return true;
+}
 
 // Sphere search (src/fast3tree.c:377-414) on tree `root` of a 3D forest.
 // on_range(start, n) receives nodes that lie entirely inside the sphere
@@ -48,37 +85,8 @@ __device__ bool sphere3(const KNode<3> *nodes, int root, const Rec *recs, const 
     while (sp) {
         const KNode<3> &nd = nodes[stack[--sp]];
         if (nd.start + nd.n <= after + 1) continue;
-        // _fast3tree_box_not_intersect_sphere
-        float d = 0.f, e;
-        bool out = false;
-#pragma unroll
-        for (int i = 0; i < 3; i++) {
-            if ((e = fsub(c[i], nd.mn[i])) < 0) {
-                d = fadd(d, fmul(e, e));
-                if (d >= r2) { out = true; break; }
-            } else if ((e = fsub(c[i], nd.mx[i])) > 0) {
-                d = fadd(d, fmul(e, e));
-                if (d >= r2) { out = true; break; }
-            }
-        }
-        if (out) continue;
-        // _fast3tree_box_inside_sphere
-        bool inside = true;
-        if (fabsf(fsub(c[0], nd.mn[0])) > r) inside = false;
-        else {
-            float dist = 0.f;
-#pragma unroll
-            for (int i = 0; i < 3; i++) {
-                float dx = fsub(nd.mn[i], c[i]);
-                dx = fmul(dx, dx);
-                float dx2 = fsub(c[i], nd.mx[i]);
-                dx2 = fmul(dx2, dx2);
-                if (dx2 > dx) dx = dx2;
-                dist = fadd(dist, dx);
-                if (dist > r2) { inside = false; break; }
-            }
-        }
-        if (inside) {
+        if (box_out3(nd, c, r2)) continue;
+        if (box_inside3(nd, c, r, r2)) {
             if (!on_range(nd.start, nd.n)) return false;
             continue;
         }
@@ -144,38 +152,8 @@ __device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float
         int kind = 0;  // 1 out, 2 inside, 3 leaf points, 4 descend
         if (m & bit) {
             kind = 1;
-            if (nd.start + nd.n > after + 1) {
-                float d = 0.f, e;
-                bool out = false;
-#pragma unroll
-                for (int i = 0; i < 3; i++) {
-                    if ((e = fsub(c[i], nd.mn[i])) < 0) {
-                        d = fadd(d, fmul(e, e));
-                        if (d >= r2) { out = true; break; }
-                    } else if ((e = fsub(c[i], nd.mx[i])) > 0) {
-                        d = fadd(d, fmul(e, e));
-                        if (d >= r2) { out = true; break; }
-                    }
-                }
-                if (!out) {
-                    bool inside = true;
-                    if (fabsf(fsub(c[0], nd.mn[0])) > r) inside = false;
-                    else {
-                        float dist = 0.f;
-#pragma unroll
-                        for (int i = 0; i < 3; i++) {
-                            float dx = fsub(nd.mn[i], c[i]);
-                            dx = fmul(dx, dx);
-                            float dx2 = fsub(c[i], nd.mx[i]);
-                            dx2 = fmul(dx2, dx2);
-                            if (dx2 > dx) dx = dx2;
-                            dist = fadd(dist, dx);
-                            if (dist > r2) { inside = false; break; }
-                        }
-                    }
-                    kind = inside ? 2 : (nd.div < 0 ? 3 : 4);
-                }
-            }
+            if (nd.start + nd.n > after + 1 && !box_out3(nd, c, r2))
+                kind = box_inside3(nd, c, r, r2) ? 2 : (nd.div < 0 ? 3 : 4);
         }
         bool stop = false;
         if (kind == 2) stop = !on_range(nd.start, nd.n);
@@ -477,48 +455,102 @@ __global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r, 
         });
 }
 
-// One frontier step of the ordered independent set: every particle decided
-// in the previous step walks its later list once; a seed marks its later
-// neighbours as skipped, and every decided particle releases one pending
-// earlier neighbour of each.  A particle with none pending that was not
-// skipped is a seed (all its earlier potential skippers are decided and
-// none of them is a seed).
-// When the lists are built one chunk of particles [c0, cend) at a time
-// (lbase = loff[c0]), a particle decided beyond cend has no list yet: it
-// keeps its state and enters the first frontier of its own chunk.
-__global__ void k_kahn(const int *front, int nf, const int64_t *loff, int64_t lbase,
-                       const int *llist, int cend, int *state, int *skipcnt, int *next,
-                       int *nnext) {
-    int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= nf) return;
-    int k = front[w];
-    int sk = state[k];
-    for (int64_t e = loff[k] - lbase + lane; e < loff[k + 1] - lbase; e += 32) {
-        int j = llist[e];
-        if (sk == 1 && atomicCAS(&state[j], 0, 2) == 0 && j < cend) next[atomicAdd(nnext, 1)] = j;
-        if (atomicSub(&skipcnt[j], 1) == 1 && atomicCAS(&state[j], 0, 1) == 0 && j < cend)
-            next[atomicAdd(nnext, 1)] = j;
+// The ordered independent set of the dense particles (the seeds), decided
+// frontier by frontier.  Every dense particle enters the queue once, when it
+// is decided (or, for a particle decided beyond the chunk being walked, when
+// its own chunk starts); a frontier is queue[head, tail).  One warp walks the
+// later list of each frontier particle k: a seed marks its later neighbours
+// as skipped, and every decided particle releases one pending earlier
+// neighbour of each.  A particle with none pending that was not skipped is a
+// seed (all its earlier potential skippers are decided and none of them is
+// a seed).  When the lists are built one chunk of particles [c0, cend) at a
+// time (lbase = loff[c0]), a particle decided beyond cend has no list yet:
+// it keeps its state and enters the first frontier of its own chunk.
+struct KahnCtl {
+    int head, tail, next, iters, hit, overflow, cend, pad;
+    int64_t lbase;
+};
+struct KahnList {
+    const int64_t *loff;
+    const int *llist;
+    int *queue, qcap;
+    KahnCtl *ctl;
+    int *state, *skipcnt;
+};
+__device__ __forceinline__ void kahn_push(int *queue, int qcap, KahnCtl *ctl, int j) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(&ctl->next, (int)g.size());
+    const int at = g.shfl(base, 0) + (int)g.thread_rank();
+    if (at < qcap) queue[at] = j;
+    else ctl->overflow = 1;
+}
+__global__ void k_kahn(KahnList L) {
+    const int lane = threadIdx.x & 31;
+    const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const KahnCtl &C = *L.ctl;
+    const int head = C.head, tail = C.tail, cend = C.cend;
+    const int64_t lbase = C.lbase;
+    for (int f = head + w0; f < tail; f += nw) {
+        const int k = L.queue[f];
+        const int sk = L.state[k];
+        const int64_t e1 = L.loff[k + 1] - lbase;
+        for (int64_t e = L.loff[k] - lbase + lane; e < e1; e += 32) {
+            const int j = L.llist[e];
+            if (sk == 1 && atomicCAS(&L.state[j], 0, 2) == 0 && j < cend)
+                kahn_push(L.queue, L.qcap, L.ctl, j);
+            if (atomicSub(&L.skipcnt[j], 1) == 1 && atomicCAS(&L.state[j], 0, 1) == 0 && j < cend)
+                kahn_push(L.queue, L.qcap, L.ctl, j);
+        }
     }
 }
-// Dense particles with no earlier potential skipper are seeds; those of
-// [0, cend) start the first frontier.
+// Next frontier: the particles queued by the step just run.  False when
+// there are none or a limit was reached.
+__device__ __forceinline__ bool kahn_advance(KahnCtl *ctl, int qcap, int limit) {
+    const int old = ctl->tail;
+    const int nt = min(ctl->next, qcap);
+    ctl->head = old;
+    ctl->tail = nt;
+    const int it = ++ctl->iters;
+    bool more = nt > old && !ctl->overflow;
+    if (more && it >= limit) {
+        ctl->hit = 1;
+        more = false;
+    }
+    return more;
+}
+__global__ void k_kahn_next(KahnCtl *ctl, int qcap, int limit) { kahn_advance(ctl, qcap, limit); }
+__global__ void k_kahn_next_g(KahnCtl *ctl, int qcap, int limit, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, kahn_advance(ctl, qcap, limit) ? 1u : 0u);
+}
+// Dense particles with no earlier potential skipper are seeds; those before
+// the first chunk's end start the first frontier.
 __global__ void k_kahn_init(const int *dense, int nd, const int *skipcnt, int cend, int *state,
-                            int *front, int *nfront) {
+                            int *queue, int qcap, KahnCtl *ctl) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nd) return;
-    int i = dense[t];
+    const int i = dense[t];
     if (skipcnt[i] == 0) {
         state[i] = 1;
-        if (i < cend) front[atomicAdd(nfront, 1)] = i;
+        if (i < cend) kahn_push(queue, qcap, ctl, i);
     }
 }
 // First frontier of a later chunk: its dense particles already decided
 // while earlier chunks were walked.
-__global__ void k_kahn_chunk(const int *dense, int nd, const int *state, int *front, int *nfront) {
+__global__ void k_kahn_chunk(const int *dense, int nd, const int *state, int *queue, int qcap,
+                             KahnCtl *ctl) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nd) return;
-    int i = dense[t];
-    if (state[i] != 0) front[atomicAdd(nfront, 1)] = i;
+    const int i = dense[t];
+    if (state[i] != 0) kahn_push(queue, qcap, ctl, i);
+}
+// A chunk's walk begins: its list range and the frontier queued for it.
+__global__ void k_kahn_start(KahnCtl *ctl, int qcap, int cend, int64_t lbase) {
+    ctl->cend = cend;
+    ctl->lbase = lbase;
+    ctl->head = ctl->tail;
+    ctl->tail = min(ctl->next, qcap);
 }
 struct ChunkTarget {
     int64_t step;
@@ -580,6 +612,58 @@ __global__ void k_iota(int *a, int n) {
 struct DFlag {
     const uint8_t *c;
     __device__ uint8_t operator()(int i) const { return c[i] > 16; }
+};
+static int sm_count() {
+    int dev = 0, v = 0;
+    RSG_CUDA(cudaGetDevice(&dev));
+    RSG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    return v > 0 ? v : 1;
+}
+// The seed frontiers of one chunk as one graph: a while node whose body runs
+// a step (k_kahn) and advances the frontier (k_kahn_next_g sets the loop
+// condition), so no step waits for the host.
+struct KahnGraph {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t e = nullptr;
+    void build(int GK, int TK, KahnList L, int limit) {
+        RSG_CUDA(cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle h;
+        RSG_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cn, wn, nn;
+        RSG_CUDA(cudaGraphAddNode(&cn, g, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        void *wargs[] = {(void *)&L};
+        cudaKernelNodeParams kp = {};
+        kp.func = (void *)k_kahn;
+        kp.gridDim = dim3(GK);
+        kp.blockDim = dim3(TK);
+        kp.kernelParams = wargs;
+        RSG_CUDA(cudaGraphAddKernelNode(&wn, body, nullptr, 0, &kp));
+        KahnCtl *ctl = L.ctl;
+        int qcap = L.qcap;
+        void *nargs[] = {(void *)&ctl, (void *)&qcap, (void *)&limit, (void *)&h};
+        kp.func = (void *)k_kahn_next_g;
+        kp.gridDim = dim3(1);
+        kp.blockDim = dim3(1);
+        kp.kernelParams = nargs;
+        RSG_CUDA(cudaGraphAddKernelNode(&nn, body, &wn, 1, &kp));
+        RSG_CUDA(cudaGraphInstantiate(&e, g, 0));
+    }
+    cudaStream_t ran = nullptr;
+    void run(cudaStream_t st) {
+        ran = st;
+        RSG_CUDA(cudaGraphLaunch(e, st));
+    }
+    ~KahnGraph() {
+        if (ran) cudaStreamSynchronize(ran);  // not destroyed while it runs
+        if (e) cudaGraphExecDestroy(e);
+        if (g) cudaGraphDestroy(g);
+    }
 };
 // Indices i < n with pred(i), ascending, into out; returns their number.
 template <class Pred>
@@ -756,10 +840,24 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     const int nchunks = (int)cb_h.size() - 1;
     int *state32 = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(state32, 0, sizeof(int) * n, st));
-    int *fa = ar.get<int>(nd + 1), *fb = ar.get<int>(nd + 1), *nf = ar.get<int>(2);
-    RSG_CUDA(cudaMemsetAsync(nf, 0, sizeof(int) * 2, st));
-    launch(k_kahn_init, nblk(nd, T), T, 0, st, dense, nd, skipcnt, cb_h[1], state32, fa, nf);
-    int rounds = 0;
+    int *queue = ar.get<int>(nd + 1);
+    const int qcap = nd + 1;
+    KahnCtl *ctl = (KahnCtl *)ar.get<int64_t>(8);
+    RSG_CUDA(cudaMemsetAsync(ctl, 0, sizeof(KahnCtl), st));
+    launch(k_kahn_init, nblk(nd, T), T, 0, st, (const int *)dense, nd, (const int *)skipcnt,
+           cb_h[1], state32, queue, qcap, ctl);
+    const KahnList KL{(const int64_t *)loff, (const int *)llist, queue, qcap, ctl, state32, skipcnt};
+    // every step but a chunk's last decides a particle
+    const int limit = nd + nchunks + 2;
+    int kres = 0;
+    RSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&kres, k_kahn, 256, 0));
+    const int TK = 256, GK = (kres > 0 ? kres : 1) * sm_count();
+    // the frontier steps run as a device-side graph loop; with per-launch
+    // event timing, and in fixed storage (instantiating a graph may take
+    // device memory), the host drives the same steps
+    const bool host_loop = launch_stats().selecting || ar.fixed;
+    KahnGraph G;
+    if (!host_loop && nd > 0) G.build(GK, TK, KL, limit);
     for (int t = 0; t < nchunks; t++) {
         int d0 = db_h[t], d1 = db_h[t + 1];
         if (d1 <= d0) continue;
@@ -767,37 +865,43 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
         launch(k_llist_w, nblk(d1 - d0, TW), TW, 0, st, F.nodes, recs, (const int *)dense + d0,
                d1 - d0, r, (const uint8_t *)cnt, (const int64_t *)loff, lbase, lcnt, llist, skipcnt,
                err);
-        if (t > 0) {
-            RSG_CUDA(cudaMemsetAsync(nf, 0, sizeof(int), st));
+        if (t > 0)
             launch(k_kahn_chunk, nblk(d1 - d0, T), T, 0, st, (const int *)dense + d0, d1 - d0,
-                   (const int *)state32, fa, nf);
+                   (const int *)state32, queue, qcap, ctl);
+        launch(k_kahn_start, 1, 1, 0, st, ctl, qcap, cb_h[t + 1], lbase);
+        if (!host_loop) {
+            G.run(st);
+            continue;
         }
-        int hf = 0;
-        RSG_CUDA(cudaMemcpyAsync(&hf, nf, sizeof(int), cudaMemcpyDeviceToHost, st));
-        RSG_CUDA(cudaStreamSynchronize(st));
-        while (hf > 0) {
-            RSG_CUDA(cudaMemsetAsync(nf + 1, 0, sizeof(int), st));
-            launch(k_kahn, nblk((int64_t)hf * 32, T), T, 0, st, fa, hf, loff, lbase, llist,
-                   cb_h[t + 1], state32, skipcnt, fb, nf + 1);
-            RSG_CUDA(cudaMemcpyAsync(&hf, nf + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        for (;;) {
+            launch(k_kahn, GK, TK, 0, st, KL);
+            launch(k_kahn_next, 1, 1, 0, st, ctl, qcap, limit);
+            KahnCtl hc;
+            RSG_CUDA(cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, st));
             RSG_CUDA(cudaStreamSynchronize(st));
-            std::swap(fa, fb);
-            if (++rounds > 10000000) {
-                set_error(RSG_ERR_LIMIT, "seed selection did not converge");
-                throw Failure();
-            }
+            if (hc.tail <= hc.head || hc.hit || hc.overflow) break;
         }
     }
+    KahnCtl kc;
+    RSG_CUDA(cudaMemcpyAsync(&kc, ctl, sizeof(kc), cudaMemcpyDeviceToHost, st));
+    RSG_CUDA(cudaStreamSynchronize(st));
+    if (kc.hit || kc.overflow || kc.next != nd) {
+        set_error(RSG_ERR_LIMIT, "3D FOF seed selection left %lld of %d dense particles undecided",
+                  (long long)nd - kc.next, nd);
+        throw Failure();
+    }
+    if (G.e) launch_stats().launches += 2 * (int64_t)kc.iters;
     phase_mark(st, "fof.elist");
-    // non-dense particles: state 2 (never seeds)
+    // non-dense particles: state 0 (never seeds)
     uint8_t *state = ar.get<uint8_t>(n);
     launch(k_state8, nblk(n, T), T, 0, st, state32, n, state);
     phase_mark(st, "fof.seeds");
     if (getenv("RSG_TIMING"))
-        fprintf(stderr, "  [fof] dense %d, later-list %lld in %d chunk(s), frontier steps %d\n",
-                nd, (long long)ne, nchunks, rounds);
+        fprintf(stderr, "  [fof] dense %d, dense pairs %lld in %d chunk(s), frontier steps %d\n",
+                nd, (long long)ne, nchunks, kc.iters);
     last_stats()[RSG_STAT_DENSE] = nd;
-    last_stats()[RSG_STAT_LATER_LIST] = ne;
+    last_stats()[RSG_STAT_DENSE_PAIRS] = ne;
+    last_stats()[RSG_STAT_SEED_STEPS] = kc.iters;
     uint8_t *skipped = ar.get<uint8_t>(n);
     RSG_CUDA(cudaMemsetAsync(skipped, 0, n, st));
     launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)state, skipped,

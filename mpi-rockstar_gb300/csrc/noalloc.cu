@@ -2,7 +2,9 @@
 // scratch buffer of the device pipeline is carved from one fixed device
 // array declared in this file, and the caller passes device buffers and a
 // stream.  (The host side keeps a few small std::vector tables on the host
-// heap; no call here allocates or frees device memory.)
+// heap; no call here allocates or frees device memory.  The seed frontiers
+// of the 3D FOF, a device-side graph loop elsewhere, are driven from the
+// host here, step by step: instantiating a graph may take device memory.)
 //
 // Who needs it: an in-situ caller -- halo finding run inside an N-body
 // code's time step on the GPU that also holds the simulation -- owns the

@@ -109,14 +109,36 @@ def test_fof_chunked_later_lists(rk, cfg_id, scale, parts, monkeypatch):
     p, box, mp, _ = rk.synth(cfg_id, scale)
     cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
     whole = rk.rockstar_fof(p, cfg)
-    ne = rk.last_stats()["later_list"]
+    ne = rk.last_stats()["dense_pairs"]
     assert ne > 4 * (1 << 17)
     monkeypatch.setenv("RSG_FOF_LIST_ENTRIES", str(ne // parts))
     chunked = rk.rockstar_fof(p, cfg)
-    assert rk.last_stats()["later_list"] == ne
+    assert rk.last_stats()["dense_pairs"] == ne
     for a, b in zip(whole, chunked):
         assert a.tobytes() == b.tobytes()
     monkeypatch.setenv("RSG_FOF_LIST_ENTRIES", "1000")
     with pytest.raises(rk.RockstarError) as e:
         rk.rockstar_fof(p, cfg)
     assert e.value.code == -4
+
+
+@pytest.mark.parametrize("cfg_id,scale", [(2, 0.25), (3, 0.01)])
+def test_fof_seed_loop_forms(rk, cfg_id, scale):
+    """The seed frontiers run as a device-side graph loop; with per-launch
+    timing selected the same steps run host-driven.  Both give the same
+    groups, byte for byte, in the same number of steps."""
+    p, box, mp, _ = rk.synth(cfg_id, scale)
+    cfg = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    graph = rk.rockstar_fof(p, cfg)
+    st = rk.last_stats()
+    assert st["dense"] > 1000 and st["dense_pairs"] > st["dense"] and st["seed_steps"] > 2
+    rk.profile_select("6k_kahnE")  # the step kernel alone (mangled name)
+    try:
+        host = rk.rockstar_fof(p, cfg)
+        launches, ms = rk.profile_read()
+    finally:
+        rk.profile_select("")
+    assert rk.last_stats()["seed_steps"] == st["seed_steps"] == launches
+    assert rk.last_stats()["dense_pairs"] == st["dense_pairs"]
+    for a, b in zip(graph, host):
+        assert a.tobytes() == b.tobytes()
