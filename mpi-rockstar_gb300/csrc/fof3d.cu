@@ -188,6 +188,115 @@ __device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float
     }
 }
 
+// Warp-cooperative form of sphere3 for one query shared by the warp (the
+// position c of particle q): every point after `after` of the reference
+// walk's result set -- the points of the nodes it takes whole and the leaf
+// points nearer than r -- is handed to exactly one lane.  All lanes call it
+// together; every lane calls visit(j, valid) in converged code, once per
+// round of up to 32 points (valid false on a lane without a point), so
+// warp-level operations may be used inside visit.
+// Down q's root-to-leaf path the reference walk only descends until a node
+// it takes whole or whose other child it would enter (not out by its test,
+// holding an index after `after`); the warp starts there.  From there it
+// takes up to 32 nodes of a stack in shared memory per round and spreads
+// the points of the whole nodes and leaves met over its lanes.  The set of
+// points is the walk's; the order is not (the reference's is ascending
+// index, left subtree first).  The stack takes 32 nodes at a time while 64
+// slots and a tree depth of margin are free, one at a time otherwise
+// (depth-first growth is bounded by the tree depth); a tree deeper than
+// RSG_STACK sets errflag, as the scalar walk does.
+#define RSG_WSTK 1024
+template <class FV>
+__device__ void warp_sphere3(const KNode<3> *nodes, const Rec *recs, int q, const float *c,
+                             float r, int after, int *S, int *errflag, FV visit) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const float r2 = fmul(r, r);
+    int x = 0;
+    for (int depth = 0; depth < RSG_STACK; depth++) {
+        const KNode<3> &nd = nodes[x];
+        if (nd.div < 0 || box_inside3(nd, c, r, r2)) break;
+        const KNode<3> &L = nodes[nd.left];
+        const bool inL = q < L.start + L.n;
+        const KNode<3> &O = inL ? nodes[nd.left + 1] : L;
+        if (O.start + O.n > after + 1 && !box_out3(O, c, r2)) break;
+        x = inL ? nd.left : nd.left + 1;
+    }
+    __syncwarp();
+    if (lane == 0) S[0] = x;
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+        const int take = (sp + 64 <= RSG_WSTK - RSG_STACK) ? min(sp, 32) : 1;
+        const int xi = lane < take ? S[sp - 1 - lane] : -1;
+        sp -= take;
+        __syncwarp();
+        // 0 nothing, 1 whole node, 2 leaf points, 3 descend
+        int kind = 0, s0 = 0, m0 = 0, left = 0;
+        if (xi >= 0) {
+            const KNode<3> &nd = nodes[xi];
+            if (nd.start + nd.n > after + 1 && !box_out3(nd, c, r2)) {
+                kind = box_inside3(nd, c, r, r2) ? 1 : (nd.div < 0 ? 2 : 3);
+                s0 = nd.start;
+                m0 = nd.n;
+                left = nd.left;
+            }
+        }
+        const unsigned dm = __ballot_sync(FULL, kind == 3);
+        const int room = (RSG_WSTK - sp) >> 1;  // child pairs that fit
+        if (kind == 3 && __popc(dm & below) < room) {
+            const int at = sp + 2 * __popc(dm & below);
+            S[at] = left + 1;
+            S[at + 1] = left;
+        }
+        if (__popc(dm) > room) {
+            if (lane == 0) atomicExch(errflag, 1);
+            return;
+        }
+        sp += 2 * __popc(dm);
+        // the points after `after` of this round's whole nodes and leaves
+        const bool pts = kind == 1 || kind == 2;
+        const int a0 = pts ? max(s0, after + 1) : 0;
+        const int np = pts ? max(0, s0 + m0 - a0) : 0;
+        int incl = np;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(FULL, incl, 31);
+        for (int base = 0; base < total; base += 32) {
+            const int flat = base + lane;
+            int o = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+                const int v = __shfl_sync(FULL, incl, o + step - 1);
+                if (v <= flat) o += step;
+            }
+            const int oi = __shfl_sync(FULL, incl, o), on = __shfl_sync(FULL, np, o);
+            const int oa = __shfl_sync(FULL, a0, o), ok = __shfl_sync(FULL, kind, o);
+            int j = -1;
+            bool v = false;
+            if (flat < total) {
+                j = oa + (flat - (oi - on));
+                v = true;
+                if (ok == 2) {
+                    float dist = 0.f;
+#pragma unroll
+                    for (int t = 0; t < 3; t++) {
+                        const float dx = fsub(c[t], recs[j].pos[t]);
+                        dist = fadd(dist, fmul(dx, dx));
+                    }
+                    v = dist < r2;
+                }
+            }
+            visit(j, v);
+        }
+        __syncwarp();
+    }
+}
+
 // ---- kernels --------------------------------------------------------------
 __global__ void k_make_recs(const rsg_particle *p, int64_t n, Rec *recs, int *bad) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -311,35 +420,138 @@ __global__ void __launch_bounds__(128) k_llist_w(const KNode<3> *nodes, const Re
         nodes, recs, c, act, r, act ? k : INT_MAX - 1, err, range, point, leaf);
     if (act && !llist) lcnt[k] = m;
 }
-// Searches with atomic updates on the points found keep one thread per
-// query: neighbouring queries of one warp would update the same points at
-// the same moment.
-__global__ void k_seed_mark(const KNode<3> *nodes, const Rec *recs, int n, float r,
-                            const uint8_t *state, uint8_t *skipped, int *err) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || state[s] != 1) return;
-    float c[3] = {recs[s].pos[0], recs[s].pos[1], recs[s].pos[2]};
-    sphere3(
-        nodes, 0, recs, c, r, err,
-        [&](int a, int m) {
-            for (int j = a; j < a + m; j++)
-                if (j > s) skipped[j] = 1;
-            return true;
-        },
-        [&](int j) {
-            if (j > s) skipped[j] = 1;
-            return true;
-        },
-        s);
+// The seeds' searches run one warp per seed (warp_sphere3): a seed's
+// spheres hold hundreds to thousands of points, and its neighbours in tree
+// order are mostly skipped particles with no search of their own, so a
+// thread per particle would leave the warp to one lane.
+#define RSG_SEED_WARPS 4
+#define SEED_LOOP(ns)                                                                  \
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < (ns);               \
+         t += (gridDim.x * blockDim.x) >> 5)
+// every point after seed s of S_r(s) is skipped (src/rockstar.c:75-77)
+__global__ void __launch_bounds__(RSG_SEED_WARPS * 32)
+    k_seed_mark_w(const KNode<3> *nodes, const Rec *recs, const int *seeds, int ns, float r,
+                  uint8_t *skipped, int *err) {
+    __shared__ int stk[RSG_SEED_WARPS][RSG_WSTK];
+    int *S = stk[threadIdx.x >> 5];
+    SEED_LOOP(ns) {
+        const int k = seeds[t];
+        const float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+        warp_sphere3(nodes, recs, k, c, r, k, S, err, [&](int j, bool v) {
+            if (v) skipped[j] = 1;
+        });
+    }
+}
+// g(j) over the seeds' spheres (see k_gtime_r)
+__global__ void __launch_bounds__(RSG_SEED_WARPS * 32)
+    k_gtime_seed_w(const KNode<3> *nodes, const Rec *recs, const int *seeds, int ns, float r,
+                   int *gtime, int *err) {
+    __shared__ int stk[RSG_SEED_WARPS][RSG_WSTK];
+    int *S = stk[threadIdx.x >> 5];
+    SEED_LOOP(ns) {
+        const int k = seeds[t];
+        const float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+        warp_sphere3(nodes, recs, k, c, r, -1, S, err, [&](int j, bool v) {
+            if (v) atomicMin(&gtime[j], k);
+        });
+    }
+}
+// f(k) of the seeds (see k_fptr3): the first particle of S_r(k) in walk
+// order -- the smallest index -- labelled before k
+__global__ void __launch_bounds__(RSG_SEED_WARPS * 32)
+    k_fptr_seed_w(const KNode<3> *nodes, const Rec *recs, const int *seeds, int ns, float r,
+                  const int *gtime, int *ptr, int *err) {
+    __shared__ int stk[RSG_SEED_WARPS][RSG_WSTK];
+    int *S = stk[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    SEED_LOOP(ns) {
+        const int k = seeds[t];
+        const int gk = gtime[k];
+        if (gk < k) {
+            if (lane == 0) ptr[k] = gk;
+            continue;
+        }
+        const float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+        int best = INT_MAX;
+        warp_sphere3(nodes, recs, k, c, r, -1, S, err, [&](int j, bool v) {
+            if (v && j < best && gtime[j] < k) best = j;
+        });
+        best = __reduce_min_sync(0xffffffffu, best);
+        if (lane == 0) ptr[k] = best == INT_MAX ? k : gtime[best];
+    }
+}
+// Candidate merges of the seeds (see k_cand3): both spheres, S_r(k) with
+// the particles labelled before k, then S_2r(k) with those labelled by k.
+// A label is emitted once per sphere at its first occurrence in walk order
+// (the smallest index, which is the key's last field): a per-warp hash
+// table keeps the smallest index of every label met; a label that finds no
+// slot is emitted at every occurrence (a repeat is a no-op merge).
+#define RSG_CAND_HT 128
+__device__ __forceinline__ void cand_emit(int k, int phase, int j, int F, int W, int64_t cap,
+                                          unsigned long long *count, uint64_t *ckey, int32_t *cF,
+                                          int32_t *cW) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+    const unsigned long long u = g.shfl(base, 0) + g.thread_rank();
+    if ((int64_t)u < cap) {
+        ckey[u] = ((uint64_t)(uint32_t)k << 32) | ((uint64_t)phase << 31) | (uint32_t)j;
+        cF[u] = F;
+        cW[u] = W;
+    }
+}
+__global__ void __launch_bounds__(RSG_SEED_WARPS * 32)
+    k_cand_seed_w(const KNode<3> *nodes, const Rec *recs, const int *seeds, int ns, float r,
+                  float r2x, const int *gtime, const int32_t *lab0, const int32_t *sfid,
+                  int64_t cap, unsigned long long *count, uint64_t *ckey, int32_t *cF,
+                  int32_t *cW, int *err) {
+    __shared__ int stk[RSG_SEED_WARPS][RSG_WSTK];
+    __shared__ int hk[RSG_SEED_WARPS][RSG_CAND_HT], hv[RSG_SEED_WARPS][RSG_CAND_HT];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int *S = stk[w], *K = hk[w], *Vv = hv[w];
+    SEED_LOOP(ns) {
+        const int k = seeds[t];
+        const int F = sfid[k];
+        const float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
+        for (int phase = 0; phase < 2; phase++) {
+            for (int e = lane; e < RSG_CAND_HT; e += 32) {
+                K[e] = -1;
+                Vv[e] = INT_MAX;
+            }
+            __syncwarp();
+            warp_sphere3(nodes, recs, k, c, phase ? r2x : r, -1, S, err, [&](int j, bool v) {
+                if (!v) return;
+                const int gj = gtime[j];
+                if (!(phase == 0 ? gj < k : gj <= k)) return;
+                const int W = lab0[j];
+                if (W == F) return;
+                const unsigned h = ((unsigned)W * 2654435761u) >> 25;  // 7 bits
+                for (int pr = 0; pr < 8; pr++) {
+                    const int e = (h + pr) & (RSG_CAND_HT - 1);
+                    const int old = atomicCAS(&K[e], -1, W);
+                    if (old == -1 || old == W) {
+                        atomicMin(&Vv[e], j);
+                        return;
+                    }
+                }
+                cand_emit(k, phase, j, F, W, cap, count, ckey, cF, cW);
+            });
+            __syncwarp();
+            for (int e = lane; e < RSG_CAND_HT; e += 32)
+                if (K[e] != -1) cand_emit(k, phase, Vv[e], F, K[e], cap, count, ckey, cF, cW);
+            __syncwarp();
+        }
+    }
 }
 
 // g(j): the first processed particle k with |S_r(k)| >= 2 (in tree order)
 // whose r-sphere holds j -- the moment link_particle_to_fof gives j its
 // label (src/fof.c:112-140).
 __global__ void k_gtime_r(const KNode<3> *nodes, const Rec *recs, int n, float r,
-                          const uint8_t *cnt, const uint8_t *skipped, int *gtime, int *err) {
+                          const uint8_t *cnt, const uint8_t *skipped, const uint8_t *state,
+                          int *gtime, int *err) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n || skipped[k] || cnt[k] < 2) return;
+    if (k >= n || skipped[k] || cnt[k] < 2 || state[k] == 1) return;  // seeds: k_gtime_seed_w
     float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
     sphere3(
         nodes, 0, recs, c, r, err,
@@ -357,10 +569,10 @@ __global__ void k_gtime_r(const KNode<3> *nodes, const Rec *recs, int n, float r
 // earlier event gave it one, else the label of the first particle of S_r(k)
 // (walk order) labelled before k, else a new set (ptr = k).  -1: no event.
 __global__ void k_fptr3(const KNode<3> *nodes, const Rec *recs, int n, float r,
-                        const uint8_t *cnt, const uint8_t *skipped, const int *gtime, int *ptr,
-                        int *err) {
+                        const uint8_t *cnt, const uint8_t *skipped, const uint8_t *state,
+                        const int *gtime, int *ptr, int *err) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
+    if (k >= n || state[k] == 1) return;  // seeds: k_fptr_seed_w
     if (skipped[k] || cnt[k] < 2) {
         ptr[k] = -1;
         return;
@@ -395,25 +607,25 @@ __global__ void k_fptr3(const KNode<3> *nodes, const Rec *recs, int n, float r,
 // Candidate merges of event k in walk order: for every particle of S_r(k)
 // labelled before k, link_particle_to_fof joins f(k)'s set to that
 // particle's set (src/fof.c:133-139); a seed then does the same for every
-// particle of S_2r(k) labelled by then (link_fof_to_fof, src/fof.c:142-158).  A label equal to f(k), or one this
-// event already emitted, changes nothing and is skipped.  Keys order the
-// candidates in time: (k, sphere, position in the result list).
+// particle of S_2r(k) labelled by then (link_fof_to_fof, src/fof.c:142-158,
+// k_cand_seed_w).  A label equal to f(k), or one this event already
+// emitted, changes nothing and is skipped.  Keys order the candidates in
+// time: (k, sphere, position in the result list), the position being the
+// particle index (the walk lists points in ascending index order).
 #define RSG_CAND_SEEN 8
-__global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r, float r2x,
+__global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r,
                         const uint8_t *cnt, const uint8_t *skipped, const uint8_t *state,
                         const int *gtime, const int32_t *lab0, const int32_t *sfid, int64_t cap,
                         unsigned long long *count, uint64_t *ckey, int32_t *cF, int32_t *cW,
                         int *err) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n || skipped[k] || cnt[k] < 2) return;
+    if (k >= n || skipped[k] || cnt[k] < 2 || state[k] == 1) return;  // seeds: k_cand_seed_w
     const int F = sfid[k];
     int seen[RSG_CAND_SEEN];
     int ns = 0;
-    uint32_t pos = 0;
-    int phase = 0;
     auto visit = [&](int j) {
         int gj = gtime[j];
-        if (phase == 0 ? gj < k : gj <= k) {
+        if (gj < k) {
             int W = lab0[j];
             bool dup = (W == F);
             for (int q = 0; q < ns; q++) dup |= (seen[q] == W);
@@ -421,30 +633,16 @@ __global__ void k_cand3(const KNode<3> *nodes, const Rec *recs, int n, float r, 
                 if (ns < RSG_CAND_SEEN) seen[ns++] = W;
                 unsigned long long t = atomicAdd(count, 1ull);
                 if ((int64_t)t < cap) {
-                    ckey[t] = ((uint64_t)(uint32_t)k << 32) | ((uint64_t)phase << 31) | pos;
+                    ckey[t] = ((uint64_t)(uint32_t)k << 32) | (uint32_t)j;
                     cF[t] = F;
                     cW[t] = W;
                 }
             }
         }
-        pos++;
     };
     float c[3] = {recs[k].pos[0], recs[k].pos[1], recs[k].pos[2]};
     sphere3(
         nodes, 0, recs, c, r, err,
-        [&](int a, int m) {
-            for (int j = a; j < a + m; j++) visit(j);
-            return true;
-        },
-        [&](int j) {
-            visit(j);
-            return true;
-        });
-    if (state[k] != 1) return;
-    phase = 1;
-    pos = 0;
-    sphere3(
-        nodes, 0, recs, c, r2x, err,
         [&](int a, int m) {
             for (int j = a; j < a + m; j++) visit(j);
             return true;
@@ -609,6 +807,10 @@ __global__ void k_iota(int *a, int n) {
     if (i < n) a[i] = i;
 }
 
+struct SeedFlag {
+    const uint8_t *state;
+    __device__ uint8_t operator()(int i) const { return state[i] == 1; }
+};
 struct DFlag {
     const uint8_t *c;
     __device__ uint8_t operator()(int i) const { return c[i] > 16; }
@@ -902,18 +1104,25 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     last_stats()[RSG_STAT_DENSE] = nd;
     last_stats()[RSG_STAT_DENSE_PAIRS] = ne;
     last_stats()[RSG_STAT_SEED_STEPS] = kc.iters;
+    int *seeds = ar.get<int>(nd + 1);
+    const int nseed = select_where(ar, n, SeedFlag{state}, seeds, st);
+    const int TS = RSG_SEED_WARPS * 32;
+    const int GS = (int)nblk((int64_t)nseed * 32, TS);
     uint8_t *skipped = ar.get<uint8_t>(n);
     RSG_CUDA(cudaMemsetAsync(skipped, 0, n, st));
-    launch(k_seed_mark, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)state, skipped,
+    launch(k_seed_mark_w, GS, TS, 0, st, F.nodes, recs, (const int *)seeds, nseed, r, skipped,
            err);
     // labels exactly as the reference's union-find leaves them (uflabels.cuh)
     int *gtime = ar.get<int>(n);
     RSG_CUDA(cudaMemsetAsync(gtime, 0x7f, sizeof(int) * n, st));  // 0x7f7f7f7f: never
     launch(k_gtime_r, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
-           (const uint8_t *)skipped, gtime, err);
+           (const uint8_t *)skipped, (const uint8_t *)state, gtime, err);
+    launch(k_gtime_seed_w, GS, TS, 0, st, F.nodes, recs, (const int *)seeds, nseed, r, gtime, err);
     int32_t *ptr = ar.get<int32_t>(n), *sfid = ar.get<int32_t>(n), *nsc = ar.get<int32_t>(n + 1);
     launch(k_fptr3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
-           (const uint8_t *)skipped, (const int *)gtime, ptr, err);
+           (const uint8_t *)skipped, (const uint8_t *)state, (const int *)gtime, ptr, err);
+    launch(k_fptr_seed_w, GS, TS, 0, st, F.nodes, recs, (const int *)seeds, nseed, r,
+           (const int *)gtime, ptr, err);
     RSG_CHECK_LAUNCH();
     int64_t S = uf_resolve(ar, ptr, n, sfid, nsc, st);
     phase_mark(st, "fof.first_links");
@@ -937,9 +1146,12 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
         cF = ar.get<int32_t>(ccap);
         cW = ar.get<int32_t>(ccap);
         RSG_CUDA(cudaMemsetAsync(ccount, 0, sizeof(unsigned long long), st));
-        launch(k_cand3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, r2x, (const uint8_t *)cnt,
+        launch(k_cand3, nblk(n, T), T, 0, st, F.nodes, recs, n, r, (const uint8_t *)cnt,
                (const uint8_t *)skipped, (const uint8_t *)state, (const int *)gtime,
                (const int32_t *)lab0, (const int32_t *)sfid, ccap, ccount, ckey, cF, cW, err);
+        launch(k_cand_seed_w, GS, TS, 0, st, F.nodes, recs, (const int *)seeds, nseed, r, r2x,
+               (const int *)gtime, (const int32_t *)lab0, (const int32_t *)sfid, ccap, ccount,
+               ckey, cF, cW, err);
         RSG_CHECK_LAUNCH();
         RSG_CUDA(cudaMemcpyAsync(&hc, ccount, sizeof(hc), cudaMemcpyDeviceToHost, st));
         RSG_CUDA(cudaStreamSynchronize(st));
