@@ -78,9 +78,22 @@ ALGO_BYTES = {
 # dram__bytes_write.sum of the captured launch over the units it processed),
 # scaled to the timed launches by their units
 NCU_TRAFFIC = {
-    "k_fof6_w": (62.18e6 / 1364736.0, "items_6d",
-                 "one ncu capture of the level-0 launch on workload 2, scaled by particles"),
+    "k_fof6_w": ((137.976064e6 + 95.008e6) / 2309888.0, "items_6d",
+                 "one ncu capture of the level-0 launch on workload 4 at 1/32 scale, "
+                 "scaled by particles"),
 }
+# Instruction issue of the search kernels from the same captures: the share
+# of cycles an instruction issued and the lanes active per instruction.  For
+# a tree walk their product -- the share of the SM's lane-issue capacity
+# doing work -- says more than an HBM fraction.
+NCU_ISSUE = {
+    "k_fof6_w": (0.774138, 27.75),
+    "k_nn": (0.662851, 4.62),
+    "k_bh_walk": (0.698618, 19.11),
+    "k_llist_w": (0.642338, 14.73),
+    "k_kahn": (0.219013, 27.52),
+}
+NCU_ISSUE_SOURCE = "ncu, workload 4 at 1/32 scale, one launch per kernel"
 
 
 def short_name(mangled):
@@ -673,6 +686,10 @@ def main():
                 "traffic_source": tsrc,
                 "algorithmic_bytes_per_launch": algo, "launches": kl, "avg_ms": avg_ms,
                 "share_of_step": share,
+                "issue": ({"issue_active": NCU_ISSUE[top][0],
+                           "lanes_per_instruction": NCU_ISSUE[top][1],
+                           "issue_x_lanes": NCU_ISSUE[top][0] * NCU_ISSUE[top][1] / 32.0,
+                           "source": NCU_ISSUE_SOURCE} if top in NCU_ISSUE else None),
                 "peak_kind": "measured copy (MEASURED_PEAKS.json hbm_gbs)"
                              if pk_kind == "measured" else "fallback 6.8 TB/s"}
     line = {"metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
