@@ -33,6 +33,7 @@ extern "C" {
 #define RSG_ERR_LIMIT (-4)      /* a bounded device loop hit its limit */
 #define RSG_ERR_INPUT (-5)      /* non-finite particle data */
 #define RSG_ERR_BUSY (-6)       /* a call that shares fixed scratch is in progress */
+#define RSG_ERR_IO (-7)         /* a catalogue file could not be opened or written */
 
 struct rsg_particle { int64_t id; float pos[6]; };
 struct rsg_fof { int64_t num_p; struct rsg_particle *particles; };
@@ -184,6 +185,42 @@ int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct
 int rsg_compute_kinetic_energy(struct rsg_potential *po, int64_t num_po, const float *vel_cen,
                                const float *pos_cen, float scale_now,
                                const struct rsg_config *cfg);
+
+/* Catalogue output (host; the halos, links and particles the calls above
+ * return, p_start relative to p).  Options of one catalogue: */
+struct rsg_catalog {
+    int64_t id_offset;        /* id of the first halo written */
+    int64_t snap, chunk;      /* binary header fields */
+    const float *bounds;      /* 6 floats (min x y z, max x y z) or NULL: every
+                                 halo is within bounds; the binary header then
+                                 gets the printed halos' extent */
+    int64_t num_p;            /* "#Total particles processed" (0: line omitted) */
+    int64_t strict_so_masses; /* STRICT_SO_MASSES (ascii header line) */
+};
+/* _should_print (src/io/meta_io.c:266-286): the halo is inside bounds, and
+ * carries ALWAYS_PRINT_FLAG or has at least MIN_HALO_OUTPUT_SIZE particles,
+ * m * UNBOUND_THRESHOLD < mgrav and mgrav >= 1.5 PARTICLE_MASS (the last
+ * when UNBOUND_THRESHOLD > 0).  Returns 1 or 0 (RSG_ERR_ARGS for NULLs);
+ * rsg_count_halos_to_print is count_halos_to_print (:462-468). */
+int rsg_should_print(const struct rsg_halo *h, const float *bounds, const struct rsg_config *cfg);
+int64_t rsg_count_halos_to_print(const struct rsg_halo *halos, int64_t num_halos,
+                                 const float *bounds, const struct rsg_config *cfg);
+/* output_ascii (src/io/meta_io.c:288-371): the out_<snap>.list table of the
+ * printable halos, ids from id_offset, to `path`, with the reference's
+ * column header, header block and number formats (mass definitions vir,
+ * 200b, 200c, 500c, 2500c, the ones the density thresholds use).  The idx,
+ * i_so (sub_of), i_ph and mmetric columns come from extra. */
+int rsg_write_ascii(const char *path, const struct rsg_halo *halos,
+                    const struct rsg_extra_halo_info *extra, int64_t num_halos,
+                    const struct rsg_catalog *opt, const struct rsg_config *cfg);
+/* output_binary with output_particles = 1 (src/io/io_internal.c:118-186):
+ * the 256-byte binary_output_header (src/io/io_internal.h:15-27; magic,
+ * cosmology, bounds, counts, format revision 2, version "1.0.0RC", add_flag
+ * 5 for the NFW chi2 and inertia-tensor layout), the printable halos with id
+ * and p_start rewritten, then the int64 ids of their particles. */
+int rsg_write_binary(const char *path, const struct rsg_halo *halos, int64_t num_halos,
+                     const struct rsg_particle *p, int64_t num_p,
+                     const struct rsg_catalog *opt, const struct rsg_config *cfg);
 
 /* Selects the potential form (0-3, as for rsg_compute_potential) that the
  * batched substructure form (rsg_find_subs_batch, rsg_path_device with

@@ -79,6 +79,11 @@ def lib():
         h.rsg_get_tuning.argtypes = [C.c_char_p, vp]
         h.rsg_debug_potentials.restype = i64
         h.rsg_debug_potentials.argtypes = [vp, i64]
+        h.rsg_should_print.argtypes = [vp, vp, vp]
+        h.rsg_count_halos_to_print.restype = i64
+        h.rsg_count_halos_to_print.argtypes = [vp, i64, vp, vp]
+        h.rsg_write_ascii.argtypes = [C.c_char_p, vp, vp, i64, vp, vp]
+        h.rsg_write_binary.argtypes = [C.c_char_p, vp, i64, vp, i64, vp, vp]
         for name, args in _EXTRA_SIGS.items():
             if hasattr(h, name):
                 getattr(h, name).argtypes = args
@@ -338,6 +343,64 @@ def profile_read():
     t = np.zeros(1, np.float64)
     _check(lib().rsg_profile_read(n.ctypes.data, t.ctypes.data))
     return int(n[0]), float(t[0])
+
+
+class CatalogOpts(C.Structure):
+    """struct rsg_catalog: options of one catalogue file."""
+    _fields_ = [("id_offset", C.c_int64), ("snap", C.c_int64), ("chunk", C.c_int64),
+                ("bounds", C.c_void_p), ("num_p", C.c_int64), ("strict_so_masses", C.c_int64)]
+
+
+def _catalog_opts(id_offset, snap, chunk, bounds, num_p, strict_so_masses):
+    b = None
+    if bounds is not None:
+        b = np.ascontiguousarray(bounds, dtype=np.float32)
+        assert b.shape == (6,)
+    o = CatalogOpts(id_offset, snap, chunk, b.ctypes.data if b is not None else None, num_p,
+                    strict_so_masses)
+    return o, b
+
+
+def should_print(halos, cfg, bounds=None):
+    """_should_print of every halo (src/io/meta_io.c:266-286), as a bool array."""
+    st = setup_config(cfg)
+    h = np.ascontiguousarray(halos, dtype=HALO)
+    o, b = _catalog_opts(0, 0, 0, bounds, 0, 0)
+    bp = b.ctypes.data if b is not None else None
+    out = np.zeros(len(h), bool)
+    for i in range(len(h)):
+        rc = lib().rsg_should_print(h[i:i + 1].ctypes.data, bp, C.byref(st))
+        if rc < 0:
+            _check(rc)
+        out[i] = rc == 1
+    n = lib().rsg_count_halos_to_print(h.ctypes.data, len(h), bp, C.byref(st))
+    if n < 0:
+        _check(int(n))
+    assert n == int(out.sum())
+    return out
+
+
+def write_ascii(path, halos, extra, cfg, id_offset=0, bounds=None, num_p=0,
+                strict_so_masses=0):
+    """The out_<snap>.list catalogue of the printable halos (output_ascii)."""
+    st = setup_config(cfg)
+    h = np.ascontiguousarray(halos, dtype=HALO)
+    e = np.ascontiguousarray(extra, dtype=EXTRA)
+    assert len(h) == len(e)
+    o, b = _catalog_opts(id_offset, 0, 0, bounds, num_p, strict_so_masses)
+    _check(lib().rsg_write_ascii(os.fsencode(path), h.ctypes.data, e.ctypes.data, len(h),
+                                 C.byref(o), C.byref(st)))
+
+
+def write_binary(path, halos, parts, cfg, id_offset=0, snap=0, chunk=0, bounds=None):
+    """The halos_<snap>.<chunk>.bin catalogue: header, printable halos, the
+    ids of their particles (output_binary)."""
+    st = setup_config(cfg)
+    h = np.ascontiguousarray(halos, dtype=HALO)
+    pa = np.ascontiguousarray(parts, dtype=PARTICLE)
+    o, b = _catalog_opts(id_offset, snap, chunk, bounds, 0, 0)
+    _check(lib().rsg_write_binary(os.fsencode(path), h.ctypes.data, len(h), pa.ctypes.data,
+                                  len(pa), C.byref(o), C.byref(st)))
 
 
 STAT_NAMES = ("particles", "groups", "halos", "pot_records", "kept_big", "kept_small",

@@ -20,6 +20,7 @@
 // A node's work at a level only touches its own particle range, so running
 // all nodes of a level at once performs the same operations, in the same
 // order per range, as the reference's depth-first walk.
+#include <cooperative_groups.h>
 #include <cub/cub.cuh>
 
 #include "kdtree_impl.cuh"
@@ -34,6 +35,8 @@
 #define RSG_SMALL 2048
 
 namespace rsg {
+
+namespace cg = cooperative_groups;
 
 // Hierarchy record of the last find_subs call (level, first position, size,
 // 6D linking length per node), kept for the test hooks.
@@ -744,16 +747,25 @@ __global__ void k_fill_eln(HierNodes N, int32_t base, int32_t *eln) {
 // each node's tree once with a shared stack, entering a node when any
 // lane's own box test admits it; at a leaf every lane tests
 // every point with its own distance test.  A lane meets exactly the points
-// of its own search, in ascending order.  MODE 2 counts every list and keeps
-// its first RSG_SLOT6 entries in a fixed slot per particle (one pass for
-// almost every particle); MODE 1 fills the CSR lists of the particles whose
-// list is longer than that.
+// of its own search, in ascending order.  MODE 2 counts every list, keeps
+// its first RSG_SLOT6 entries in a fixed slot per particle and the rest in
+// chunks of RSG_SLOT6 entries taken from a pool and chained per particle
+// (Chains); a particle whose chunk the pool could not give is flagged
+// (Chains::redo) and MODE 1 fills its CSR list with a second search.
 #define RSG_SLOT6 32
+struct Chains {
+    int32_t *pool;     // cap chunks of RSG_SLOT6 entries
+    int32_t *next;     // next chunk of a chain, -1 at the end
+    int32_t *head;     // first chunk of a particle's chain, -1 for none
+    int32_t *redo;     // 1: the list did not fit (MODE 1 refills it)
+    unsigned *cursor;  // chunks taken
+    int32_t cap;
+};
 template <int MODE>
 __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec *W, int64_t M,
                                                 HierNodes N, int32_t base, const int32_t *eln,
                                                 const int32_t *noff, int32_t *ncnt, int32_t *nbr,
-                                                int *err, unsigned long long *near) {
+                                                Chains CH, int *err, unsigned long long *near) {
     const unsigned FULL = 0xffffffffu;
     int64_t w0 = ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5) * 32;
     int lane = threadIdx.x & 31;
@@ -765,9 +777,11 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
 #pragma unroll
     for (int d = 0; d < 6; d++) c[d] = (valid && k >= 0) ? W[i].pos[d] : 0.f;
     int cnt = 0;
-    bool part = valid && k >= 0 && (MODE != 1 || ncnt[i] > RSG_SLOT6);
+    bool part = valid && k >= 0 && (MODE != 1 || CH.redo[i]);
     int o = (MODE == 1 && part) ? noff[i] : 0;
     int32_t *slot = (MODE == 2) ? nbr + (int64_t)i * RSG_SLOT6 : nullptr;
+    int chunk = -1;     // MODE 2: the chunk being filled
+    bool lost = false;  // MODE 2: the pool ran out for this list
     unsigned pending = __ballot_sync(FULL, part);
     int stack[RSG_STACK6];
     while (pending) {
@@ -796,7 +810,28 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
                     float d = dist6(c, q);
                     if (need && j > i && d < r2) {
                         if (MODE == 1) nbr[o + cnt] = j;
-                        if (MODE == 2 && cnt < RSG_SLOT6) slot[cnt] = j;
+                        if (MODE == 2) {
+                            if (cnt < RSG_SLOT6) {
+                                slot[cnt] = j;
+                            } else if (!lost) {
+                                const int e = (cnt - RSG_SLOT6) % RSG_SLOT6;
+                                if (e == 0) {
+                                    cg::coalesced_group g = cg::coalesced_threads();
+                                    unsigned b = 0;
+                                    if (g.thread_rank() == 0) b = atomicAdd(CH.cursor, g.size());
+                                    const unsigned c2 = g.shfl(b, 0) + g.thread_rank();
+                                    if (c2 < (unsigned)CH.cap) {
+                                        CH.next[c2] = -1;
+                                        if (chunk < 0) CH.head[i] = (int32_t)c2;
+                                        else CH.next[chunk] = (int32_t)c2;
+                                        chunk = (int32_t)c2;
+                                    } else {
+                                        lost = true;
+                                    }
+                                }
+                                if (!lost) CH.pool[(int64_t)chunk * RSG_SLOT6 + e] = j;
+                            }
+                        }
                         cnt++;
                     }
                     // pairs within 1e-6 of the linking length (relative, in
@@ -815,18 +850,28 @@ __global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec
             stack[sp++] = x.left;
         }
     }
-    if (MODE == 2 && part) ncnt[i] = cnt;
+    if (MODE == 2 && part) {
+        ncnt[i] = cnt;
+        CH.redo[i] = lost;
+    }
 }
 // CSR lists from the fixed slots of the lists that fit in them.
 __global__ void k_slots_csr(const int32_t *eln, int64_t M, const int32_t *ncnt,
-                            const int32_t *noff, const int32_t *slots, int32_t *nbr) {
+                            const int32_t *noff, const int32_t *slots, Chains CH, int32_t *nbr) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= M || eln[i] < 0) return;
-    int n = ncnt[i];
-    if (n > RSG_SLOT6) return;
+    if (i >= M || eln[i] < 0 || CH.redo[i]) return;
+    const int n = ncnt[i];
     const int32_t *sl = slots + i * RSG_SLOT6;
     int32_t *dst = nbr + noff[i];
-    for (int t = 0; t < n; t++) dst[t] = sl[t];
+    const int ns = n < RSG_SLOT6 ? n : RSG_SLOT6;
+    for (int t = 0; t < ns; t++) dst[t] = sl[t];
+    int c = n > RSG_SLOT6 ? CH.head[i] : -1;
+    for (int t = RSG_SLOT6; t < n; t += RSG_SLOT6) {
+        const int32_t *src = CH.pool + (int64_t)c * RSG_SLOT6;
+        const int m = (n - t) < RSG_SLOT6 ? (n - t) : RSG_SLOT6;
+        for (int u = 0; u < m; u++) dst[t + u] = src[u];
+        c = CH.next[c];
+    }
 }
 
 template <class T>
@@ -2424,15 +2469,25 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
             int32_t *ncnt = par, *noff = root;
             RSG_CUDA(cudaMemsetAsync(ncnt, 0, 4 * (M + 1), st));
             int32_t *slots = ar.get<int32_t>((size_t)M * RSG_SLOT6);
+            // overflow chunks: room for half a slot's worth per particle
+            Chains CH;
+            CH.cap = (int32_t)std::min<int64_t>(M / 2 + 1024, INT32_MAX / RSG_SLOT6);
+            CH.pool = ar.get<int32_t>((size_t)CH.cap * RSG_SLOT6);
+            CH.next = ar.get<int32_t>(CH.cap);
+            CH.head = ar.get<int32_t>(M);
+            CH.redo = ar.get<int32_t>(M);
+            CH.cursor = ar.get<unsigned>(1);
+            RSG_CUDA(cudaMemsetAsync(CH.cursor, 0, sizeof(unsigned), st));
             launch(k_fof6_w<2>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
-                   (const int32_t *)nullptr, ncnt, slots, err, near);
+                   (const int32_t *)nullptr, ncnt, slots, CH, err, near);
             check_i32_total(ar, ncnt, M + 1, "6D neighbour lists", st);
             int32_t ne = excl_scan(ar, ncnt, noff, (int32_t)(M + 1), st);
             int32_t *nbr = ar.get<int32_t>(ne + 1);
             launch(k_slots_csr, nblk(M, 256), 256, 0, st, eln, M, (const int32_t *)ncnt,
-                   (const int32_t *)noff, (const int32_t *)slots, nbr);
+                   (const int32_t *)noff, (const int32_t *)slots, CH, nbr);
+            // lists the pool could not hold (none unless it ran out): searched again
             launch(k_fof6_w<1>, nblk(M, 128), 128, 0, st, F.nodes, W, M, N, base, eln,
-                   (const int32_t *)noff, ncnt, nbr, err, near);
+                   (const int32_t *)noff, ncnt, nbr, CH, err, near);
             phase_mark(st, "d.fof6d");
             exact_labels_csr(ar, M, eln, N.start + base, noff, nbr, phalo, st);
         }

@@ -18,17 +18,22 @@
  *                                called at src/properties.c:548-550)
  *   analyze_halos_gpu(base, nh)  calls the analyze_halo_generic hook
  *                                (src/io/io_generic.h:12-18) per halo
+ *   output_catalogs_gpu(...)     in place of output_halos' two catalogue
+ *                                writers, output_ascii and output_binary
+ *                                (src/io/meta_io.c:490-499)
  * Errors: the library never exits; a non-zero return is mapped onto the
  * reference's rockstar_abort (src/error.h:17-20). */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <strings.h>
 
 #include "config_vars.h"
 #include "error.h"
 #include "fof.h"
 #include "groupies.h"
 #include "io/io_generic.h"
+#include "io/meta_io.h"
 #include "potential.h"
 #include "rockstar.h"
 #include "rockstar_gb300.h"
@@ -201,4 +206,30 @@ void analyze_halos_gpu(int64_t base, int64_t nh) {
     free(po);
     free(first);
     free(cnt);
+}
+
+/* ---- catalogue output -------------------------------------------------------
+ * The out_<snap>.list and halos_<snap>.<chunk>.bin catalogues of output_halos
+ * (src/io/meta_io.c:490-499) for OUTPUT_FORMAT ASCII, BINARY or BOTH, written
+ * by the library from halos, extra_info and p, with the reference's file
+ * names.  The full-particle, dump and lensing outputs of output_halos stay
+ * with the reference. */
+void output_catalogs_gpu(int64_t id_offset, int64_t snap, int64_t chunk, float *bounds) {
+    struct rsg_config c;
+    char buffer[1024];
+    gpu_config(&c);
+    struct rsg_catalog o = {id_offset, snap, chunk, bounds, num_p, STRICT_SO_MASSES};
+    if (!strcasecmp(OUTPUT_FORMAT, "BOTH") || !strcasecmp(OUTPUT_FORMAT, "ASCII")) {
+        get_output_filename(buffer, 1024, snap, chunk, "ascii");
+        if (rsg_write_ascii(buffer, (struct rsg_halo *)halos,
+                            (struct rsg_extra_halo_info *)extra_info, num_halos, &o, &c))
+            gpu_fail("rsg_write_ascii");
+    }
+    if (!strcasecmp(OUTPUT_FORMAT, "BOTH") || !strcasecmp(OUTPUT_FORMAT, "BINARY") ||
+        (TEMPORAL_HALO_FINDING && !LIGHTCONE)) {
+        get_output_filename(buffer, 1024, snap, chunk, "bin");
+        if (rsg_write_binary(buffer, (struct rsg_halo *)halos, num_halos,
+                             (struct rsg_particle *)p, num_p, &o, &c))
+            gpu_fail("rsg_write_binary");
+    }
 }

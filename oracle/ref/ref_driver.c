@@ -39,18 +39,54 @@ int64_t *bg_set_sizes = NULL;
 int64_t *bg_set_indices = NULL;
 int64_t our_chunk = 0;
 
+/* get_output_filename (src/io/meta_io.c) builds names from OUTBASE; here the
+ * one catalogue file a ref_output_binary call writes (temporal halo
+ * finding, the other caller, is switched off). */
+static const char *ref_out_path = NULL;
 void get_output_filename(char *buffer, int maxlen, int64_t snap, int64_t chunk,
                          char *type) {
-    (void)buffer; (void)maxlen; (void)snap; (void)chunk; (void)type;
-    fprintf(stderr, "oracle: temporal halo finding is disabled\n");
-    abort();
+    (void)snap; (void)chunk; (void)type;
+    if (!ref_out_path) {
+        fprintf(stderr, "oracle: temporal halo finding is disabled\n");
+        abort();
+    }
+    snprintf(buffer, maxlen, "%s", ref_out_path);
 }
-struct binary_output_header;
-void load_binary_header(int64_t snap, int64_t chunk,
-                        struct binary_output_header *bh) {
-    (void)snap; (void)chunk; (void)bh;
-    fprintf(stderr, "oracle: temporal halo finding is disabled\n");
-    abort();
+/* _within_bounds / _should_print, restated from src/io/meta_io.c:266-286
+ * (meta_io.c itself needs the tirpc library's headers and is not built):
+ * output_binary (src/io/io_internal.c, compiled here) calls it. */
+int _should_print(struct halo *h, float *bounds) {
+    int64_t i;
+    if (bounds)
+        for (i = 0; i < 3; i++)
+            if (h->pos[i] < bounds[i] || h->pos[i] > bounds[i + 3]) return 0;
+    if (h->flags & ALWAYS_PRINT_FLAG) return 1;
+    if ((h->num_p < MIN_HALO_OUTPUT_SIZE) || (h->m * UNBOUND_THRESHOLD >= h->mgrav) ||
+        ((h->mgrav < 1.5 * PARTICLE_MASS) && UNBOUND_THRESHOLD > 0))
+        return 0;
+    return 1;
+}
+void output_binary(int64_t id_offset, int64_t snap, int64_t chunk, float *bounds,
+                   int64_t output_particles);
+/* The reference's output_binary over the given halos and particles (the
+ * globals it reads are pointed at them for the call). */
+void ref_output_binary(const char *path, struct halo *h, int64_t nh, struct particle *parts,
+                       int64_t np, int64_t id_offset, int64_t snap, int64_t chunk,
+                       float *bounds) {
+    struct halo *sh = halos;
+    int64_t snh = num_halos, snp = num_p;
+    struct particle *sp = p;
+    halos = h;
+    num_halos = nh;
+    p = parts;
+    num_p = np;
+    ref_out_path = path;
+    output_binary(id_offset, snap, chunk, bounds, 1);
+    ref_out_path = NULL;
+    halos = sh;
+    num_halos = snh;
+    p = sp;
+    num_p = snp;
 }
 
 void realloc_halos(int64_t new_num_halos) {

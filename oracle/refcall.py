@@ -55,6 +55,7 @@ def lib():
         h.ref_compute_kinetic_energy.argtypes = [vp, i64, vp, vp, C.c_float]
         h.ref_time_path.restype = i64
         h.ref_time_path.argtypes = [vp, i64, C.c_int, vp, vp]
+        h.ref_output_binary.argtypes = [C.c_char_p, vp, i64, vp, i64, i64, i64, i64, vp]
         assert h.ref_sizeof_halo() == L.HALO.itemsize
         assert h.ref_sizeof_extra() == L.EXTRA.itemsize
         assert h.ref_sizeof_potential() == L.POTENTIAL.itemsize
@@ -131,3 +132,14 @@ def time_path(parts, nthreads):
     nh = lib().ref_time_path(parts.ctypes.data, len(parts), nthreads,
                              tf.ctypes.data, ts.ctypes.data)
     return float(tf[0]), float(ts[0]), int(nh)
+
+
+def output_binary(path, halos, parts, id_offset=0, snap=0, chunk=0, bounds=None):
+    """The reference's output_binary (src/io/io_internal.c:118-186) writing
+    `halos` and the ids of their particles in `parts` to `path` (after
+    setup())."""
+    h = np.array(halos, dtype=L.HALO, copy=True)
+    pa = np.ascontiguousarray(parts, dtype=L.PARTICLE)
+    b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.float32)
+    lib().ref_output_binary(os.fsencode(path), h.ctypes.data, len(h), pa.ctypes.data, len(pa),
+                            id_offset, snap, chunk, b.ctypes.data if b is not None else None)

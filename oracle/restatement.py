@@ -58,6 +58,9 @@ def lib():
         h.oracle_find_subs.argtypes = [vp, vp, vp, i64, vp, vp]
         h.oracle_compute_potential.argtypes = [vp, i64]
         h.oracle_kinetic_energy.argtypes = [vp, i64, vp, vp, C.c_float]
+        h.oracle_should_print.argtypes = [vp, vp]
+        h.oracle_write_ascii.argtypes = [C.c_char_p, vp, vp, i64, i64, vp, i64, i64]
+        h.oracle_write_binary.argtypes = [C.c_char_p, vp, i64, vp, i64, i64, i64, vp]
         h.oracle_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
         h.oracle_hierarchy.restype = i64
         h.oracle_hierarchy.argtypes = [vp, vp, vp, i64]
@@ -140,3 +143,34 @@ def kinetic_energy(po, vel_cen, pos_cen, scale_now):
     lib().oracle_kinetic_energy(po.ctypes.data, len(po), vc.ctypes.data, pc.ctypes.data,
                                 C.c_float(scale_now))
     return po
+
+
+def _bounds(bounds):
+    if bounds is None:
+        return None, None
+    b = np.ascontiguousarray(bounds, dtype=np.float32)
+    return b, b.ctypes.data
+
+
+def should_print(halos, bounds=None):
+    """_should_print of every halo (after setup())."""
+    h = np.ascontiguousarray(halos, dtype=L.HALO)
+    b, bp = _bounds(bounds)
+    return np.array([lib().oracle_should_print(h[i:i + 1].ctypes.data, bp) == 1
+                     for i in range(len(h))], bool)
+
+
+def write_ascii(path, halos, extra, id_offset=0, bounds=None, num_p=0, strict_so_masses=0):
+    h = np.ascontiguousarray(halos, dtype=L.HALO)
+    e = np.ascontiguousarray(extra, dtype=L.EXTRA)
+    b, bp = _bounds(bounds)
+    assert lib().oracle_write_ascii(os.fsencode(path), h.ctypes.data, e.ctypes.data, len(h),
+                                    id_offset, bp, num_p, strict_so_masses) == 0
+
+
+def write_binary(path, halos, parts, id_offset=0, snap=0, chunk=0, bounds=None):
+    h = np.ascontiguousarray(halos, dtype=L.HALO)
+    pa = np.ascontiguousarray(parts, dtype=L.PARTICLE)
+    b, bp = _bounds(bounds)
+    assert lib().oracle_write_binary(os.fsencode(path), h.ctypes.data, len(h), pa.ctypes.data,
+                                     id_offset, snap, chunk, bp) == 0

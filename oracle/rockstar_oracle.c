@@ -1435,3 +1435,177 @@ void oracle_tree_order(struct particle *pa, int64_t n, int dim, int leaf) {
     kbuild(&t, pa, sizeof(struct particle), 8, dim, leaf, n);
     kfree(&t);
 }
+
+/* ------------------------------------------------- catalogue output ----
+ * _within_bounds / _should_print (src/io/meta_io.c:266-286), output_ascii
+ * with print_ascii_header_info (:288-371) and output_binary with
+ * fill_binary_header (src/io/io_internal.c:16-41,104-186; header
+ * src/io/io_internal.h:6-27), with the file name given by the caller.  The
+ * reference's meta_io.c does not compile here (its reader headers need the
+ * tirpc library's rpc/types.h), so the ascii writer is pinned by this
+ * restatement alone; output_binary itself is compiled from io_internal.c into
+ * oracle/_ref and pins the binary writer where the reference is present. */
+#include <inttypes.h>
+#define ORC_ALWAYS_PRINT 16                      /* src/groupies.h:12 */
+static const char *orc_mass_def[5] = {"vir", "200b", "200c", "500c", "2500c"};
+
+static int orc_within_bounds(const struct halo *h, const float *bounds) {
+    int64_t i;
+    if (!bounds) return 1;
+    for (i = 0; i < 3; i++)
+        if (h->pos[i] < bounds[i] || h->pos[i] > bounds[i + 3]) return 0;
+    return 1;
+}
+int oracle_should_print(const struct halo *h, const float *bounds) {
+    if (!orc_within_bounds(h, bounds)) return 0;
+    if (h->flags & ORC_ALWAYS_PRINT) return 1;
+    if ((h->num_p < C.min_halo_output_size) || (h->m * C.unbound_threshold >= h->mgrav) ||
+        ((h->mgrav < 1.5 * C.particle_mass) && C.unbound_threshold > 0))
+        return 0;
+    return 1;
+}
+
+static void orc_header_info(FILE *output, const float *bounds, int64_t np, int64_t strict_so) {
+    fprintf(output, "#a = %f\n", C.scale_now);
+    if (bounds)
+        fprintf(output, "#Bounds: (%f, %f, %f) - (%f, %f, %f)\n", bounds[0], bounds[1],
+                bounds[2], bounds[3], bounds[4], bounds[5]);
+    fprintf(output, "#Om = %f; Ol = %f; h = %f\n", C.om, C.ol, C.h0);
+    fprintf(output, "#FOF linking length: %f\n", C.fof_linking_length);
+    fprintf(output, "#Unbound Threshold: %f; FOF Refinement Threshold: %f\n",
+            C.unbound_threshold, C.fof_fraction);
+    fprintf(output, "#Particle mass: %.5e Msun/h\n", C.particle_mass);
+    fprintf(output, "#Box size: %f Mpc/h\n", C.box_size);
+    if (np) fprintf(output, "#Total particles processed: %" PRId64 "\n", np);
+    fprintf(output, "#Force resolution assumed: %g Mpc/h\n", C.force_res);
+    if (strict_so && !np) fprintf(output, "#Using Strict Spherical Overdensity Masses\n");
+    fprintf(output,
+            "#Units: Masses in Msun / h\n"
+            "#Units: Positions in Mpc / h (comoving)\n"
+            "#Units: Velocities in km / s (physical, peculiar)\n"
+            "#Units: Halo Distances, Lengths, and Radii in kpc / h (comoving)\n"
+            "#Units: Angular Momenta in (Msun/h) * (Mpc/h) * km/s (physical)\n"
+            "#Units: Spins are dimensionless\n");
+    if (np)
+        fprintf(output,
+                "#Units: Total energy in (Msun/h)*(km/s)^2"
+                " (physical)\n"
+                "#Note: idx, i_so, and i_ph are internal debugging quantities\n");
+    fprintf(output, "#Np is an internal debugging quantity.\n");
+    fprintf(output, "#MPI-Rockstar Version: %s\n", "1.0.0RC");   /* src/version.h:4 */
+}
+
+int oracle_write_ascii(const char *path, const struct halo *halos, const struct extra *ex,
+                       int64_t num_halos, int64_t id_offset, const float *bounds, int64_t np,
+                       int64_t strict_so) {
+    int64_t i, id = 0;
+    const struct halo *th;
+    const char **M = orc_mass_def;
+    FILE *output = fopen(path, "w");
+    if (!output) return -1;
+    fprintf(output,
+            "#id num_p m%s mbound_%s r%s vmax rvmax vrms x y z vx vy vz Jx Jy "
+            "Jz E Spin PosUncertainty VelUncertainty bulk_vx bulk_vy bulk_vz "
+            "BulkVelUnc n_core m%s m%s m%s m%s Xoff Voff spin_bullock b_to_a "
+            "c_to_a A[x] A[y] A[z] b_to_a(%s) c_to_a(%s) A[x](%s) A[y](%s) "
+            "A[z](%s) Rs Rs_Klypin T/|U| M_pe_Behroozi M_pe_Diemer "
+            "Halfmass_Radius idx i_so i_ph num_cp mmetric\n",
+            M[0], M[0], M[0], M[1], M[2], M[3], M[4], M[3], M[3], M[3], M[3], M[3]);
+    orc_header_info(output, bounds, np, strict_so);
+    for (i = 0; i < num_halos; i++) {
+        if (!oracle_should_print(halos + i, bounds)) continue;
+        th = halos + i;
+        fprintf(output,
+                "%" PRId64 " %" PRId64 " %.3e %.3e"
+                " %f %f %f %f %f %f %f %f %f %f %g %g %g %g %g %f %f %f %f %f "
+                "%f %" PRId64 " %e %e %e %e %f %f %f %f %f %f %f %f %f %f %f "
+                "%f %f %f %f %f %e %e %f %" PRId64 " %" PRId64 " %" PRId64
+                " %" PRId64 " %f\n",
+                id + id_offset, th->num_p, th->m, th->mgrav, th->r, th->vmax, th->rvmax,
+                th->vrms, th->pos[0], th->pos[1], th->pos[2], th->pos[3], th->pos[4],
+                th->pos[5], th->J[0], th->J[1], th->J[2], th->energy, th->spin,
+                sqrt(th->min_pos_err), sqrt(th->min_vel_err), th->bulkvel[0], th->bulkvel[1],
+                th->bulkvel[2], sqrt(th->min_bulkvel_err), th->n_core, th->alt_m[0],
+                th->alt_m[1], th->alt_m[2], th->alt_m[3], th->Xoff, th->Voff,
+                th->bullock_spin, th->b_to_a, th->c_to_a, th->A[0], th->A[1], th->A[2],
+                th->b_to_a2, th->c_to_a2, th->A2[0], th->A2[1], th->A2[2], th->rs,
+                th->klypin_rs, th->kin_to_pot, th->m_pe_b, th->m_pe_d, th->halfmass_radius, i,
+                ex[i].sub_of, ex[i].ph, th->num_child_particles, ex[i].max_metric);
+        id++;
+    }
+    fclose(output);
+    return 0;
+}
+
+struct orc_bin_header {                           /* src/io/io_internal.h:15-27 */
+    uint64_t magic;
+    int64_t snap, chunk;
+    float scale, Om, Ol, h0;
+    float bounds[6];
+    int64_t num_halos, num_particles;
+    float box_size, particle_mass;
+    int64_t particle_type;
+    int32_t format_revision;
+    char rockstar_version[12];
+    int32_t add_flag;
+    char unused[256 - 12 - 4 * 12 - 4 * 2 - 8 * 6];
+};
+
+int oracle_write_binary(const char *path, const struct halo *halos, int64_t num_halos,
+                        const struct particle *p, int64_t id_offset, int64_t snap,
+                        int64_t chunk, const float *bounds) {
+    float max[3] = {0}, min[3] = {0};
+    struct halo tmp;
+    int64_t i, j, id = 0;
+    struct orc_bin_header bh;
+    FILE *output = fopen(path, "wb");
+    if (!output) return -1;
+    memset(&bh, 0, sizeof bh);
+    fwrite(&bh, sizeof bh, 1, output);
+    if (num_halos) {
+        memcpy(min, halos[0].pos, sizeof(float) * 3);
+        memcpy(max, halos[0].pos, sizeof(float) * 3);
+    }
+    for (i = 0; i < num_halos; i++) {
+        if (!oracle_should_print(halos + i, bounds)) continue;
+        for (j = 0; j < 3; j++) {
+            if (min[j] > halos[i].pos[j]) min[j] = halos[i].pos[j];
+            if (max[j] < halos[i].pos[j]) max[j] = halos[i].pos[j];
+        }
+        tmp = halos[i];
+        tmp.id = id + id_offset;
+        tmp.p_start = bh.num_particles;
+        fwrite(&tmp, sizeof tmp, 1, output);
+        bh.num_halos++;
+        bh.num_particles += tmp.num_p;
+        id++;
+    }
+    for (i = 0; i < num_halos; i++) {
+        if (!oracle_should_print(halos + i, bounds)) continue;
+        for (j = 0; j < halos[i].num_p; j++)
+            fwrite(&(p[halos[i].p_start + j].id), sizeof(int64_t), 1, output);
+    }
+    bh.magic = 0xfadedacec0c0d0d0ULL;
+    bh.snap = snap;
+    bh.chunk = chunk;
+    bh.scale = C.scale_now;
+    bh.Om = C.om;
+    bh.Ol = C.ol;
+    bh.h0 = C.h0;
+    bh.box_size = C.box_size;
+    bh.particle_mass = C.particle_mass;
+    snprintf(bh.rockstar_version, 12, "%s", "1.0.0RC");
+    bh.format_revision = 2;                       /* HALO_FORMAT_REVISION, src/halo.h:4 */
+    bh.add_flag = 1 | 4;                          /* OUTPUT_NFW_CHI2 | OUTPUT_INERTIA_TENSOR */
+    bh.particle_type = 1;                         /* PARTICLE_TYPE_IDS */
+    if (bounds)
+        memcpy(bh.bounds, bounds, sizeof(float) * 6);
+    else {
+        memcpy(bh.bounds, min, sizeof(float) * 3);
+        memcpy(&(bh.bounds[3]), max, sizeof(float) * 3);
+    }
+    rewind(output);
+    fwrite(&bh, sizeof bh, 1, output);
+    fclose(output);
+    return 0;
+}

@@ -1,0 +1,173 @@
+"""Catalogue output: the reference's halo filter (_should_print) and its ascii
+and binary halo catalogues (src/io/meta_io.c:266-371,
+src/io/io_internal.c:16-41,118-186), written by the library from halos,
+links and particles.  Checked against the oracle's restatement of the same
+functions on any machine, and against the reference's own output_binary
+where the reference is built (oracle/_ref).  Host code: no GPU needed."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libref_rockstar.so")
+CASES = [(1, 0.05), (2, 1 / 32)]
+
+
+def _case(rk, oracle, cfg_id, scale):
+    p, box, mp, _ = rk.synth(cfg_id, scale)
+    c = rk.Config(particle_mass=mp, box_size=box, total_particles=len(p))
+    oracle.setup(c)
+    fp, off, sz = oracle.fof(p)
+    parts, halos, extra = oracle.find_subs(fp, off, sz)
+    return c, box, parts, halos, extra
+
+
+def _bounds(box):
+    # a sub-box: some halos fall outside it
+    return np.array([0.1 * box, 0.0, 0.2 * box, 0.8 * box, box, 0.9 * box], np.float32)
+
+
+@pytest.mark.parametrize("cfg_id,scale", CASES)
+def test_should_print(rk, oracle, cfg_id, scale):
+    c, box, parts, h, e = _case(rk, oracle, cfg_id, scale)
+    for b in (None, _bounds(box)):
+        a = rk.should_print(h, c, b)
+        assert np.array_equal(a, oracle.should_print(h, b))
+        assert 0 < a.sum() < len(a)  # the filter takes some halos and drops others
+    # ALWAYS_PRINT_FLAG (src/groupies.h:12) overrides the size and boundness
+    # cuts, but not the bounds
+    drop = np.flatnonzero(~rk.should_print(h, c))
+    h2 = h.copy()
+    h2["flags"][drop] |= 16
+    assert rk.should_print(h2, c).all()
+    assert np.array_equal(rk.should_print(h2, c, _bounds(box)), oracle.should_print(h2, _bounds(box)))
+
+
+@pytest.mark.parametrize("cfg_id,scale", CASES)
+def test_ascii_matches_oracle(rk, oracle, tmp_path, cfg_id, scale):
+    c, box, parts, h, e = _case(rk, oracle, cfg_id, scale)
+    for k, (b, np_, off) in enumerate([(None, len(parts), 0), (_bounds(box), 0, 1000)]):
+        ours, ref = tmp_path / ("a%d.list" % k), tmp_path / ("b%d.list" % k)
+        rk.write_ascii(str(ours), h, e, c, id_offset=off, bounds=b, num_p=np_)
+        oracle.write_ascii(str(ref), h, e, id_offset=off, bounds=b, num_p=np_)
+        got, want = ours.read_bytes(), ref.read_bytes()
+        assert got == want
+        lines = got.decode().splitlines()
+        rows = [ln for ln in lines if not ln.startswith("#")]
+        assert len(rows) == int(rk.should_print(h, c, b).sum())
+        assert rows[0].split()[0] == str(off)  # ids count from id_offset
+        assert len(rows[0].split()) == len(lines[0].split())  # one value per column
+
+
+@pytest.mark.parametrize("cfg_id,scale", CASES)
+def test_binary_matches_oracle(rk, oracle, tmp_path, cfg_id, scale):
+    c, box, parts, h, e = _case(rk, oracle, cfg_id, scale)
+    for k, b in enumerate((None, _bounds(box))):
+        ours, ref = tmp_path / ("a%d.bin" % k), tmp_path / ("b%d.bin" % k)
+        rk.write_binary(str(ours), h, parts, c, id_offset=5, snap=3, chunk=1, bounds=b)
+        oracle.write_binary(str(ref), h, parts, id_offset=5, snap=3, chunk=1, bounds=b)
+        assert ours.read_bytes() == ref.read_bytes()
+
+
+@pytest.mark.skipif(not os.path.exists(REF_LIB), reason="reference oracle not built")
+@pytest.mark.parametrize("cfg_id,scale", CASES)
+def test_binary_matches_reference(rk, oracle, tmp_path, cfg_id, scale):
+    """The same bytes as the reference's own output_binary."""
+    from oracle import refcall
+    c, box, parts, h, e = _case(rk, oracle, cfg_id, scale)
+    refcall.setup(c)
+    for k, b in enumerate((None, _bounds(box))):
+        ours, ref = tmp_path / ("a%d.bin" % k), tmp_path / ("r%d.bin" % k)
+        rk.write_binary(str(ours), h, parts, c, id_offset=5, snap=3, chunk=1, bounds=b)
+        refcall.output_binary(str(ref), h, parts, id_offset=5, snap=3, chunk=1, bounds=b)
+        assert ours.read_bytes() == ref.read_bytes()
+
+
+def test_binary_layout(rk, oracle, tmp_path):
+    """Header fields, halo records and particle ids of the binary file."""
+    c, box, parts, h, e = _case(rk, oracle, 1, 0.05)
+    path = tmp_path / "h.bin"
+    rk.write_binary(str(path), h, parts, c, id_offset=7, snap=12, chunk=2)
+    raw = path.read_bytes()
+    magic, snap, chunk = struct.unpack_from("<Qqq", raw, 0)
+    scale, om, ol, h0 = struct.unpack_from("<4f", raw, 24)
+    bounds = struct.unpack_from("<6f", raw, 40)
+    nh, npart = struct.unpack_from("<qq", raw, 64)
+    box_size, pmass = struct.unpack_from("<2f", raw, 80)
+    ptype, rev = struct.unpack_from("<qi", raw, 88)
+    version = raw[100:112].split(b"\0")[0]
+    add_flag = struct.unpack_from("<i", raw, 112)[0]
+    assert (magic, snap, chunk) == (0xfadedacec0c0d0d0, 12, 2)
+    assert (ptype, rev, version, add_flag) == (1, 2, b"1.0.0RC", 5)
+    assert np.isclose(box_size, box) and np.isclose(om, c.om)
+    keep = rk.should_print(h, c)
+    assert nh == keep.sum() and npart == h["num_p"][keep].sum()
+    assert len(raw) == 256 + nh * h.dtype.itemsize + npart * 8
+    recs = np.frombuffer(raw, h.dtype, nh, 256)
+    assert np.array_equal(recs["id"], 7 + np.arange(nh))
+    assert np.array_equal(recs["p_start"], np.concatenate([[0], np.cumsum(recs["num_p"])[:-1]]))
+    ids = np.frombuffer(raw, np.int64, npart, 256 + nh * h.dtype.itemsize)
+    want = np.concatenate([parts["id"][s:s + n] for s, n in
+                           zip(h["p_start"][keep], h["num_p"][keep])])
+    assert np.array_equal(ids, want)
+    pos = h["pos"][keep][:, :3]
+    # extent of the printed halos; the running min/max start from halo 0
+    lo = np.minimum(pos.min(0), h["pos"][0, :3])
+    hi = np.maximum(pos.max(0), h["pos"][0, :3])
+    assert np.array_equal(np.array(bounds, np.float32), np.concatenate([lo, hi]))
+
+
+def test_empty_and_bad_arguments(rk, oracle, tmp_path):
+    c, box, parts, h, e = _case(rk, oracle, 1, 0.05)
+    empty = h[:0]
+    rk.write_binary(str(tmp_path / "e.bin"), empty, parts, c)
+    oracle.write_binary(str(tmp_path / "o.bin"), empty, parts)
+    assert (tmp_path / "e.bin").read_bytes() == (tmp_path / "o.bin").read_bytes()
+    assert len((tmp_path / "e.bin").read_bytes()) == 256
+    rk.write_ascii(str(tmp_path / "e.list"), empty, e[:0], c)
+    oracle.write_ascii(str(tmp_path / "o.list"), empty, e[:0])
+    assert (tmp_path / "e.list").read_bytes() == (tmp_path / "o.list").read_bytes()
+    # a halo whose particles lie outside the given particle array
+    bad = h.copy()
+    keep = np.flatnonzero(rk.should_print(h, c))
+    bad["p_start"][keep[0]] = len(parts)
+    with pytest.raises(rk.RockstarError) as ex:
+        rk.write_binary(str(tmp_path / "x.bin"), bad, parts, c)
+    assert ex.value.code == -1
+    with pytest.raises(rk.RockstarError) as ex:
+        rk.write_ascii(str(tmp_path / "no" / "such" / "dir.list"), h, e, c)
+    assert ex.value.code == -7
+
+
+def _canon_nan(h):
+    # NaN payloads differ between the GPU and a host CPU (0/0 gives a
+    # different bit pattern, printed "nan" or "-nan"); the catalogue compare
+    # is about the writer and the values, so NaNs are made one pattern
+    h = h.copy()
+    for name in h.dtype.names:
+        a = h[name]
+        if a.dtype.kind == "f":
+            a[np.isnan(a)] = np.float32("nan")
+    return h
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg_id,scale", CASES)
+def test_catalog_from_gpu_path(rk, oracle, tmp_path, cfg_id, scale):
+    """End to end: the 3D FOF and the plain substructure form on the GPU, then
+    the catalogues, against the oracle's path and writers."""
+    c, box, parts, h, e = _case(rk, oracle, cfg_id, scale)
+    p, _, _, _ = rk.synth(cfg_id, scale)
+    fp, off, sz = rk.rockstar_fof(p, c)
+    gparts, gh, ge = rk.find_subs(fp, off, sz, c)
+    assert gparts.tobytes() == parts.tobytes()
+    gh, h = _canon_nan(gh), _canon_nan(h)
+    rk.write_ascii(str(tmp_path / "g.list"), gh, ge, c, num_p=len(gparts))
+    oracle.write_ascii(str(tmp_path / "o.list"), h, e, num_p=len(parts))
+    assert (tmp_path / "g.list").read_bytes() == (tmp_path / "o.list").read_bytes()
+    rk.write_binary(str(tmp_path / "g.bin"), gh, gparts, c)
+    oracle.write_binary(str(tmp_path / "o.bin"), h, parts)
+    assert (tmp_path / "g.bin").read_bytes() == (tmp_path / "o.bin").read_bytes()
