@@ -762,7 +762,7 @@ struct Chains {
     int32_t cap;
 };
 template <int MODE>
-__global__ void __launch_bounds__(128) k_fof6_w(const KNode<6> *nodes, const Rec *W, int64_t M,
+__global__ void __launch_bounds__(128, 16) k_fof6_w(const KNode<6> *nodes, const Rec *W, int64_t M,
                                                 HierNodes N, int32_t base, const int32_t *eln,
                                                 const int32_t *noff, int32_t *ncnt, int32_t *nbr,
                                                 Chains CH, int *err, unsigned long long *near) {
@@ -1551,14 +1551,16 @@ __device__ void basic_vmax(rsg_halo &hh, const int *bins, int do_bins, float rsc
 // calc_basic_halo_props + estimate_vmax (src/properties.c:39-125); one
 // block per listed halo.
 __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, const DevCfg *C,
-                              int seq_max, int big) {
+                              int seq_max, int big, int small) {
     __shared__ double sm[40];
     __shared__ double mean[6], p2[6];
     __shared__ int bins[50];
     int h = list[blockIdx.x];
     rsg_halo &hh = H[h];
     int ps = (int)hh.p_start, np = (int)hh.num_p;
-    if (np > big) return;  // chunked path (batched form)
+    // chunked and warp paths (batched form); halos emptied by the assignment
+    // (num_p 0) are still processed, as the reference processes them
+    if (np > big || np <= small) return;
     if (np <= seq_max) {
         // in array order (src/properties.c:76-87): the block stages values,
         // thread 0 adds them
@@ -1644,6 +1646,63 @@ __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, co
     }
     __syncthreads();
     if (threadIdx.x == 0) basic_vmax(hh, bins, do_bins, rsc_s, C);
+}
+
+// Batched form, halos of at most RSG_BP_WARP particles: the same steps with
+// one warp per halo (a block per halo of tens of particles leaves most of
+// its threads idle and spends its time in barriers).  The FP64 sums are
+// added by lane and then across the warp (the batched form's sums are not in
+// the reference's order anyway); lane 0 takes the decisions.
+#define RSG_BP_WARP 1024
+__global__ void __launch_bounds__(256) k_basic_props_w(const Rec *W, rsg_halo *H,
+                                                       const int32_t *list, int32_t nl,
+                                                       const DevCfg *C) {
+    __shared__ int bins_s[8][50];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * 8 + w;
+    if (t >= nl) return;
+    rsg_halo &hh = H[list[t]];
+    const int ps = (int)hh.p_start, np = (int)hh.num_p;
+    if (np > RSG_BP_WARP) return;  // the block kernel's
+    double acc[6] = {0, 0, 0, 0, 0, 0}, mean[6], p2[6];
+    for (int i = lane; i < np; i += 32)
+#pragma unroll
+        for (int d = 0; d < 6; d++) acc[d] += (double)W[ps + i].pos[d];
+#pragma unroll
+    for (int d = 0; d < 6; d++) {
+        // warp_sum_d leaves the total in lane 0; every lane needs the mean
+        mean[d] = __shfl_sync(0xffffffffu, warp_sum_d(acc[d]), 0) / (double)np;
+        acc[d] = 0;
+    }
+    for (int i = lane; i < np; i += 32)
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            const double x = (double)W[ps + i].pos[d] - mean[d];
+            acc[d] += x * x;
+        }
+#pragma unroll
+    for (int d = 0; d < 6; d++) p2[d] = warp_sum_d(acc[d]);  // lane 0's are used
+    int db = 0;
+    float rs = 0.f;
+    if (lane == 0) basic_decide(hh, mean, p2, np, C, &db, &rs);
+    db = __shfl_sync(0xffffffffu, db, 0);
+    rs = __shfl_sync(0xffffffffu, rs, 0);
+    int *bins = bins_s[w];
+    for (int k = lane; k < 50; k += 32) bins[k] = 0;
+    __syncwarp();  // also orders lane 0's halo writes before the reads below
+    if (db) {
+        const float c0 = hh.pos[0], c1 = hh.pos[1], c2 = hh.pos[2];
+        for (int i = lane; i < np; i += 32) {
+            float dx, ds = 0.f;
+            dx = fsub(c0, W[ps + i].pos[0]); ds = fadd(ds, fmul(dx, dx));
+            dx = fsub(c1, W[ps + i].pos[1]); ds = fadd(ds, fmul(dx, dx));
+            dx = fsub(c2, W[ps + i].pos[2]); ds = fadd(ds, fmul(dx, dx));
+            const int key = vmax_bin(ds, rs);
+            if (key >= 0) atomicAdd(&bins[key], 1);
+        }
+    }
+    __syncwarp();
+    if (lane == 0) basic_vmax(hh, bins, db, rs, C);
 }
 
 // Batched form, halos above Tuning::bp_big particles: calc_basic_halo_props
@@ -2082,8 +2141,9 @@ static void basic_props(Arena &ar, const Rec *W, rsg_halo *H, const int32_t *lis
     const int T = 256;
     if (nl <= 0) return;
     launch(k_basic_props, nl, T, 0, st, W, H, list, d_dc, exact ? seq_max : 0,
-           exact ? 0x7fffffff : tuning().bp_big);
+           exact ? 0x7fffffff : tuning().bp_big, exact ? -1 : RSG_BP_WARP);
     if (exact) return;
+    launch(k_basic_props_w, nblk(nl, 8), 256, 0, st, W, H, list, nl, d_dc);
     size_t mark = ar.used;
     int32_t *nch = ar.get<int32_t>(nl + 1), *c0 = ar.get<int32_t>(nl + 1);
     const int bpbig = tuning().bp_big, bpch = tuning().bp_chunk;
