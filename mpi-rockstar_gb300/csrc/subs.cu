@@ -26,6 +26,7 @@
 #include "kdtree_impl.cuh"
 #include "lsort.cuh"
 #include "subs.cuh"
+#include "df64.cuh"
 #include "uflabels.cuh"
 
 // Ranges up to this size are summed by one thread in array order, so FP64
@@ -1533,7 +1534,11 @@ __device__ void basic_vmax(rsg_halo &hh, const int *bins, int do_bins, float rsc
         float rsc = rsc_s, vm = 0.f;
         int64_t tp = 0;
         for (int i = 0; i < 50; i++) {
-            float r = (float)((i + 1.0) / (double)rsc);
+            // (float)((i + 1.0) / (double)rsc), src/properties.c:58, as one FP32
+            // division: the exact quotient of a small integer by a float lies
+            // either on a float rounding midpoint or more than 2^-48 (relative)
+            // from every one, so the FP64 quotient rounds to the same float
+            float r = __fdiv_rn((float)(i + 1), rsc);
             if ((double)r < C->force_res) r = (float)C->force_res;
             tp += bins[i];
             float vc = __fdiv_rn(__ll2float_rn(tp), r);
@@ -1650,9 +1655,10 @@ __global__ void k_basic_props(const Rec *W, rsg_halo *H, const int32_t *list, co
 
 // Batched form, halos of at most RSG_BP_WARP particles: the same steps with
 // one warp per halo (a block per halo of tens of particles leaves most of
-// its threads idle and spends its time in barriers).  The FP64 sums are
-// added by lane and then across the warp (the batched form's sums are not in
-// the reference's order anyway); lane 0 takes the decisions.
+// its threads idle and spends its time in barriers).  Each lane sums in
+// double-float on the FP32 pipe (df64.cuh; the FP64 pipe bound the FP64
+// form), the lanes' sums are added in FP64 (the batched form's sums are not
+// in the reference's order anyway); lane 0 takes the decisions.
 #define RSG_BP_WARP 1024
 __global__ void __launch_bounds__(256) k_basic_props_w(const Rec *W, rsg_halo *H,
                                                        const int32_t *list, int32_t nl,
@@ -1664,24 +1670,27 @@ __global__ void __launch_bounds__(256) k_basic_props_w(const Rec *W, rsg_halo *H
     rsg_halo &hh = H[list[t]];
     const int ps = (int)hh.p_start, np = (int)hh.num_p;
     if (np > RSG_BP_WARP) return;  // the block kernel's
-    double acc[6] = {0, 0, 0, 0, 0, 0}, mean[6], p2[6];
+    DF acc[6];
+    double mean[6], p2[6];
+#pragma unroll
+    for (int d = 0; d < 6; d++) acc[d] = DF{0.f, 0.f};
     for (int i = lane; i < np; i += 32)
 #pragma unroll
-        for (int d = 0; d < 6; d++) acc[d] += (double)W[ps + i].pos[d];
+        for (int d = 0; d < 6; d++) acc[d] = df_add_f(acc[d], W[ps + i].pos[d]);
+    DF md[6];
 #pragma unroll
     for (int d = 0; d < 6; d++) {
         // warp_sum_d leaves the total in lane 0; every lane needs the mean
-        mean[d] = __shfl_sync(0xffffffffu, warp_sum_d(acc[d]), 0) / (double)np;
-        acc[d] = 0;
+        mean[d] = __shfl_sync(0xffffffffu, warp_sum_d(df_to_double(acc[d])), 0) / (double)np;
+        md[d] = df_from_double(mean[d]);
+        acc[d] = DF{0.f, 0.f};
     }
     for (int i = lane; i < np; i += 32)
 #pragma unroll
-        for (int d = 0; d < 6; d++) {
-            const double x = (double)W[ps + i].pos[d] - mean[d];
-            acc[d] += x * x;
-        }
+        for (int d = 0; d < 6; d++)
+            acc[d] = df_add(acc[d], df_sqr(df_sub_from_f(W[ps + i].pos[d], md[d])));
 #pragma unroll
-    for (int d = 0; d < 6; d++) p2[d] = warp_sum_d(acc[d]);  // lane 0's are used
+    for (int d = 0; d < 6; d++) p2[d] = warp_sum_d(df_to_double(acc[d]));  // lane 0's are used
     int db = 0;
     float rs = 0.f;
     if (lane == 0) basic_decide(hh, mean, p2, np, C, &db, &rs);
