@@ -673,34 +673,57 @@ __global__ void __launch_bounds__(RSG_CT) k_sh_sum(const Chunk *CH, const PotRec
     if (s.done) return;
     const float hp0 = H[c.halo].pos[0], hp1 = H[c.halo].pos[1], hp2 = H[c.halo].pos[2];
     const int ws = (int)Cp->weighted_shapes;
-    double o[3][3], ieg[3];  // 1 / eigenvalue: a multiply per record instead of an FP64 divide
-    for (int k = 0; k < 3; k++) {
-        ieg[k] = 1.0 / s.eig[k];
-        for (int l = 0; l < 3; l++) o[k][l] = s.orth[k][l];
+    // The ellipsoidal radius r = sum_q (o_q . d)^2 / eig_q as the quadratic
+    // form d^T M d with M = O^T diag(1/eig) O, formed once per block, on the
+    // six products d_k d_l the tensor sums need anyway (about 40 FP64
+    // operations per record instead of 90: GB300's FP64 pipe bounds this
+    // pass).  The value differs from the reference's expression by rounding
+    // only, as the batched form's order of summation does already.
+    double Mq[6] = {0, 0, 0, 0, 0, 0};  // M00 M11 M22 2M01 2M02 2M12
+    for (int q = 0; q < 3; q++) {
+        const double iq = 1.0 / s.eig[q];
+        const double o0 = s.orth[q][0], o1 = s.orth[q][1], o2 = s.orth[q][2];
+        Mq[0] += iq * o0 * o0;
+        Mq[1] += iq * o1 * o1;
+        Mq[2] += iq * o2 * o2;
+        Mq[3] += 2.0 * iq * o0 * o1;
+        Mq[4] += 2.0 * iq * o0 * o2;
+        Mq[5] += 2.0 * iq * o1 * o2;
     }
+    const double minr = (double)s.minr;
     D9 a = {{0, 0, 0, 0, 0, 0, 0, 0, 0}};
     for (int k = threadIdx.x; k < c.n; k += RSG_CT) {
         int64_t rec = c.start + k;
         if (c.first + k >= s.set) break;
         if (!flag[rec]) continue;
         const float *p = PO[rec].pos;
-        double dd[3] = {(double)fsub(p[0], hp0), (double)fsub(p[1], hp1), (double)fsub(p[2], hp2)};
-        double r = 0, dr;
-        for (int q = 0; q < 3; q++) {
-            dr = 0;
-            for (int l = 0; l < 3; l++) dr += o[q][l] * dd[l];
-            r += dr * dr * ieg[q];
-        }
-        if (r < (double)s.minr) r = s.minr;
+        const double d0 = (double)fsub(p[0], hp0), d1 = (double)fsub(p[1], hp1),
+                     d2 = (double)fsub(p[2], hp2);
+        const double p00 = d0 * d0, p11 = d1 * d1, p22 = d2 * d2, p01 = d0 * d1, p02 = d0 * d2,
+                     p12 = d1 * d2;
+        double r = Mq[0] * p00 + Mq[1] * p11 + Mq[2] * p22 + Mq[3] * p01 + Mq[4] * p02 +
+                   Mq[5] * p12;
+        if (r < minr) r = minr;
         if (r > 0 && r <= 1) {
-            double tw = ws ? 1.0 / r : 1.0;
+            double tw = 1.0;
+            if (ws) {
+                // 1/r: an FP32 estimate and two Newton steps in FP64 (about
+                // 2^-52 relative, for an FP64 divide's many operations)
+                if (r > 1e-30) {
+                    tw = (double)__frcp_rn((float)r);
+                    tw = fma(tw, fma(-r, tw, 1.0), tw);
+                    tw = fma(tw, fma(-r, tw, 1.0), tw);
+                } else {
+                    tw = 1.0 / r;
+                }
+            }
             a.v[0] += tw;
-            a.v[1] += dd[0] * dd[0] * tw;
-            a.v[2] += dd[1] * dd[1] * tw;
-            a.v[3] += dd[2] * dd[2] * tw;
-            a.v[4] += dd[0] * dd[1] * tw;
-            a.v[5] += dd[0] * dd[2] * tw;
-            a.v[6] += dd[1] * dd[2] * tw;
+            a.v[1] += p00 * tw;
+            a.v[2] += p11 * tw;
+            a.v[3] += p22 * tw;
+            a.v[4] += p01 * tw;
+            a.v[5] += p02 * tw;
+            a.v[6] += p12 * tw;
         }
     }
     a = R(tmp).Reduce(a, SumD9());
