@@ -886,6 +886,14 @@ static int select_where(Arena &ar, int n, Pred pred, int *out, cudaStream_t st) 
     return h;
 }
 
+// The later-dense list buffer of the calls whose list does not fit in the
+// arena, kept per host thread (see fof3d_device).
+struct ListCache {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+static thread_local ListCache g_list_cache;
+
 struct FofOut {
     int64_t num_p;
     int64_t nfofs;
@@ -971,12 +979,9 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     // RSG_FOF_LIST_ENTRIES entries when that is set); when the whole list
     // does not fit, it is built and walked one chunk of particles at a time,
     // chunks in particle order.  A fixed arena holds the list whole or fails.
-    struct ListBuf {
-        void *p = nullptr;
-        ~ListBuf() {
-            if (p) cudaFree(p);
-        }
-    } lbuf;
+    // That allocation stays with the host thread for its later calls, as the
+    // arena does: allocating and freeing a hundred gigabytes costs tens of
+    // milliseconds each, and the free waits for the device.
     int *llist;
     int64_t lcap = ne > 0 ? ne : 1;  // entries the list buffer holds
     size_t lat = (ar.used + 255) & ~(size_t)255;
@@ -985,13 +990,22 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     if (ar.fixed || (!lforce && lat + sizeof(int) * (size_t)lcap + (size_t)256 * n + (64u << 20) <= ar.cap)) {
         llist = ar.get<int>(lcap);
     } else {
+        ListCache &lc = g_list_cache;
         size_t fb = 0, tb = 0;
         RSG_CUDA(cudaMemGetInfo(&fb, &tb));
+        fb += lc.bytes;  // the kept buffer is this call's to use
         int64_t avail = fb > ((size_t)1 << 30) ? (int64_t)((fb - ((size_t)1 << 30)) / sizeof(int)) : 0;
         if (lforce > 0) avail = lforce;
         if (avail < lcap) lcap = avail;
-        RSG_CUDA(cudaMalloc(&lbuf.p, sizeof(int) * (size_t)(lcap > 0 ? lcap : 1)));
-        llist = (int *)lbuf.p;
+        const size_t need = sizeof(int) * (size_t)(lcap > 0 ? lcap : 1);
+        if (lc.bytes < need) {
+            if (lc.p) RSG_CUDA(cudaFree(lc.p));
+            lc.p = nullptr;
+            lc.bytes = 0;
+            RSG_CUDA(cudaMalloc(&lc.p, need));
+            lc.bytes = need;
+        }
+        llist = (int *)lc.p;
     }
     // chunk boundaries: particles c[t] .. c[t+1], dense entries d[t] .. d[t+1]
     std::vector<int> cb_h(2, 0), db_h(2, 0);

@@ -730,90 +730,120 @@ __device__ float total_energy(const PotRec *po, int64_t tot, float *ratio, const
     return (float)((ke - tphi) * C.particle_mass * RSG_GC / (double)sn);
 }
 
-// _calc_pseudo_evolution_masses (src/properties.c:351-382)
-// calc_shape for one halo on one warp, with the reference's summation order:
-// the lanes compute the terms of 32 records at a time (ellipsoid radius,
-// weight, products), lane c < 7 then adds accumulator c over them in record
-// order, and lane 0 takes the iteration's decisions (Jacobi, 1% rule) as
-// shape() does.  `sv` is this warp's staging area in shared memory.
-struct ShapeWarpBuf {
+// calc_shape (src/properties.c:216-326) for 32 halos per warp, in the
+// reference's summation order.  Each iteration runs the record phase of
+// every halo still iterating in turn -- the lanes compute the terms of 32
+// records at a time (ellipsoid radius, weight, products) and lane c < 7 adds
+// accumulator c over them in record order -- and then the 32 halos'
+// decisions (Jacobi, the 1% rule) side by side, one per lane: left to one
+// lane, that FP64 work occupied the narrow FP64 pipe for a single lane's
+// result.  `B` is this warp's state in shared memory.
+struct ShapeBatch {
     double v[32][7];
-    double orth[3][3], eig[3];
-    uint32_t skip;
-    int done;
+    double acc[32][7];
+    double orth[32][3][3], eig[32][3];
+    float minr[32], hp[32][3];
+    int it[32], done[32];
+    int set[32];  // records of halo base + q, -1 for a halo this warp skips
 };
-__device__ void shape_warp(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
-                           const DevCfg &C, ShapeWarpBuf &sv) {
+__device__ void shape_batch(rsg_halo *H, const int32_t *toff, const PotRec *PO, int32_t base,
+                            int32_t NH, int bound, const DevCfg &C, ShapeBatch &B) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    int cl = 0;
-    for (int64_t j = lane; j < tot; j += 32) cl += !(bound && unbound(po[j]));
-    for (int o = 16; o; o >>= 1) cl += __shfl_xor_sync(FULL, cl, o);
-    const int64_t an = cl;
-    int64_t it = C.shape_iterations;
-    float minr = fmul((float)C.force_res, (float)C.force_res);
-    if (lane == 0) {
-        h.b_to_a = h.c_to_a = 0;
-        h.A[0] = h.A[1] = h.A[2] = 0;
-    }
-    if (!(h.r > 0)) return;
-    minr = (float)((double)minr * (1e6 / (double)fmul(h.r, h.r)));
-    if (an < 3) return;
-    if (an < it) it = an;
-    if (lane == 0) {
-        for (int i = 0; i < 3; i++) {
-            for (int k = 0; k < 3; k++) sv.orth[i][k] = 0;
-            sv.orth[i][i] = 1;
-            sv.eig[i] = (double)fmul(h.r, h.r) * 1e-6;
+    {
+        // lane q sets up halo base + q (the loop's prologue, src/properties.c:222-250)
+        const int32_t hq = base + lane;
+        int done = 1, itq = 0;
+        float minr = 0.f;
+        if (hq < NH && B.set[lane] >= 0) {
+            rsg_halo &h = H[hq];
+            const PotRec *po = PO + toff[hq];
+            const int64_t tot = B.set[lane];
+            int64_t an = 0;
+            for (int64_t j = 0; j < tot; j++) an += !(bound && unbound(po[j]));
+            int64_t it = C.shape_iterations;
+            minr = fmul((float)C.force_res, (float)C.force_res);
+            h.b_to_a = h.c_to_a = 0;
+            h.A[0] = h.A[1] = h.A[2] = 0;
+            if (h.r > 0) {
+                minr = (float)((double)minr * (1e6 / (double)fmul(h.r, h.r)));
+                if (an >= 3) {
+                    if (an < it) it = an;
+                    itq = (int)it;
+                    done = itq <= 0;
+                    for (int i = 0; i < 3; i++) {
+                        for (int k = 0; k < 3; k++) B.orth[lane][i][k] = 0;
+                        B.orth[lane][i][i] = 1;
+                        B.eig[lane][i] = (double)fmul(h.r, h.r) * 1e-6;
+                    }
+                }
+            }
+            B.hp[lane][0] = h.pos[0];
+            B.hp[lane][1] = h.pos[1];
+            B.hp[lane][2] = h.pos[2];
         }
-        sv.done = 0;
+        B.done[lane] = done;
+        B.it[lane] = itq;
+        B.minr[lane] = minr;
     }
     __syncwarp();
-    const float hp0 = h.pos[0], hp1 = h.pos[1], hp2 = h.pos[2];
-    for (int64_t i = 0; i < it; i++) {
-        double a = 0;  // lane c < 7 owns accumulator c (w, m00, m11, m22, m10, m20, m21)
-        for (int64_t b0 = 0; b0 < tot; b0 += 32) {
-            const int64_t j = b0 + lane;
-            bool sk = true;
-            double vv[7];
-            if (j < tot && !(bound && unbound(po[j]))) {
-                const float *p = po[j].pos;
-                double dd[3] = {(double)fsub(p[0], hp0), (double)fsub(p[1], hp1),
-                                (double)fsub(p[2], hp2)};
-                double r = 0, dr;
-                for (int k = 0; k < 3; k++) {
-                    dr = 0;
-                    for (int l = 0; l < 3; l++) dr += sv.orth[k][l] * dd[l];
-                    r += dr * dr / sv.eig[k];
+    int maxit = 0;
+    for (int q = 0; q < 32; q++) maxit = max(maxit, B.done[q] ? 0 : B.it[q]);
+    for (int i = 0; i < maxit; i++) {
+        for (int q = 0; q < 32; q++) {
+            if (B.done[q] || i >= B.it[q]) continue;
+            const int32_t hq = base + q;
+            const PotRec *po = PO + toff[hq];
+            const int64_t tot = B.set[q];
+            const float hp0 = B.hp[q][0], hp1 = B.hp[q][1], hp2 = B.hp[q][2];
+            const double minr = (double)B.minr[q];
+            double a = 0;  // lane c < 7 owns accumulator c (w, m00, m11, m22, m10, m20, m21)
+            for (int64_t b0 = 0; b0 < tot; b0 += 32) {
+                const int64_t j = b0 + lane;
+                bool sk = true;
+                double vv[7];
+                if (j < tot && !(bound && unbound(po[j]))) {
+                    const float *p = po[j].pos;
+                    double dd[3] = {(double)fsub(p[0], hp0), (double)fsub(p[1], hp1),
+                                    (double)fsub(p[2], hp2)};
+                    double r = 0, dr;
+                    for (int k = 0; k < 3; k++) {
+                        dr = 0;
+                        for (int l = 0; l < 3; l++) dr += B.orth[q][k][l] * dd[l];
+                        r += dr * dr / B.eig[q][k];
+                    }
+                    if (r < minr) r = minr;
+                    if (r > 0 && r <= 1) {
+                        double tw = (C.weighted_shapes) ? 1.0 / r : 1.0;
+                        vv[0] = tw;
+                        vv[1] = dd[0] * dd[0] * tw;
+                        vv[2] = dd[1] * dd[1] * tw;
+                        vv[3] = dd[2] * dd[2] * tw;
+                        vv[4] = dd[0] * dd[1] * tw;
+                        vv[5] = dd[0] * dd[2] * tw;
+                        vv[6] = dd[1] * dd[2] * tw;
+                        sk = false;
+                        for (int c = 0; c < 7; c++) B.v[lane][c] = vv[c];
+                    }
                 }
-                if (r < (double)minr) r = minr;
-                if (r > 0 && r <= 1) {
-                    double tw = (C.weighted_shapes) ? 1.0 / r : 1.0;
-                    vv[0] = tw;
-                    vv[1] = dd[0] * dd[0] * tw;
-                    vv[2] = dd[1] * dd[1] * tw;
-                    vv[3] = dd[2] * dd[2] * tw;
-                    vv[4] = dd[0] * dd[1] * tw;
-                    vv[5] = dd[0] * dd[2] * tw;
-                    vv[6] = dd[1] * dd[2] * tw;
-                    sk = false;
-                    for (int c = 0; c < 7; c++) sv.v[lane][c] = vv[c];
+                const uint32_t skip = __ballot_sync(FULL, sk);
+                __syncwarp();
+                if (lane < 7) {
+                    const int m = (tot - b0) < 32 ? (int)(tot - b0) : 32;
+                    for (int t = 0; t < m; t++)
+                        if (!((skip >> t) & 1u)) a += B.v[t][lane];
                 }
+                __syncwarp();
             }
-            const uint32_t skip = __ballot_sync(FULL, sk);
-            __syncwarp();
-            if (lane < 7) {
-                const int m = (tot - b0) < 32 ? (int)(tot - b0) : 32;
-                for (int t = 0; t < m; t++)
-                    if (!((skip >> t) & 1u)) a += sv.v[t][lane];
-            }
-            __syncwarp();
+            if (lane < 7) B.acc[q][lane] = a;
         }
-        double acc[7];
-        for (int c = 0; c < 7; c++) acc[c] = __shfl_sync(FULL, a, c);
-        if (lane == 0) {
+        __syncwarp();
+        // the decisions of every halo still iterating, one per lane
+        if (!B.done[lane] && i < B.it[lane]) {
+            rsg_halo &h = H[base + lane];
+            const double *acc = B.acc[lane];
             double w = acc[0];
-            if (!w) sv.done = 1;
+            if (!w) B.done[lane] = 1;
             else {
                 double m[3][3] = {{acc[1], acc[4], acc[5]}, {acc[4], acc[2], acc[6]},
                                   {acc[5], acc[6], acc[3]}};
@@ -828,23 +858,23 @@ __device__ void shape_warp(rsg_halo &h, const PotRec *po, int64_t tot, int bound
                 if (e2[2] > e2[b]) { c = b; b = 2; }
                 if (e2[b] > e2[a2]) { int t = a2; a2 = b; b = t; }
                 for (int k = 0; k < 3; k++) {
-                    sv.eig[k] = e2[k];
-                    for (int l = 0; l < 3; l++) sv.orth[k][l] = o2[k][l];
+                    B.eig[lane][k] = e2[k];
+                    for (int l = 0; l < 3; l++) B.orth[lane][k][l] = o2[k][l];
                 }
-                if (!e2[a2] || !e2[b] || !e2[c]) sv.done = 1;
+                if (!e2[a2] || !e2[b] || !e2[c]) B.done[lane] = 1;
                 else {
                     float ba = (float)sqrt(e2[b] / e2[a2]);
                     float ca = (float)sqrt(e2[c] / e2[a2]);
                     if ((fabs((double)fsub(ba, h.b_to_a)) < 0.01 * (double)h.b_to_a) &&
                         (fabs((double)fsub(ca, h.c_to_a)) < 0.01 * (double)h.c_to_a))
-                        sv.done = 1;
+                        B.done[lane] = 1;
                     else {
                         h.b_to_a = (ba > 0) ? ba : 0;
                         h.c_to_a = (ca > 0) ? ca : 0;
                         double rr = sqrt(e2[a2]);
                         for (int k = 0; k < 3; k++) {
                             h.A[k] = (float)(1e3 * rr * o2[a2][k]);
-                            sv.eig[k] *= ((double)fmul(h.r, h.r) * 1e-6) / (rr * rr);
+                            B.eig[lane][k] *= ((double)fmul(h.r, h.r) * 1e-6) / (rr * rr);
                         }
                         h.inertia_tensor[0] = (float)mt2[0][0];
                         h.inertia_tensor[1] = (float)mt2[1][1];
@@ -857,10 +887,10 @@ __device__ void shape_warp(rsg_halo &h, const PotRec *po, int64_t tot, int bound
             }
         }
         __syncwarp();
-        if (sv.done) return;
     }
 }
 
+// _calc_pseudo_evolution_masses (src/properties.c:351-382)
 __device__ void pseudo_masses(rsg_halo &h, const PotRec *po, int64_t tot, int bound,
                               const DevCfg &C) {
     int64_t np_ = 0, npd = 0;
@@ -2029,7 +2059,7 @@ static void seg_props(Arena &ar, const DevCfg &dc, const DevCfg *d_dc, PotRec *P
         phase_mark(st, "p.passes");
         for (int which = 0; which < 2; which++) {
             launch(k_sh_init, HB, HT, 0, st, NH, H, cnt, toff, d_dc, which, S);
-            launch(k_sh_small, nblk((int64_t)NH * 32, 128), 128, 0, st, NH, H, toff,
+            launch(k_sh_small, nblk(NH, 128), 128, 0, st, NH, H, toff,
                    (const PotRec *)PO, d_dc, (const HS *)S, bound);
             for (int64_t i = 0; i < dc.shape_iterations; i++) {
                 launch(k_sh_sum, nc, RSG_CT, 0, st, CH, PO, H, flag, S, d_dc, cp);

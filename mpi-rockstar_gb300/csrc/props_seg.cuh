@@ -654,14 +654,19 @@ __global__ void k_sh_init(int32_t NH, rsg_halo *H, const int32_t *cnt, const int
     s.it = (int32_t)it;
     if (it <= 0) s.done = 1;
 }
-// The small sets of k_sh_init: shape_warp, one warp per halo.
+// The small sets of k_sh_init: shape_batch, 32 halos per warp.
 __global__ void __launch_bounds__(128) k_sh_small(int32_t NH, rsg_halo *H, const int32_t *toff,
                                                   const PotRec *PO, const DevCfg *Cp,
                                                   const HS *S, int bound) {
-    __shared__ ShapeWarpBuf buf[4];
-    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (h >= NH || H[h].num_p < 1 || S[h].set > RSG_SHAPE_SEQ) return;
-    shape_warp(H[h], PO + toff[h], S[h].set, bound, *Cp, buf[threadIdx.x >> 5]);
+    __shared__ ShapeBatch sb[4];
+    ShapeBatch &B = sb[threadIdx.x >> 5];
+    const int32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    if (base >= NH) return;
+    const int lane = threadIdx.x & 31;
+    const int32_t h = base + lane;
+    B.set[lane] = (h < NH && H[h].num_p >= 1 && S[h].set <= RSG_SHAPE_SEQ) ? S[h].set : -1;
+    __syncwarp();
+    shape_batch(H, toff, PO, base, NH, bound, *Cp, B);
 }
 __global__ void __launch_bounds__(RSG_CT) k_sh_sum(const Chunk *CH, const PotRec *PO,
                                                    const rsg_halo *H, const uint8_t *flag,
