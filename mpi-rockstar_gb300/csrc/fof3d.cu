@@ -129,10 +129,18 @@ __device__ bool sphere3(const KNode<3> *nodes, int root, const Rec *recs, const 
 struct NoLeaf {
     __device__ void operator()(int, bool) const {}
 };
-template <class FR, class FP, bool LEAF = false, class FL = NoLeaf>
+// on_coop(m2, start, n), when given (COOP = true), replaces on_range: every
+// lane calls it, in converged code, for a node that the lanes of mask m2 take
+// whole (all of them meet the same node in a shared walk), so the warp can
+// work through the node's points together.  It cannot end a walk.
+struct NoCoop {
+    __device__ void operator()(unsigned, int, int) const {}
+};
+template <class FR, class FP, bool LEAF = false, class FL = NoLeaf, bool COOP = false,
+          class FC = NoCoop>
 __device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float *c, bool active,
                              float r, int after, int *errflag, FR on_range, FP on_point,
-                             FL on_leaf = FL()) {
+                             FL on_leaf = FL(), FC on_coop = FC()) {
     const unsigned FULL = 0xffffffffu;
     const unsigned bit = 1u << (threadIdx.x & 31);
     const float r2 = fmul(r, r);
@@ -156,7 +164,12 @@ __device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float
                 kind = box_inside3(nd, c, r, r2) ? 2 : (nd.div < 0 ? 3 : 4);
         }
         bool stop = false;
-        if (kind == 2) stop = !on_range(nd.start, nd.n);
+        if (COOP) {
+            const unsigned m2 = __ballot_sync(FULL, kind == 2);
+            if (m2) on_coop(m2, nd.start, nd.n);
+        } else if (kind == 2) {
+            stop = !on_range(nd.start, nd.n);
+        }
         if (__any_sync(FULL, kind == 3)) {
             for (int k = 0; k < nd.n; k++) {
                 int j = nd.start + k;
@@ -376,11 +389,18 @@ __global__ void __launch_bounds__(128) k_count_w(const KNode<3> *nodes, const Re
 // counted then listed; skipcnt[j] counts the dense k that can skip j.
 // With llist, k's entries go to llist[loff[k] - lbase ...] (lbase: the
 // offset of the first particle of the chunk being listed).
+// The counting pass takes whole nodes together (the lanes meeting a node
+// share it): each lane counts its later dense points from the prefix count
+// dpfx (dense particles before an index), and the lanes stride over the
+// node's points, each dense point j getting one atomic that adds the number
+// of queries below j (the queries ascend with the lane, so those lanes are a
+// prefix of the warp).
+template <bool FILL>
 __global__ void __launch_bounds__(128) k_llist_w(const KNode<3> *nodes, const Rec *recs,
                                                  const int *dense, int nd, float r,
-                                                 const uint8_t *cnt, const int64_t *loff,
-                                                 int64_t lbase, int *lcnt, int *llist,
-                                                 int *skipcnt, int *err) {
+                                                 const uint8_t *cnt, const int *dpfx,
+                                                 const int64_t *loff, int64_t lbase, int *lcnt,
+                                                 int *llist, int *skipcnt, int *err) {
     if (warp_idle(nd)) return;
     int k;
     bool act = warp_query(dense, nd, &k);
@@ -416,8 +436,27 @@ __global__ void __launch_bounds__(128) k_llist_w(const KNode<3> *nodes, const Re
         add(j);
         return true;
     };
-    sphere3_warp<decltype(range), decltype(point), true, decltype(leaf)>(
-        nodes, recs, c, act, r, act ? k : INT_MAX - 1, err, range, point, leaf);
+    const int kq = act ? k : INT_MAX;
+    auto coop = [&](unsigned m2, int s, int q) {
+        if ((m2 >> lane) & 1u) {
+            const int a = max(s, k + 1);
+            if (a < s + q) m += dpfx[s + q] - dpfx[a];
+        }
+        const int k31 = __shfl_sync(0xffffffffu, kq, 31);
+        for (int b = 0; b < q; b += 32) {
+            const int j = s + b + lane;
+            int p = 0;  // lanes whose query is below j
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1)
+                if (__shfl_sync(0xffffffffu, kq, p + step - 1) < j) p += step;
+            if (p == 31 && k31 < j) p = 32;
+            const int c2 = __popc(m2 & (p >= 32 ? 0xffffffffu : ((1u << p) - 1u)));
+            if (j < s + q && c2 && cnt[j] > 16) atomicAdd(&skipcnt[j], c2);
+        }
+    };
+    sphere3_warp<decltype(range), decltype(point), true, decltype(leaf), !FILL,
+                 decltype(coop)>(nodes, recs, c, act, r, act ? k : INT_MAX - 1, err, range,
+                                 point, leaf, coop);
     if (act && !llist) lcnt[k] = m;
 }
 // The seeds' searches run one warp per seed (warp_sphere3): a seed's
@@ -815,6 +854,9 @@ struct DFlag {
     const uint8_t *c;
     __device__ uint8_t operator()(int i) const { return c[i] > 16; }
 };
+struct DenseI {
+    __host__ __device__ int operator()(uint8_t c) const { return c > 16; }
+};
 static int sm_count() {
     int dev = 0, v = 0;
     RSG_CUDA(cudaGetDevice(&dev));
@@ -960,9 +1002,20 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
     int64_t *loff = ar.get<int64_t>(n + 1);
     RSG_CUDA(cudaMemsetAsync(lcnt, 0, sizeof(int) * (n + 1), st));
     RSG_CUDA(cudaMemsetAsync(skipcnt, 0, sizeof(int) * n, st));
-    launch(k_llist_w, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
-           (const uint8_t *)cnt, (const int64_t *)nullptr, (int64_t)0, lcnt, (int *)nullptr,
-           skipcnt, err);
+    // dense particles before every index (the counting pass's whole nodes)
+    int *dpfx = ar.get<int>(n + 1);
+    {
+        thrust::transform_iterator<DenseI, const uint8_t *, int> dit((const uint8_t *)cnt, DenseI{});
+        size_t pb = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, pb, dit, dpfx, n + 1, st);
+        size_t m0 = ar.used;
+        void *pt = ar.take(pb + 256);
+        cub::DeviceScan::ExclusiveSum(pt, pb, dit, dpfx, n + 1, st);
+        ar.used = m0;
+    }
+    launch(k_llist_w<false>, nblk(nd, TW), TW, 0, st, F.nodes, recs, (const int *)dense, nd, r,
+           (const uint8_t *)cnt, (const int *)dpfx, (const int64_t *)nullptr, (int64_t)0, lcnt,
+           (int *)nullptr, skipcnt, err);
     size_t cb = 0;
     thrust::transform_iterator<ToI64, const int32_t *, int64_t> lc64((const int32_t *)lcnt, ToI64{});
     cub::DeviceScan::ExclusiveSum(nullptr, cb, lc64, loff, n + 1, st);
@@ -1078,9 +1131,9 @@ FofOut fof3d_device(Arena &ar, const rsg_particle *d_in, int64_t n64, const rsg_
         int d0 = db_h[t], d1 = db_h[t + 1];
         if (d1 <= d0) continue;
         int64_t lbase = lb_h.size() > 1 ? lb_h[t] : 0;
-        launch(k_llist_w, nblk(d1 - d0, TW), TW, 0, st, F.nodes, recs, (const int *)dense + d0,
-               d1 - d0, r, (const uint8_t *)cnt, (const int64_t *)loff, lbase, lcnt, llist, skipcnt,
-               err);
+        launch(k_llist_w<true>, nblk(d1 - d0, TW), TW, 0, st, F.nodes, recs,
+               (const int *)dense + d0, d1 - d0, r, (const uint8_t *)cnt, (const int *)dpfx,
+               (const int64_t *)loff, lbase, lcnt, llist, skipcnt, err);
         if (t > 0)
             launch(k_kahn_chunk, nblk(d1 - d0, T), T, 0, st, (const int *)dense + d0, d1 - d0,
                    (const int *)state32, queue, qcap, ctl);
