@@ -454,55 +454,72 @@ __device__ __forceinline__ bool box_out6(const KNode<6> &nd, const float *c, flo
 // recursion unrolled onto an explicit stack; the running radius threads
 // through the visits in the reference's order.
 __device__ float next_closest(const KNode<6> *nodes, int root, const Rec *W, const float *c,
-                              int *err) {
+                              bool valid, int *err) {
+    const unsigned FULL = 0xffffffffu;
     int nd = root;
-    while (nodes[nd].div >= 0) {
-        const KNode<6> &x = nodes[nd];
-        nd = (c[x.div] <= nodes[x.left].mx[x.div]) ? x.left : x.left + 1;
-    }
-    while (nd != root) {
-        int pdv = nodes[nodes[nd].parent].div;
-        if (nodes[nd].mn[pdv] == nodes[nd].mx[pdv]) nd = nodes[nd].parent;
-        else break;
-    }
-    const KNode<6> &o = nodes[nd];
-    float md = 0.f;
-    for (int j = 0; j < 6; j++) {
-        float dx = fsub(o.mx[j], o.mn[j]);
-        md = fadd(md, fmul(dx, dx));
-    }
-    for (int i = 0; i < o.n; i++) {
-        float d = dist6(c, W[o.start + i].pos);
-        if (d && d < md) md = d;
-    }
-    float r = sqrt_fd(md);
+    float r = 0.f;
     int stack[RSG_STACK6];
     int sp = 0;
-    stack[sp++] = root;
-    while (sp) {
-        int ni = stack[--sp];
-        const KNode<6> &x = nodes[ni];
-        if (box_out6(x, c, r) || ni == nd) continue;
-        if (x.div < 0) {
+    if (valid) {
+        while (nodes[nd].div >= 0) {
+            const KNode<6> &x = nodes[nd];
+            nd = (c[x.div] <= nodes[x.left].mx[x.div]) ? x.left : x.left + 1;
+        }
+        while (nd != root) {
+            int pdv = nodes[nodes[nd].parent].div;
+            if (nodes[nd].mn[pdv] == nodes[nd].mx[pdv]) nd = nodes[nd].parent;
+            else break;
+        }
+        const KNode<6> &o = nodes[nd];
+        float md = 0.f;
+        for (int j = 0; j < 6; j++) {
+            float dx = fsub(o.mx[j], o.mn[j]);
+            md = fadd(md, fmul(dx, dx));
+        }
+        for (int i = 0; i < o.n; i++) {
+            float d = dist6(c, W[o.start + i].pos);
+            if (d && d < md) md = d;
+        }
+        r = sqrt_fd(md);
+        stack[sp++] = root;
+    }
+    // Each lane walks its own depth-first order (the reference's, with its
+    // own pruning radius) until it reaches its next leaf; then the lanes
+    // holding a leaf test their leaves together.  A lane's sequence of node
+    // tests and leaf updates is unchanged; only its interleaving with the
+    // other lanes is.
+    while (__any_sync(FULL, sp > 0)) {
+        int leaf = -1;
+        while (sp) {
+            const int ni = stack[--sp];
+            const KNode<6> &x = nodes[ni];
+            if (box_out6(x, c, r) || ni == nd) continue;
+            if (x.div < 0) {
+                leaf = ni;
+                break;
+            }
+            int a = x.left, b = x.left + 1;
+            if (c[x.div] > fmul(0.5f, fadd(x.mn[x.div], x.mx[x.div]))) {
+                a = x.left + 1;
+                b = x.left;
+            }
+            if (sp + 2 > RSG_STACK6) {
+                atomicExch(err, 1);
+                sp = 0;
+                break;
+            }
+            stack[sp++] = b;
+            stack[sp++] = a;
+        }
+        if (leaf >= 0) {
+            const KNode<6> &x = nodes[leaf];
             float r2 = fmul(r, r);
             for (int i = 0; i < x.n; i++) {
                 float d = dist6(c, W[x.start + i].pos);
                 if (d < r2) r2 = d;
             }
             r = sqrt_fd(r2);
-            continue;
         }
-        int a = x.left, b = x.left + 1;
-        if (c[x.div] > fmul(0.5f, fadd(x.mn[x.div], x.mx[x.div]))) {
-            a = x.left + 1;
-            b = x.left;
-        }
-        if (sp + 2 > RSG_STACK6) {
-            atomicExch(err, 1);
-            return r;
-        }
-        stack[sp++] = b;
-        stack[sp++] = a;
     }
     return r;
 }
@@ -534,7 +551,9 @@ __global__ void k_nn(const KNode<6> *nodes, const Rec *W, HierNodes N, int32_t b
                      int32_t count, const int32_t *soff, const int32_t *sidx, float *prad,
                      int64_t total, int exact, int *err, const uint32_t *order) {
     int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= total) return;
+    // lanes past the end stay (next_closest synchronises the warp)
+    const bool valid = q < total;
+    if (!valid) q = total - 1;
     int64_t g = order ? (int64_t)order[q] : q;
     // node of sample g: last k with soff[k] <= g
     int lo = 0, hi = count - 1;
@@ -552,7 +571,8 @@ __global__ void k_nn(const KNode<6> *nodes, const Rec *W, HierNodes N, int32_t b
     float c[6];
 #pragma unroll
     for (int d = 0; d < 6; d++) c[d] = W[s + j].pos[d];
-    prad[g] = next_closest(nodes, k, W, c, err);
+    const float rr = next_closest(nodes, k, W, c, valid, err);
+    if (valid) prad[g] = rr;
 }
 
 // find_median_r / rad_partition (src/groupies.c:735-786), run as is on the
