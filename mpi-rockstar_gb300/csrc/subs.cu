@@ -141,48 +141,81 @@ __global__ void k_norm_seq(Rec *W, HierNodes N, int32_t base, int32_t count, int
     norm_sigmas(c, level0, ims, sig + 2 * k);
 }
 
-// Batched form, nodes up to RSG_SMALL particles: one warp per node, sums in
-// lane-strided order reduced by shuffles (deterministic).
-__global__ void k_norm_warp(Rec *W, HierNodes N, int32_t base, int32_t count, int level0,
-                            double ims, double *sig) {
-    int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (k >= count) return;
-    int node = base + k;
-    int s = N.start[node], n = N.n[node];
-    if (n <= 0 || n > RSG_SMALL) return;
-    double mean[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = lane; i < n; i += 32)
-        for (int d = 0; d < 6; d++) mean[d] += (double)W[s + i].pos[d];
-    for (int d = 0; d < 6; d++) {
-        for (int o = 16; o; o >>= 1) mean[d] += __shfl_xor_sync(0xffffffffu, mean[d], o);
-        mean[d] /= (double)n;
-    }
-    // The 21 second moments of the float products, each kept as an unevaluated
-    // float pair (hi + lo, Knuth's two-sum): about 48 bits, enough for at most
-    // RSG_SMALL terms, on the FP32 pipe (GB300's FP64 pipe is narrow).
-    float ch[21], cl[21];
-    for (int j = 0; j < 21; j++) ch[j] = cl[j] = 0.f;
-    for (int i = lane; i < n; i += 32) {
-        float q[6];
+// Batched form, nodes up to RSG_SMALL particles: 32 nodes per warp.  For
+// each node in turn the lanes stride over its particles: the means are summed
+// in double-float (df64.cuh), the centred coordinate float(x - mean) is
+// formed from the exact two-sum of x and the mean's high part, and the 21
+// second moments of the float products are kept as float pairs (hi + lo,
+// Knuth's two-sum: about 48 bits, enough for RSG_SMALL terms) -- all on the
+// FP32 pipe, as GB300's FP64 pipe is narrow; the lanes' sums are combined by
+// shuffles (deterministic).  Then the 32 nodes' sigmas (two 3x3 eigenvalue
+// problems each, in FP64) run side by side, one node per lane, instead of on
+// lane 0 of a warp per node.
+#define RSG_NORM_WARPS 4
+__global__ void __launch_bounds__(RSG_NORM_WARPS * 32)
+    k_norm_warp(Rec *W, HierNodes N, int32_t base, int32_t count, int level0, double ims,
+                double *sig) {
+    __shared__ double cs[RSG_NORM_WARPS][32][21];
+    const unsigned FULL = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int32_t k0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    if (k0 >= count) return;
+    for (int q = 0; q < 32; q++) {
+        const int32_t k = k0 + q;
+        if (k >= count) break;
+        const int node = base + k;
+        const int s = N.start[node], n = N.n[node];
+        if (n <= 0 || n > RSG_SMALL) continue;
+        DF acc[6];
+#pragma unroll
+        for (int d = 0; d < 6; d++) acc[d] = DF{0.f, 0.f};
+        for (int i = lane; i < n; i += 32)
+#pragma unroll
+            for (int d = 0; d < 6; d++) acc[d] = df_add_f(acc[d], W[s + i].pos[d]);
+        DF md[6];
+#pragma unroll
         for (int d = 0; d < 6; d++) {
-            q[d] = __double2float_rn((double)W[s + i].pos[d] - mean[d]);
-            W[s + i].pos[d] = q[d];
+            for (int o = 16; o; o >>= 1) {
+                DF y{__shfl_xor_sync(FULL, acc[d].hi, o), __shfl_xor_sync(FULL, acc[d].lo, o)};
+                acc[d] = df_add(acc[d], y);
+            }
+            md[d] = df_from_double(df_to_double(acc[d]) / (double)n);
         }
-        int j = 0;
-        for (int x = 0; x < 6; x++)
-            for (int y = x; y < 6; y++, j++) two_sum_acc(ch[j], cl[j], fmul(q[x], q[y]));
-    }
-    double c[21];
-    for (int j = 0; j < 21; j++) {
-        for (int o = 16; o; o >>= 1) {
-            float h2 = __shfl_xor_sync(0xffffffffu, ch[j], o);
-            float l2 = __shfl_xor_sync(0xffffffffu, cl[j], o);
-            two_sum_acc(ch[j], cl[j], h2);
-            cl[j] = fadd(cl[j], l2);
+        float ch[21], cl[21];
+        for (int jj = 0; jj < 21; jj++) ch[jj] = cl[jj] = 0.f;
+        for (int i = lane; i < n; i += 32) {
+            float qv[6];
+#pragma unroll
+            for (int d = 0; d < 6; d++) {
+                const DF t = df_two_sum(W[s + i].pos[d], -md[d].hi);
+                qv[d] = __fadd_rn(t.hi, __fsub_rn(t.lo, md[d].lo));
+                W[s + i].pos[d] = qv[d];
+            }
+            int jj = 0;
+            for (int x = 0; x < 6; x++)
+                for (int y = x; y < 6; y++, jj++) two_sum_acc(ch[jj], cl[jj], fmul(qv[x], qv[y]));
         }
-        c[j] = ((double)ch[j] + (double)cl[j]) / (double)n;
+        for (int jj = 0; jj < 21; jj++) {
+            for (int o = 16; o; o >>= 1) {
+                float h2 = __shfl_xor_sync(FULL, ch[jj], o);
+                float l2 = __shfl_xor_sync(FULL, cl[jj], o);
+                two_sum_acc(ch[jj], cl[jj], h2);
+                cl[jj] = fadd(cl[jj], l2);
+            }
+        }
+        if (lane < 21) {
+            double v = 0;
+            for (int jj = 0; jj < 21; jj++)
+                if (jj == lane) v = ((double)ch[jj] + (double)cl[jj]) / (double)n;
+            cs[w][q][lane] = v;
+        }
     }
-    if (lane == 0) norm_sigmas(c, level0, ims, sig + 2 * k);
+    __syncwarp();
+    const int32_t k = k0 + lane;
+    if (k < count) {
+        const int n = N.n[base + k];
+        if (n > 0 && n <= RSG_SMALL) norm_sigmas(cs[w][lane], level0, ims, sig + 2 * k);
+    }
 }
 
 // Mid-size nodes: the block stages particles in shared memory and computes
@@ -2447,8 +2480,8 @@ SubsOut find_subs_device(Arena &ar, rsg_particle *d_p, int64_t num_p, const int6
                 launch(k_norm_seq, nblk(cnt, 32), 32, 0, st, W, N, base, cnt, L == 0,
                        cfg.initial_metric_scaling, sig);
             else
-                launch(k_norm_warp, nblk((int64_t)cnt * 32, 256), 256, 0, st, W, N, base, cnt,
-                       L == 0, cfg.initial_metric_scaling, sig);
+                launch(k_norm_warp, nblk(cnt, RSG_NORM_WARPS * 32), RSG_NORM_WARPS * 32, 0, st, W,
+                       N, base, cnt, L == 0, cfg.initial_metric_scaling, sig);
             launch(k_norm_blk, cnt, 256, 0, st, W, N, base, L == 0, cfg.initial_metric_scaling, sig,
                    seq_lo, RSG_SEQ_MAX);
             if (exact) {
