@@ -134,16 +134,69 @@ __device__ __forceinline__ int rt_find(int32_t *R, int a) {
     return r;
 }
 // One component per thread: its spanning merges in time order, each keeping
-// the root of the link's set (merge_smallfofs, src/fof.c:72-90).
+// the root of the link's set (merge_smallfofs, src/fof.c:72-90).  Components
+// with more than RSG_UF_WARP merges are k_uf_replay_w's.
+#define RSG_UF_WARP 64
 __global__ void k_uf_replay(const int32_t *eid, const int32_t *rs, int32_t nr, int32_t ne,
                             const int32_t *cF, const int32_t *cW, int32_t *R) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nr) return;
     int e1 = (t + 1 < nr) ? rs[t + 1] : ne;
+    if (e1 - rs[t] > RSG_UF_WARP) return;
     for (int i = rs[t]; i < e1; i++) {
         int c = eid[i];
         int rl = rt_find(R, cW[c]), rc = rt_find(R, cF[c]);
         if (rl != rc) R[rc] = rl;
+    }
+}
+// The large components: one warp per component, 32 merges at a time.  The
+// lanes find the roots of their merge's two sets in the state before the
+// batch, in parallel; then the merges are applied in time order, lane by
+// lane.  A root that an earlier merge of the batch ended is replaced by the
+// root it was joined to (one forward pass over the batch's merges resolves a
+// chain: a replacement can only be ended by a later merge), and a merge of
+// two different sets makes W's root the parent of F's, as the sequential
+// replay does.
+#define RSG_UF_WARPS 4
+__global__ void __launch_bounds__(RSG_UF_WARPS * 32)
+    k_uf_replay_w(const int32_t *eid, const int32_t *rs, int32_t nr, int32_t ne,
+                  const int32_t *cF, const int32_t *cW, int32_t *R) {
+    __shared__ int32_t killed_s[RSG_UF_WARPS][32], into_s[RSG_UF_WARPS][32];
+    const unsigned FULL = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (t >= nr) return;
+    const int e0 = rs[t], e1 = (t + 1 < nr) ? rs[t + 1] : ne;
+    if (e1 - e0 <= RSG_UF_WARP) return;
+    int32_t *killed = killed_s[w], *into = into_s[w];
+    for (int b = e0; b < e1; b += 32) {
+        const int i = b + lane;
+        int rl = -1, rc = -1;
+        if (i < e1) {
+            const int c = eid[i];
+            rl = rt_find(R, cW[c]);
+            rc = rt_find(R, cF[c]);
+        }
+        __syncwarp();
+        const int m = min(32, e1 - b);
+        int nk = 0;
+        for (int q = 0; q < m; q++) {
+            int done = 0;
+            if (lane == q) {
+                for (int k = 0; k < nk; k++) {
+                    if (rl == killed[k]) rl = into[k];
+                    if (rc == killed[k]) rc = into[k];
+                }
+                if (rl != rc) {
+                    R[rc] = rl;
+                    killed[nk] = rc;
+                    into[nk] = rl;
+                    done = 1;
+                }
+            }
+            nk += __shfl_sync(FULL, done, q);
+            __syncwarp();
+        }
     }
 }
 __global__ void k_uf_rootall(int32_t *R, int64_t S, int32_t *root) {
@@ -242,6 +295,8 @@ void uf_roots(Arena &ar, const int32_t *cF, const int32_t *cW, int64_t nc, int64
             int32_t nr = sel_flagged(ar, thrust::counting_iterator<int32_t>(0), rflag, rs, ne, st);
             launch(k_uf_replay, nblk(nr, 64), 64, 0, st, (const int32_t *)eid2, (const int32_t *)rs,
                    nr, ne, cF, cW, R);
+            launch(k_uf_replay_w, nblk((int64_t)nr * 32, RSG_UF_WARPS * 32), RSG_UF_WARPS * 32, 0,
+                   st, (const int32_t *)eid2, (const int32_t *)rs, nr, ne, cF, cW, R);
         }
     }
     launch(k_uf_rootall, nblk(S, T), T, 0, st, R, S, root);
