@@ -458,14 +458,51 @@ __global__ void k_sample_idx(HierNodes N, int32_t base, int32_t count, const int
     sidx[g] = (int32_t)j;
 }
 
-__device__ __forceinline__ float dist6(const float *c, const float *p) {
-    float d = 0.f;
-#pragma unroll
-    for (int j = 0; j < 6; j++) {
-        float dx = fsub(c[j], p[j]);
-        d = fadd(d, fmul(dx, dx));
-    }
-    return d;
+// The squared 6D distance of the reference's searches: dx = c[j] - p[j],
+// d += dx * dx for j = 0..5 in order, each operation rounded to float
+// (src/fast3tree.c:401-405 with FAST3TREE_DIM 6).
+// dist6_p computes it with the subtractions and squares done two dimensions
+// per instruction (Blackwell's packed FP32 arithmetic, each lane rounded as
+// the scalar operation): c2 and q2 hold coordinates (0,1), (2,3), (4,5) as
+// float pairs, the lower-addressed coordinate in the low half.  The sum runs
+// over j = 0..5 in order as in dist6, so the result is the same float.
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_sqr(unsigned long long a) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(r) : "l"(a));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_split(unsigned long long v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ float dist6_p(const unsigned long long *c2, const unsigned long long *q2) {
+    float p0, p1, p2, p3, p4, p5;
+    f2_split(f2_sqr(f2_sub(c2[0], q2[0])), p0, p1);
+    f2_split(f2_sqr(f2_sub(c2[1], q2[1])), p2, p3);
+    f2_split(f2_sqr(f2_sub(c2[2], q2[2])), p4, p5);
+    float d = fadd(0.f, p0);
+    d = fadd(d, p1);
+    d = fadd(d, p2);
+    d = fadd(d, p3);
+    d = fadd(d, p4);
+    return fadd(d, p5);
+}
+// A record's coordinates as three float pairs (two 16-byte loads).
+__device__ __forceinline__ void rec_pairs(const Rec *w, unsigned long long *q2) {
+    const ulonglong2 a = reinterpret_cast<const ulonglong2 *>(w)[0];
+    const ulonglong2 b = reinterpret_cast<const ulonglong2 *>(w)[1];
+    q2[0] = a.x;
+    q2[1] = a.y;
+    q2[2] = b.x;
 }
 __device__ __forceinline__ bool box_out6(const KNode<6> &nd, const float *c, float r) {
     float d = 0.f, e;
@@ -509,8 +546,12 @@ __device__ float next_closest(const KNode<6> *nodes, int root, const Rec *W, con
             float dx = fsub(o.mx[j], o.mn[j]);
             md = fadd(md, fmul(dx, dx));
         }
+        const unsigned long long c2[3] = {f2_pack(c[0], c[1]), f2_pack(c[2], c[3]),
+                                          f2_pack(c[4], c[5])};
         for (int i = 0; i < o.n; i++) {
-            float d = dist6(c, W[o.start + i].pos);
+            unsigned long long q2[3];
+            rec_pairs(W + o.start + i, q2);
+            float d = dist6_p(c2, q2);
             if (d && d < md) md = d;
         }
         r = sqrt_fd(md);
@@ -546,9 +587,13 @@ __device__ float next_closest(const KNode<6> *nodes, int root, const Rec *W, con
         }
         if (leaf >= 0) {
             const KNode<6> &x = nodes[leaf];
+            const unsigned long long c2[3] = {f2_pack(c[0], c[1]), f2_pack(c[2], c[3]),
+                                              f2_pack(c[4], c[5])};
             float r2 = fmul(r, r);
             for (int i = 0; i < x.n; i++) {
-                float d = dist6(c, W[x.start + i].pos);
+                unsigned long long q2[3];
+                rec_pairs(W + x.start + i, q2);
+                float d = dist6_p(c2, q2);
                 if (d < r2) r2 = d;
             }
             r = sqrt_fd(r2);
@@ -830,6 +875,8 @@ __global__ void __launch_bounds__(128, 16) k_fof6_w(const KNode<6> *nodes, const
     float c[6];
 #pragma unroll
     for (int d = 0; d < 6; d++) c[d] = (valid && k >= 0) ? W[i].pos[d] : 0.f;
+    const unsigned long long c2[3] = {f2_pack(c[0], c[1]), f2_pack(c[2], c[3]),
+                                      f2_pack(c[4], c[5])};
     int cnt = 0;
     bool part = valid && k >= 0 && (MODE != 1 || CH.redo[i]);
     int o = (MODE == 1 && part) ? noff[i] : 0;
@@ -858,10 +905,9 @@ __global__ void __launch_bounds__(128, 16) k_fof6_w(const KNode<6> *nodes, const
                 for (int j = j0; j < x.start + x.n; j++) {
                     // the record as two 16-byte loads (the same address in
                     // every lane: one broadcast transaction each)
-                    const float4 qa = reinterpret_cast<const float4 *>(W + j)[0];
-                    const float4 qb = reinterpret_cast<const float4 *>(W + j)[1];
-                    const float q[6] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y};
-                    float d = dist6(c, q);
+                    unsigned long long q2[3];
+                    rec_pairs(W + j, q2);
+                    float d = dist6_p(c2, q2);
                     if (need && j > i && d < r2) {
                         if (MODE == 1) nbr[o + cnt] = j;
                         if (MODE == 2) {
