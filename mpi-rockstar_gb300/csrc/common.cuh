@@ -127,4 +127,27 @@ Tuning &tuning();
 #define RSG_STACK 96
 #define RSG_STACK6 128
 
+// Blackwell's packed FP32 arithmetic: two floats per 64-bit register (the
+// lower-addressed value in the low half), each lane rounded as the scalar
+// operation (.rn), so a packed subtraction or square gives the same floats
+// as two scalar ones.
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_sqr(unsigned long long a) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(r) : "l"(a));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_split(unsigned long long v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
 }  // namespace rsg

@@ -35,6 +35,18 @@ namespace rsg {
 
 namespace cg = cooperative_groups;
 
+// The reference's squared distance of a leaf point (dx = c[t] - q[t], dist
+// += dx * dx for t = 0, 1, 2 in order, each rounded; src/fast3tree.c:
+// 398-405), x and y subtracted and squared as one packed pair; cxy holds
+// c[0], c[1].  dist starts at 0 and the first square is not negative, so
+// 0 + dx0^2 is dx0^2.
+__device__ __forceinline__ float dist3_p(unsigned long long cxy, float cz, const Rec &q) {
+    const unsigned long long qxy = *reinterpret_cast<const unsigned long long *>(q.pos);
+    float p0, p1;
+    f2_split(f2_sqr(f2_sub(cxy, qxy)), p0, p1);
+    const float dz = fsub(cz, q.pos[2]);
+    return fadd(fadd(p0, p1), fmul(dz, dz));
+}
 // The reference's two box tests, in its operation order:
 // _fast3tree_box_not_intersect_sphere and _fast3tree_box_inside_sphere
 // (src/fast3tree.c:293-330).
@@ -91,16 +103,10 @@ __device__ bool sphere3(const KNode<3> *nodes, int root, const Rec *recs, const 
             continue;
         }
         if (nd.div < 0) {
+            const unsigned long long cxy = f2_pack(c[0], c[1]);
             for (int k = 0; k < nd.n; k++) {
                 int j = nd.start + k;
-                const Rec &q = recs[j];
-                float dist = 0.f;
-#pragma unroll
-                for (int t = 0; t < 3; t++) {
-                    float dx = fsub(c[t], q.pos[t]);
-                    dist = fadd(dist, fmul(dx, dx));
-                }
-                if (dist < r2)
+                if (dist3_p(cxy, c[2], recs[j]) < r2)
                     if (!on_point(j)) return false;
             }
             continue;
@@ -171,17 +177,11 @@ __device__ void sphere3_warp(const KNode<3> *nodes, const Rec *recs, const float
             stop = !on_range(nd.start, nd.n);
         }
         if (__any_sync(FULL, kind == 3)) {
+            const unsigned long long cxy = f2_pack(c[0], c[1]);
             for (int k = 0; k < nd.n; k++) {
                 int j = nd.start + k;
-                float q0 = recs[j].pos[0], q1 = recs[j].pos[1], q2 = recs[j].pos[2];
                 bool hit = false;
-                if (kind == 3 && !stop) {
-                    float dist = 0.f, dx;
-                    dx = fsub(c[0], q0); dist = fadd(dist, fmul(dx, dx));
-                    dx = fsub(c[1], q1); dist = fadd(dist, fmul(dx, dx));
-                    dx = fsub(c[2], q2); dist = fadd(dist, fmul(dx, dx));
-                    hit = dist < r2;
-                }
+                if (kind == 3 && !stop) hit = dist3_p(cxy, c[2], recs[j]) < r2;
                 if (LEAF) on_leaf(j, hit);
                 else if (hit) stop = !on_point(j);
             }
@@ -294,15 +294,7 @@ __device__ void warp_sphere3(const KNode<3> *nodes, const Rec *recs, int q, cons
             if (flat < total) {
                 j = oa + (flat - (oi - on));
                 v = true;
-                if (ok == 2) {
-                    float dist = 0.f;
-#pragma unroll
-                    for (int t = 0; t < 3; t++) {
-                        const float dx = fsub(c[t], recs[j].pos[t]);
-                        dist = fadd(dist, fmul(dx, dx));
-                    }
-                    v = dist < r2;
-                }
+                if (ok == 2) v = dist3_p(f2_pack(c[0], c[1]), c[2], recs[j]) < r2;
             }
             visit(j, v);
         }

@@ -466,24 +466,6 @@ __global__ void k_sample_idx(HierNodes N, int32_t base, int32_t count, const int
 // the scalar operation): c2 and q2 hold coordinates (0,1), (2,3), (4,5) as
 // float pairs, the lower-addressed coordinate in the low half.  The sum runs
 // over j = 0..5 in order as in dist6, so the result is the same float.
-__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
-    unsigned long long r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ unsigned long long f2_sqr(unsigned long long a) {
-    unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %1;" : "=l"(r) : "l"(a));
-    return r;
-}
-__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
-    unsigned long long r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void f2_split(unsigned long long v, float &lo, float &hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
 __device__ __forceinline__ float dist6_p(const unsigned long long *c2, const unsigned long long *q2) {
     float p0, p1, p2, p3, p4, p5;
     f2_split(f2_sqr(f2_sub(c2[0], q2[0])), p0, p1);
