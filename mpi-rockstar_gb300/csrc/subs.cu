@@ -142,13 +142,13 @@ __global__ void k_norm_seq(Rec *W, HierNodes N, int32_t base, int32_t count, int
 }
 
 // Batched form, nodes up to RSG_SMALL particles: 32 nodes per warp.  For
-// each node in turn the lanes stride over its particles: the means are summed
-// in double-float (df64.cuh), the centred coordinate float(x - mean) is
-// formed from the exact two-sum of x and the mean's high part, and the 21
-// second moments of the float products are kept as float pairs (hi + lo,
-// Knuth's two-sum: about 48 bits, enough for RSG_SMALL terms) -- all on the
-// FP32 pipe, as GB300's FP64 pipe is narrow; the lanes' sums are combined by
-// shuffles (deterministic).  Then the 32 nodes' sigmas (two 3x3 eigenvalue
+// each node in turn the lanes stride over its particles: the means and the
+// centred coordinates float((double)x - mean) in FP64, as the reference
+// forms them (a double-float mean or centring moved coordinates by an ulp
+// measurably more often), and the 21 second moments of the float products as
+// float pairs on the FP32 pipe (hi + lo, Knuth's two-sum: about 48 bits,
+// enough for RSG_SMALL terms); the lanes' sums are combined by shuffles
+// (deterministic).  Then the 32 nodes' sigmas (two 3x3 eigenvalue
 // problems each, in FP64) run side by side, one node per lane, instead of on
 // lane 0 of a warp per node.
 #define RSG_NORM_WARPS 4
@@ -166,20 +166,15 @@ __global__ void __launch_bounds__(RSG_NORM_WARPS * 32)
         const int node = base + k;
         const int s = N.start[node], n = N.n[node];
         if (n <= 0 || n > RSG_SMALL) continue;
-        DF acc[6];
-#pragma unroll
-        for (int d = 0; d < 6; d++) acc[d] = DF{0.f, 0.f};
+        double acc[6] = {0, 0, 0, 0, 0, 0};
         for (int i = lane; i < n; i += 32)
 #pragma unroll
-            for (int d = 0; d < 6; d++) acc[d] = df_add_f(acc[d], W[s + i].pos[d]);
-        DF md[6];
+            for (int d = 0; d < 6; d++) acc[d] += (double)W[s + i].pos[d];
+        double mean[6];
 #pragma unroll
         for (int d = 0; d < 6; d++) {
-            for (int o = 16; o; o >>= 1) {
-                DF y{__shfl_xor_sync(FULL, acc[d].hi, o), __shfl_xor_sync(FULL, acc[d].lo, o)};
-                acc[d] = df_add(acc[d], y);
-            }
-            md[d] = df_from_double(df_to_double(acc[d]) / (double)n);
+            for (int o = 16; o; o >>= 1) acc[d] += __shfl_xor_sync(FULL, acc[d], o);
+            mean[d] = acc[d] / (double)n;
         }
         float ch[21], cl[21];
         for (int jj = 0; jj < 21; jj++) ch[jj] = cl[jj] = 0.f;
@@ -187,8 +182,7 @@ __global__ void __launch_bounds__(RSG_NORM_WARPS * 32)
             float qv[6];
 #pragma unroll
             for (int d = 0; d < 6; d++) {
-                const DF t = df_two_sum(W[s + i].pos[d], -md[d].hi);
-                qv[d] = __fadd_rn(t.hi, __fsub_rn(t.lo, md[d].lo));
+                qv[d] = __double2float_rn((double)W[s + i].pos[d] - mean[d]);
                 W[s + i].pos[d] = qv[d];
             }
             int jj = 0;
