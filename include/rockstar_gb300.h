@@ -31,9 +31,9 @@ extern "C" {
 #define RSG_ERR_CUDA (-2)       /* a CUDA call failed */
 #define RSG_ERR_NO_DEVICE (-3)  /* no usable GPU */
 #define RSG_ERR_LIMIT (-4)      /* a bounded device loop hit its limit */
-#define RSG_ERR_INPUT (-5)      /* non-finite particle data */
+#define RSG_ERR_INPUT (-5)      /* non-finite particle data, or an input file the reader refuses */
 #define RSG_ERR_BUSY (-6)       /* a call that shares fixed scratch is in progress */
-#define RSG_ERR_IO (-7)         /* a catalogue file could not be opened or written */
+#define RSG_ERR_IO (-7)         /* a file could not be opened, read or written */
 
 struct rsg_particle { int64_t id; float pos[6]; };
 struct rsg_fof { int64_t num_p; struct rsg_particle *particles; };
@@ -221,6 +221,38 @@ int rsg_write_ascii(const char *path, const struct rsg_halo *halos,
 int rsg_write_binary(const char *path, const struct rsg_halo *halos, int64_t num_halos,
                      const struct rsg_particle *p, int64_t num_p,
                      const struct rsg_catalog *opt, const struct rsg_config *cfg);
+
+/* Particle input (host buffers; the records are assembled and sorted on the
+ * device).  Options of a GADGET-2 file, named after src/config.template.h: */
+struct rsg_gadget_opts {
+    int64_t halo_particle_type;    /* GADGET_HALO_PARTICLE_TYPE (1) */
+    int64_t skip_non_halo;         /* GADGET_SKIP_NON_HALO_PARTICLES (1) */
+    double length_conversion;      /* GADGET_LENGTH_CONVERSION (1.0) */
+    double mass_conversion;        /* GADGET_MASS_CONVERSION (1e10) */
+    int64_t rescale_particle_mass; /* RESCALE_PARTICLE_MASS (0) */
+    int64_t lightcone;             /* LIGHTCONE (0) */
+    int64_t lgadget;               /* FILE_FORMAT "LGADGET" (0: "GADGET2") */
+};
+/* load_particles_gadget2 (src/io/io_gadget.c:200-254) for one file: the
+ * particles of the halo type (or all), in file order, as the reference's
+ * records -- positions times length_conversion, velocities times sqrt(a)
+ * (1 for a lightcone), 4-byte ids widened as unsigned -- for any of the
+ * three GADGET variants (untagged, 4- or 8-byte block tags), either byte
+ * order, 4- or 8-byte ids and float or double coordinates.  cfg is updated
+ * as gadget2_extract_header_info updates the reference's globals (:122-179):
+ * om, ol, h0, box_size, total_particles, scale_now, particle_mass (from the
+ * header's mass, unless it is 0 and cfg already has one, or from the
+ * cosmology with rescale_particle_mass) and avg_particle_spacing.  With p
+ * NULL only the count is returned in *num_p.  RSG_ERR_IO for an unreadable
+ * or malformed file, RSG_ERR_INPUT for a curved cosmology (the reference
+ * exits). */
+int rsg_read_gadget2(const char *path, const struct rsg_gadget_opts *opt, struct rsg_config *cfg,
+                     struct rsg_particle *p, int64_t max_p, int64_t *num_p);
+/* The reference sorts the particles by id before halo finding
+ * (std::sort, src/mpi_main.cpp:2021-2024); this sorts p[0..n) by id on the
+ * device (radix sort, stable: particles with equal ids, for which the
+ * reference's order is unspecified, keep their input order). */
+int rsg_sort_particles_by_id(struct rsg_particle *p, int64_t n);
 
 /* Selects the potential form (0-3, as for rsg_compute_potential) that the
  * batched substructure form (rsg_find_subs_batch, rsg_path_device with

@@ -79,6 +79,8 @@ def lib():
         h.rsg_get_tuning.argtypes = [C.c_char_p, vp]
         h.rsg_debug_potentials.restype = i64
         h.rsg_debug_potentials.argtypes = [vp, i64]
+        h.rsg_read_gadget2.argtypes = [C.c_char_p, vp, vp, vp, i64, vp]
+        h.rsg_sort_particles_by_id.argtypes = [vp, i64]
         h.rsg_should_print.argtypes = [vp, vp, vp]
         h.rsg_count_halos_to_print.restype = i64
         h.rsg_count_halos_to_print.argtypes = [vp, i64, vp, vp]
@@ -343,6 +345,43 @@ def profile_read():
     t = np.zeros(1, np.float64)
     _check(lib().rsg_profile_read(n.ctypes.data, t.ctypes.data))
     return int(n[0]), float(t[0])
+
+
+class GadgetOpts(C.Structure):
+    """struct rsg_gadget_opts."""
+    _fields_ = [("halo_particle_type", C.c_int64), ("skip_non_halo", C.c_int64),
+                ("length_conversion", C.c_double), ("mass_conversion", C.c_double),
+                ("rescale_particle_mass", C.c_int64), ("lightcone", C.c_int64),
+                ("lgadget", C.c_int64)]
+
+
+GADGET_CFG_FIELDS = ("om", "ol", "h0", "box_size", "total_particles", "scale_now",
+                     "particle_mass", "avg_particle_spacing")
+
+
+def read_gadget2(path, cfg, halo_particle_type=1, skip_non_halo=1, length_conversion=1.0,
+                 mass_conversion=1e10, rescale_particle_mass=0, lightcone=0, lgadget=0):
+    """One GADGET-2 file: (particles in file order, dict of the configuration
+    values the header sets).  cfg supplies PARTICLE_MASS for a header
+    without one."""
+    st = config_struct(cfg)
+    o = GadgetOpts(halo_particle_type, skip_non_halo, length_conversion, mass_conversion,
+                   rescale_particle_mass, lightcone, lgadget)
+    n = np.zeros(1, np.int64)
+    _check(lib().rsg_read_gadget2(os.fsencode(path), C.byref(o), C.byref(st), None, 0,
+                                  n.ctypes.data))
+    pa = np.zeros(int(n[0]), PARTICLE)
+    st = config_struct(cfg)
+    _check(lib().rsg_read_gadget2(os.fsencode(path), C.byref(o), C.byref(st),
+                                  pa.ctypes.data if len(pa) else None, len(pa), n.ctypes.data))
+    return pa, {k: getattr(st, k) for k in GADGET_CFG_FIELDS}
+
+
+def sort_by_id(parts):
+    """The particles sorted by id on the device (a new array)."""
+    pa = np.array(parts, dtype=PARTICLE, copy=True)
+    _check(lib().rsg_sort_particles_by_id(pa.ctypes.data if len(pa) else None, len(pa)))
+    return pa
 
 
 class CatalogOpts(C.Structure):

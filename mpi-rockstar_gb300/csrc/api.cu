@@ -60,6 +60,16 @@ Ctx &ctx() {
     return *g_ctx;
 }
 
+// The calling thread's arena, reserved for `bytes` and reset, and its stream
+// (for the entry points of other translation units).
+Arena &call_arena(size_t bytes, cudaStream_t *st) {
+    Ctx &C = ctx();
+    C.ar.reserve(bytes);
+    C.ar.reset();
+    *st = C.st;
+    return C.ar;
+}
+
 // ---- configuration (host) ----------------------------------------------
 static const double RHO_C = 2.77519737e11;  // src/universal_constants.h:5
 static const double GRAV = 4.30117902e-9;   // src/universal_constants.h:4

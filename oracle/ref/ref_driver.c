@@ -281,3 +281,37 @@ int64_t ref_time_path(const struct particle *in, int64_t n, int nthreads,
     free(h); free(e); free(off); free(np_); free(parts);
     return nh;
 }
+
+/* The reference's GADGET-2 reader (src/io/io_gadget.c, compiled here) on one
+ * file with the given reader settings: the particles in file order and the
+ * configuration values it sets (Om, Ol, h0, BOX_SIZE, TOTAL_PARTICLES,
+ * SCALE_NOW, PARTICLE_MASS, AVG_PARTICLE_SPACING). */
+void load_particles_gadget2(char *filename, struct particle **p, int64_t *num_p);
+int64_t ref_load_gadget2(const char *path, int64_t type, int64_t skip_non_halo, double lconv,
+                         double mconv, int64_t rescale, int64_t lightcone, int64_t lgadget,
+                         double particle_mass, struct particle *out, int64_t max_p,
+                         double *cfg_out) {
+    static char gadget2[] = "GADGET2", lgad[] = "LGADGET";
+    GADGET_HALO_PARTICLE_TYPE = type;
+    GADGET_SKIP_NON_HALO_PARTICLES = skip_non_halo;
+    GADGET_LENGTH_CONVERSION = lconv;
+    GADGET_MASS_CONVERSION = mconv;
+    RESCALE_PARTICLE_MASS = rescale;
+    LIGHTCONE = lightcone;
+    FILE_FORMAT = lgadget ? lgad : gadget2;
+    PARTICLE_MASS = particle_mass;
+    struct particle *pp = NULL;
+    int64_t n = 0;
+    load_particles_gadget2((char *)path, &pp, &n);
+    if (n <= max_p) memcpy(out, pp, sizeof(struct particle) * n);
+    free(pp);
+    cfg_out[0] = Om;
+    cfg_out[1] = Ol;
+    cfg_out[2] = h0;
+    cfg_out[3] = BOX_SIZE;
+    cfg_out[4] = (double)TOTAL_PARTICLES;
+    cfg_out[5] = SCALE_NOW;
+    cfg_out[6] = PARTICLE_MASS;
+    cfg_out[7] = AVG_PARTICLE_SPACING;
+    return n;
+}

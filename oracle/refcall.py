@@ -56,6 +56,9 @@ def lib():
         h.ref_time_path.restype = i64
         h.ref_time_path.argtypes = [vp, i64, C.c_int, vp, vp]
         h.ref_output_binary.argtypes = [C.c_char_p, vp, i64, vp, i64, i64, i64, i64, vp]
+        h.ref_load_gadget2.restype = i64
+        h.ref_load_gadget2.argtypes = [C.c_char_p, i64, i64, C.c_double, C.c_double, i64, i64,
+                                       i64, C.c_double, vp, i64, vp]
         assert h.ref_sizeof_halo() == L.HALO.itemsize
         assert h.ref_sizeof_extra() == L.EXTRA.itemsize
         assert h.ref_sizeof_potential() == L.POTENTIAL.itemsize
@@ -143,3 +146,22 @@ def output_binary(path, halos, parts, id_offset=0, snap=0, chunk=0, bounds=None)
     b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.float32)
     lib().ref_output_binary(os.fsencode(path), h.ctypes.data, len(h), pa.ctypes.data, len(pa),
                             id_offset, snap, chunk, b.ctypes.data if b is not None else None)
+
+
+GADGET_CFG_FIELDS = ("om", "ol", "h0", "box_size", "total_particles", "scale_now",
+                     "particle_mass", "avg_particle_spacing")
+
+
+def load_gadget2(path, halo_particle_type=1, skip_non_halo=1, length_conversion=1.0,
+                 mass_conversion=1e10, rescale_particle_mass=0, lightcone=0, lgadget=0,
+                 particle_mass=0.0, max_p=1 << 22):
+    """The reference's load_particles_gadget2 on one file: (particles in file
+    order, dict of the configuration values it sets)."""
+    out = np.zeros(max_p, L.PARTICLE)
+    cfg = np.zeros(8, np.float64)
+    n = lib().ref_load_gadget2(os.fsencode(path), halo_particle_type, skip_non_halo,
+                               length_conversion, mass_conversion, rescale_particle_mass,
+                               lightcone, lgadget, particle_mass, out.ctypes.data, max_p,
+                               cfg.ctypes.data)
+    assert n <= max_p
+    return out[:n].copy(), dict(zip(GADGET_CFG_FIELDS, cfg.tolist()))
