@@ -25,7 +25,9 @@ cpu_baseline: the C restatement of the reference (oracle/) on one host core
 """
 import argparse
 import json
+import math
 import os
+import struct
 import subprocess
 import sys
 import tempfile
@@ -454,6 +456,97 @@ def profile_only(rk, cfg_id, scale, warmup):
                       "kernel_ms": {r[0]: float(r[2]) for r in rows[:12]}}))
 
 
+IO_BOX, IO_SCALE = 250.0, 0.5  # box (Mpc/h) and scale factor of the input file
+
+
+def io_write_gadget(path, n):
+    """A GADGET-2 file of n type-1 particles: tagged variant (8-byte block
+    tags), little-endian, float coordinates, 8-byte ids in a random order,
+    header mass 1e-3 (1e7 Msun/h)."""
+    rng = np.random.default_rng(SEED)
+    pos = rng.uniform(0, IO_BOX, (n, 3)).astype("<f4")
+    vel = rng.normal(0, 300.0, (n, 3)).astype("<f4")
+    ids = (rng.permutation(n).astype("<i8") + 1) * 3
+    a = IO_SCALE
+    npart = [0, n, 0, 0, 0, 0]
+    hdr = struct.pack("<6I6ddd2i6I2i4d2i6ii", *npart, 0, 1e-3, 0, 0, 0, 0, a, 1 / a - 1, 0, 0,
+                      *npart, 0, 1, IO_BOX, 0.3, 0.7, 0.7, 0, 0, 0, 0, 0, 0, 0, 0, 0)
+    with open(path, "wb") as f:
+        for tag, blob in ((b"HEAD", hdr.ljust(256, b"\0")), (b"POS ", pos.tobytes()),
+                          (b"VEL ", vel.tobytes()), (b"ID  ", ids.tobytes())):
+            f.write(struct.pack("<I4sII", 8, tag, len(blob) + 8, 8))
+            f.write(struct.pack("<I", len(blob)) + blob + struct.pack("<I", len(blob)))
+
+
+def io_cpu_read(path, n, particle_dtype):
+    """One-thread numpy restatement of load_particles_gadget2
+    (src/io/io_gadget.c:200-254) for the file of io_write_gadget: positions
+    as stored (length conversion 1), velocities times sqrt(a) in double
+    rounded to float, ids as stored."""
+    o = 16 + 264  # HEAD tag record, header record
+    out = np.zeros(n, particle_dtype)
+    for k in range(2):
+        o += 16 + 4  # block tag record, record marker
+        blk = np.fromfile(path, "<f4", 3 * n, offset=o).reshape(n, 3)
+        fac = 1.0 if k == 0 else math.sqrt(IO_SCALE)
+        out["pos"][:, 3 * k:3 * k + 3] = (blk.astype(np.float64) * fac).astype(np.float32)
+        o += 12 * n + 4
+    out["id"] = np.fromfile(path, "<i8", n, offset=o + 16 + 4)
+    return out
+
+
+def io_table(rk, n, reps=3):
+    """Particle input at n particles: the file of io_write_gadget read by
+    rsg_read_gadget2 (host records, device assembly, records back to the
+    host), then rsg_sort_particles_by_id on the file-order records (host ->
+    device radix sort -> host), each best of `reps` after one untimed call.
+    Beside each: the one-thread numpy restatement of the reference's reader
+    and of its id sort (std::sort by id, src/mpi_main.cpp:2021-2024; here
+    numpy's stable sort), with the outputs compared byte for byte.  The file
+    is written first, so reads come from the page cache.  One JSON line."""
+    fd, path = tempfile.mkstemp(suffix=".gadget2")
+    os.close(fd)
+
+    def best(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = fn()
+            ts.append(time.perf_counter() - t0)
+        return min(ts), out
+
+    try:
+        io_write_gadget(path, n)
+        file_bytes = os.path.getsize(path)
+        t_cpu_read, p_cpu = best(lambda: io_cpu_read(path, n, rk.PARTICLE))
+        t_cpu_sort, s_cpu = best(lambda: p_cpu[np.argsort(p_cpu["id"], kind="stable")])
+        import torch
+        torch.cuda.set_device(0)
+        rk.build()
+        cfg = rk.Config(particle_mass=1e9, box_size=IO_BOX, total_particles=n)
+        t_read, (p_gpu, _) = best(lambda: rk.read_gadget2(path, cfg))
+        t_sort, s_gpu = best(lambda: rk.sort_by_id(p_gpu))
+    finally:
+        os.unlink(path)
+    rec_bytes = n * rk.PARTICLE.itemsize
+    print(json.dumps({
+        "workload": "GADGET-2 file, %d particles (%d bytes), tagged variant, float "
+                    "coordinates, 8-byte ids in random order" % (n, file_bytes),
+        "reader": {"particles_per_s": n / t_read, "s": t_read,
+                   "cpu_port_particles_per_s": n / t_cpu_read, "cpu_port_s": t_cpu_read,
+                   "h2d_bytes": n * (12 + 12 + 8), "d2h_bytes": rec_bytes,
+                   "identical": p_gpu.tobytes() == p_cpu.tobytes()},
+        "id_sort": {"particles_per_s": n / t_sort, "s": t_sort,
+                    "cpu_port_particles_per_s": n / t_cpu_sort, "cpu_port_s": t_cpu_sort,
+                    "h2d_bytes": rec_bytes, "d2h_bytes": rec_bytes,
+                    "identical": s_gpu.tobytes() == s_cpu.tobytes(),
+                    "sorted": bool(np.all(np.diff(s_gpu["id"]) > 0))},
+        "cpu_port": {"cores": 1, "kind": "port",
+                     "what": "numpy restatement of the reader; numpy stable sort for the id sort"},
+        "reps": reps}))
+
+
 def run_autotune(rk, cfg_id, scale):
     """Size-class thresholds by measurement (mpi-rockstar_gb300/autotune.py)."""
     from mpi_rockstar_gb300 import autotune
@@ -504,6 +597,10 @@ def main():
                     help="instead of the bench line: the reference's CPU path (FOF serial, "
                          "find_subs on every host core) per workload, best of 3, for "
                          "'cfg:scale,cfg:scale,...'; one JSON line each")
+    ap.add_argument("--io-table", type=int, default=0,
+                    help="instead of the bench line: particle input (GADGET-2 reader and id "
+                         "sort) at this many particles against a one-thread CPU restatement; "
+                         "one JSON line")
     ap.add_argument("--precision-forms", default="3,0,1,2",
                     help="potential forms of the study; the first is the reference "
                          "(3: FP64 direct sum, O(n^2) per group)")
@@ -522,6 +619,10 @@ def main():
     if args.profile_only:
         if rank == 0:
             profile_only(rk, args.cfg, args.scale, args.warmup)
+        return
+    if args.io_table:
+        if rank == 0:
+            io_table(rk, args.io_table)
         return
     if args.cpu_table:
         if rank == 0:

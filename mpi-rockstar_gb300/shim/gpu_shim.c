@@ -21,6 +21,11 @@
  *   output_catalogs_gpu(...)     in place of output_halos' two catalogue
  *                                writers, output_ascii and output_binary
  *                                (src/io/meta_io.c:490-499)
+ *   load_particles_gadget2_gpu   in place of load_particles_gadget2
+ *                                (src/io/io_gadget.h:29-30, called at
+ *                                src/io/meta_io.c:170)
+ *   sort_particles_by_id_gpu     in place of the std::sort by id before
+ *                                find_halos (src/mpi_main.cpp:2021-2024)
  * Errors: the library never exits; a non-zero return is mapped onto the
  * reference's rockstar_abort (src/error.h:17-20). */
 #include <stdio.h>
@@ -28,6 +33,7 @@
 #include <string.h>
 #include <strings.h>
 
+#include "check_syscalls.h"
 #include "config_vars.h"
 #include "error.h"
 #include "fof.h"
@@ -232,4 +238,45 @@ void output_catalogs_gpu(int64_t id_offset, int64_t snap, int64_t chunk, float *
                              (struct rsg_particle *)p, num_p, &o, &c))
             gpu_fail("rsg_write_binary");
     }
+}
+
+/* ---- particle input -----------------------------------------------------------
+ * One GADGET-2 (or LGADGET) file appended to *p, with the same arguments and
+ * effects as load_particles_gadget2: the configuration globals its header
+ * sets (Om, Ol, h0, BOX_SIZE, TOTAL_PARTICLES, SCALE_NOW, PARTICLE_MASS,
+ * AVG_PARTICLE_SPACING) and *num_p advanced by the particles read.  A file the
+ * reference would stop on (unreadable, truncated, curved cosmology) aborts. */
+void load_particles_gadget2_gpu(char *filename, struct particle **p, int64_t *num_p) {
+    struct rsg_config c;
+    struct rsg_gadget_opts o = {GADGET_HALO_PARTICLE_TYPE,
+                                GADGET_SKIP_NON_HALO_PARTICLES,
+                                GADGET_LENGTH_CONVERSION,
+                                GADGET_MASS_CONVERSION,
+                                RESCALE_PARTICLE_MASS,
+                                LIGHTCONE,
+                                !strncasecmp(FILE_FORMAT, "LGADGET", 7)};
+    int64_t n = 0;
+    gpu_config(&c);
+    if (rsg_read_gadget2(filename, &o, &c, NULL, 0, &n)) gpu_fail("rsg_read_gadget2");
+    *p = (struct particle *)check_realloc(*p, ((*num_p) + n) * sizeof(struct particle),
+                                          "Allocating particles.");
+    gpu_config(&c);
+    if (rsg_read_gadget2(filename, &o, &c, (struct rsg_particle *)(*p + *num_p), n, &n))
+        gpu_fail("rsg_read_gadget2");
+    Om = c.om;
+    Ol = c.ol;
+    h0 = c.h0;
+    BOX_SIZE = c.box_size;
+    TOTAL_PARTICLES = c.total_particles;
+    SCALE_NOW = c.scale_now;
+    PARTICLE_MASS = c.particle_mass;
+    AVG_PARTICLE_SPACING = c.avg_particle_spacing;
+    *num_p += n;
+}
+
+/* The particles sorted by id on the device (the reference's std::sort before
+ * find_halos; equal ids keep their order). */
+void sort_particles_by_id_gpu(struct particle *parts, int64_t n) {
+    if (rsg_sort_particles_by_id((struct rsg_particle *)parts, n))
+        gpu_fail("rsg_sort_particles_by_id");
 }

@@ -124,3 +124,21 @@ def test_read_gadget2_errors(rk, tmp_path):
     with pytest.raises(rk.RockstarError) as e:
         rk.read_gadget2(str(tmp_path / "missing.g2"), c)
     assert e.value.code == -7
+
+
+@pytest.mark.skipif(not os.path.exists(REF_LIB), reason="reference oracle not built")
+def test_bench_input_port_equals_reference(tmp_path):
+    """The CPU restatement bench.py times beside the device reader reads its
+    file as the reference's reader does."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import refcall
+    rk_dtype = np.dtype([("id", "<i8"), ("pos", "<f4", (6,))])
+    for n in (1, 4321):
+        path = str(tmp_path / ("io%d.g2" % n))
+        bench.io_write_gadget(path, n)
+        got = bench.io_cpu_read(path, n, rk_dtype)
+        want, cfg = refcall.load_gadget2(path, particle_mass=1e9)
+        assert got.tobytes() == want.view(np.uint8).tobytes()
+        assert cfg["scale_now"] == bench.IO_SCALE and cfg["total_particles"] == n
