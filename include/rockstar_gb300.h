@@ -248,11 +248,21 @@ struct rsg_gadget_opts {
  * exits). */
 int rsg_read_gadget2(const char *path, const struct rsg_gadget_opts *opt, struct rsg_config *cfg,
                      struct rsg_particle *p, int64_t max_p, int64_t *num_p);
+/* The same with the records left in device memory: d_p (device) has room
+ * for max_p records and holds the file's particles when the call returns, so
+ * a snapshot goes from the file to rsg_sort_particles_by_id_device and
+ * rsg_path_device without passing through host memory as records.  No
+ * reference counterpart (the reference's reader fills host memory). */
+int rsg_read_gadget2_device(const char *path, const struct rsg_gadget_opts *opt,
+                            struct rsg_config *cfg, struct rsg_particle *d_p, int64_t max_p,
+                            int64_t *num_p);
 /* The reference sorts the particles by id before halo finding
  * (std::sort, src/mpi_main.cpp:2021-2024); this sorts p[0..n) by id on the
  * device (radix sort, stable: particles with equal ids, for which the
  * reference's order is unspecified, keep their input order). */
 int rsg_sort_particles_by_id(struct rsg_particle *p, int64_t n);
+/* The same on device-resident records d_p[0..n), in place. */
+int rsg_sort_particles_by_id_device(struct rsg_particle *d_p, int64_t n);
 
 /* Selects the potential form (0-3, as for rsg_compute_potential) that the
  * batched substructure form (rsg_find_subs_batch, rsg_path_device with

@@ -81,6 +81,8 @@ def lib():
         h.rsg_debug_potentials.argtypes = [vp, i64]
         h.rsg_read_gadget2.argtypes = [C.c_char_p, vp, vp, vp, i64, vp]
         h.rsg_sort_particles_by_id.argtypes = [vp, i64]
+        h.rsg_read_gadget2_device.argtypes = [C.c_char_p, vp, vp, vp, i64, vp]
+        h.rsg_sort_particles_by_id_device.argtypes = [vp, i64]
         h.rsg_should_print.argtypes = [vp, vp, vp]
         h.rsg_count_halos_to_print.restype = i64
         h.rsg_count_halos_to_print.argtypes = [vp, i64, vp, vp]
@@ -377,9 +379,50 @@ def read_gadget2(path, cfg, halo_particle_type=1, skip_non_halo=1, length_conver
     return pa, {k: getattr(st, k) for k in GADGET_CFG_FIELDS}
 
 
-def sort_by_id(parts):
-    """The particles sorted by id on the device (a new array)."""
-    pa = np.array(parts, dtype=PARTICLE, copy=True)
+def read_gadget2_device(path, cfg, **opts):
+    """read_gadget2 with the records left on the device: (torch uint8 CUDA
+    tensor of n PARTICLE records, dict of the header's configuration values);
+    the tensor's data pointer feeds DevicePath.run and sort_by_id_device."""
+    import torch
+    st = config_struct(cfg)
+    o = GadgetOpts(opts.get("halo_particle_type", 1), opts.get("skip_non_halo", 1),
+                   opts.get("length_conversion", 1.0), opts.get("mass_conversion", 1e10),
+                   opts.get("rescale_particle_mass", 0), opts.get("lightcone", 0),
+                   opts.get("lgadget", 0))
+    n = np.zeros(1, np.int64)
+    _check(lib().rsg_read_gadget2_device(os.fsencode(path), C.byref(o), C.byref(st), None, 0,
+                                         n.ctypes.data))
+    out = torch.empty(max(int(n[0]), 1) * PARTICLE.itemsize, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()  # the library works on its own stream
+    st = config_struct(cfg)
+    _check(lib().rsg_read_gadget2_device(os.fsencode(path), C.byref(o), C.byref(st),
+                                         out.data_ptr(), int(n[0]), n.ctypes.data))
+    return out[: int(n[0]) * PARTICLE.itemsize], {k: getattr(st, k) for k in GADGET_CFG_FIELDS}
+
+
+def sort_by_id_device(d_parts, n=None):
+    """Device-resident records (a torch CUDA tensor of PARTICLE bytes, or a
+    device pointer with n) sorted by id in place."""
+    if n is None:
+        n = d_parts.numel() // PARTICLE.itemsize
+    ptr = d_parts if isinstance(d_parts, int) else d_parts.data_ptr()
+    if not isinstance(d_parts, int):
+        import torch
+        torch.cuda.synchronize()
+    _check(lib().rsg_sort_particles_by_id_device(ptr if n else None, n))
+
+
+def sort_by_id(parts, inplace=False):
+    """The particles sorted by id on the device: a new array, or with
+    inplace=True the caller's (contiguous PARTICLE) array itself, as the
+    reference's std::sort sorts p."""
+    if inplace:
+        if not (isinstance(parts, np.ndarray) and parts.dtype == PARTICLE
+                and parts.flags.c_contiguous and parts.flags.writeable):
+            raise ValueError("inplace needs a writeable contiguous PARTICLE array")
+        pa = parts
+    else:
+        pa = np.array(parts, dtype=PARTICLE, copy=True)
     _check(lib().rsg_sort_particles_by_id(pa.ctypes.data if len(pa) else None, len(pa)))
     return pa
 
