@@ -792,6 +792,18 @@ def main():
         h2d = n * 32 + len(fp) * 32 + 16 * len(off)
         d2h = len(fp) * 32 + 16 * len(off) + len(fp) * 32 + len(halos) * (312 + 48)
     e2e_v = n * world / min(e2e_t)
+    # the same two calls on pageable memory, as the reference's malloc'd p
+    # arrives through the drop-in (large pageable buffers take the library's
+    # staging threads)
+    pageable = np.empty(n, rk.PARTICLE)
+    e2e_pg = []
+    for it in range(2):
+        np.copyto(pageable.view(np.uint8), p.view(np.uint8))
+        t0 = time.perf_counter()
+        fp, off, sz = rk.rockstar_fof(pageable, cfg, inplace=True)
+        rk.find_subs(fp, off, sz, cfg, batched=True, inplace=True)
+        e2e_pg.append(time.perf_counter() - t0)
+    del pageable
 
     parity = None
     if sample is not None:
@@ -843,6 +855,9 @@ def main():
                        "plain_gpu_launches": plain_launches,
                        "tuning": rk.get_tuning(),
                        "tuning_source": "mpi-rockstar_gb300/tuning.json" if tuned else "defaults"},
+            "e2e_pageable": {"value": n * world / min(e2e_pg), "unit": "particles/s",
+                             "what": "the e2e calls on a pageable (malloc'd) particle array, "
+                                     "best of 2"},
             "e2e": {"value": e2e_v, "unit": "particles/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu, "parity": parity,

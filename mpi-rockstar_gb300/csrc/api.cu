@@ -6,6 +6,7 @@
 #include <atomic>
 #include <vector>
 
+#include "hoststage.cuh"
 #include "kdtree_impl.cuh"
 #include "subs.cuh"
 
@@ -156,14 +157,14 @@ int rsg_rockstar_fof(struct rsg_particle *p, int64_t *num_p, const struct rsg_co
         C.ar.reset();
         rsg_particle *d_in = C.ar.get<rsg_particle>(n), *d_out = C.ar.get<rsg_particle>(n);
         int64_t *d_off = C.ar.get<int64_t>(n / 2 + 1), *d_sz = C.ar.get<int64_t>(n / 2 + 1);
-        RSG_CUDA(cudaMemcpyAsync(d_in, p, sizeof(rsg_particle) * n, cudaMemcpyHostToDevice, C.st));
+        host_to_device(d_in, p, sizeof(rsg_particle) * n, C.st);
         FofOut o = fof3d_device(C.ar, d_in, n, *cfg, d_out, d_off, d_sz, C.st);
         if (o.nfofs > max_fofs) {
             set_error(RSG_ERR_ARGS, "rsg_rockstar_fof: %lld groups exceed max_fofs %lld",
                       (long long)o.nfofs, (long long)max_fofs);
             return RSG_ERR_ARGS;
         }
-        RSG_CUDA(cudaMemcpyAsync(p, d_out, sizeof(rsg_particle) * o.num_p, cudaMemcpyDeviceToHost, C.st));
+        device_to_host(p, d_out, sizeof(rsg_particle) * o.num_p, C.st);
         if (o.nfofs) {
             RSG_CUDA(cudaMemcpyAsync(fof_offsets, d_off, sizeof(int64_t) * o.nfofs, cudaMemcpyDeviceToHost, C.st));
             RSG_CUDA(cudaMemcpyAsync(fof_sizes, d_sz, sizeof(int64_t) * o.nfofs, cudaMemcpyDeviceToHost, C.st));
@@ -199,7 +200,7 @@ static int find_subs_host(struct rsg_particle *p, int64_t num_p, const int64_t *
         rsg_particle *d_p = C.ar.get<rsg_particle>(num_p);
         rsg_halo *d_h = C.ar.get<rsg_halo>(hcap);
         rsg_extra_halo_info *d_e = C.ar.get<rsg_extra_halo_info>(hcap);
-        RSG_CUDA(cudaMemcpyAsync(d_p, p, sizeof(rsg_particle) * num_p, cudaMemcpyHostToDevice, C.st));
+        host_to_device(d_p, p, sizeof(rsg_particle) * num_p, C.st);
         SubsOut o = find_subs_device(C.ar, d_p, num_p, fof_offsets, fof_sizes, num_fofs, *cfg,
                                      d_h, d_e, hcap, C.st, exact);
         if (o.nhalos > max_halos) {
@@ -207,10 +208,10 @@ static int find_subs_host(struct rsg_particle *p, int64_t num_p, const int64_t *
                       (long long)o.nhalos, (long long)max_halos);
             return RSG_ERR_ARGS;
         }
-        RSG_CUDA(cudaMemcpyAsync(p, d_p, sizeof(rsg_particle) * num_p, cudaMemcpyDeviceToHost, C.st));
+        device_to_host(p, d_p, sizeof(rsg_particle) * num_p, C.st);
         if (o.nhalos) {
-            RSG_CUDA(cudaMemcpyAsync(halos, d_h, sizeof(rsg_halo) * o.nhalos, cudaMemcpyDeviceToHost, C.st));
-            RSG_CUDA(cudaMemcpyAsync(extra, d_e, sizeof(rsg_extra_halo_info) * o.nhalos, cudaMemcpyDeviceToHost, C.st));
+            device_to_host(halos, d_h, sizeof(rsg_halo) * o.nhalos, C.st);
+            device_to_host(extra, d_e, sizeof(rsg_extra_halo_info) * o.nhalos, C.st);
         }
         RSG_CUDA(cudaStreamSynchronize(C.st));
         *num_halos = o.nhalos;
@@ -297,14 +298,14 @@ int rsg_compute_potential(struct rsg_potential *po, int64_t num_po, const struct
         int32_t *seg = C.ar.get<int32_t>(2);
         int *err = C.ar.get<int>(2);
         int32_t hseg[2] = {0, (int32_t)num_po};
-        RSG_CUDA(cudaMemcpyAsync(d, po, sizeof(PotRec) * num_po, cudaMemcpyHostToDevice, C.st));
+        host_to_device(d, po, sizeof(PotRec) * num_po, C.st);
         RSG_CUDA(cudaMemcpyAsync(seg, hseg, sizeof(hseg), cudaMemcpyHostToDevice, C.st));
         RSG_CUDA(cudaMemsetAsync(err, 0, 2 * sizeof(int), C.st));
         launch(k_zero_pe, nblk(num_po, 256), 256, 0, C.st, d, num_po);
         bh_potential(C.ar, d, num_po, seg, seg + 1, 1, cfg->particle_mass, cfg->force_res, err,
                      C.st, form);
         int herr[2];
-        RSG_CUDA(cudaMemcpyAsync(po, d, sizeof(PotRec) * num_po, cudaMemcpyDeviceToHost, C.st));
+        device_to_host(po, d, sizeof(PotRec) * num_po, C.st);
         RSG_CUDA(cudaMemcpyAsync(herr, err, sizeof(herr), cudaMemcpyDeviceToHost, C.st));
         RSG_CUDA(cudaStreamSynchronize(C.st));
         if (herr[0]) {
@@ -331,10 +332,10 @@ int rsg_compute_kinetic_energy(struct rsg_potential *po, int64_t num_po, const f
         C.ar.reserve((size_t)num_po * sizeof(PotRec) + (16u << 20));
         C.ar.reset();
         PotRec *d = C.ar.get<PotRec>(num_po);
-        RSG_CUDA(cudaMemcpyAsync(d, po, sizeof(PotRec) * num_po, cudaMemcpyHostToDevice, C.st));
+        host_to_device(d, po, sizeof(PotRec) * num_po, C.st);
         kinetic_energy_device(d, num_po, vel_cen, pos_cen, scale_now, hubble100(*cfg, scale_now),
                               C.st);
-        RSG_CUDA(cudaMemcpyAsync(po, d, sizeof(PotRec) * num_po, cudaMemcpyDeviceToHost, C.st));
+        device_to_host(po, d, sizeof(PotRec) * num_po, C.st);
         RSG_CUDA(cudaStreamSynchronize(C.st));
         return RSG_OK;
     } catch (Failure &) {

@@ -230,4 +230,37 @@ void stage_d2h(void *dst, const void *src, size_t bytes) {
     rethrow(S, nullptr);
 }
 
+namespace {
+// pageable host memory of at least four chunks: worth the staging threads
+bool staged(const void *h, size_t bytes) {
+    if (bytes < 4 * kChunk) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();  // clear the error the query recorded
+        return false;
+    }
+    return a.type == cudaMemoryTypeUnregistered;
+}
+}  // namespace
+
+void host_to_device(void *d, const void *h, size_t bytes, cudaStream_t st) {
+    if (!bytes) return;
+    if (!staged(h, bytes)) {
+        RSG_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st));
+        return;
+    }
+    RSG_CUDA(cudaStreamSynchronize(st));  // d may still be read by earlier work
+    stage_h2d({{-1, 0, h, d, bytes}}, nullptr);
+}
+
+void device_to_host(void *h, const void *d, size_t bytes, cudaStream_t st) {
+    if (!bytes) return;
+    if (!staged(h, bytes)) {
+        RSG_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, st));
+        return;
+    }
+    RSG_CUDA(cudaStreamSynchronize(st));  // the producing work ends first
+    stage_d2h(h, d, bytes);
+}
+
 }  // namespace rsg

@@ -14,6 +14,8 @@
 
 #include <vector>
 
+#include <cuda_runtime.h>
+
 namespace rsg {
 
 // One contiguous region of a host-to-device transfer.
@@ -32,5 +34,12 @@ void stage_h2d(const std::vector<HostPiece> &pieces, const char *what);
 
 // dst[0..bytes) (any host memory) <- src (device); returns when done.
 void stage_d2h(void *dst, const void *src, size_t bytes);
+
+// A caller's host buffer to or from the device around work on stream st.
+// Page-locked memory, and buffers of a few chunks, are copied with
+// cudaMemcpyAsync on st; larger pageable buffers go through the staging
+// threads, after st has been synchronised, and are complete on return.
+void host_to_device(void *d, const void *h, size_t bytes, cudaStream_t st);
+void device_to_host(void *h, const void *d, size_t bytes, cudaStream_t st);
 
 }  // namespace rsg
