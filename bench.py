@@ -550,6 +550,18 @@ def io_table(rk, n, reps=3):
                 ts.append(time.perf_counter() - t0)
         t_dsort = min(ts)
         d_sort_ok = d_gpu.cpu().numpy().tobytes() == s_cpu.tobytes()
+        del d_gpu, pristine
+        # the internal format (the records verbatim after a 256-byte header):
+        # the reference's single fread restated as one np.fromfile
+        rk.write_internal(path, s_cpu, cfg)
+        t_icpu, i_cpu = best(lambda: np.fromfile(path, rk.PARTICLE, offset=256))
+        t_ihost, (i_host, _) = best(lambda: rk.read_internal(path, cfg))
+        t_idev, (i_dev, _) = best(lambda: rk.read_internal_device(path, cfg))
+        internal = {"cpu_port_s": t_icpu, "host_s": t_ihost, "device_s": t_idev,
+                    "device_particles_per_s": n / t_idev,
+                    "identical": i_host.tobytes() == i_cpu.tobytes() == s_cpu.tobytes()
+                    and i_dev.cpu().numpy().tobytes() == s_cpu.tobytes()}
+        del i_dev
     finally:
         os.unlink(path)
     rec_bytes = n * rk.PARTICLE.itemsize
@@ -576,6 +588,7 @@ def io_table(rk, n, reps=3):
                                  "frac": 2 * rec_bytes / t_dsort / 1e9 / hbm,
                                  "note": "records read and written once; host-timed call "
                                          "including the id-range read-back"}},
+        "internal_format": internal,
         "cpu_port": {"cores": 1, "kind": "port",
                      "what": "numpy restatement of the reader; numpy stable sort for the id sort"},
         "reps": reps}))

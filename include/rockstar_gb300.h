@@ -256,6 +256,25 @@ int rsg_read_gadget2(const char *path, const struct rsg_gadget_opts *opt, struct
 int rsg_read_gadget2_device(const char *path, const struct rsg_gadget_opts *opt,
                             struct rsg_config *cfg, struct rsg_particle *d_p, int64_t max_p,
                             int64_t *num_p);
+/* The reference's internal particle format (FILE_FORMAT "INTERNAL"; the
+ * DUMP_PARTICLES output): load_particles_internal (src/io/io_internal.c:85-100)
+ * on one file -- the 256-byte binary header (magic, PARTICLE_TYPE_FULL) and
+ * the records verbatim.  cfg's scale_now, om, ol, h0, box_size and
+ * particle_mass take the header's values, as read_binary_header_config does
+ * (:43-50).  With p NULL only the count is returned in *num_p.  RSG_ERR_IO
+ * for an unreadable, truncated or foreign file (the reference asserts).
+ * The host variant reads with parallel preads and needs no device; the
+ * device variant leaves the records in d_p (device memory). */
+int rsg_read_internal(const char *path, struct rsg_config *cfg, struct rsg_particle *p,
+                      int64_t max_p, int64_t *num_p);
+int rsg_read_internal_device(const char *path, struct rsg_config *cfg, struct rsg_particle *d_p,
+                             int64_t max_p, int64_t *num_p);
+/* output_particles_internal(snap, chunk, 1) (src/io/io_internal.c:52-83):
+ * the header of fill_binary_header with num_particles = num_p and
+ * PARTICLE_TYPE_FULL, then p[0..num_p).  The random subsample of a fraction
+ * in (0, 1) (the weak-lensing output) is not provided. */
+int rsg_write_internal(const char *path, const struct rsg_particle *p, int64_t num_p,
+                       int64_t snap, int64_t chunk, const struct rsg_config *cfg);
 /* The reference sorts the particles by id before halo finding
  * (std::sort, src/mpi_main.cpp:2021-2024); this sorts p[0..n) by id on the
  * device (radix sort, stable: particles with equal ids, for which the

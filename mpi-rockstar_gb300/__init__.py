@@ -83,6 +83,9 @@ def lib():
         h.rsg_sort_particles_by_id.argtypes = [vp, i64]
         h.rsg_read_gadget2_device.argtypes = [C.c_char_p, vp, vp, vp, i64, vp]
         h.rsg_sort_particles_by_id_device.argtypes = [vp, i64]
+        h.rsg_read_internal.argtypes = [C.c_char_p, vp, vp, i64, vp]
+        h.rsg_read_internal_device.argtypes = [C.c_char_p, vp, vp, i64, vp]
+        h.rsg_write_internal.argtypes = [C.c_char_p, vp, i64, i64, i64, vp]
         h.rsg_should_print.argtypes = [vp, vp, vp]
         h.rsg_count_halos_to_print.restype = i64
         h.rsg_count_halos_to_print.argtypes = [vp, i64, vp, vp]
@@ -398,6 +401,45 @@ def read_gadget2_device(path, cfg, **opts):
     _check(lib().rsg_read_gadget2_device(os.fsencode(path), C.byref(o), C.byref(st),
                                          out.data_ptr(), int(n[0]), n.ctypes.data))
     return out[: int(n[0]) * PARTICLE.itemsize], {k: getattr(st, k) for k in GADGET_CFG_FIELDS}
+
+
+INTERNAL_CFG_FIELDS = ("scale_now", "om", "ol", "h0", "box_size", "particle_mass")
+
+
+def read_internal(path, cfg):
+    """One file of the reference's internal particle format: (particles,
+    dict of the configuration values its header sets)."""
+    st = config_struct(cfg)
+    n = np.zeros(1, np.int64)
+    _check(lib().rsg_read_internal(os.fsencode(path), C.byref(st), None, 0, n.ctypes.data))
+    pa = np.zeros(int(n[0]), PARTICLE)
+    _check(lib().rsg_read_internal(os.fsencode(path), C.byref(st),
+                                   pa.ctypes.data if len(pa) else None, len(pa), n.ctypes.data))
+    return pa, {k: getattr(st, k) for k in INTERNAL_CFG_FIELDS}
+
+
+def read_internal_device(path, cfg):
+    """read_internal with the records left on the device: (torch uint8 CUDA
+    tensor of PARTICLE records, dict of the header's values)."""
+    import torch
+    st = config_struct(cfg)
+    n = np.zeros(1, np.int64)
+    _check(lib().rsg_read_internal_device(os.fsencode(path), C.byref(st), None, 0,
+                                          n.ctypes.data))
+    out = torch.empty(max(int(n[0]), 1) * PARTICLE.itemsize, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()  # the copies run on the library's streams
+    _check(lib().rsg_read_internal_device(os.fsencode(path), C.byref(st), out.data_ptr(),
+                                          int(n[0]), n.ctypes.data))
+    return out[: int(n[0]) * PARTICLE.itemsize], {k: getattr(st, k) for k in INTERNAL_CFG_FIELDS}
+
+
+def write_internal(path, parts, cfg, snap=0, chunk=0):
+    """The particles in the reference's internal format
+    (output_particles_internal with fraction 1)."""
+    pa = np.ascontiguousarray(parts, dtype=PARTICLE)
+    st = config_struct(cfg)
+    _check(lib().rsg_write_internal(os.fsencode(path), pa.ctypes.data if len(pa) else None,
+                                    len(pa), snap, chunk, C.byref(st)))
 
 
 def sort_by_id_device(d_parts, n=None):

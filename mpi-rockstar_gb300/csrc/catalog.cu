@@ -16,33 +16,12 @@
 
 #include <vector>
 
+#include "binheader.cuh"
 #include "common.cuh"
 
 namespace rsg {
 namespace {
 
-// struct binary_output_header (src/io/io_internal.h:15-27): 256 bytes
-struct BinHeader {
-    uint64_t magic;
-    int64_t snap, chunk;
-    float scale, Om, Ol, h0;
-    float bounds[6];
-    int64_t num_halos, num_particles;
-    float box_size, particle_mass;
-    int64_t particle_type;
-    int32_t format_revision;
-    char version[12];
-    int32_t add_flag;
-    char unused[256 - 12 - 4 * 12 - 4 * 2 - 8 * 6];
-};
-static_assert(sizeof(BinHeader) == 256, "binary header is 256 bytes");
-
-const uint64_t kMagic = 0xfadedacec0c0d0d0ull;   // ROCKSTAR_MAGIC
-const int32_t kFormatRevision = 2;               // HALO_FORMAT_REVISION, src/halo.h:4
-const char *const kVersion = "1.0.0RC";          // ROCKSTAR_VERSION, src/version.h:4
-// OUTPUT_NFW_CHI2 (1) | OUTPUT_INERTIA_TENSOR (4): the build flags the halo
-// layout follows (src/io/io_internal.c:30-40)
-const int32_t kAddFlag = 1 | 4;
 const int64_t kAlwaysPrint = 16;  // ALWAYS_PRINT_FLAG, src/groupies.h:12
 // the mass definitions the density thresholds are derived with
 // (src/config.template.h:9-13)
@@ -232,19 +211,11 @@ extern "C" int rsg_write_binary(const char *path, const struct rsg_halo *h, int6
         for (int64_t j = 0; j < h[i].num_p; j++) ids[j] = p[h[i].p_start + j].id;
         if (!ids.empty()) fwrite(ids.data(), sizeof(int64_t), ids.size(), o);
     }
-    H.magic = kMagic;
-    H.snap = opt->snap;
-    H.chunk = opt->chunk;
-    H.scale = (float)c.scale_now;
-    H.Om = (float)c.om;
-    H.Ol = (float)c.ol;
-    H.h0 = (float)c.h0;
-    H.box_size = (float)c.box_size;
-    H.particle_mass = (float)c.particle_mass;
-    snprintf(H.version, sizeof H.version, "%s", kVersion);
-    H.format_revision = kFormatRevision;
-    H.add_flag = kAddFlag;
-    H.particle_type = 1;  // PARTICLE_TYPE_IDS
+    const int64_t nhalos = H.num_halos, nparts = H.num_particles;
+    fill_header(H, opt->snap, opt->chunk, c);
+    H.num_halos = nhalos;
+    H.num_particles = nparts;
+    H.particle_type = kParticleTypeIds;
     if (bounds) {
         memcpy(H.bounds, bounds, sizeof(float) * 6);
     } else {

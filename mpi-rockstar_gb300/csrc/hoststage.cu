@@ -230,6 +230,32 @@ void stage_d2h(void *dst, const void *src, size_t bytes) {
     rethrow(S, nullptr);
 }
 
+void read_file_parallel(int fd, int64_t off, void *dst, size_t bytes, const char *what) {
+    if (!bytes) return;
+    const size_t nch = (bytes + kChunk - 1) / kChunk;
+    const unsigned hc = std::thread::hardware_concurrency();
+    const int n = (int)std::min<size_t>((size_t)std::max(1, std::min(kMaxWorkers, hc ? (int)hc : 4)),
+                                        nch);
+    Shared S;
+    run_workers(n, [&](int) {
+        while (!S.failed) {
+            const size_t c = S.next.fetch_add(1);
+            if (c >= nch) break;
+            const size_t o = c * kChunk, b = std::min(kChunk, bytes - o);
+            size_t got = 0;
+            while (got < b) {
+                const ssize_t r = pread(fd, (char *)dst + o + got, b - got,
+                                        (off_t)(off + (int64_t)(o + got)));
+                if (r < 0 && errno == EINTR) continue;
+                if (r <= 0) break;
+                got += (size_t)r;
+            }
+            if (got < b) S.fail(RSG_ERR_IO, "file is truncated");
+        }
+    });
+    rethrow(S, what);
+}
+
 namespace {
 // pageable host memory of at least four chunks: worth the staging threads
 bool staged(const void *h, size_t bytes) {

@@ -35,6 +35,11 @@ void stage_h2d(const std::vector<HostPiece> &pieces, const char *what);
 // dst[0..bytes) (any host memory) <- src (device); returns when done.
 void stage_d2h(void *dst, const void *src, size_t bytes);
 
+// bytes of file fd from offset off into host memory dst, by up to eight
+// threads reading 8 MiB chunks with pread (no device involved); a short read
+// fails with RSG_ERR_IO naming `what`.
+void read_file_parallel(int fd, int64_t off, void *dst, size_t bytes, const char *what);
+
 // A caller's host buffer to or from the device around work on stream st.
 // Page-locked memory, and buffers of a few chunks, are copied with
 // cudaMemcpyAsync on st; larger pageable buffers go through the staging

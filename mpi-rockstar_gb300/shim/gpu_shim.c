@@ -26,6 +26,11 @@
  *                                src/io/meta_io.c:170)
  *   sort_particles_by_id_gpu     in place of the std::sort by id before
  *                                find_halos (src/mpi_main.cpp:2021-2024)
+ *   load_particles_internal_gpu  in place of load_particles_internal
+ *                                (src/io/io_internal.h:35-36, called at
+ *                                src/io/meta_io.c:175)
+ *   output_particles_internal_gpu in place of output_particles_internal(snap,
+ *                                chunk, 1) (src/io/meta_io.c:505)
  * Errors: the library never exits; a non-zero return is mapped onto the
  * reference's rockstar_abort (src/error.h:17-20). */
 #include <stdio.h>
@@ -279,4 +284,37 @@ void load_particles_gadget2_gpu(char *filename, struct particle **p, int64_t *nu
 void sort_particles_by_id_gpu(struct particle *parts, int64_t n) {
     if (rsg_sort_particles_by_id((struct rsg_particle *)parts, n))
         gpu_fail("rsg_sort_particles_by_id");
+}
+
+/* The internal particle format (FILE_FORMAT "INTERNAL"): as
+ * load_particles_internal, *p is replaced by the file's particles (not
+ * appended to) and SCALE_NOW, Om, Ol, h0, BOX_SIZE and PARTICLE_MASS take the
+ * header's values.  The records are read with the library's parallel reads. */
+void load_particles_internal_gpu(char *filename, struct particle **parts, int64_t *num_parts) {
+    struct rsg_config c;
+    int64_t n = 0;
+    gpu_config(&c);
+    if (rsg_read_internal(filename, &c, NULL, 0, &n)) gpu_fail("rsg_read_internal");
+    *parts = (struct particle *)check_realloc(*parts, (n ? n : 1) * sizeof(struct particle),
+                                              "Allocating particles.");
+    if (rsg_read_internal(filename, &c, (struct rsg_particle *)*parts, n, &n))
+        gpu_fail("rsg_read_internal");
+    SCALE_NOW = c.scale_now;
+    Om = c.om;
+    Ol = c.ol;
+    h0 = c.h0;
+    BOX_SIZE = c.box_size;
+    PARTICLE_MASS = c.particle_mass;
+    *num_parts = n;
+}
+
+/* output_particles_internal(snap, chunk, 1): p[0..num_p) with the
+ * reference's header, to the reference's file name. */
+void output_particles_internal_gpu(int64_t snap, int64_t chunk) {
+    struct rsg_config c;
+    char buffer[1024];
+    gpu_config(&c);
+    get_output_filename(buffer, 1024, snap, chunk, "rbin");
+    if (rsg_write_internal(buffer, (struct rsg_particle *)p, num_p, snap, chunk, &c))
+        gpu_fail("rsg_write_internal");
 }

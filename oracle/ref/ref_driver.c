@@ -282,6 +282,56 @@ int64_t ref_time_path(const struct particle *in, int64_t n, int nthreads,
     return nh;
 }
 
+/* The reference's internal particle format (src/io/io_internal.c, compiled
+ * here): output_particles_internal(snap, chunk, 1) over the given particles
+ * with the configuration cfg_in = {SCALE_NOW, Om, Ol, h0, BOX_SIZE,
+ * PARTICLE_MASS}, and load_particles_internal on one file, returning the
+ * particles and the same six values after the read. */
+void output_particles_internal(int64_t snap, int64_t chunk, double fraction);
+void load_particles_internal(char *filename, struct particle **part, int64_t *num_part);
+static void ref_cfg_get(double *c) {
+    c[0] = SCALE_NOW;
+    c[1] = Om;
+    c[2] = Ol;
+    c[3] = h0;
+    c[4] = BOX_SIZE;
+    c[5] = PARTICLE_MASS;
+}
+static void ref_cfg_set(const double *c) {
+    SCALE_NOW = c[0];
+    Om = c[1];
+    Ol = c[2];
+    h0 = c[3];
+    BOX_SIZE = c[4];
+    PARTICLE_MASS = c[5];
+}
+void ref_output_particles_internal(const char *path, struct particle *parts, int64_t np,
+                                   int64_t snap, int64_t chunk, const double *cfg_in) {
+    double saved[6];
+    ref_cfg_get(saved);
+    struct particle *sp = p;
+    int64_t snp = num_p;
+    ref_cfg_set(cfg_in);
+    p = parts;
+    num_p = np;
+    ref_out_path = path;
+    output_particles_internal(snap, chunk, 1);
+    ref_out_path = NULL;
+    p = sp;
+    num_p = snp;
+    ref_cfg_set(saved);
+}
+int64_t ref_load_internal(const char *path, struct particle *out, int64_t max_p,
+                          double *cfg_out) {
+    struct particle *pp = NULL;
+    int64_t n = 0;
+    load_particles_internal((char *)path, &pp, &n);
+    if (n <= max_p) memcpy(out, pp, sizeof(struct particle) * n);
+    free(pp);
+    ref_cfg_get(cfg_out);
+    return n;
+}
+
 /* The reference's GADGET-2 reader (src/io/io_gadget.c, compiled here) on one
  * file with the given reader settings: the particles in file order and the
  * configuration values it sets (Om, Ol, h0, BOX_SIZE, TOTAL_PARTICLES,

@@ -56,6 +56,9 @@ def lib():
         h.ref_time_path.restype = i64
         h.ref_time_path.argtypes = [vp, i64, C.c_int, vp, vp]
         h.ref_output_binary.argtypes = [C.c_char_p, vp, i64, vp, i64, i64, i64, i64, vp]
+        h.ref_output_particles_internal.argtypes = [C.c_char_p, vp, i64, i64, i64, vp]
+        h.ref_load_internal.restype = i64
+        h.ref_load_internal.argtypes = [C.c_char_p, vp, i64, vp]
         h.ref_load_gadget2.restype = i64
         h.ref_load_gadget2.argtypes = [C.c_char_p, i64, i64, C.c_double, C.c_double, i64, i64,
                                        i64, C.c_double, vp, i64, vp]
@@ -146,6 +149,29 @@ def output_binary(path, halos, parts, id_offset=0, snap=0, chunk=0, bounds=None)
     b = None if bounds is None else np.ascontiguousarray(bounds, dtype=np.float32)
     lib().ref_output_binary(os.fsencode(path), h.ctypes.data, len(h), pa.ctypes.data, len(pa),
                             id_offset, snap, chunk, b.ctypes.data if b is not None else None)
+
+
+INTERNAL_CFG_FIELDS = ("scale_now", "om", "ol", "h0", "box_size", "particle_mass")
+
+
+def output_particles_internal(path, parts, cfg, snap=0, chunk=0):
+    """The reference's output_particles_internal(snap, chunk, 1)
+    (src/io/io_internal.c:52-83) writing `parts` to `path` with the
+    configuration values of the dict `cfg` (INTERNAL_CFG_FIELDS)."""
+    pa = np.ascontiguousarray(parts, dtype=L.PARTICLE)
+    c = np.array([cfg[k] for k in INTERNAL_CFG_FIELDS], np.float64)
+    lib().ref_output_particles_internal(os.fsencode(path), pa.ctypes.data, len(pa), snap,
+                                        chunk, c.ctypes.data)
+
+
+def load_internal(path, max_p=1 << 22):
+    """The reference's load_particles_internal on one file: (particles, dict
+    of the configuration values read_binary_header_config sets)."""
+    out = np.zeros(max_p, L.PARTICLE)
+    cfg = np.zeros(6, np.float64)
+    n = lib().ref_load_internal(os.fsencode(path), out.ctypes.data, max_p, cfg.ctypes.data)
+    assert n <= max_p
+    return out[:n].copy(), dict(zip(INTERNAL_CFG_FIELDS, cfg.tolist()))
 
 
 GADGET_CFG_FIELDS = ("om", "ol", "h0", "box_size", "total_particles", "scale_now",

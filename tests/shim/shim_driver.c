@@ -18,6 +18,7 @@
 
 void rockstar_gpu(void);
 void do_halo_finding_gpu(int batched);
+void load_particles_internal_gpu(char *filename, struct particle **parts, int64_t *num_parts);
 
 static void on_abort(int code, const char *file, int line) {
     printf("rockstar_abort(%d) raised at %s:%d\n", code, file, line);
@@ -25,9 +26,18 @@ static void on_abort(int code, const char *file, int line) {
     _exit(42);
 }
 
-int main(void) {
+int main(int argc, char **argv) {
     rockstar_set_error_handler(on_abort);
     do_config(NULL);
+    if (argc > 1) {  /* an internal-format file: read through the shim (no device step) */
+        struct particle *q = NULL;
+        int64_t nq = 0, sum = 0;
+        load_particles_internal_gpu(argv[1], &q, &nq);
+        for (int64_t i = 0; i < nq; i++) sum += q[i].id;
+        printf("internal: %lld particles, id sum %lld, scale %.6f, box %.3f\n", (long long)nq,
+               (long long)sum, SCALE_NOW, BOX_SIZE);
+        free(q);
+    }
     PARTICLE_MASS = 1e9;
     BOX_SIZE = 40;
     setup_config();

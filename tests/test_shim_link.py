@@ -56,7 +56,24 @@ def test_shim_links_and_aborts_without_gpu(tmp_path):
                         "-L", LIBDIR, "-lrockstar_gb300", "-Wl,-rpath," + LIBDIR, "-lstdc++",
                         "-lm", "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    # an internal-format particle file, read through the shim before the FOF
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("layouts_only", os.path.join(
+        ROOT, "mpi-rockstar_gb300", "layouts.py"))
+    L = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(L)
+    import ctypes
+    import numpy as np
+    q = np.zeros(300, L.PARTICLE)
+    q["id"] = np.arange(300) * 3
+    cfg = L.config_struct(L.Config(scale_now=0.5, box_size=75.0))
+    rbin = str(tmp_path / "q.rbin")
+    so = ctypes.CDLL(lib)
+    assert so.rsg_write_internal(rbin.encode(), ctypes.c_void_p(q.ctypes.data),
+                                 ctypes.c_int64(300), ctypes.c_int64(0), ctypes.c_int64(0),
+                                 ctypes.byref(cfg)) == 0
+    run = subprocess.run([str(exe), rbin], capture_output=True, text=True, timeout=300)
+    assert "internal: 300 particles, id sum 134550, scale 0.500000, box 75.000" in run.stdout
     try:
         import torch
         has_gpu = torch.cuda.is_available()
