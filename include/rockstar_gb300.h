@@ -222,6 +222,33 @@ int rsg_write_binary(const char *path, const struct rsg_halo *halos, int64_t num
                      const struct rsg_particle *p, int64_t num_p,
                      const struct rsg_catalog *opt, const struct rsg_config *cfg);
 
+/* struct binary_output_header (src/io/io_internal.h:15-27), 256 bytes: the
+ * header of the halo catalogue (halos_<snap>.<chunk>.bin) and of the
+ * internal particle format. */
+struct rsg_binary_header {
+    uint64_t magic; /* 0xfadedacec0c0d0d0 */
+    int64_t snap, chunk;
+    float scale, Om, Ol, h0;
+    float bounds[6];
+    int64_t num_halos, num_particles;
+    float box_size, particle_mass;
+    int64_t particle_type; /* 0 none, 1 ids, 2 full records */
+    int32_t format_revision;
+    char rockstar_version[12];
+    int32_t add_flag;
+    char unused[256 - 12 - 4 * 12 - 4 * 2 - 8 * 6];
+};
+/* load_binary_halos (src/io/io_internal.c:199-225) on one catalogue file:
+ * the header, the halo records and the particle ids, and cfg's scale_now,
+ * om, ol, h0, box_size and particle_mass from the header
+ * (read_binary_header_config).  With halos and ids NULL only the header is
+ * read (its num_halos and num_particles size the arrays).  RSG_ERR_IO for an
+ * unreadable, truncated or foreign file (the reference asserts or exits);
+ * RSG_ERR_ARGS if max_halos or max_ids is too small.  File I/O only (parallel
+ * reads), no device step. */
+int rsg_read_binary(const char *path, struct rsg_binary_header *header, struct rsg_config *cfg,
+                    struct rsg_halo *halos, int64_t max_halos, int64_t *ids, int64_t max_ids);
+
 /* Particle input (host buffers; the records are assembled and sorted on the
  * device).  Options of a GADGET-2 file, named after src/config.template.h: */
 struct rsg_gadget_opts {

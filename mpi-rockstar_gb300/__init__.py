@@ -84,6 +84,7 @@ def lib():
         h.rsg_read_gadget2_device.argtypes = [C.c_char_p, vp, vp, vp, i64, vp]
         h.rsg_sort_particles_by_id_device.argtypes = [vp, i64]
         h.rsg_read_internal.argtypes = [C.c_char_p, vp, vp, i64, vp]
+        h.rsg_read_binary.argtypes = [C.c_char_p, vp, vp, vp, i64, vp, i64]
         h.rsg_read_internal_device.argtypes = [C.c_char_p, vp, vp, i64, vp]
         h.rsg_write_internal.argtypes = [C.c_char_p, vp, i64, i64, i64, vp]
         h.rsg_should_print.argtypes = [vp, vp, vp]
@@ -514,6 +515,32 @@ def write_ascii(path, halos, extra, cfg, id_offset=0, bounds=None, num_p=0,
     o, b = _catalog_opts(id_offset, 0, 0, bounds, num_p, strict_so_masses)
     _check(lib().rsg_write_ascii(os.fsencode(path), h.ctypes.data, e.ctypes.data, len(h),
                                  C.byref(o), C.byref(st)))
+
+
+class BinaryHeader(C.Structure):
+    """struct rsg_binary_header (the reference's binary_output_header)."""
+    _fields_ = [("magic", C.c_uint64), ("snap", C.c_int64), ("chunk", C.c_int64),
+                ("scale", C.c_float), ("Om", C.c_float), ("Ol", C.c_float), ("h0", C.c_float),
+                ("bounds", C.c_float * 6), ("num_halos", C.c_int64),
+                ("num_particles", C.c_int64), ("box_size", C.c_float),
+                ("particle_mass", C.c_float), ("particle_type", C.c_int64),
+                ("format_revision", C.c_int32), ("rockstar_version", C.c_char * 12),
+                ("add_flag", C.c_int32), ("unused", C.c_char * 140)]
+
+
+def read_binary(path, cfg):
+    """A halo catalogue file (halos_<snap>.<chunk>.bin) read back, as
+    load_binary_halos does: (header, halos, particle ids, dict of the
+    configuration values the header sets)."""
+    hdr = BinaryHeader()
+    st = config_struct(cfg)
+    _check(lib().rsg_read_binary(os.fsencode(path), C.byref(hdr), C.byref(st), None, 0, None, 0))
+    h = np.zeros(hdr.num_halos, HALO)
+    ids = np.zeros(hdr.num_particles, np.int64)
+    _check(lib().rsg_read_binary(os.fsencode(path), C.byref(hdr), C.byref(st),
+                                 h.ctypes.data if len(h) else None, len(h),
+                                 ids.ctypes.data if len(ids) else None, len(ids)))
+    return hdr, h, ids, {k: getattr(st, k) for k in INTERNAL_CFG_FIELDS}
 
 
 def write_binary(path, halos, parts, cfg, id_offset=0, snap=0, chunk=0, bounds=None):

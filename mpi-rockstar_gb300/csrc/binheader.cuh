@@ -11,19 +11,7 @@
 
 namespace rsg {
 
-struct BinHeader {
-    uint64_t magic;
-    int64_t snap, chunk;
-    float scale, Om, Ol, h0;
-    float bounds[6];
-    int64_t num_halos, num_particles;
-    float box_size, particle_mass;
-    int64_t particle_type;
-    int32_t format_revision;
-    char version[12];
-    int32_t add_flag;
-    char unused[256 - 12 - 4 * 12 - 4 * 2 - 8 * 6];
-};
+using BinHeader = rsg_binary_header;
 static_assert(sizeof(BinHeader) == 256, "binary header is 256 bytes");
 
 constexpr uint64_t kMagic = 0xfadedacec0c0d0d0ull;  // ROCKSTAR_MAGIC
@@ -48,7 +36,7 @@ inline void fill_header(BinHeader &H, int64_t snap, int64_t chunk, const rsg_con
     H.h0 = (float)c.h0;
     H.box_size = (float)c.box_size;
     H.particle_mass = (float)c.particle_mass;
-    snprintf(H.version, sizeof H.version, "%s", kVersion);
+    snprintf(H.rockstar_version, sizeof H.rockstar_version, "%s", kVersion);
     H.format_revision = kFormatRevision;
     H.add_flag = kAddFlag;
 }

@@ -6,18 +6,24 @@
 //   rsg_write_binary   output_binary with fill_binary_header
 //                      (src/io/io_internal.c:16-41,118-186; header layout
 //                      src/io/io_internal.h:6-27): halos_<snap>.<chunk>.bin
+//   rsg_read_binary    load_binary_halos (src/io/io_internal.c:199-225): the
+//                      same file read back
 // Host code: formatting and file writes.  The file name is the caller's (the
 // reference builds it from OUTBASE, snap and chunk in get_output_filename).
+#include <fcntl.h>
 #include <inttypes.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include <vector>
 
 #include "binheader.cuh"
 #include "common.cuh"
+#include "hoststage.cuh"
 
 namespace rsg {
 namespace {
@@ -228,5 +234,65 @@ extern "C" int rsg_write_binary(const char *path, const struct rsg_halo *h, int6
         set_error(RSG_ERR_IO, "rsg_write_binary: write to %s failed", path);
         return RSG_ERR_IO;
     }
+    return 0;
+}
+
+extern "C" int rsg_read_binary(const char *path, struct rsg_binary_header *header,
+                               struct rsg_config *cfg, struct rsg_halo *halos, int64_t max_halos,
+                               int64_t *ids, int64_t max_ids) {
+    if (!path || !header || !cfg || max_halos < 0 || max_ids < 0 || (max_halos && !halos) ||
+        (max_ids && !ids)) {
+        set_error(RSG_ERR_ARGS, "rsg_read_binary: bad arguments");
+        return RSG_ERR_ARGS;
+    }
+    int fd = open(path, O_RDONLY);
+    struct stat sb;
+    if (fd < 0 || fstat(fd, &sb) != 0) {
+        if (fd >= 0) close(fd);
+        set_error(RSG_ERR_IO, "rsg_read_binary: cannot open %s", path);
+        return RSG_ERR_IO;
+    }
+    struct Closer {
+        int fd;
+        ~Closer() { close(fd); }
+    } closer{fd};
+    BinHeader H;
+    if (pread(fd, &H, sizeof H, 0) != (ssize_t)sizeof H) {
+        set_error(RSG_ERR_IO, "rsg_read_binary: file is truncated in %s", path);
+        return RSG_ERR_IO;
+    }
+    // the reference asserts the magic and the counts and exits on a short
+    // read (src/io/io_internal.c:212-222)
+    const int64_t hb = (int64_t)sizeof(rsg_halo), need_h = H.num_halos, need_i = H.num_particles;
+    const char *bad =
+        H.magic != kMagic                ? "not a Rockstar binary file"
+        : need_h < 0 || need_i < 0       ? "negative counts"
+        : need_h > ((int64_t)1 << 40) / hb || need_i > ((int64_t)1 << 40) / 8 ? "implausible counts"
+        : (int64_t)sb.st_size < (int64_t)sizeof H + need_h * hb + need_i * 8 ? "file is truncated"
+                                                                             : nullptr;
+    if (bad) {
+        set_error(RSG_ERR_IO, "rsg_read_binary: %s in %s", bad, path);
+        return RSG_ERR_IO;
+    }
+    *header = H;
+    if (!halos && !ids) return 0;  // the header alone
+    if (need_h > max_halos || need_i > max_ids) {
+        set_error(RSG_ERR_ARGS, "rsg_read_binary: %lld halos / %lld ids for %lld / %lld places",
+                  (long long)need_h, (long long)need_i, (long long)max_halos, (long long)max_ids);
+        return RSG_ERR_ARGS;
+    }
+    try {
+        read_file_parallel(fd, sizeof H, halos, (size_t)(need_h * hb), path);
+        read_file_parallel(fd, (int64_t)sizeof H + need_h * hb, ids, (size_t)(need_i * 8), path);
+    } catch (Failure &) {
+        return error_code();
+    }
+    // read_binary_header_config
+    cfg->scale_now = H.scale;
+    cfg->om = H.Om;
+    cfg->ol = H.Ol;
+    cfg->h0 = H.h0;
+    cfg->box_size = H.box_size;
+    cfg->particle_mass = H.particle_mass;
     return 0;
 }

@@ -31,6 +31,9 @@
  *                                src/io/meta_io.c:175)
  *   output_particles_internal_gpu in place of output_particles_internal(snap,
  *                                chunk, 1) (src/io/meta_io.c:505)
+ *   load_binary_halos_gpu        in place of load_binary_halos
+ *                                (src/io/io_internal.h:41-44, the merger
+ *                                tree's catalogue reader)
  * Errors: the library never exits; a non-zero return is mapped onto the
  * reference's rockstar_abort (src/error.h:17-20). */
 #include <stdio.h>
@@ -44,6 +47,7 @@
 #include "fof.h"
 #include "groupies.h"
 #include "io/io_generic.h"
+#include "io/io_internal.h"
 #include "io/meta_io.h"
 #include "potential.h"
 #include "rockstar.h"
@@ -317,4 +321,33 @@ void output_particles_internal_gpu(int64_t snap, int64_t chunk) {
     get_output_filename(buffer, 1024, snap, chunk, "rbin");
     if (rsg_write_internal(buffer, (struct rsg_particle *)p, num_p, snap, chunk, &c))
         gpu_fail("rsg_write_internal");
+}
+
+/* load_binary_halos: the catalogue of (snap, chunk) read back into *halos
+ * and *part_ids (reallocated), its header into *bheader, and the six
+ * configuration globals read_binary_header_config sets. */
+void load_binary_halos_gpu(int64_t snap, int64_t chunk, struct binary_output_header *bheader,
+                           struct halo **hs, int64_t **part_ids, int64_t coalesced) {
+    struct rsg_config c;
+    char buffer[1024];
+    _Static_assert(sizeof(struct binary_output_header) == sizeof(struct rsg_binary_header),
+                   "binary header layout");
+    gpu_config(&c);
+    get_output_filename(buffer, 1024, snap, chunk, coalesced ? "coalesced.bin" : "bin");
+    struct rsg_binary_header *h = (struct rsg_binary_header *)bheader;
+    if (rsg_read_binary(buffer, h, &c, NULL, 0, NULL, 0)) gpu_fail("rsg_read_binary");
+    *hs = (struct halo *)check_realloc(*hs, (h->num_halos ? h->num_halos : 1) * sizeof(struct halo),
+                                       "Allocating halos.");
+    *part_ids = (int64_t *)check_realloc(
+        *part_ids, (h->num_particles ? h->num_particles : 1) * sizeof(int64_t),
+        "Allocating particle IDs.");
+    if (rsg_read_binary(buffer, h, &c, (struct rsg_halo *)*hs, h->num_halos, *part_ids,
+                        h->num_particles))
+        gpu_fail("rsg_read_binary");
+    SCALE_NOW = c.scale_now;
+    Om = c.om;
+    Ol = c.ol;
+    h0 = c.h0;
+    BOX_SIZE = c.box_size;
+    PARTICLE_MASS = c.particle_mass;
 }

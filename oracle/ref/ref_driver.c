@@ -29,6 +29,7 @@
 #include "potential.h"
 #include "config.h"
 #include "config_vars.h"
+#include "io/io_internal.h"
 
 /* boundary-group globals named by src/interleaving.h:21-27 */
 int64_t num_new_bp = 0;
@@ -330,6 +331,28 @@ int64_t ref_load_internal(const char *path, struct particle *out, int64_t max_p,
     free(pp);
     ref_cfg_get(cfg_out);
     return n;
+}
+
+/* The reference's load_binary_halos (src/io/io_internal.c:199-225) on one
+ * catalogue file: header, halos and particle ids, and the six configuration
+ * values read_binary_header_config sets.  Returns the number of halos. */
+void load_binary_halos(int64_t snap, int64_t chunk, struct binary_output_header *bheader,
+                       struct halo **halos, int64_t **part_ids, int64_t coalesced);
+int64_t ref_load_binary(const char *path, void *header_out, struct halo *h_out, int64_t max_h,
+                        int64_t *ids_out, int64_t max_ids, double *cfg_out) {
+    struct binary_output_header bh;
+    struct halo *hh = NULL;
+    int64_t *ids = NULL;
+    ref_out_path = path;
+    load_binary_halos(0, 0, &bh, &hh, &ids, 0);
+    ref_out_path = NULL;
+    memcpy(header_out, &bh, sizeof bh);
+    if (bh.num_halos <= max_h) memcpy(h_out, hh, sizeof(struct halo) * bh.num_halos);
+    if (bh.num_particles <= max_ids) memcpy(ids_out, ids, sizeof(int64_t) * bh.num_particles);
+    free(hh);
+    free(ids);
+    ref_cfg_get(cfg_out);
+    return bh.num_halos;
 }
 
 /* The reference's GADGET-2 reader (src/io/io_gadget.c, compiled here) on one

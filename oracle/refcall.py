@@ -59,6 +59,8 @@ def lib():
         h.ref_output_particles_internal.argtypes = [C.c_char_p, vp, i64, i64, i64, vp]
         h.ref_load_internal.restype = i64
         h.ref_load_internal.argtypes = [C.c_char_p, vp, i64, vp]
+        h.ref_load_binary.restype = i64
+        h.ref_load_binary.argtypes = [C.c_char_p, vp, vp, i64, vp, i64, vp]
         h.ref_load_gadget2.restype = i64
         h.ref_load_gadget2.argtypes = [C.c_char_p, i64, i64, C.c_double, C.c_double, i64, i64,
                                        i64, C.c_double, vp, i64, vp]
@@ -162,6 +164,21 @@ def output_particles_internal(path, parts, cfg, snap=0, chunk=0):
     c = np.array([cfg[k] for k in INTERNAL_CFG_FIELDS], np.float64)
     lib().ref_output_particles_internal(os.fsencode(path), pa.ctypes.data, len(pa), snap,
                                         chunk, c.ctypes.data)
+
+
+def load_binary(path, max_h=1 << 20, max_ids=1 << 24):
+    """The reference's load_binary_halos on one catalogue file: (the 256
+    header bytes, halos, particle ids, dict of the configuration values it
+    sets)."""
+    hdr = np.zeros(256, np.uint8)
+    h = np.zeros(max_h, L.HALO)
+    ids = np.zeros(max_ids, np.int64)
+    cfg = np.zeros(6, np.float64)
+    nh = lib().ref_load_binary(os.fsencode(path), hdr.ctypes.data, h.ctypes.data, max_h,
+                               ids.ctypes.data, max_ids, cfg.ctypes.data)
+    nids = int(hdr[72:80].view(np.int64)[0])
+    assert nh <= max_h and nids <= max_ids
+    return hdr, h[:nh].copy(), ids[:nids].copy(), dict(zip(INTERNAL_CFG_FIELDS, cfg.tolist()))
 
 
 def load_internal(path, max_p=1 << 22):

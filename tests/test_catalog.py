@@ -1,9 +1,11 @@
 """Catalogue output: the reference's halo filter (_should_print) and its ascii
 and binary halo catalogues (src/io/meta_io.c:266-371,
 src/io/io_internal.c:16-41,118-186), written by the library from halos,
-links and particles.  Checked against the oracle's restatement of the same
-functions on any machine, and against the reference's own output_binary
-where the reference is built (oracle/_ref).  Host code: no GPU needed."""
+links and particles, and the binary catalogue read back (load_binary_halos,
+src/io/io_internal.c:199-225).  Checked against the oracle's restatement of
+the same functions on any machine, and against the reference's own
+output_binary and load_binary_halos where the reference is built
+(oracle/_ref).  Host code: no GPU needed."""
 import os
 import struct
 
@@ -171,3 +173,64 @@ def test_catalog_from_gpu_path(rk, oracle, tmp_path, cfg_id, scale):
     rk.write_binary(str(tmp_path / "g.bin"), gh, gparts, c)
     oracle.write_binary(str(tmp_path / "o.bin"), h, parts)
     assert (tmp_path / "g.bin").read_bytes() == (tmp_path / "o.bin").read_bytes()
+
+
+@pytest.mark.parametrize("cfg_id,scale", CASES)
+def test_read_binary_round_trip(rk, oracle, tmp_path, cfg_id, scale):
+    """rsg_read_binary returns what rsg_write_binary wrote: the printable
+    halos (id and p_start rewritten), their particles' ids, the header and
+    the configuration values read_binary_header_config sets."""
+    c, box, parts, h, e = _case(rk, oracle, cfg_id, scale)
+    path = str(tmp_path / "c.bin")
+    rk.write_binary(path, h, parts, c, id_offset=7, snap=4, chunk=2)
+    hdr, hh, ids, cfg = rk.read_binary(path, rk.Config())
+    keep = rk.should_print(h, c)
+    kept = h[keep]
+    assert hdr.magic == 0xfadedacec0c0d0d0 and hdr.snap == 4 and hdr.chunk == 2
+    assert hdr.num_halos == len(kept) == len(hh) and hdr.particle_type == 1
+    assert np.array_equal(hh["id"], np.arange(len(kept)) + 7)
+    starts = np.concatenate([[0], np.cumsum(kept["num_p"])[:-1]])
+    assert np.array_equal(hh["p_start"], starts)
+    for f in ("num_p", "m", "r", "vmax", "pos"):
+        assert hh[f].tobytes() == kept[f].tobytes()
+    want = np.concatenate([parts["id"][s:s + n] for s, n in zip(kept["p_start"], kept["num_p"])])
+    assert np.array_equal(ids, want)
+    assert cfg["box_size"] == float(np.float32(c.box_size))
+    assert cfg["particle_mass"] == float(np.float32(c.particle_mass))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_LIB), reason="reference oracle not built")
+@pytest.mark.parametrize("cfg_id,scale", CASES)
+def test_read_binary_matches_reference(rk, oracle, tmp_path, cfg_id, scale):
+    """The same header, halos, ids and configuration values as the
+    reference's load_binary_halos on the reference's own output_binary."""
+    from oracle import refcall
+    c, box, parts, h, e = _case(rk, oracle, cfg_id, scale)
+    path = str(tmp_path / "r.bin")
+    refcall.output_binary(path, h, parts, id_offset=3, snap=9, chunk=0, bounds=_bounds(box))
+    rhdr, rh, rids, rcfg = refcall.load_binary(path)
+    hdr, hh, ids, cfg = rk.read_binary(path, rk.Config())
+    assert bytes(hdr) == rhdr.tobytes()
+    assert hh.tobytes() == rh.tobytes() and np.array_equal(ids, rids)
+    assert cfg == rcfg
+
+
+def test_read_binary_errors(rk, tmp_path):
+    c = rk.Config()
+    good = str(tmp_path / "empty.bin")
+    rk.write_binary(good, np.zeros(0, rk.HALO), np.zeros(0, rk.PARTICLE), c)
+    hdr, hh, ids, _ = rk.read_binary(good, c)
+    assert hdr.num_halos == 0 and len(hh) == 0 and len(ids) == 0
+    raw = open(good, "rb").read()
+    cases = {
+        "short.bin": raw[:200],
+        "magic.bin": b"\1" + raw[1:],
+        "count.bin": raw[:64] + struct.pack("<q", 3) + raw[72:],  # 3 halos announced, none stored
+        "neg.bin": raw[:72] + struct.pack("<q", -1) + raw[80:],
+    }
+    for name, data in cases.items():
+        path = str(tmp_path / name)
+        open(path, "wb").write(data)
+        with pytest.raises(rk.RockstarError) as ex:
+            rk.read_binary(path, c)
+        assert ex.value.code == -7, name
