@@ -222,6 +222,21 @@ int rsg_write_binary(const char *path, const struct rsg_halo *halos, int64_t num
                      const struct rsg_particle *p, int64_t num_p,
                      const struct rsg_catalog *opt, const struct rsg_config *cfg);
 
+/* output_full_particles with print_child_particles (src/io/meta_io.c:378-461):
+ * the halos_<snap>.<chunk>.particles table.  opt supplies id_offset, bounds,
+ * num_p and strict_so_masses; unfiltered is UNFILTERED_HALO_OUTPUT and
+ * every_n OUTPUT_EVERY_N_PARTICLES.  The printable halos get ids from
+ * id_offset, the others -1 (listed only when unfiltered); every listed halo's
+ * particles are followed, recursively, by its children's (extra child /
+ * next_cochild).  ids_out (num_halos entries, or NULL) receives the ids the
+ * reference writes back into halos[].id.  RSG_ERR_ARGS for a halo whose
+ * particles lie outside p or a child link that leaves the halos or loops. */
+int rsg_write_particles(const char *path, const struct rsg_halo *halos,
+                        const struct rsg_extra_halo_info *extra, int64_t num_halos,
+                        const struct rsg_particle *p, int64_t num_p,
+                        const struct rsg_catalog *opt, int64_t unfiltered, int64_t every_n,
+                        const struct rsg_config *cfg, int64_t *ids_out);
+
 /* struct binary_output_header (src/io/io_internal.h:15-27), 256 bytes: the
  * header of the halo catalogue (halos_<snap>.<chunk>.bin) and of the
  * internal particle format. */

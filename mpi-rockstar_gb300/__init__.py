@@ -91,6 +91,8 @@ def lib():
         h.rsg_count_halos_to_print.restype = i64
         h.rsg_count_halos_to_print.argtypes = [vp, i64, vp, vp]
         h.rsg_write_ascii.argtypes = [C.c_char_p, vp, vp, i64, vp, vp]
+        h.rsg_write_particles.argtypes = [C.c_char_p, vp, vp, i64, vp, i64, vp, i64, i64, vp,
+                                          vp]
         h.rsg_write_binary.argtypes = [C.c_char_p, vp, i64, vp, i64, vp, vp]
         for name, args in _EXTRA_SIGS.items():
             if hasattr(h, name):
@@ -515,6 +517,23 @@ def write_ascii(path, halos, extra, cfg, id_offset=0, bounds=None, num_p=0,
     o, b = _catalog_opts(id_offset, 0, 0, bounds, num_p, strict_so_masses)
     _check(lib().rsg_write_ascii(os.fsencode(path), h.ctypes.data, e.ctypes.data, len(h),
                                  C.byref(o), C.byref(st)))
+
+
+def write_particles(path, halos, extra, parts, cfg, id_offset=0, bounds=None, num_p=0,
+                    strict_so_masses=0, unfiltered=0, every_n=0):
+    """The halos_<snap>.<chunk>.particles table (output_full_particles);
+    returns the ids it assigns to the halos (-1 for the unprintable ones)."""
+    st = setup_config(cfg)
+    h = np.ascontiguousarray(halos, dtype=HALO)
+    e = np.ascontiguousarray(extra, dtype=EXTRA)
+    pa = np.ascontiguousarray(parts, dtype=PARTICLE)
+    assert len(h) == len(e)
+    o, b = _catalog_opts(id_offset, 0, 0, bounds, num_p, strict_so_masses)
+    ids = np.zeros(max(len(h), 1), np.int64)
+    _check(lib().rsg_write_particles(os.fsencode(path), h.ctypes.data, e.ctypes.data, len(h),
+                                     pa.ctypes.data if len(pa) else None, len(pa), C.byref(o),
+                                     unfiltered, every_n, C.byref(st), ids.ctypes.data))
+    return ids[:len(h)]
 
 
 class BinaryHeader(C.Structure):

@@ -159,6 +159,122 @@ extern "C" int rsg_write_ascii(const char *path, const struct rsg_halo *h,
     return 0;
 }
 
+extern "C" int rsg_write_particles(const char *path, const struct rsg_halo *h,
+                                   const struct rsg_extra_halo_info *e, int64_t nh,
+                                   const struct rsg_particle *p, int64_t num_p,
+                                   const struct rsg_catalog *opt, int64_t unfiltered,
+                                   int64_t every_n, const struct rsg_config *cfg,
+                                   int64_t *ids_out) {
+    if (!path || (nh && (!h || !e)) || !opt || !cfg || nh < 0 || num_p < 0 || (!p && num_p)) {
+        set_error(RSG_ERR_ARGS, "rsg_write_particles: bad arguments");
+        return RSG_ERR_ARGS;
+    }
+    const rsg_config &c = *cfg;
+    // the ids output_full_particles assigns (and writes back into the halos)
+    std::vector<int64_t> ids((size_t)nh);
+    int64_t next = 0;
+    for (int64_t i = 0; i < nh; i++)
+        ids[i] = should_print(h[i], opt->bounds, c) ? opt->id_offset + next++ : -1;
+    // the halos whose particles are listed, and everything their child links
+    // reach, must stay inside p and the halo array, without cycles
+    auto listed = [&](int64_t i) { return unfiltered || ids[i] > -1; };
+    std::vector<int64_t> seen((size_t)nh, -1), stack;
+    for (int64_t top = 0; top < nh; top++) {
+        if (!listed(top)) continue;
+        stack.assign(1, top);
+        while (!stack.empty()) {
+            const int64_t i = stack.back();
+            stack.pop_back();
+            if (i < 0 || i >= nh || seen[i] == top || h[i].p_start < 0 || h[i].num_p < 0 ||
+                h[i].p_start + h[i].num_p > num_p) {
+                set_error(RSG_ERR_ARGS, "rsg_write_particles: bad halo or child link below halo %" PRId64,
+                          top);
+                return RSG_ERR_ARGS;
+            }
+            seen[i] = top;
+            for (int64_t ch = e[i].child; ch > -1; ch = (ch < nh ? e[ch].next_cochild : -1)) {
+                if (ch >= nh || (int64_t)stack.size() > nh) {
+                    set_error(RSG_ERR_ARGS, "rsg_write_particles: bad child link below halo %" PRId64,
+                              top);
+                    return RSG_ERR_ARGS;
+                }
+                stack.push_back(ch);
+            }
+        }
+    }
+    File F;
+    F.f = fopen(path, "w");
+    if (!F.f) {
+        set_error(RSG_ERR_IO, "rsg_write_particles: cannot open %s", path);
+        return RSG_ERR_IO;
+    }
+    FILE *o = F.f;
+    const char *M0 = kMassDef[0];
+    fputs("#Halo table:\n", o);
+    fprintf(o,
+            "#id internal_id num_p m%s mbound_%s r%s vmax rvmax vrms x y z vx vy vz Jx Jy Jz "
+            "energy spin\n",
+            M0, M0, M0);
+    fputs("#Particle table:\n"
+          "#x y z vx vy vz particle_id assigned_internal_haloid internal_haloid "
+          "external_haloid\n",
+          o);
+    if (every_n > 1)
+        fprintf(o, "#Notes: Only particles with IDs divisible by %" PRId64 " are printed.\n",
+                every_n);
+    fputs("#Notes: As not all halos are printed, some halos may not have external halo ids.  "
+          "(Hence the need to print internal halo ids).  Each particle is assigned to a unique "
+          "halo; however, some properties (such as halo bound mass) are calculated including "
+          "all substructure.  As such, particles belonging to subhalos are included in "
+          "outputs; to exclude substructure, verify that the internal halo id is the same as "
+          "the assigned internal halo id.\n",
+          o);
+    header_info(o, opt->bounds, opt->num_p, opt->strict_so_masses, c);
+    fputs("#Halo table begins here:\n", o);
+    for (int64_t i = 0; i < nh; i++) {
+        if (!listed(i)) continue;
+        const rsg_halo &t = h[i];
+        fprintf(o,
+                "#%" PRId64 " %" PRId64 " %" PRId64 " %.3e %.3e %f %f %f %f %f %f %f %f %f %f "
+                "%g %g %g %g %g\n",
+                ids[i], i, t.num_p, t.m, t.mgrav, t.r, t.vmax, t.rvmax, t.vrms, t.pos[0], t.pos[1],
+                t.pos[2], t.pos[3], t.pos[4], t.pos[5], t.J[0], t.J[1], t.J[2], t.energy, t.spin);
+    }
+    fputs("#Particle table begins here:\n", o);
+    // each listed halo's particles, then its children's in child /
+    // next_cochild order, depth first (print_child_particles)
+    auto emit = [&](int64_t i, int64_t top) {
+        for (int64_t j = 0; j < h[i].num_p; j++) {
+            const rsg_particle &q = p[h[i].p_start + j];
+            if (every_n <= 1 || !(q.id % every_n))
+                fprintf(o, "%f %f %f %f %f %f %" PRId64 " %" PRId64 " %" PRId64 " %" PRId64 "\n",
+                        q.pos[0], q.pos[1], q.pos[2], q.pos[3], q.pos[4], q.pos[5], q.id, i, top,
+                        ids[top]);
+        }
+    };
+    for (int64_t top = 0; top < nh; top++) {
+        if (!listed(top)) continue;
+        emit(top, top);
+        stack.assign(1, e[top].child);  // the next child to visit at each depth
+        while (!stack.empty()) {
+            const int64_t ch = stack.back();
+            if (ch < 0) {
+                stack.pop_back();
+                continue;
+            }
+            stack.back() = e[ch].next_cochild;
+            emit(ch, top);
+            stack.push_back(e[ch].child);
+        }
+    }
+    if (ids_out) memcpy(ids_out, ids.data(), sizeof(int64_t) * (size_t)nh);
+    if (ferror(o)) {
+        set_error(RSG_ERR_IO, "rsg_write_particles: write to %s failed", path);
+        return RSG_ERR_IO;
+    }
+    return 0;
+}
+
 extern "C" int rsg_write_binary(const char *path, const struct rsg_halo *h, int64_t nh,
                                 const struct rsg_particle *p, int64_t num_p,
                                 const struct rsg_catalog *opt, const struct rsg_config *cfg) {

@@ -18,9 +18,9 @@
  *                                called at src/properties.c:548-550)
  *   analyze_halos_gpu(base, nh)  calls the analyze_halo_generic hook
  *                                (src/io/io_generic.h:12-18) per halo
- *   output_catalogs_gpu(...)     in place of output_halos' two catalogue
- *                                writers, output_ascii and output_binary
- *                                (src/io/meta_io.c:490-499)
+ *   output_catalogs_gpu(...)     in place of output_halos (src/io/meta_io.c:
+ *                                489-509): output_ascii, output_binary,
+ *                                output_full_particles and the particle dump
  *   load_particles_gadget2_gpu   in place of load_particles_gadget2
  *                                (src/io/io_gadget.h:29-30, called at
  *                                src/io/meta_io.c:170)
@@ -223,12 +223,16 @@ void analyze_halos_gpu(int64_t base, int64_t nh) {
     free(cnt);
 }
 
+void output_particles_internal_gpu(int64_t snap, int64_t chunk);
+
 /* ---- catalogue output -------------------------------------------------------
- * The out_<snap>.list and halos_<snap>.<chunk>.bin catalogues of output_halos
- * (src/io/meta_io.c:490-499) for OUTPUT_FORMAT ASCII, BINARY or BOTH, written
- * by the library from halos, extra_info and p, with the reference's file
- * names.  The full-particle, dump and lensing outputs of output_halos stay
- * with the reference. */
+ * output_halos (src/io/meta_io.c:489-509) with the library's writers, from
+ * halos, extra_info and p, under the reference's file names and conditions:
+ * the out_<snap>.list and halos_<snap>.<chunk>.bin catalogues (OUTPUT_FORMAT
+ * ASCII, BINARY or BOTH), the .particles table for chunk < FULL_PARTICLE_CHUNKS
+ * (writing back the halo ids it assigns, as output_full_particles does) and
+ * the DUMP_PARTICLES dump.  The weak-lensing subsample, drawn with the C
+ * library's rand(), is left to the reference's own output_particles_internal. */
 void output_catalogs_gpu(int64_t id_offset, int64_t snap, int64_t chunk, float *bounds) {
     struct rsg_config c;
     char buffer[1024];
@@ -247,6 +251,21 @@ void output_catalogs_gpu(int64_t id_offset, int64_t snap, int64_t chunk, float *
                              (struct rsg_particle *)p, num_p, &o, &c))
             gpu_fail("rsg_write_binary");
     }
+    if (chunk < FULL_PARTICLE_CHUNKS) {
+        int64_t *ids = (int64_t *)check_realloc(NULL, (num_halos ? num_halos : 1) * sizeof(int64_t),
+                                                "Allocating halo ids.");
+        get_output_filename(buffer, 1024, snap, chunk, "particles");
+        if (rsg_write_particles(buffer, (struct rsg_halo *)halos,
+                                (struct rsg_extra_halo_info *)extra_info, num_halos,
+                                (struct rsg_particle *)p, num_p, &o, UNFILTERED_HALO_OUTPUT,
+                                OUTPUT_EVERY_N_PARTICLES, &c, ids))
+            gpu_fail("rsg_write_particles");
+        for (int64_t i = 0; i < num_halos; i++) halos[i].id = ids[i];
+        free(ids);
+    }
+    if (DUMP_PARTICLES[0] && (chunk >= DUMP_PARTICLES[1] && chunk <= DUMP_PARTICLES[2]))
+        output_particles_internal_gpu(snap, chunk);
+    if (WEAK_LENSING_FRACTION > 0) output_particles_internal(snap, chunk, WEAK_LENSING_FRACTION);
 }
 
 /* ---- particle input -----------------------------------------------------------

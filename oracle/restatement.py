@@ -61,6 +61,8 @@ def lib():
         h.oracle_should_print.argtypes = [vp, vp]
         h.oracle_write_ascii.argtypes = [C.c_char_p, vp, vp, i64, i64, vp, i64, i64]
         h.oracle_write_binary.argtypes = [C.c_char_p, vp, i64, vp, i64, i64, i64, vp]
+        h.oracle_write_particles.argtypes = [C.c_char_p, vp, vp, i64, vp, i64, vp, i64, i64, i64,
+                                             i64, vp]
         h.oracle_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
         h.oracle_hierarchy.restype = i64
         h.oracle_hierarchy.argtypes = [vp, vp, vp, i64]
@@ -166,6 +168,20 @@ def write_ascii(path, halos, extra, id_offset=0, bounds=None, num_p=0, strict_so
     b, bp = _bounds(bounds)
     assert lib().oracle_write_ascii(os.fsencode(path), h.ctypes.data, e.ctypes.data, len(h),
                                     id_offset, bp, num_p, strict_so_masses) == 0
+
+
+def write_particles(path, halos, extra, parts, id_offset=0, bounds=None, num_p=0,
+                    strict_so_masses=0, unfiltered=0, every_n=0):
+    """output_full_particles to `path`; returns the ids it assigns."""
+    h = np.ascontiguousarray(halos, dtype=L.HALO)
+    e = np.ascontiguousarray(extra, dtype=L.EXTRA)
+    pa = np.ascontiguousarray(parts, dtype=L.PARTICLE)
+    b, bp = _bounds(bounds)
+    ids = np.zeros(max(len(h), 1), np.int64)
+    assert lib().oracle_write_particles(os.fsencode(path), h.ctypes.data, e.ctypes.data, len(h),
+                                        pa.ctypes.data, id_offset, bp, num_p, strict_so_masses,
+                                        unfiltered, every_n, ids.ctypes.data) == 0
+    return ids[:len(h)]
 
 
 def write_binary(path, halos, parts, id_offset=0, snap=0, chunk=0, bounds=None):

@@ -1609,3 +1609,83 @@ int oracle_write_binary(const char *path, const struct halo *halos, int64_t num_
     fclose(output);
     return 0;
 }
+
+/* output_full_particles with print_child_particles (src/io/meta_io.c:378-461)
+ * to the caller's file name: the halo table (ids assigned to the printable
+ * halos from id_offset, -1 for the others, printed only with
+ * UNFILTERED_HALO_OUTPUT), then every listed halo's particles followed,
+ * recursively, by its children's.  ids_out receives the ids the reference
+ * writes back into halos[].id. */
+static void orc_child_particles(FILE *output, const struct halo *halos, const struct extra *ex,
+                                const struct particle *p, int64_t i, int64_t pid, int64_t eid,
+                                int64_t every_n) {
+    int64_t j, child;
+    const struct particle *p2;
+    for (j = 0; j < halos[i].num_p; j++) {
+        p2 = p + halos[i].p_start + j;
+        if (every_n <= 1 || !(p2->id % every_n))
+            fprintf(output,
+                    "%f %f %f %f %f %f %" PRId64 " %" PRId64 " %" PRId64 " %" PRId64 "\n",
+                    p2->pos[0], p2->pos[1], p2->pos[2], p2->pos[3], p2->pos[4], p2->pos[5],
+                    p2->id, i, pid, eid);
+    }
+    child = ex[i].child;
+    while (child > -1) {
+        orc_child_particles(output, halos, ex, p, child, pid, eid, every_n);
+        child = ex[child].next_cochild;
+    }
+}
+
+int oracle_write_particles(const char *path, const struct halo *halos, const struct extra *ex,
+                           int64_t num_halos, const struct particle *p, int64_t id_offset,
+                           const float *bounds, int64_t np, int64_t strict_so, int64_t unfiltered,
+                           int64_t every_n, int64_t *ids_out) {
+    int64_t i, id = 0;
+    const struct halo *th;
+    const char **M = orc_mass_def;
+    FILE *output = fopen(path, "w");
+    if (!output) return -1;
+    fprintf(output, "#Halo table:\n");
+    fprintf(output,
+            "#id internal_id num_p m%s mbound_%s r%s vmax rvmax vrms x y z vx "
+            "vy vz Jx Jy Jz energy spin\n",
+            M[0], M[0], M[0]);
+    fprintf(output, "#Particle table:\n");
+    fprintf(output, "#x y z vx vy vz particle_id assigned_internal_haloid "
+                    "internal_haloid external_haloid\n");
+    if (every_n > 1)
+        fprintf(output, "#Notes: Only particles with IDs divisible by %" PRId64 " are printed.\n",
+                every_n);
+    fprintf(output,
+            "#Notes: As not all halos are printed, some halos may not have "
+            "external halo ids.  (Hence the need to print internal halo ids).  "
+            "Each particle is assigned to a unique halo; however, some "
+            "properties (such as halo bound mass) are calculated including all "
+            "substructure.  As such, particles belonging to subhalos are "
+            "included in outputs; to exclude substructure, verify that the "
+            "internal halo id is the same as the assigned internal halo id.\n");
+    orc_header_info(output, bounds, np, strict_so);
+    fprintf(output, "#Halo table begins here:\n");
+    for (i = 0; i < num_halos; i++) {
+        th = halos + i;
+        if (oracle_should_print(th, bounds)) {
+            ids_out[i] = id + id_offset;
+            id++;
+        } else {
+            ids_out[i] = -1;
+            if (!unfiltered) continue;
+        }
+        fprintf(output,
+                "#%" PRId64 " %" PRId64 " %" PRId64 " %.3e %.3e"
+                " %f %f %f %f %f %f %f %f %f %f %g %g %g %g %g\n",
+                ids_out[i], i, th->num_p, th->m, th->mgrav, th->r, th->vmax, th->rvmax, th->vrms,
+                th->pos[0], th->pos[1], th->pos[2], th->pos[3], th->pos[4], th->pos[5], th->J[0],
+                th->J[1], th->J[2], th->energy, th->spin);
+    }
+    fprintf(output, "#Particle table begins here:\n");
+    for (i = 0; i < num_halos; i++)
+        if (unfiltered || ids_out[i] > -1)
+            orc_child_particles(output, halos, ex, p, i, i, ids_out[i], every_n);
+    fclose(output);
+    return 0;
+}

@@ -234,3 +234,35 @@ def test_read_binary_errors(rk, tmp_path):
         with pytest.raises(rk.RockstarError) as ex:
             rk.read_binary(path, c)
         assert ex.value.code == -7, name
+
+
+@pytest.mark.parametrize("cfg_id,scale", CASES)
+def test_particles_table_matches_oracle(rk, oracle, tmp_path, cfg_id, scale):
+    """output_full_particles: filtered and unfiltered, every particle or
+    every n-th id, with and without bounds; same bytes and same ids."""
+    c, box, parts, h, e = _case(rk, oracle, cfg_id, scale)
+    assert (e["child"] > -1).any()  # the recursion over children is exercised
+    opts = [dict(), dict(unfiltered=1), dict(every_n=7, id_offset=100),
+            dict(bounds=_bounds(box), num_p=0, strict_so_masses=1)]
+    for k, kw in enumerate(opts):
+        ours, ref = tmp_path / ("a%d.particles" % k), tmp_path / ("b%d.particles" % k)
+        kw.setdefault("num_p", len(parts))
+        ids = rk.write_particles(str(ours), h, e, parts, c, **kw)
+        want = oracle.write_particles(str(ref), h, e, parts, **kw)
+        assert ours.read_bytes() == ref.read_bytes()
+        assert np.array_equal(ids, want)
+        assert np.array_equal(ids > -1, rk.should_print(h, c, kw.get("bounds")))
+
+
+def test_particles_table_bad_links(rk, oracle, tmp_path):
+    c, box, parts, h, e = _case(rk, oracle, 1, 0.05)
+    parent = int(np.flatnonzero(e["child"] > -1)[0])
+    for bad in ("loop", "range"):
+        e2 = e.copy()
+        if bad == "loop":
+            e2["child"][e["child"][parent]] = parent
+        else:
+            e2["next_cochild"][e["child"][parent]] = len(h) + 5
+        with pytest.raises(rk.RockstarError) as ex:
+            rk.write_particles(str(tmp_path / "x.particles"), h, e2, parts, c, unfiltered=1)
+        assert ex.value.code == -1
