@@ -11,6 +11,19 @@ Function names follow the reference calls they replace:
                        as the loop of src/mpi_main.cpp:1363-1389 runs it
   compute_potential <- compute_potential()          src/potential.c:183-192
   compute_kinetic_energy <- compute_kinetic_energy() src/potential.c:194-211
+  should_print, write_ascii, write_binary, write_particles
+                    <- _should_print, output_ascii, output_binary,
+                       output_full_particles        src/io/meta_io.c:266-461,
+                                                    src/io/io_internal.c:118-186
+  read_binary       <- load_binary_halos()          src/io/io_internal.c:199-225
+  read_gadget2      <- load_particles_gadget2()     src/io/io_gadget.c:200-254
+  read_internal, write_internal
+                    <- load_particles_internal(), output_particles_internal()
+                                                    src/io/io_internal.c:52-100
+  sort_by_id        <- the std::sort by id          src/mpi_main.cpp:2021-2024
+The *_device variants keep the records in device memory.  The file-format
+calls that need no conversion (the catalogue writers and readers, the
+internal-format host reader and writer) are host I/O with no device step.
 """
 import ctypes as C
 import os
