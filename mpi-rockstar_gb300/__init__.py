@@ -3,7 +3,8 @@
 The compute runs in the CUDA library _build/librockstar_gb300.so (kernels for
 sm_103a behind the C ABI of include/rockstar_gb300.h); this module only
 moves numpy arrays across that ABI with ctypes.  There is no CPU fallback:
-if the library cannot be loaded or no GPU is present, every call raises.
+if the library cannot be loaded every call raises, and without a GPU every
+call that computes or moves data to the device raises.
 
 Function names follow the reference calls they replace:
   rockstar_fof      <- rockstar(NULL, 1)            src/rockstar.c:53-128
