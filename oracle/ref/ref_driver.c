@@ -355,6 +355,34 @@ int64_t ref_load_binary(const char *path, void *header_out, struct halo *h_out, 
     return bh.num_halos;
 }
 
+/* The merger tree's descendant rule (src/merger.c, compiled here): halos1 /
+ * part1 of one snapshot against halos2 / part2 of the next, through
+ * init_descendants, connect_particle_ids_to_halo_ids and
+ * calculate_descendants; desc_out receives halos1[i].desc. */
+#include "merger.h"
+void ref_descendants(const struct halo *h1, int64_t nh1, const int64_t *p1, int64_t np1,
+                     const struct halo *h2, int64_t nh2, const int64_t *p2, int64_t np2,
+                     int64_t *desc_out) {
+    clear_merger_tree();
+    halos1 = malloc(sizeof(struct halo) * (nh1 ? nh1 : 1));
+    halos2 = malloc(sizeof(struct halo) * (nh2 ? nh2 : 1));
+    part1 = malloc(sizeof(int64_t) * (np1 ? np1 : 1));
+    part2 = malloc(sizeof(int64_t) * (np2 ? np2 : 1));
+    memcpy(halos1, h1, sizeof(struct halo) * nh1);
+    memcpy(halos2, h2, sizeof(struct halo) * nh2);
+    memcpy(part1, p1, sizeof(int64_t) * np1);
+    memcpy(part2, p2, sizeof(int64_t) * np2);
+    head1.num_halos = nh1;
+    head1.num_particles = np1;
+    head2.num_halos = nh2;
+    head2.num_particles = np2;
+    init_descendants();
+    connect_particle_ids_to_halo_ids();
+    calculate_descendants();
+    for (int64_t i = 0; i < nh1; i++) desc_out[i] = halos1[i].desc;
+    clear_merger_tree();
+}
+
 /* The reference's GADGET-2 reader (src/io/io_gadget.c, compiled here) on one
  * file with the given reader settings: the particles in file order and the
  * configuration values it sets (Om, Ol, h0, BOX_SIZE, TOTAL_PARTICLES,

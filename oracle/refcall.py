@@ -59,6 +59,7 @@ def lib():
         h.ref_output_particles_internal.argtypes = [C.c_char_p, vp, i64, i64, i64, vp]
         h.ref_load_internal.restype = i64
         h.ref_load_internal.argtypes = [C.c_char_p, vp, i64, vp]
+        h.ref_descendants.argtypes = [vp, i64, vp, i64, vp, i64, vp, i64, vp]
         h.ref_load_binary.restype = i64
         h.ref_load_binary.argtypes = [C.c_char_p, vp, vp, i64, vp, i64, vp]
         h.ref_load_gadget2.restype = i64
@@ -208,3 +209,16 @@ def load_gadget2(path, halo_particle_type=1, skip_non_halo=1, length_conversion=
                                cfg.ctypes.data)
     assert n <= max_p
     return out[:n].copy(), dict(zip(GADGET_CFG_FIELDS, cfg.tolist()))
+
+
+def descendants(halos1, part1, halos2, part2):
+    """The reference's merger-tree descendants (src/merger.c:45-101) of
+    halos1 (ids in part1) among halos2 (ids in part2)."""
+    h1 = np.ascontiguousarray(halos1, dtype=L.HALO)
+    h2 = np.ascontiguousarray(halos2, dtype=L.HALO)
+    p1 = np.ascontiguousarray(part1, dtype=np.int64)
+    p2 = np.ascontiguousarray(part2, dtype=np.int64)
+    out = np.zeros(max(len(h1), 1), np.int64)
+    lib().ref_descendants(h1.ctypes.data, len(h1), p1.ctypes.data, len(p1), h2.ctypes.data,
+                          len(h2), p2.ctypes.data, len(p2), out.ctypes.data)
+    return out[:len(h1)]

@@ -64,6 +64,7 @@ def lib():
         h.oracle_write_particles.argtypes = [C.c_char_p, vp, vp, i64, vp, i64, vp, i64, i64, i64,
                                              i64, vp]
         h.oracle_tree_order.argtypes = [vp, i64, C.c_int, C.c_int]
+        h.oracle_descendants.argtypes = [vp, i64, vp, vp, i64, vp, vp]
         h.oracle_hierarchy.restype = i64
         h.oracle_hierarchy.argtypes = [vp, vp, vp, i64]
         _lib = h
@@ -190,3 +191,16 @@ def write_binary(path, halos, parts, id_offset=0, snap=0, chunk=0, bounds=None):
     b, bp = _bounds(bounds)
     assert lib().oracle_write_binary(os.fsencode(path), h.ctypes.data, len(h), pa.ctypes.data,
                                      id_offset, snap, chunk, bp) == 0
+
+
+def descendants(halos1, part1, halos2, part2):
+    """The merger tree's descendant of every halo of halos1 (ids in part1)
+    among halos2 (ids in part2), by the rule of src/merger.c:45-101."""
+    h1 = np.ascontiguousarray(halos1, dtype=L.HALO)
+    h2 = np.ascontiguousarray(halos2, dtype=L.HALO)
+    p1 = np.ascontiguousarray(part1, dtype=np.int64)
+    p2 = np.ascontiguousarray(part2, dtype=np.int64)
+    out = np.zeros(max(len(h1), 1), np.int64)
+    lib().oracle_descendants(h1.ctypes.data, len(h1), p1.ctypes.data, h2.ctypes.data, len(h2),
+                             p2.ctypes.data, out.ctypes.data)
+    return out[:len(h1)]

@@ -1689,3 +1689,66 @@ int oracle_write_particles(const char *path, const struct halo *halos, const str
     fclose(output);
     return 0;
 }
+
+/* ------------------------------------------------------- merger trees ----
+ * The descendant rule of src/merger.c:45-101 (connect_particle_ids_to_halo_ids
+ * + calculate_descendants): every particle id listed by a halo of the later
+ * catalogue (halos2 in order, each halo's ids in order) maps to that halo's
+ * id, a later listing replacing an earlier one; a halo of the earlier
+ * catalogue takes as descendant the id that most of its particles map to,
+ * the smallest such id on a tie, or -1 when none maps.  Restated here as a
+ * sort-based join over (particle id, listing order). */
+struct orc_pid_hid { int64_t pid, ord, hid; };
+static int orc_cmp_pid_ord(const void *a, const void *b) {
+    const struct orc_pid_hid *x = a, *y = b;
+    if (x->pid != y->pid) return x->pid < y->pid ? -1 : 1;
+    return (x->ord > y->ord) - (x->ord < y->ord);
+}
+static int orc_cmp_i64(const void *a, const void *b) {
+    int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+    return (x > y) - (x < y);
+}
+void oracle_descendants(const struct halo *h1, int64_t nh1, const int64_t *p1,
+                        const struct halo *h2, int64_t nh2, const int64_t *p2,
+                        int64_t *desc_out) {
+    int64_t i, j, n = 0, m = 0, k;
+    for (i = 0; i < nh2; i++) n += h2[i].num_p > 0 ? h2[i].num_p : 0;
+    struct orc_pid_hid *map = malloc(sizeof *map * (n ? n : 1));
+    for (i = 0; i < nh2; i++)
+        for (j = h2[i].p_start; j < h2[i].p_start + h2[i].num_p; j++) {
+            map[m].pid = p2[j];
+            map[m].ord = m;
+            map[m].hid = h2[i].id;
+            m++;
+        }
+    qsort(map, m, sizeof *map, orc_cmp_pid_ord);
+    /* keep the last listing of each id */
+    for (i = 0, k = 0; i < m; i++)
+        if (i + 1 == m || map[i + 1].pid != map[i].pid) map[k++] = map[i];
+    m = k;
+    int64_t cap = 1;
+    for (i = 0; i < nh1; i++) if (h1[i].num_p > cap) cap = h1[i].num_p;
+    int64_t *hits = malloc(sizeof(int64_t) * cap);
+    for (i = 0; i < nh1; i++) {
+        desc_out[i] = -1;
+        for (j = 0, k = 0; j < h1[i].num_p; j++) {
+            int64_t pid = p1[h1[i].p_start + j], lo = 0, hi = m;
+            while (lo < hi) {
+                int64_t mid = lo + (hi - lo) / 2;
+                if (map[mid].pid < pid) lo = mid + 1; else hi = mid;
+            }
+            if (lo < m && map[lo].pid == pid) hits[k++] = map[lo].hid;
+        }
+        if (!k) continue;
+        qsort(hits, k, sizeof(int64_t), orc_cmp_i64);
+        int64_t best = -1, best_n = 0, run = 1;
+        for (j = 1; j <= k; j++) {
+            if (j < k && hits[j] == hits[j - 1]) { run++; continue; }
+            if (run > best_n) { best_n = run; best = hits[j - 1]; }
+            run = 1;
+        }
+        desc_out[i] = best;
+    }
+    free(hits);
+    free(map);
+}
