@@ -120,3 +120,21 @@ def test_read_internal_device_large(rk, tmp_path):
     assert d.cpu().numpy().tobytes() == p.tobytes()
     rk.sort_by_id_device(d)
     assert d.cpu().numpy().tobytes() == p[::-1].tobytes()
+
+
+def test_internal_io_arguments(rk, tmp_path):
+    import ctypes as C
+    z = fixture("rbin_777")
+    path = str(tmp_path / "in.rbin")
+    z["raw_file"].tofile(path)
+    st = rk.config_struct(rk.Config())
+    n = np.zeros(1, np.int64)
+    buf = np.zeros(10, rk.PARTICLE)
+    # too few places for the file's particles
+    rc = rk.lib().rsg_read_internal(path.encode(), C.byref(st), buf.ctypes.data, len(buf),
+                                    n.ctypes.data)
+    assert rc == -1 and n[0] == 777
+    # an unwritable destination
+    with pytest.raises(rk.RockstarError) as e:
+        rk.write_internal(str(tmp_path / "no" / "dir" / "x.rbin"), buf, rk.Config())
+    assert e.value.code == -7
